@@ -1,0 +1,463 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 spectral random-field summators.
+
+Metric: Gpoint*modes/s (points x Fourier modes summed per second) on one
+GB300, for the chosen computation form, next to the plain FP64 kernel.
+
+Workloads (synthetic, seeded numpy default_rng; the reference publishes no
+benchmark data):
+  c1  plain 2-D unstructured: 100,000 points in [0,100]^2, 1000 modes,
+      Gaussian spectrum (k ~ N(0, 2/l^2), l = 10)
+  c2  structured 3-D scalar: 256^3 grid, spacing 1, 2000 modes, exponential
+      spectrum (multivariate Student-t nu=1, / l, l = 20)        [default]
+  c3  unstructured 3-D: 16,777,216 points in [0,1000]^3, 4096 modes,
+      exponential spectrum l = 5
+  c4  incompressible 3-D: 192^3 grid, 2048 modes, Gaussian spectrum l = 8
+
+One step = one full summation of the workload.  `value` is timed with CUDA
+events on the launch stream, inputs resident in HBM, L2 flushed (a 256 MiB
+write) before every timed step; `e2e` is the same metric through the public
+host API (numpy in, numpy out, host<->device copies inside the timed call).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2] [--form auto]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gstools-core_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = ("Gpoint*modes/s on 1 GB300 at stated error vs FP64; chosen form vs plain FP64 "
+          "kernel")
+UNIT = "Gpoint*modes/s"
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def student_t(rng, dim, n, ell):
+    return rng.standard_normal((dim, n)) / np.sqrt(rng.chisquare(1, n)) / ell
+
+
+def workload(name: str):
+    """Returns dict(dim, cov, z1, z2, pos=None | axes=None, incompr, desc)."""
+    rng = np.random.default_rng(0)
+    if name == "c1":
+        pos = rng.uniform(0, 100, (2, 100000))
+        cov = rng.normal(0, np.sqrt(2) / 10, (2, 1000))
+        z1, z2 = rng.standard_normal(1000), rng.standard_normal(1000)
+        return dict(dim=2, cov=cov, z1=z1, z2=z2, pos=pos, axes=None, incompr=False,
+                    desc="plain 2-D unstructured, 1e5 points x 1000 modes, Gaussian l=10")
+    if name == "c2":
+        cov = student_t(rng, 3, 2000, 20.0)
+        z1, z2 = rng.standard_normal(2000), rng.standard_normal(2000)
+        ax = np.arange(256, dtype=np.float64)
+        return dict(dim=3, cov=cov, z1=z1, z2=z2, pos=None, axes=(ax, ax, ax), incompr=False,
+                    desc="structured 3-D scalar, 256^3 grid x 2000 modes, exponential l=20")
+    if name == "c3":
+        pos = rng.uniform(0, 1000, (3, 16777216))
+        cov = student_t(rng, 3, 4096, 5.0)
+        z1, z2 = rng.standard_normal(4096), rng.standard_normal(4096)
+        return dict(dim=3, cov=cov, z1=z1, z2=z2, pos=pos, axes=None, incompr=False,
+                    desc="unstructured 3-D, 16777216 points x 4096 modes, exponential l=5")
+    if name == "c4":
+        cov = rng.normal(0, np.sqrt(2) / 8, (3, 2048))
+        z1, z2 = rng.standard_normal(2048), rng.standard_normal(2048)
+        ax = np.arange(192, dtype=np.float64)
+        return dict(dim=3, cov=cov, z1=z1, z2=z2, pos=None, axes=(ax, ax, ax), incompr=True,
+                    desc="incompressible 3-D, 192^3 grid x 2048 modes, Gaussian l=8")
+    raise SystemExit(f"unknown workload {name}")
+
+
+def flat_grid(axes):
+    return np.ascontiguousarray(
+        np.array(np.meshgrid(*axes, indexing="ij")).reshape(len(axes), -1))
+
+
+def n_points(w):
+    if w["pos"] is not None:
+        return w["pos"].shape[1]
+    return int(np.prod([len(a) for a in w["axes"]]))
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]) if f[3] not in ("[N/A]", "N/A") else 0.0, f[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [r[0] for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[3]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# reference arm / CPU baseline: the oracle on the host cores
+# ---------------------------------------------------------------------------
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_sample(w, target_s=2.0, max_points=None):
+    """A bounded, seeded subset of the workload's points with all modes."""
+    import oracle
+    P = n_points(w)
+    rng = np.random.default_rng(1234)
+    cores = host_cores()
+    # size the sample: calibrate on a small batch
+    probe = min(P, 4 * cores)
+    idx = np.sort(rng.choice(P, size=probe, replace=False))
+    pos = sample_points(w, idx)
+    fn = oracle.summator_incompr if w["incompr"] else oracle.summator
+    t0 = time.perf_counter()
+    fn(w["cov"], w["z1"], w["z2"], pos, num_threads=cores)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    m = int(min(P, max(probe, probe * target_s / dt)))
+    if max_points:
+        m = min(m, max_points)
+    idx = np.sort(rng.choice(P, size=m, replace=False))
+    return sample_points(w, idx), fn, cores
+
+
+def sample_points(w, idx):
+    if w["pos"] is not None:
+        return np.ascontiguousarray(w["pos"][:, idx])
+    shape = [len(a) for a in w["axes"]]
+    sub = np.unravel_index(idx, shape)
+    return np.ascontiguousarray(np.array([w["axes"][d][sub[d]] for d in range(len(shape))]))
+
+
+def time_cpu(w, steps, target_s):
+    pos, fn, cores = cpu_sample(w, target_s)
+    n = w["cov"].shape[1]
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        fn(w["cov"], w["z1"], w["z2"], pos, num_threads=cores)
+        times.append(time.perf_counter() - t0)
+    work = pos.shape[1] * n
+    return work / np.mean(times) / 1e9, cores, pos.shape[1], np.mean(times)
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (weak scaling: every rank runs the full workload)
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import torch
+    import gstools_core as gsc
+    import oracle
+
+    torch.cuda.set_device(local)
+    w = workload(args.workload)
+    P, N = n_points(w), w["cov"].shape[1]
+    work = float(P) * N
+    form = args.form
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    pos_h = w["pos"] if w["pos"] is not None else flat_grid(w["axes"])
+    cov_d = torch.from_numpy(np.ascontiguousarray(w["cov"])).to(dev)
+    z1_d = torch.from_numpy(w["z1"]).to(dev)
+    z2_d = torch.from_numpy(w["z2"]).to(dev)
+    pos_d = torch.from_numpy(pos_h).to(dev)
+    nout = w["dim"] if w["incompr"] else 1
+    out_d = torch.empty((nout, P) if w["incompr"] else (P,), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    call = gsc.summate_incompr_device if w["incompr"] else gsc.summate_device
+
+    def step(timing=False):
+        call(cov_d, z1_d, z2_d, pos_d, out_d, form=form, stream=stream.cuda_stream,
+             timing=timing)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region ------------------------------------------------------
+    per_step, kern = [], {}
+    launches = 0
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1)                       # evict L2 (129 MB) between steps
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(timing=True)
+            b.record(stream)
+            b.synchronize()
+            per_step.append(a.elapsed_time(b))
+            tl = gsc.last_timings()
+            launches += len(tl)
+            for name, ms in tl:
+                kern.setdefault(name, []).append(ms)
+        torch.cuda.synchronize()
+        barrier(world)
+        t_wall = time.perf_counter() - t_wall
+    ms_step = max_over_ranks(world, float(np.mean(per_step)))
+    value = work * world / (ms_step * 1e-3) / 1e9
+
+    # ---- dominant kernel roofline ------------------------------------------
+    dom = max(kern, key=lambda k: sum(kern[k]))
+    per_launch = kern[dom]
+    launches_per_step = len(per_launch) / args.steps
+    dom_ms = float(np.mean(per_launch))
+    roof = roofline(args, w, dom, dom_ms, launches_per_step)
+
+    # ---- parity spot check of this very output against the oracle ----------
+    err = None
+    if not args.no_check:
+        rng = np.random.default_rng(7)
+        idx = np.sort(rng.choice(P, size=min(P, 2048), replace=False))
+        pos_s = sample_points(w, idx) if w["pos"] is None else np.ascontiguousarray(w["pos"][:, idx])
+        fn = oracle.summator_incompr if w["incompr"] else oracle.summator
+        ref = fn(w["cov"], w["z1"], w["z2"], pos_s, num_threads=host_cores())
+        got = out_d.cpu().numpy()
+        got = got[:, idx] if w["incompr"] else got[idx]
+        rms = float(np.sqrt(np.mean(ref ** 2)))
+        err = {"max_abs_over_rms": float(np.max(np.abs(got - ref)) / rms),
+               "rms_over_rms": float(np.sqrt(np.mean((got - ref) ** 2)) / rms),
+               "points_checked": int(len(idx))}
+
+    # ---- e2e through the public host API -----------------------------------
+    e2e = None
+    if not args.no_e2e:
+        host_call = gsc.summate_incompr if w["incompr"] else gsc.summate
+        host_call(w["cov"], w["z1"], w["z2"], pos_h, form=form)   # warm the staging
+        ts = []
+        for _ in range(max(1, min(args.steps, 3))):
+            barrier(world)
+            t0 = time.perf_counter()
+            host_call(w["cov"], w["z1"], w["z2"], pos_h, form=form)
+            ts.append(time.perf_counter() - t0)
+        t_e2e = max_over_ranks(world, float(np.mean(ts)))
+        h2d = (w["cov"].size + 2 * N + pos_h.size) * 8
+        e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nout * P * 8),
+               "ms_per_step": t_e2e * 1e3, "api": "gstools_core." + host_call.__name__}
+
+    # ---- CPU baseline (rank 0, N=1 only) -----------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, m, t = time_cpu(w, 1, args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{m} seeded points of the workload x all {N} modes, "
+                         f"{t:.1f} s on {cores} threads (oracle/field_oracle.c, "
+                         f"a restatement of src/field.rs; the Rust crate cannot be built here)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded numpy default_rng)",
+        "config": {"workload": args.workload, "desc": w["desc"], "points": P, "modes": N,
+                   "form": form, "path": "flattened meshgrid" if w["pos"] is None else "points",
+                   "l2": "flushed by a 256 MiB write before every timed step",
+                   "wall_s": t_wall},
+        "error_vs_oracle": err,
+        "kernels_ms_per_step": {k: float(np.sum(v) / args.steps) for k, v in kern.items()},
+        "gpu_launches": int(launches),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+def roofline(args, w, dom, dom_ms, launches_per_step):
+    """Roofline entry for the dominant kernel.  The plain summators are bound by
+    the FP64 pipe: algorithmic FLOPs per point*mode = 2d+3 (+1 sincos) for the
+    scalar field and 4d+2 for the incompressible one."""
+    import torch
+    P, N, d = n_points(w), w["cov"].shape[1], w["dim"]
+    flops_pm = (4 * d + 2) if w["incompr"] else (2 * d + 3)
+    per_launch_units = P * N / max(launches_per_step, 1)
+    achieved = flops_pm * per_launch_units / (dom_ms * 1e-3) / 1e12
+    peak, how = fp64_peak(torch)
+    return {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+            "peak_source": how,
+            "note": f"{flops_pm} algorithmic FLOPs per point*mode plus one sincos; the "
+                    f"sincos cost is not counted"}
+
+
+_FP64_PEAK = None
+
+
+def fp64_peak(torch):
+    """FP64 peak as delivered by cuBLAS DGEMM on this GPU (measured here, best
+    of 5, 8192^3), since MEASURED_PEAKS.json carries no FP64 figure."""
+    global _FP64_PEAK
+    if _FP64_PEAK is None:
+        n = 8192
+        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        _FP64_PEAK = 2 * n ** 3 / (best * 1e-3) / 1e12
+        del a, b
+    return _FP64_PEAK, "measured: cuBLAS DGEMM 8192^3, best of 5"
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, world, rank):
+    """The reference's CPU algorithm (oracle restatement) on the host cores."""
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    N = w["cov"].shape[1]
+    v, cores, m, t = time_cpu(w, max(1, args.steps), args.cpu_seconds)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy default_rng)",
+        "config": {"workload": args.workload, "desc": w["desc"], "points": n_points(w),
+                   "modes": N, "form": "reference CPU (rayon-equivalent restatement)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{m} seeded points x all {N} modes per step"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the Rust crate cannot be compiled here (no cargo/rustc); the arm times "
+                "oracle/field_oracle.c, a bit-exact restatement of src/field.rs, on all host "
+                "threads",
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--form", default="auto")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

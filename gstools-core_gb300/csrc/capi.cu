@@ -1,0 +1,439 @@
+// capi.cu -- the extern "C" entry points declared in
+// include/gstools_core_gb300.h: argument validation, per-device contexts,
+// host staging for host-pointer calls, CUDA-event timing, error strings.
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace gsc {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string t_error;
+
+int set_error(int code, const std::string &msg) {
+    t_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? GSC_ERR_NOMEM
+                     : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+                         ? GSC_ERR_NO_DEVICE
+                         : GSC_ERR_CUDA;
+    cudaGetLastError();   // clear a non-sticky error so the next call is clean
+    return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+const char *kernel_name(int32_t id) {
+    static const char *names[K_COUNT] = {
+        "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
+        "split_reduce", "generic_f64",
+    };
+    return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
+}
+
+// ---------------------------------------------------------------------------
+// timing: CUDA events recorded on the launch stream around each kernel
+// ---------------------------------------------------------------------------
+struct TimingRec {
+    int32_t id;
+    cudaEvent_t a, b;
+};
+static thread_local bool t_timing = false;
+static thread_local std::vector<TimingRec> t_recs;
+static thread_local std::vector<cudaEvent_t> t_event_pool;
+
+static cudaEvent_t pooled_event() {
+    if (!t_event_pool.empty()) {
+        cudaEvent_t e = t_event_pool.back();
+        t_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+void timing_reset(bool enabled) {
+    for (auto &r : t_recs) {
+        t_event_pool.push_back(r.a);
+        t_event_pool.push_back(r.b);
+    }
+    t_recs.clear();
+    t_timing = enabled;
+}
+bool timing_enabled() { return t_timing; }
+
+TimedLaunch::TimedLaunch(cudaStream_t s) : st(s) {}
+
+void TimedLaunch::begin(int32_t kid) {
+    on = t_timing;
+    id = kid;
+    if (!on) return;
+    TimingRec r{kid, pooled_event(), pooled_event()};
+    if (!r.a || !r.b) {
+        on = false;
+        return;
+    }
+    cudaEventRecord(r.a, st);
+    t_recs.push_back(r);
+}
+
+void TimedLaunch::end() {
+    if (!on) return;
+    cudaEventRecord(t_recs.back().b, st);
+}
+
+// ---------------------------------------------------------------------------
+// device contexts
+// ---------------------------------------------------------------------------
+static std::mutex g_ctx_mu;
+static DeviceCtx *g_ctx[64] = {nullptr};
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    int set(int dev) {
+        GSC_CUDA(cudaGetDevice(&prev));
+        if (prev != dev) {
+            GSC_CUDA(cudaSetDevice(dev));
+            changed = true;
+        }
+        return GSC_OK;
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+int get_ctx(int device, DeviceCtx **out) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return set_error(GSC_ERR_NO_DEVICE,
+                         std::string("no usable CUDA device (") +
+                             (e == cudaSuccess ? "count is 0" : cudaGetErrorString(e)) +
+                             "); this library has no CPU path");
+    }
+    if (device < 0) GSC_CUDA(cudaGetDevice(&device));
+    if (device >= count || device >= 64)
+        return set_error(GSC_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    if (!g_ctx[device]) {
+        DeviceGuard g;
+        GSC_TRY(g.set(device));
+        auto *c = new DeviceCtx();
+        c->device = device;
+        GSC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        GSC_CUDA(cudaEventCreateWithFlags(&c->scratch_ready, cudaEventDisableTiming));
+        GSC_CUDA(cudaEventRecord(c->scratch_ready, c->stream));
+        g_ctx[device] = c;
+    }
+    *out = g_ctx[device];
+    return GSC_OK;
+}
+
+static size_t grow_size(size_t bytes) {
+    const size_t two_mb = size_t(2) << 20;
+    size_t want = bytes + bytes / 4;
+    return (want + two_mb - 1) / two_mb * two_mb;
+}
+
+int ensure_dev(DeviceCtx &ctx, DevBuf &buf, size_t bytes) {
+    if (buf.bytes >= bytes && buf.ptr) return GSC_OK;
+    if (buf.ptr) {
+        // the old buffer may still be read by queued work on any stream
+        GSC_CUDA(cudaEventSynchronize(ctx.scratch_ready));
+        GSC_CUDA(cudaStreamSynchronize(ctx.stream));
+        GSC_CUDA(cudaFree(buf.ptr));
+        buf.ptr = nullptr;
+        buf.bytes = 0;
+    }
+    const size_t n = grow_size(bytes);
+    void *p = nullptr;
+    GSC_CUDA(cudaMalloc(&p, n));
+    buf.ptr = p;
+    buf.bytes = n;
+    return GSC_OK;
+}
+
+int ensure_pinned(DeviceCtx &ctx, size_t bytes) {
+    if (ctx.pinned_bytes >= bytes && ctx.pinned) return GSC_OK;
+    if (ctx.pinned) {
+        GSC_CUDA(cudaStreamSynchronize(ctx.stream));
+        GSC_CUDA(cudaFreeHost(ctx.pinned));
+        ctx.pinned = nullptr;
+        ctx.pinned_bytes = 0;
+    }
+    const size_t n = grow_size(bytes);
+    void *p = nullptr;
+    GSC_CUDA(cudaHostAlloc(&p, n, cudaHostAllocDefault));
+    ctx.pinned = p;
+    ctx.pinned_bytes = n;
+    return GSC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// options and validation
+// ---------------------------------------------------------------------------
+struct Resolved {
+    int form = GSC_FORM_AUTO;
+    int device = -1;
+    int flags = 0;
+    cudaStream_t stream = nullptr;
+    double tolerance = 1e-12;
+};
+
+static int resolve_opts(const gsc_opts *o, Resolved *r) {
+    if (!o) return GSC_OK;
+    if (o->struct_size < static_cast<int32_t>(sizeof(gsc_opts)))
+        return set_error(GSC_ERR_INVALID, "gsc_opts.struct_size is smaller than sizeof(gsc_opts)");
+    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_PLAIN_F64_LIBM)
+        return set_error(GSC_ERR_INVALID, "unknown form");
+    r->form = o->form;
+    r->device = o->device;
+    r->flags = o->flags;
+    r->stream = static_cast<cudaStream_t>(o->stream);
+    if (o->tolerance > 0) r->tolerance = o->tolerance;
+    return GSC_OK;
+}
+
+static int check_sizes(int64_t dim, int64_t n_modes, int64_t n_points) {
+    if (dim < 0 || n_modes < 0 || n_points < 0)
+        return set_error(GSC_ERR_INVALID, "negative dimension, mode count or point count");
+    if (dim > 65536) return set_error(GSC_ERR_INVALID, "dimension too large");
+    return GSC_OK;
+}
+
+static int need_ptr(const void *p, bool needed, const char *name) {
+    if (needed && !p) return set_error(GSC_ERR_INVALID, std::string(name) + " is NULL");
+    return GSC_OK;
+}
+
+static int check_device_ptr(const void *p, const char *name) {
+    if (!p) return GSC_OK;
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(GSC_ERR_INVALID, std::string(name) + " is not a CUDA pointer");
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged &&
+        at.type != cudaMemoryTypeHost)
+        return set_error(GSC_ERR_INVALID,
+                         std::string(name) + " is not device-accessible memory");
+    return GSC_OK;
+}
+
+static int plain_variant(const Resolved &r) { return r.form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0; }
+
+// gathers a strided (rows, cols) host view into dense row-major dst
+static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int64_t cols,
+                    double *dst) {
+    for (int64_t i = 0; i < rows; ++i) {
+        const double *row = src + i * s0;
+        double *o = dst + i * cols;
+        if (s1 == 1) {
+            memcpy(o, row, sizeof(double) * static_cast<size_t>(cols));
+        } else {
+            for (int64_t j = 0; j < cols; ++j) o[j] = row[j * s1];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host-pointer path shared by the scalar and incompressible summators
+// ---------------------------------------------------------------------------
+static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
+                      int64_t z1s, const double *z2, int64_t z2s, const double *pos,
+                      int64_t ps_d, int64_t ps_p, int64_t dim, int64_t N, int64_t P,
+                      double *out, int64_t os_d, int64_t os_p, bool incompr,
+                      const gsc_opts *opts) {
+    Resolved ro;
+    GSC_TRY(resolve_opts(opts, &ro));
+    GSC_TRY(check_sizes(dim, N, P));
+    if (incompr && dim != 2 && dim != 3)
+        return set_error(GSC_ERR_DIM, "Only two- and three-dimensional problems are supported.");
+    GSC_TRY(need_ptr(cov, dim * N > 0, "cov_samples"));
+    GSC_TRY(need_ptr(z1, N > 0, "z1"));
+    GSC_TRY(need_ptr(z2, N > 0, "z2"));
+    GSC_TRY(need_ptr(pos, dim * P > 0, "pos"));
+    GSC_TRY(need_ptr(out, P > 0, "out"));
+    timing_reset(ro.flags & GSC_FLAG_TIMING);
+    if (P == 0) return GSC_OK;
+
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(ro.device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    cudaStream_t st = ctx->stream;
+
+    const int64_t nout = incompr ? dim : 1;
+    const size_t n_cov = static_cast<size_t>(dim * N), n_pos = static_cast<size_t>(dim * P);
+    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_pos;
+    const size_t n_out = static_cast<size_t>(nout * P);
+    const size_t bytes = (n_in + n_out) * sizeof(double);
+    GSC_TRY(ensure_pinned(*ctx, bytes));
+    GSC_TRY(ensure_dev(*ctx, ctx->io, bytes));
+
+    double *h = static_cast<double *>(ctx->pinned);
+    gather2(cov, cs_d, cs_n, dim, N, h);
+    gather2(z1, 0, z1s, 1, N, h + n_cov);
+    gather2(z2, 0, z2s, 1, N, h + n_cov + N);
+    gather2(pos, ps_d, ps_p, dim, P, h + n_cov + 2 * N);
+
+    double *d = static_cast<double *>(ctx->io.ptr);
+    GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    PlainArgs a;
+    a.cov = d;
+    a.z1 = d + n_cov;
+    a.z2 = d + n_cov + N;
+    a.pos = d + n_cov + 2 * N;
+    a.dim = dim;
+    a.n_modes = N;
+    a.n_points = P;
+    a.incompr = incompr;
+    a.out = d + n_in;
+    a.out_sd = P;
+    a.out_sp = 1;
+    a.variant = plain_variant(ro);
+    GSC_TRY(plain_run(*ctx, a, st));
+    double *ho = h + n_in;
+    GSC_CUDA(cudaMemcpyAsync(ho, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GSC_CUDA(cudaStreamSynchronize(st));
+    for (int64_t i = 0; i < nout; ++i) {
+        if (os_p == 1 && (nout == 1 || os_d == P)) {
+            memcpy(out + i * os_d, ho + i * P, sizeof(double) * static_cast<size_t>(P));
+        } else {
+            for (int64_t p = 0; p < P; ++p) out[i * os_d + p * os_p] = ho[i * P + p];
+        }
+    }
+    return GSC_OK;
+}
+
+static int dev_plain(const double *cov, const double *z1, const double *z2, const double *pos,
+                     int64_t dim, int64_t N, int64_t P, double *out, bool incompr,
+                     const gsc_opts *opts) {
+    Resolved ro;
+    GSC_TRY(resolve_opts(opts, &ro));
+    GSC_TRY(check_sizes(dim, N, P));
+    if (incompr && dim != 2 && dim != 3)
+        return set_error(GSC_ERR_DIM, "Only two- and three-dimensional problems are supported.");
+    GSC_TRY(need_ptr(cov, dim * N > 0, "cov_samples"));
+    GSC_TRY(need_ptr(z1, N > 0, "z1"));
+    GSC_TRY(need_ptr(z2, N > 0, "z2"));
+    GSC_TRY(need_ptr(pos, dim * P > 0, "pos"));
+    GSC_TRY(need_ptr(out, P > 0, "out"));
+    timing_reset(ro.flags & GSC_FLAG_TIMING);
+    if (P == 0) return GSC_OK;
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(ro.device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    GSC_TRY(check_device_ptr(cov, "cov_samples"));
+    GSC_TRY(check_device_ptr(z1, "z1"));
+    GSC_TRY(check_device_ptr(z2, "z2"));
+    GSC_TRY(check_device_ptr(pos, "pos"));
+    GSC_TRY(check_device_ptr(out, "out"));
+    PlainArgs a;
+    a.cov = cov;
+    a.z1 = z1;
+    a.z2 = z2;
+    a.pos = pos;
+    a.dim = dim;
+    a.n_modes = N;
+    a.n_points = P;
+    a.incompr = incompr;
+    a.out = out;
+    a.out_sd = P;
+    a.out_sp = 1;
+    a.variant = plain_variant(ro);
+    return plain_run(*ctx, a, ro.stream);
+}
+
+}  // namespace gsc
+
+using namespace gsc;
+
+extern "C" {
+
+const char *gsc_version(void) { return "1.1.0+gb300"; }
+
+const char *gsc_last_error(void) { return t_error.c_str(); }
+
+int gsc_device_count(int32_t *count) {
+    if (!count) return set_error(GSC_ERR_INVALID, "count is NULL");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return GSC_OK;
+}
+
+int gsc_last_timings(int32_t *ids, double *ms, int32_t cap) {
+    int32_t n = 0;
+    for (auto &r : t_recs) {
+        if (n >= cap) break;
+        float f = 0.f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&f, r.a, r.b) != cudaSuccess) {
+            cudaGetLastError();
+            f = -1.f;
+        }
+        if (ids) ids[n] = r.id;
+        if (ms) ms[n] = f;
+        ++n;
+    }
+    return n;
+}
+
+const char *gsc_kernel_name(int32_t id) { return kernel_name(id); }
+
+int gsc_summate_f64(const double *cov, int64_t cov_stride_d, int64_t cov_stride_n,
+                    const double *z1, int64_t z1_stride, const double *z2, int64_t z2_stride,
+                    const double *pos, int64_t pos_stride_d, int64_t pos_stride_p, int64_t dim,
+                    int64_t n_modes, int64_t n_points, double *out, int64_t out_stride,
+                    const gsc_opts *opts) {
+    return host_plain(cov, cov_stride_d, cov_stride_n, z1, z1_stride, z2, z2_stride, pos,
+                      pos_stride_d, pos_stride_p, dim, n_modes, n_points, out, 0, out_stride,
+                      false, opts);
+}
+
+int gsc_summate_dev(const double *cov, const double *z1, const double *z2, const double *pos,
+                    int64_t dim, int64_t n_modes, int64_t n_points, double *out,
+                    const gsc_opts *opts) {
+    return dev_plain(cov, z1, z2, pos, dim, n_modes, n_points, out, false, opts);
+}
+
+int gsc_summate_incompr_f64(const double *cov, int64_t cov_stride_d, int64_t cov_stride_n,
+                            const double *z1, int64_t z1_stride, const double *z2,
+                            int64_t z2_stride, const double *pos, int64_t pos_stride_d,
+                            int64_t pos_stride_p, int64_t dim, int64_t n_modes,
+                            int64_t n_points, double *out, int64_t out_stride_d,
+                            int64_t out_stride_p, const gsc_opts *opts) {
+    return host_plain(cov, cov_stride_d, cov_stride_n, z1, z1_stride, z2, z2_stride, pos,
+                      pos_stride_d, pos_stride_p, dim, n_modes, n_points, out, out_stride_d,
+                      out_stride_p, true, opts);
+}
+
+int gsc_summate_incompr_dev(const double *cov, const double *z1, const double *z2,
+                            const double *pos, int64_t dim, int64_t n_modes, int64_t n_points,
+                            double *out, const gsc_opts *opts) {
+    return dev_plain(cov, z1, z2, pos, dim, n_modes, n_points, out, true, opts);
+}
+
+}  // extern "C"

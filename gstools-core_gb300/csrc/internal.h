@@ -1,0 +1,95 @@
+// internal.h -- declarations shared by the translation units of the GB300
+// summator library.  Not installed; the public surface is
+// include/gstools_core_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "gstools_core_gb300.h"
+
+namespace gsc {
+
+// ---- status helpers -------------------------------------------------------
+int set_error(int code, const std::string &msg);   // records msg, returns code
+int cuda_fail(cudaError_t e, const char *what);     // GSC_ERR_CUDA / NOMEM
+
+#define GSC_CUDA(call)                                         \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return ::gsc::cuda_fail(e_, #call); \
+    } while (0)
+
+#define GSC_TRY(expr)                  \
+    do {                               \
+        int rc_ = (expr);              \
+        if (rc_ != GSC_OK) return rc_; \
+    } while (0)
+
+// ---- kernel ids (gsc_kernel_name / gsc_last_timings) ----------------------
+enum KernelId : int32_t {
+    K_MODE_TABLE = 0,      // per-mode angle tables and projector weights
+    K_PLAIN_SCALAR = 1,    // FP64 scalar summator, table-driven sincos
+    K_PLAIN_INCOMPR = 2,   // FP64 incompressible summator, table-driven sincos
+    K_PLAIN_LIBM = 3,      // FP64 summators on CUDA's sincos()
+    K_SPLIT_REDUCE = 4,    // ordered sum of mode-split partials
+    K_GENERIC = 5,         // any dimension, one thread per point
+    K_COUNT
+};
+const char *kernel_name(int32_t id);
+
+// ---- per-device context ---------------------------------------------------
+// A grow-only device buffer.  `ready` orders reuse across streams: every
+// launch that touches the buffer waits on it first and records it after.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct DeviceCtx {
+    int device = -1;
+    cudaStream_t stream = nullptr;   // stream of host-pointer calls
+    cudaEvent_t scratch_ready = nullptr;
+    std::mutex mu;                   // serialises users of the buffers below
+    DevBuf io;                       // inputs+outputs of host-pointer calls
+    DevBuf scratch;                  // tables and partial sums
+    void *pinned = nullptr;          // pinned host staging
+    size_t pinned_bytes = 0;
+};
+
+// Returns the context of `device` (-1 = current), initialising it once.
+int get_ctx(int device, DeviceCtx **out);
+// Makes `buf` hold at least `bytes`; waits for in-flight users before growing.
+int ensure_dev(DeviceCtx &ctx, DevBuf &buf, size_t bytes);
+int ensure_pinned(DeviceCtx &ctx, size_t bytes);
+
+// ---- timing ---------------------------------------------------------------
+struct TimedLaunch {
+    explicit TimedLaunch(cudaStream_t s);
+    bool on = false;
+    cudaStream_t st = nullptr;
+    int32_t id = 0;
+    void begin(int32_t kid);   // records a start event when timing is on
+    void end();                // records the stop event
+};
+void timing_reset(bool enabled);
+bool timing_enabled();
+
+// ---- plain FP64 summators (plain.cu) --------------------------------------
+struct PlainArgs {
+    const double *cov;   // (dim, n_modes) row-major, device
+    const double *z1;    // (n_modes), device
+    const double *z2;
+    const double *pos;   // (dim, n_points) row-major, device
+    int64_t dim, n_modes, n_points;
+    bool incompr;        // vector field (dim outputs) instead of scalar
+    double *out;         // device
+    int64_t out_sd, out_sp;  // element strides of out[i, p] (scalar: 0, 1)
+    int variant;         // 0 table-driven sincos, 1 CUDA sincos()
+};
+int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st);
+
+}  // namespace gsc

@@ -1,0 +1,434 @@
+// plain.cu -- FP64 randomization-method summators for GB300 (sm_103a).
+//
+// Computes, in FP64 end to end,
+//   scalar   u[p]    = sum_j z1_j cos(k_j.x_p) + z2_j sin(k_j.x_p)
+//            (reference: src/field.rs:37-65)
+//   incompr  u[i, p] = sum_j w_ij (z1_j cos(k_j.x_p) + z2_j sin(k_j.x_p)),
+//            w_0j = 1 - k_0j k_0j/|k_j|^2, w_ij = -k_ij k_0j/|k_j|^2
+//            (reference: src/field.rs:97-182)
+//
+// Design.  GB300's FP64 pipe is narrow, so the kernel is built to spend as
+// few FP64 instructions per point*mode as possible while staying FP64
+// accurate:
+//  * phase k.x is formed exactly as the reference forms it:
+//    ((k0*x0 + k1*x1) + k2*x2), no FMA, so every phase has the reference's
+//    bits (src/field.rs:57, src/short_vec.rs:30-33);
+//  * sincos is table driven (Tang-style): phase = n*(2pi/M) + r with a
+//    two-constant Cody-Waite reduction (exact first step under FMA) and
+//    |r| <= pi/M, M = 256; e^{ir} by short Taylor polynomials (truncation
+//    below 5e-15), and the angle n*(2pi/M) folded into a per-mode table
+//    W_j[a] = (z1_j - i z2_j) e^{i 2 pi a/M}, so
+//    z1 cos(phase) + z2 sin(phase) = Re(W_j[n mod M] e^{ir})
+//    = Re W cos r - Im W sin r: 18 FP64 operations per point*mode for d=3;
+//  * per-mode tables live in global memory and are staged tile by tile into
+//    shared memory with cp.async double buffering; each thread keeps R
+//    points in registers, so one staged tile serves T*R points;
+//  * phases beyond |k.x| ~ 1e13 (where the one-step reduction would lose
+//    accuracy) take CUDA's sincos() for the whole tile (warp-uniform test);
+//  * when there are too few points to fill 152 SMs, the modes are split
+//    across blockIdx.y and the partial sums are added in split order by a
+//    second kernel (deterministic; no atomics).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "internal.h"
+
+namespace gsc {
+namespace {
+
+constexpr int kM = 256;                             // table angles per turn
+constexpr double kInvStep = 40.74366543152521;      // M / (2 pi)
+constexpr double kStepHi = 0.02454369260617026;     // fl(2 pi / M) = fl(pi)/128
+constexpr double kStepLo = 9.567553118338697e-19;   // fl(2 pi / M - kStepHi)
+constexpr double kRound = 6755399441055744.0;       // 1.5 * 2^52: x + kRound rounds x
+constexpr double kSafePhase = 1.0e13;               // table path bound on |k.x|
+constexpr int kRec = 12;                            // doubles per mode record
+constexpr int kThreads = 128;                       // threads per block
+constexpr int kTileModes = 8;                       // modes per staged tile
+constexpr int64_t kChunkModes = 16384;              // modes per table build
+
+// Mode record layout (doubles): k0 k1 k2 | sum|k| | z1 z2 | w0 w1 w2 | pad
+enum { R_K0 = 0, R_KABS = 3, R_Z1 = 4, R_Z2 = 5, R_W0 = 6 };
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// ---------------------------------------------------------------------------
+// Per-mode tables: W_j[a] = (z1 - i z2) e^{i 2 pi a / M} and the mode record.
+// grid (nc), block (kM)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kM)
+mode_table_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+                  const double *__restrict__ z2, int64_t dim, int64_t n_modes, int64_t j0,
+                  int incompr, int want_table, double2 *__restrict__ wtab,
+                  double *__restrict__ rec) {
+    const int64_t jl = blockIdx.x;
+    const int64_t j = j0 + jl;
+    const int a = threadIdx.x;
+    const double z1j = z1[j], z2j = z2[j];
+    if (want_table) {
+        double s, c;
+        sincospi(a * (1.0 / (kM / 2)), &s, &c);       // angle 2 pi a / M
+        wtab[jl * kM + a] = make_double2(z1j * c + z2j * s, z1j * s - z2j * c);
+    }
+    if (a == 0) {
+        double k[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
+        double *r = rec + jl * kRec;
+        r[R_K0 + 0] = k[0];
+        r[R_K0 + 1] = k[1];
+        r[R_K0 + 2] = k[2];
+        r[R_KABS] = fabs(k[0]) + fabs(k[1]) + fabs(k[2]);
+        r[R_Z1] = z1j;
+        r[R_Z2] = z2j;
+        double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+        if (incompr) {
+            // src/field.rs:138: k_2 = k0 / k.k, ShortVec::dot order, no FMA
+            double kk = 0.0;
+            for (int d = 0; d < dim; ++d) kk = __dadd_rn(kk, __dmul_rn(k[d], k[d]));
+            const double k_2 = __ddiv_rn(k[0], kk);
+            w0 = __dadd_rn(1.0, -__dmul_rn(k[0], k_2));          // :148
+            w1 = -__dmul_rn(k[1], k_2);                            // :150-152
+            w2 = -__dmul_rn(k[2], k_2);
+        }
+        r[R_W0 + 0] = w0;
+        r[R_W0 + 1] = w1;
+        r[R_W0 + 2] = w2;
+        r[9] = r[10] = r[11] = 0.0;
+    }
+}
+
+// phase = k.x in the reference's order (ndarray dot on strided columns)
+template <int D>
+__device__ __forceinline__ double phase_of(const double *k, const double *x) {
+    double ph = __dmul_rn(k[0], x[0]);
+    if (D > 1) ph = __dadd_rn(ph, __dmul_rn(k[1], x[1]));
+    if (D > 2) ph = __dadd_rn(ph, __dmul_rn(k[2], x[2]));
+    return ph;
+}
+
+// z1 cos(ph) + z2 sin(ph) through the mode's angle table (see file header).
+__device__ __forceinline__ double table_term(double ph, const double2 *__restrict__ tab) {
+    const double s = fma(ph, kInvStep, kRound);
+    const double n = s - kRound;
+    const int a = __double2loint(s) & (kM - 1);
+    double r = fma(-n, kStepHi, ph);          // exact
+    r = fma(-n, kStepLo, r);
+    const double r2 = r * r;
+    const double cr = fma(r2, fma(r2, 1.0 / 24.0, -0.5), 1.0);
+    const double sr = fma(r * r2, fma(r2, 1.0 / 120.0, -1.0 / 6.0), r);
+    const double2 w = tab[a];
+    return fma(w.x, cr, -(w.y * sr));
+}
+
+// ---------------------------------------------------------------------------
+// Main kernel.  grid (ceil(P / (T*R)), splits), block T.
+// Split s handles modes [s*mps, min(nc, (s+1)*mps)) of the current chunk and
+// writes (accumulate=0) or adds (accumulate=1) its sums at
+// dst + s*split_stride + i*sd + p*sp.
+// ---------------------------------------------------------------------------
+template <int D, int R, bool INC, bool LIBM>
+__global__ void __launch_bounds__(kThreads)
+plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restrict__ wtab,
+             const double *__restrict__ rec, int64_t nc, int64_t mps, int accumulate,
+             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    constexpr int NOUT = INC ? D : 1;
+    constexpr int TAB_BYTES = LIBM ? 0 : kTileModes * kM * 16;
+    constexpr int REC_BYTES = kTileModes * kRec * 8;
+    constexpr int STAGE = TAB_BYTES + REC_BYTES;
+    extern __shared__ __align__(16) unsigned char smem[];
+
+    const int tid = threadIdx.x;
+    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * (kThreads * R) + tid;
+    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
+    const int64_t je = min(nc, jb + mps);
+
+    double x[R][D];
+    double acc[R][NOUT];
+    double xabs = 0.0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int64_t p = p0 + r * kThreads;
+        double s = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            x[r][d] = p < P ? pos[d * P + p] : 0.0;
+            s += fabs(x[r][d]);
+        }
+        xabs = fmax(xabs, s);
+#pragma unroll
+        for (int i = 0; i < NOUT; ++i) acc[r][i] = 0.0;
+    }
+    // warp-uniform bound on |x| for the table-path range test
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) xabs = fmax(xabs, __shfl_xor_sync(0xffffffffu, xabs, o));
+
+    auto stage_tile = [&](int buf, int64_t t0) {
+        const int tm = static_cast<int>(min(static_cast<int64_t>(kTileModes), je - t0));
+        unsigned char *base = smem + buf * STAGE;
+        if (!LIBM) {
+            const int chunks = tm * kM;                      // 16-byte chunks
+            const double2 *src = wtab + (t0)*kM;
+            for (int c = tid; c < chunks; c += kThreads) cp_async16(base + c * 16, src + c);
+        }
+        const int rchunks = tm * kRec / 2;
+        const double *rsrc = rec + t0 * kRec;
+        for (int c = tid; c < rchunks; c += kThreads)
+            cp_async16(base + TAB_BYTES + c * 16, rsrc + 2 * c);
+        cp_async_commit();
+    };
+
+    if (jb < je) stage_tile(0, jb);
+    int buf = 0;
+    for (int64_t t0 = jb; t0 < je; t0 += kTileModes, buf ^= 1) {
+        const int tm = static_cast<int>(min(static_cast<int64_t>(kTileModes), je - t0));
+        if (t0 + kTileModes < je) {
+            stage_tile(buf ^ 1, t0 + kTileModes);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const unsigned char *base = smem + buf * STAGE;
+        const double2 *tab = reinterpret_cast<const double2 *>(base);
+        const double *rc = reinterpret_cast<const double *>(base + TAB_BYTES);
+        for (int m = 0; m < tm; ++m) {
+            const double *mr = rc + m * kRec;
+            double k[3] = {mr[R_K0], mr[R_K0 + 1], mr[R_K0 + 2]};
+            double w[3] = {mr[R_W0], mr[R_W0 + 1], mr[R_W0 + 2]};
+            const bool table_ok = !LIBM && (mr[R_KABS] * xabs < kSafePhase);
+            if (table_ok) {
+                const double2 *mt = tab + m * kM;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const double z12 = table_term(phase_of<D>(k, x[r]), mt);
+                    if (INC) {
+#pragma unroll
+                        for (int i = 0; i < NOUT; ++i) acc[r][i] = fma(w[i], z12, acc[r][i]);
+                    } else {
+                        acc[r][0] = __dadd_rn(acc[r][0], z12);
+                    }
+                }
+            } else {
+                const double z1 = mr[R_Z1], z2 = mr[R_Z2];
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    double sn, cs;
+                    sincos(phase_of<D>(k, x[r]), &sn, &cs);
+                    const double z12 = __dadd_rn(__dmul_rn(z1, cs), __dmul_rn(z2, sn));
+                    if (INC) {
+#pragma unroll
+                        for (int i = 0; i < NOUT; ++i) acc[r][i] = fma(w[i], z12, acc[r][i]);
+                    } else {
+                        acc[r][0] = __dadd_rn(acc[r][0], z12);
+                    }
+                }
+            }
+        }
+        __syncthreads();   // buffer `buf` is refilled two tiles later
+    }
+
+    double *d0 = dst + static_cast<int64_t>(blockIdx.y) * split_stride;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int64_t p = p0 + r * kThreads;
+        if (p >= P) continue;
+#pragma unroll
+        for (int i = 0; i < NOUT; ++i) {
+            double *o = d0 + i * sd + p * sp;
+            *o = accumulate ? *o + acc[r][i] : acc[r][i];
+        }
+    }
+}
+
+// out[i*sd + p*sp] = sum_s part[s][i][p], s ascending
+__global__ void split_reduce_kernel(const double *__restrict__ part, int64_t S, int64_t nout,
+                                    int64_t P, double *__restrict__ out, int64_t sd, int64_t sp) {
+    const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= nout * P) return;
+    const int64_t i = t / P, p = t - i * P;
+    double s = 0.0;
+    for (int64_t k = 0; k < S; ++k) s += part[k * nout * P + t];
+    out[i * sd + p * sp] = s;
+}
+
+// Any dimension (0 or > 3), scalar field: one thread per point, CUDA sincos.
+__global__ void generic_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+                               const double *__restrict__ z2, const double *__restrict__ pos,
+                               int64_t dim, int64_t N, int64_t P, double *__restrict__ out,
+                               int64_t sp) {
+    const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    double sum = 0.0;
+    for (int64_t j = 0; j < N; ++j) {
+        double ph = 0.0;
+        for (int64_t d = 0; d < dim; ++d) ph = __dadd_rn(ph, __dmul_rn(cov[d * N + j], pos[d * P + p]));
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        sum = __dadd_rn(sum, __dadd_rn(__dmul_rn(z1[j], cs), __dmul_rn(z2[j], sn)));
+    }
+    out[p * sp] = sum;
+}
+
+template <int D, int R, bool INC, bool LIBM>
+int launch_main(dim3 grid, size_t smem, cudaStream_t st, const double *pos, int64_t P,
+                const double2 *wtab, const double *rec, int64_t nc, int64_t mps, int accumulate,
+                double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    auto fn = plain_kernel<D, R, INC, LIBM>;
+    static bool configured = false;   // per instantiation
+    if (!configured) {
+        GSC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+        configured = true;
+    }
+    fn<<<grid, kThreads, smem, st>>>(pos, P, wtab, rec, nc, mps, accumulate, dst, sd, sp,
+                                     split_stride);
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+template <int R, bool INC, bool LIBM>
+int dispatch_dim(int64_t dim, dim3 grid, size_t smem, cudaStream_t st, const double *pos,
+                 int64_t P, const double2 *wtab, const double *rec, int64_t nc, int64_t mps,
+                 int accumulate, double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    switch (dim) {
+        case 1:
+            if (!INC)
+                return launch_main<1, R, INC, LIBM>(grid, smem, st, pos, P, wtab, rec, nc, mps,
+                                                    accumulate, dst, sd, sp, split_stride);
+            break;
+        case 2:
+            return launch_main<2, R, INC, LIBM>(grid, smem, st, pos, P, wtab, rec, nc, mps,
+                                                accumulate, dst, sd, sp, split_stride);
+        case 3:
+            return launch_main<3, R, INC, LIBM>(grid, smem, st, pos, P, wtab, rec, nc, mps,
+                                                accumulate, dst, sd, sp, split_stride);
+    }
+    return set_error(GSC_ERR_DIM, "unsupported dimension for the plain kernel");
+}
+
+int sm_count(int device) {
+    static int cached[64] = {0};
+    if (device >= 0 && device < 64 && cached[device]) return cached[device];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0)
+        n = 152;
+    if (device >= 0 && device < 64) cached[device] = n;
+    return n;
+}
+
+}  // namespace
+
+int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
+    constexpr int R = 4;
+    const int64_t P = a.n_points, N = a.n_modes, dim = a.dim;
+    if (P == 0) return GSC_OK;
+    const int64_t nout = a.incompr ? dim : 1;
+    const bool libm = a.variant == 1;
+
+    if (!a.incompr && (dim == 0 || dim > 3)) {
+        TimedLaunch tl(st);
+        tl.begin(K_GENERIC);
+        const int tpb = 128;
+        generic_kernel<<<static_cast<unsigned>((P + tpb - 1) / tpb), tpb, 0, st>>>(
+            a.cov, a.z1, a.z2, a.pos, dim, N, P, a.out, a.out_sp);
+        tl.end();
+        GSC_CUDA(cudaGetLastError());
+        return GSC_OK;
+    }
+    if (a.incompr && dim != 2 && dim != 3)
+        return set_error(GSC_ERR_DIM, "Only two- and three-dimensional problems are supported.");
+
+    // ---- launch geometry ---------------------------------------------------
+    const int64_t pts_per_block = static_cast<int64_t>(kThreads) * R;
+    const int64_t bx = (P + pts_per_block - 1) / pts_per_block;
+    if (bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
+    const int64_t chunk = std::min<int64_t>(N, kChunkModes);
+    const int64_t want_blocks = static_cast<int64_t>(sm_count(ctx.device)) * 6;
+    int64_t S = std::max<int64_t>(1, (want_blocks + bx - 1) / bx);
+    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kTileModes)));
+    S = std::min<int64_t>(S, 64);
+    int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
+    mps = (mps + kTileModes - 1) / kTileModes * kTileModes;
+    if (mps > 0) S = std::max<int64_t>(1, (chunk + mps - 1) / mps);
+    if (N == 0) S = 1;
+
+    // ---- scratch: tables of one chunk, mode records, split partials --------
+    const size_t tab_bytes = libm ? 0 : static_cast<size_t>(chunk) * kM * sizeof(double2);
+    const size_t rec_bytes = static_cast<size_t>(chunk) * kRec * sizeof(double);
+    const size_t part_bytes = S > 1 ? static_cast<size_t>(S) * nout * P * sizeof(double) : 0;
+    const size_t off_rec = (tab_bytes + 255) / 256 * 256;
+    const size_t off_part = off_rec + (rec_bytes + 255) / 256 * 256;
+    GSC_TRY(ensure_dev(ctx, ctx.scratch, off_part + part_bytes + 256));
+    GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
+    unsigned char *sbase = static_cast<unsigned char *>(ctx.scratch.ptr);
+    double2 *wtab = reinterpret_cast<double2 *>(sbase);
+    double *rec = reinterpret_cast<double *>(sbase + off_rec);
+    double *part = reinterpret_cast<double *>(sbase + off_part);
+
+    double *dst = S > 1 ? part : a.out;
+    const int64_t sd = S > 1 ? P : a.out_sd;
+    const int64_t sp = S > 1 ? 1 : a.out_sp;
+    const int64_t split_stride = S > 1 ? nout * P : 0;
+    const size_t smem = 2 * ((libm ? 0 : kTileModes * kM * 16) + kTileModes * kRec * 8);
+    const dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(S));
+
+    int64_t j0 = 0;
+    int first = 1;
+    do {
+        const int64_t nc = std::min<int64_t>(N - j0, kChunkModes);
+        if (nc > 0) {
+            TimedLaunch tl(st);
+            tl.begin(K_MODE_TABLE);
+            mode_table_kernel<<<static_cast<unsigned>(nc), kM, 0, st>>>(
+                a.cov, a.z1, a.z2, dim, N, j0, a.incompr ? 1 : 0, libm ? 0 : 1, wtab, rec);
+            tl.end();
+            GSC_CUDA(cudaGetLastError());
+        }
+        const int64_t mps_c = nc > 0 ? std::min<int64_t>(mps, nc) : 0;
+        const dim3 g(grid.x, static_cast<unsigned>(
+                                 nc > 0 ? std::min<int64_t>(S, (nc + mps_c - 1) / mps_c) : 1));
+        // on later chunks, splits past the end of a short chunk are not
+        // launched and keep their sums
+        const dim3 gl = first ? grid : g;
+        TimedLaunch tl(st);
+        tl.begin(a.incompr ? K_PLAIN_INCOMPR : (libm ? K_PLAIN_LIBM : K_PLAIN_SCALAR));
+        int rc;
+        if (a.incompr) {
+            rc = libm ? dispatch_dim<R, true, true>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
+                                                    mps_c, !first, dst, sd, sp, split_stride)
+                      : dispatch_dim<R, true, false>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
+                                                     mps_c, !first, dst, sd, sp, split_stride);
+        } else {
+            rc = libm ? dispatch_dim<R, false, true>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
+                                                     mps_c, !first, dst, sd, sp, split_stride)
+                      : dispatch_dim<R, false, false>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
+                                                      mps_c, !first, dst, sd, sp, split_stride);
+        }
+        tl.end();
+        if (rc != GSC_OK) return rc;
+        first = 0;
+        j0 += nc;
+    } while (j0 < N);
+
+    if (S > 1) {
+        TimedLaunch tl(st);
+        tl.begin(K_SPLIT_REDUCE);
+        const int64_t tot = nout * P;
+        split_reduce_kernel<<<static_cast<unsigned>((tot + 255) / 256), 256, 0, st>>>(
+            part, S, nout, P, a.out, a.out_sd, a.out_sp);
+        tl.end();
+        GSC_CUDA(cudaGetLastError());
+    }
+    GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+    return GSC_OK;
+}
+
+}  // namespace gsc

@@ -1,0 +1,194 @@
+"""gstools_core -- GB300 (sm_103a) drop-in for GSTools-Core's field summators.
+
+Mirrors the Python module that GSTools-Core's PyO3 layer exposes
+(reference ``src/lib.rs:29-65``):
+
+    summate(cov_samples, z1, z2, pos, num_threads=None) -> ndarray (n_points,)
+    summate_incompr(cov_samples, z1, z2, pos, num_threads=None)
+        -> ndarray (dim, n_points), Fortran ordered like the reference
+    __version__
+
+Same argument names, dtypes, shapes and return values.  The work runs on the
+GPU through the C ABI of ``include/gstools_core_gb300.h``; there is no CPU
+path.  Differences from the reference, all at its failure points:
+
+* a shape mismatch or an unsupported dimension raises ``ValueError``
+  (the reference panics, and its release build aborts the process);
+* ``num_threads`` is validated like PyO3's ``Option<usize>`` and otherwise
+  ignored: GPU parallelism is not set by a thread count.
+
+Keyword-only extensions (not in the reference): ``form`` selects a
+computation form and ``tolerance`` the error budget that ``form="auto"``
+may spend (default 1e-12 of the field RMS, the plain FP64 bar).
+"""
+from __future__ import annotations
+
+import ctypes
+import operator
+
+import numpy as np
+
+from . import _native
+from ._native import GscError, device_count, last_timings
+
+__all__ = ["summate", "summate_incompr", "summate_device", "summate_incompr_device",
+           "device_count", "last_timings", "GscError", "__version__"]
+
+__version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
+native_version = _native.lib.gsc_version().decode()
+
+
+# ---------------------------------------------------------------------------
+# argument extraction with PyO3/numpy's error behaviour
+# ---------------------------------------------------------------------------
+def _array(obj, name: str, ndim: int) -> np.ndarray:
+    if not isinstance(obj, np.ndarray):
+        raise TypeError(f"argument '{name}': '{type(obj).__name__}' object cannot be "
+                        f"converted to 'PyArray<T, D>'")
+    if obj.ndim != ndim:
+        raise TypeError(f"argument '{name}': dimensionality mismatch:\n from={obj.ndim}, to={ndim}")
+    if obj.dtype != np.float64:
+        raise TypeError(f"argument '{name}': type mismatch:\n from={obj.dtype}, to=float64")
+    return obj
+
+
+def _num_threads(num_threads) -> None:
+    if num_threads is None:
+        return
+    try:
+        n = operator.index(num_threads)
+    except TypeError:
+        raise TypeError(f"argument 'num_threads': '{type(num_threads).__name__}' object "
+                        "cannot be interpreted as an integer") from None
+    if n < 0:
+        raise OverflowError("argument 'num_threads': can't convert negative int to unsigned")
+
+
+def _assert_eq(left: int, right: int) -> None:
+    if left != right:
+        raise ValueError(f"assertion `left == right` failed\n  left: {left}\n right: {right}")
+
+
+def _strides(a: np.ndarray):
+    return tuple(s // a.itemsize for s in a.strides)
+
+
+def _opts(form, tolerance, timing, device=-1, stream=None):
+    flags = _native.GSC_FLAG_TIMING if timing else 0
+    return _native.make_opts(form=form, device=device, flags=flags, stream=stream,
+                             tolerance=tolerance or 0.0)
+
+
+def _prepare(cov_samples, z1, z2, pos, num_threads):
+    cov = _array(cov_samples, "cov_samples", 2)
+    z1 = _array(z1, "z1", 1)
+    z2 = _array(z2, "z2", 1)
+    pos = _array(pos, "pos", 2)
+    _num_threads(num_threads)
+    # the reference's asserts, in its order (src/field.rs:44-46, 104-106)
+    _assert_eq(cov.shape[0], pos.shape[0])
+    _assert_eq(cov.shape[1], z1.shape[0])
+    _assert_eq(cov.shape[1], z2.shape[0])
+    return cov, z1, z2, pos
+
+
+# ---------------------------------------------------------------------------
+# reference API
+# ---------------------------------------------------------------------------
+def summate(cov_samples, z1, z2, pos, num_threads=None, *, form="auto", tolerance=None,
+            timing=False, device=-1):
+    """Scalar randomization method (reference ``src/field.rs:37-65``).
+
+    u[p] = sum_j z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)
+    with k_j = cov_samples[:, j] and x_p = pos[:, p].
+    """
+    cov, z1, z2, pos = _prepare(cov_samples, z1, z2, pos, num_threads)
+    dim, n = cov.shape
+    p = pos.shape[1]
+    out = np.empty(p, dtype=np.float64)
+    cs, zs1, zs2, ps = _strides(cov), _strides(z1), _strides(z2), _strides(pos)
+    o = _opts(form, tolerance, timing, device)
+    _native.check(_native.lib.gsc_summate_f64(
+        cov.ctypes.data, cs[0], cs[1], z1.ctypes.data, zs1[0], z2.ctypes.data, zs2[0],
+        pos.ctypes.data, ps[0], ps[1], dim, n, p, out.ctypes.data, 1, ctypes.byref(o)))
+    return out
+
+
+def summate_incompr(cov_samples, z1, z2, pos, num_threads=None, *, form="auto", tolerance=None,
+                    timing=False, device=-1):
+    """Incompressible vector field (reference ``src/field.rs:97-182``).
+
+    u[i, p] = sum_j p_i(k_j) (z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)),
+    p(k) = e_1 - k k_0 / |k|^2; dim must be 2 or 3.  Returns a
+    Fortran-ordered (dim, n_points) array, as the reference does.
+    """
+    cov, z1, z2, pos = _prepare(cov_samples, z1, z2, pos, num_threads)
+    dim, n = cov.shape
+    if dim not in (2, 3):
+        raise ValueError("Only two- and three-dimensional problems are supported.")
+    p = pos.shape[1]
+    out = np.empty((dim, p), dtype=np.float64, order="F")
+    cs, zs1, zs2, ps = _strides(cov), _strides(z1), _strides(z2), _strides(pos)
+    os_ = _strides(out)
+    o = _opts(form, tolerance, timing, device)
+    _native.check(_native.lib.gsc_summate_incompr_f64(
+        cov.ctypes.data, cs[0], cs[1], z1.ctypes.data, zs1[0], z2.ctypes.data, zs2[0],
+        pos.ctypes.data, ps[0], ps[1], dim, n, p, out.ctypes.data, os_[0], os_[1],
+        ctypes.byref(o)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# device-resident API (arrays exposing __cuda_array_interface__, e.g. torch)
+# ---------------------------------------------------------------------------
+def _cuda_view(obj, name: str, shape):
+    iface = getattr(obj, "__cuda_array_interface__", None)
+    if iface is None:
+        raise TypeError(f"argument '{name}': expected a CUDA array (__cuda_array_interface__)")
+    if iface["typestr"] != "<f8":
+        raise TypeError(f"argument '{name}': type mismatch:\n from={iface['typestr']}, to=<f8")
+    if tuple(iface["shape"]) != tuple(shape):
+        raise ValueError(f"argument '{name}': shape {tuple(iface['shape'])} != {tuple(shape)}")
+    strides = iface.get("strides")
+    if strides is not None:
+        expect, acc = [], 8
+        for s in reversed(shape):
+            expect.append(acc)
+            acc *= s
+        if tuple(strides) != tuple(reversed(expect)) and int(np.prod(shape)) > 1:
+            raise ValueError(f"argument '{name}': must be C-contiguous")
+    return iface["data"][0]
+
+
+def _dev_shapes(cov_samples, pos):
+    cs = cov_samples.__cuda_array_interface__["shape"]
+    ps = pos.__cuda_array_interface__["shape"]
+    if len(cs) != 2 or len(ps) != 2:
+        raise TypeError("cov_samples and pos must be 2-D")
+    _assert_eq(cs[0], ps[0])
+    return cs[0], cs[1], ps[1]
+
+
+def summate_device(cov_samples, z1, z2, pos, out, *, form="auto", tolerance=None, stream=None,
+                   timing=False, device=-1):
+    """``summate`` on device-resident, C-contiguous float64 arrays; writes
+    ``out`` (n_points,) and returns without synchronising ``stream``."""
+    dim, n, p = _dev_shapes(cov_samples, pos)
+    args = [_cuda_view(cov_samples, "cov_samples", (dim, n)), _cuda_view(z1, "z1", (n,)),
+            _cuda_view(z2, "z2", (n,)), _cuda_view(pos, "pos", (dim, p))]
+    o = _opts(form, tolerance, timing, device, stream)
+    _native.check(_native.lib.gsc_summate_dev(*args, dim, n, p,
+                                              _cuda_view(out, "out", (p,)), ctypes.byref(o)))
+    return out
+
+
+def summate_incompr_device(cov_samples, z1, z2, pos, out, *, form="auto", tolerance=None,
+                           stream=None, timing=False, device=-1):
+    """``summate_incompr`` on device arrays; ``out`` is (dim, n_points), C order."""
+    dim, n, p = _dev_shapes(cov_samples, pos)
+    args = [_cuda_view(cov_samples, "cov_samples", (dim, n)), _cuda_view(z1, "z1", (n,)),
+            _cuda_view(z2, "z2", (n,)), _cuda_view(pos, "pos", (dim, p))]
+    o = _opts(form, tolerance, timing, device, stream)
+    _native.check(_native.lib.gsc_summate_incompr_dev(
+        *args, dim, n, p, _cuda_view(out, "out", (dim, p)), ctypes.byref(o)))
+    return out

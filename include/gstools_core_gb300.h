@@ -1,0 +1,135 @@
+/*
+ * gstools_core_gb300.h -- C ABI of the GB300 (sm_103a) spectral random-field
+ * summators.  This is the seam a foreign caller links against: plain C
+ * types, pointers and sizes; no CUDA, torch or C++ types in any signature.
+ *
+ * Reference interface being replaced (GeoStat-Framework/GSTools-Core 1.1.0):
+ *   Rust   pub fn field::summator(cov_samples, z1, z2, pos, num_threads)
+ *            src/field.rs:37-43            -> gsc_summate_f64
+ *          pub fn field::summator_incompr(...)
+ *            src/field.rs:97-103           -> gsc_summate_incompr_f64
+ *   Python gstools_core.summate / summate_incompr (PyO3)
+ *            src/lib.rs:33-48, 50-65       -> same two entry points, bound by
+ *                                             the package gstools_core
+ *
+ * Conventions
+ *  - Arrays are float64.  Strides are in ELEMENTS (ndarray / numpy strides
+ *    divided by 8), so any view the reference accepts can be passed as is:
+ *    cov_samples[d, j] = cov[d * cov_stride_d + j * cov_stride_n], etc.
+ *  - `*_f64` entry points take HOST pointers (what the Rust/PyO3 caller
+ *    holds).  The call copies inputs to the GPU, runs, copies the result
+ *    back into the caller-owned `out`, and returns when `out` is written.
+ *  - `*_dev` entry points take DEVICE pointers to dense row-major arrays and
+ *    enqueue on `opts->stream` without synchronising.
+ *  - Every entry point returns GSC_OK (0) or a nonzero status; the message
+ *    is available from gsc_last_error() on the calling thread.  Where the
+ *    reference panics (shape asserts src/field.rs:44-46, 104-106; dimension
+ *    src/field.rs:180) these return GSC_ERR_INVALID / GSC_ERR_DIM instead of
+ *    aborting the process.
+ *  - Calls are thread safe.  Host-pointer calls on one device are
+ *    serialised; device-pointer calls order their use of the library's
+ *    internal scratch buffers with CUDA events, so calls on different streams
+ *    are correct but do not overlap.
+ *  - There is no CPU fallback: without a usable CUDA device every compute
+ *    entry point returns GSC_ERR_NO_DEVICE.
+ */
+#ifndef GSTOOLS_CORE_GB300_H
+#define GSTOOLS_CORE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GSC_OK             0
+#define GSC_ERR_INVALID    1  /* bad shape, stride, pointer or option       */
+#define GSC_ERR_DIM        2  /* unsupported spatial dimension              */
+#define GSC_ERR_CUDA       3  /* a CUDA runtime call failed                 */
+#define GSC_ERR_NO_DEVICE  4  /* no usable CUDA device                      */
+#define GSC_ERR_NOMEM      5  /* device or pinned host allocation failed    */
+#define GSC_ERR_KERNEL     6  /* a kernel reported an error status          */
+
+/* ---- computation forms ----------------------------------------------- */
+#define GSC_FORM_AUTO       0  /* library choice for the requested tolerance */
+#define GSC_FORM_PLAIN_F64  1  /* FP64 end to end, table-driven FP64 sincos   */
+#define GSC_FORM_PLAIN_F64_LIBM 2  /* FP64 end to end on CUDA's sincos()    */
+
+/* ---- flags ----------------------------------------------------------- */
+#define GSC_FLAG_TIMING     1  /* record per-kernel CUDA-event timings      */
+
+/* Options.  Pass NULL for the defaults (form AUTO at tolerance 1e-12,
+ * current device, library stream for host-pointer calls and the legacy
+ * default stream for device-pointer calls). */
+typedef struct gsc_opts {
+    int32_t struct_size;  /* sizeof(gsc_opts); lets the struct grow       */
+    int32_t form;         /* GSC_FORM_*                                   */
+    int32_t device;       /* CUDA device ordinal, -1 = current device     */
+    int32_t flags;        /* GSC_FLAG_*                                   */
+    void   *stream;       /* cudaStream_t, NULL = see above               */
+    double  tolerance;    /* max |err| / field RMS that AUTO may spend;
+                             <= 0 means 1e-12 (the plain FP64 bar)        */
+} gsc_opts;
+
+/* ---- library information --------------------------------------------- */
+
+/* Version string: the reference crate version this build mirrors plus the
+ * GB300 build tag, e.g. "1.1.0+gb300". */
+const char *gsc_version(void);
+
+/* Message of the last failing call made on this thread ("" if none). */
+const char *gsc_last_error(void);
+
+/* Number of CUDA devices the library can use (0 when there are none). */
+int gsc_device_count(int32_t *count);
+
+/* Per-kernel timings of the last GSC_FLAG_TIMING call on this thread:
+ * writes up to `cap` (name-index, milliseconds) pairs and returns how many
+ * kernels were recorded.  Names come from gsc_kernel_name(). */
+int gsc_last_timings(int32_t *kernel_ids, double *ms, int32_t cap);
+const char *gsc_kernel_name(int32_t kernel_id);
+
+/* ---- scalar randomization method: src/field.rs:37-65 ------------------ */
+/* u[p] = sum_j z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)
+ * cov (dim, n_modes), z1/z2 (n_modes), pos (dim, n_points), out (n_points).
+ * Replaces field::summator (src/field.rs:37) / PyO3 summate (src/lib.rs:35). */
+int gsc_summate_f64(const double *cov, int64_t cov_stride_d, int64_t cov_stride_n,
+                    const double *z1, int64_t z1_stride,
+                    const double *z2, int64_t z2_stride,
+                    const double *pos, int64_t pos_stride_d, int64_t pos_stride_p,
+                    int64_t dim, int64_t n_modes, int64_t n_points,
+                    double *out, int64_t out_stride,
+                    const gsc_opts *opts);
+
+/* Device-pointer form: cov (dim, n_modes) row-major, pos (dim, n_points)
+ * row-major, out (n_points).  Enqueued on opts->stream. */
+int gsc_summate_dev(const double *cov, const double *z1, const double *z2,
+                    const double *pos, int64_t dim, int64_t n_modes,
+                    int64_t n_points, double *out, const gsc_opts *opts);
+
+/* ---- incompressible vector field: src/field.rs:97-182 ----------------- */
+/* u[i, p] = sum_j p_i(k_j) (z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)),
+ * p(k) = e_1 - k k_0 / |k|^2, dim in {2, 3}; out (dim, n_points) written
+ * at out[i * out_stride_d + p * out_stride_p] (the reference returns the
+ * Fortran-ordered array: out_stride_d = 1, out_stride_p = dim).
+ * Replaces field::summator_incompr (src/field.rs:97) / PyO3 summate_incompr
+ * (src/lib.rs:52). */
+int gsc_summate_incompr_f64(const double *cov, int64_t cov_stride_d, int64_t cov_stride_n,
+                            const double *z1, int64_t z1_stride,
+                            const double *z2, int64_t z2_stride,
+                            const double *pos, int64_t pos_stride_d, int64_t pos_stride_p,
+                            int64_t dim, int64_t n_modes, int64_t n_points,
+                            double *out, int64_t out_stride_d, int64_t out_stride_p,
+                            const gsc_opts *opts);
+
+/* Device-pointer form: out (dim, n_points) row-major. */
+int gsc_summate_incompr_dev(const double *cov, const double *z1, const double *z2,
+                            const double *pos, int64_t dim, int64_t n_modes,
+                            int64_t n_points, double *out, const gsc_opts *opts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSTOOLS_CORE_GB300_H */
