@@ -1,11 +1,13 @@
 """Builds the native library ``libgstools_core_gb300.so`` in-tree.
 
-Every CUDA translation unit under ``gstools-core_gb300/csrc`` is compiled for
+Lives outside the ``gstools_core`` package so that it can be imported (and
+run) before the library exists.  Every CUDA translation unit under
+``gstools-core_gb300/csrc`` is compiled for
 sm_103a only (``-gencode arch=compute_103a,code=sm_103a``), in parallel, then
 linked into one shared library placed next to this file.  nvcc cross-compiles,
 so this runs on a machine without a GPU.
 
-    python -m gstools_core._build [--force]
+    python gstools-core_gb300/gsc_build.py [--force]
 """
 from __future__ import annotations
 
@@ -15,8 +17,8 @@ import os
 import subprocess
 import sys
 
-PKG_DIR = os.path.dirname(os.path.abspath(__file__))
-ROOT = os.path.dirname(PKG_DIR)                 # gstools-core_gb300/
+ROOT = os.path.dirname(os.path.abspath(__file__))     # gstools-core_gb300/
+PKG_DIR = os.path.join(ROOT, "gstools_core")
 CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 BUILD_DIR = os.path.join(ROOT, "_build")
@@ -67,7 +69,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcuda"]
+    cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -9,7 +9,7 @@ from __future__ import annotations
 import ctypes
 import os
 
-from ._build import LIB_PATH
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgstools_core_gb300.so")
 
 GSC_OK = 0
 GSC_ERR_INVALID = 1
@@ -71,7 +71,7 @@ def _load():
         raise ImportError(
             f"gstools_core: native library {LIB_PATH} is not built; run "
             "`python -c 'import __graft_entry__ as g; g.build()'` or "
-            "`python -m gstools_core._build` (there is no CPU fallback)")
+            "`python gstools-core_gb300/gsc_build.py` (there is no CPU fallback)")
     lib = ctypes.CDLL(LIB_PATH)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)

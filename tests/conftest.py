@@ -41,7 +41,7 @@ def ulps_eq(a: float, b: float, max_ulps: int = 6, epsilon: float = np.finfo(np.
 def _build_native():
     """Builds the CUDA library (cross-compiles without a GPU) once per session."""
     import shutil
-    from gstools_core._build import build, LIB_PATH, _up_to_date
+    from gsc_build import build, LIB_PATH, _up_to_date
     if not _up_to_date():
         if not (shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")):
             pytest.skip("nvcc not available to build the native library")
