@@ -37,7 +37,8 @@ int cuda_fail(cudaError_t e, const char *what) {
 const char *kernel_name(int32_t id) {
     static const char *names[K_COUNT] = {
         "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
-        "split_reduce", "generic_f64",
+        "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
+        "grid_expand",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -138,6 +139,8 @@ int get_ctx(int device, DeviceCtx **out) {
         GSC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         GSC_CUDA(cudaEventCreateWithFlags(&c->scratch_ready, cudaEventDisableTiming));
         GSC_CUDA(cudaEventRecord(c->scratch_ready, c->stream));
+        GSC_CUDA(cudaMalloc(&c->status, 256));
+        GSC_CUDA(cudaMemset(c->status, 0, 256));
         g_ctx[device] = c;
     }
     *out = g_ctx[device];
@@ -199,7 +202,7 @@ static int resolve_opts(const gsc_opts *o, Resolved *r) {
     if (!o) return GSC_OK;
     if (o->struct_size < static_cast<int32_t>(sizeof(gsc_opts)))
         return set_error(GSC_ERR_INVALID, "gsc_opts.struct_size is smaller than sizeof(gsc_opts)");
-    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_PLAIN_F64_LIBM)
+    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_SEP_BF16X3)
         return set_error(GSC_ERR_INVALID, "unknown form");
     r->form = o->form;
     r->device = o->device;
@@ -238,6 +241,41 @@ static int check_device_ptr(const void *p, const char *name) {
 
 static int plain_variant(const Resolved &r) { return r.form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0; }
 
+static bool is_sep(int form) { return form == GSC_FORM_SEP_F16X3 || form == GSC_FORM_SEP_BF16X3; }
+
+static int unstructured_form(const Resolved &r) {
+    if (is_sep(r.form))
+        return set_error(GSC_ERR_INVALID,
+                         "separable (tensor-core) forms need a structured grid; use the "
+                         "gsc_summate*_structured entry points");
+    return GSC_OK;
+}
+
+// Largest max|err| / field RMS each form is validated to (tests and bench
+// measure it); AUTO picks the fastest form whose bound fits the tolerance.
+constexpr double kBoundSepF16x3 = 2e-6;
+
+static int structured_form(const Resolved &r, int64_t dim) {
+    int f = r.form;
+    if (f == GSC_FORM_AUTO) f = r.tolerance >= kBoundSepF16x3 ? GSC_FORM_SEP_F16X3 : GSC_FORM_PLAIN_F64;
+    if (is_sep(f) && dim < 2) f = GSC_FORM_PLAIN_F64;   // 1-D: nothing to contract
+    return f;
+}
+
+// Reads and clears the sticky status word after the stream has finished.
+static int check_status(DeviceCtx &ctx, cudaStream_t st) {
+    int v = 0;
+    GSC_CUDA(cudaMemcpyAsync(&v, ctx.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GSC_CUDA(cudaStreamSynchronize(st));
+    if (v != 0) {
+        GSC_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(int), st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        return set_error(GSC_ERR_KERNEL, "a tensor-core pipeline wait gave up (status " +
+                                             std::to_string(v) + "); the output is invalid");
+    }
+    return GSC_OK;
+}
+
 // gathers a strided (rows, cols) host view into dense row-major dst
 static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int64_t cols,
                     double *dst) {
@@ -270,6 +308,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(need_ptr(z2, N > 0, "z2"));
     GSC_TRY(need_ptr(pos, dim * P > 0, "pos"));
     GSC_TRY(need_ptr(out, P > 0, "out"));
+    GSC_TRY(unstructured_form(ro));
     timing_reset(ro.flags & GSC_FLAG_TIMING);
     if (P == 0) return GSC_OK;
 
@@ -336,6 +375,7 @@ static int dev_plain(const double *cov, const double *z1, const double *z2, cons
     GSC_TRY(need_ptr(z2, N > 0, "z2"));
     GSC_TRY(need_ptr(pos, dim * P > 0, "pos"));
     GSC_TRY(need_ptr(out, P > 0, "out"));
+    GSC_TRY(unstructured_form(ro));
     timing_reset(ro.flags & GSC_FLAG_TIMING);
     if (P == 0) return GSC_OK;
     DeviceCtx *ctx = nullptr;
@@ -362,6 +402,165 @@ static int dev_plain(const double *cov, const double *z1, const double *z2, cons
     a.out_sp = 1;
     a.variant = plain_variant(ro);
     return plain_run(*ctx, a, ro.stream);
+}
+
+// ---------------------------------------------------------------------------
+// structured grids
+// ---------------------------------------------------------------------------
+static int check_structured(int64_t dim, int64_t N, const int64_t *n, bool incompr) {
+    GSC_TRY(check_sizes(dim, N, 0));
+    if (dim < 1 || dim > 3)
+        return set_error(incompr ? GSC_ERR_DIM : GSC_ERR_INVALID,
+                         incompr ? "Only two- and three-dimensional problems are supported."
+                                 : "structured grids need 1, 2 or 3 axes");
+    if (incompr && dim == 1)
+        return set_error(GSC_ERR_DIM, "Only two- and three-dimensional problems are supported.");
+    for (int d = 0; d < dim; ++d)
+        if (n[d] < 0) return set_error(GSC_ERR_INVALID, "negative axis length");
+    int64_t P = 1;
+    for (int d = 0; d < dim; ++d) {
+        if (n[d] > 0 && P > (int64_t(1) << 40) / n[d])
+            return set_error(GSC_ERR_INVALID, "grid too large");
+        P *= n[d];
+    }
+    if (N > (int64_t(1) << 30)) return set_error(GSC_ERR_INVALID, "too many modes");
+    return GSC_OK;
+}
+
+// All pointers are device pointers; out is (ncomp, P) row-major.
+static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov, const double *z1,
+                          const double *z2, int64_t dim, int64_t N, const double *const *axis,
+                          const int64_t *n, bool incompr, double *out, cudaStream_t st) {
+    int64_t P = 1;
+    for (int d = 0; d < dim; ++d) P *= n[d];
+    if (P == 0) return GSC_OK;
+    const int form = structured_form(ro, dim);
+    if (is_sep(form)) {
+        SepArgs a;
+        a.cov = cov;
+        a.z1 = z1;
+        a.z2 = z2;
+        a.dim = dim;
+        a.n_modes = N;
+        for (int d = 0; d < 3; ++d) {
+            a.axis[d] = d < dim ? axis[d] : nullptr;
+            a.n[d] = d < dim ? n[d] : 1;
+        }
+        a.incompr = incompr;
+        a.form = form;
+        a.chunk_kblocks = 0;
+        a.out = out;
+        a.status = ctx.status;
+        return sep_tc_run(ctx, a, st);
+    }
+    // plain FP64 forms on the expanded grid
+    const double *pos = axis[0];
+    if (dim > 1) {
+        GSC_TRY(ensure_dev(ctx, ctx.grid, static_cast<size_t>(dim * P) * sizeof(double)));
+        GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
+        TimedLaunch tl(st);
+        tl.begin(K_GRID_EXPAND);
+        GSC_TRY(grid_expand(axis, n, dim, static_cast<double *>(ctx.grid.ptr), st));
+        tl.end();
+        pos = static_cast<const double *>(ctx.grid.ptr);
+    }
+    PlainArgs a;
+    a.cov = cov;
+    a.z1 = z1;
+    a.z2 = z2;
+    a.pos = pos;
+    a.dim = dim;
+    a.n_modes = N;
+    a.n_points = P;
+    a.incompr = incompr;
+    a.out = out;
+    a.out_sd = P;
+    a.out_sp = 1;
+    a.variant = form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0;
+    return plain_run(ctx, a, st);
+}
+
+static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
+                           int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
+                           const double *const *ax, const int64_t *n, const int64_t *sx,
+                           double *out, bool incompr, const gsc_opts *opts) {
+    Resolved ro;
+    GSC_TRY(resolve_opts(opts, &ro));
+    GSC_TRY(check_structured(dim, N, n, incompr));
+    int64_t P = 1;
+    for (int d = 0; d < dim; ++d) P *= n[d];
+    GSC_TRY(need_ptr(cov, dim * N > 0, "cov_samples"));
+    GSC_TRY(need_ptr(z1, N > 0, "z1"));
+    GSC_TRY(need_ptr(z2, N > 0, "z2"));
+    for (int d = 0; d < dim; ++d) GSC_TRY(need_ptr(ax[d], n[d] > 0, "axis"));
+    GSC_TRY(need_ptr(out, P > 0, "out"));
+    timing_reset(ro.flags & GSC_FLAG_TIMING);
+    if (P == 0) return GSC_OK;
+
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(ro.device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    cudaStream_t st = ctx->stream;
+
+    const int64_t nout = incompr ? dim : 1;
+    const size_t n_cov = static_cast<size_t>(dim * N);
+    size_t n_ax = 0;
+    for (int d = 0; d < dim; ++d) n_ax += static_cast<size_t>(n[d]);
+    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_ax;
+    const size_t n_out = static_cast<size_t>(nout * P);
+    GSC_TRY(ensure_pinned(*ctx, n_in * sizeof(double)));
+    GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out) * sizeof(double) + 1024));
+    double *h = static_cast<double *>(ctx->pinned);
+    gather2(cov, cs_d, cs_n, dim, N, h);
+    gather2(z1, 0, z1s, 1, N, h + n_cov);
+    gather2(z2, 0, z2s, 1, N, h + n_cov + N);
+    size_t off = n_cov + 2 * N;
+    double *d = static_cast<double *>(ctx->io.ptr);
+    const double *dax[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < dim; ++k) {
+        gather2(ax[k], 0, sx[k], 1, n[k], h + off);
+        dax[k] = d + off;
+        off += static_cast<size_t>(n[k]);
+    }
+    GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    // output buffer 128-byte aligned after the inputs
+    double *dout = reinterpret_cast<double *>(
+        (reinterpret_cast<uintptr_t>(d + n_in) + 127) & ~static_cast<uintptr_t>(127));
+    GSC_TRY(run_structured(*ctx, ro, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr, dout,
+                           st));
+    GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GSC_TRY(check_status(*ctx, st));
+    return GSC_OK;
+}
+
+static int dev_structured(const double *cov, const double *z1, const double *z2, int64_t dim,
+                          int64_t N, const double *const *ax, const int64_t *n, double *out,
+                          bool incompr, const gsc_opts *opts) {
+    Resolved ro;
+    GSC_TRY(resolve_opts(opts, &ro));
+    GSC_TRY(check_structured(dim, N, n, incompr));
+    int64_t P = 1;
+    for (int d = 0; d < dim; ++d) P *= n[d];
+    GSC_TRY(need_ptr(cov, dim * N > 0, "cov_samples"));
+    GSC_TRY(need_ptr(z1, N > 0, "z1"));
+    GSC_TRY(need_ptr(z2, N > 0, "z2"));
+    for (int d = 0; d < dim; ++d) GSC_TRY(need_ptr(ax[d], n[d] > 0, "axis"));
+    GSC_TRY(need_ptr(out, P > 0, "out"));
+    timing_reset(ro.flags & GSC_FLAG_TIMING);
+    if (P == 0) return GSC_OK;
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(ro.device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    GSC_TRY(check_device_ptr(cov, "cov_samples"));
+    GSC_TRY(check_device_ptr(z1, "z1"));
+    GSC_TRY(check_device_ptr(z2, "z2"));
+    for (int d = 0; d < dim; ++d) GSC_TRY(check_device_ptr(ax[d], "axis"));
+    GSC_TRY(check_device_ptr(out, "out"));
+    return run_structured(*ctx, ro, cov, z1, z2, dim, N, ax, n, incompr, out, ro.stream);
 }
 
 }  // namespace gsc
@@ -434,6 +633,59 @@ int gsc_summate_incompr_dev(const double *cov, const double *z1, const double *z
                             const double *pos, int64_t dim, int64_t n_modes, int64_t n_points,
                             double *out, const gsc_opts *opts) {
     return dev_plain(cov, z1, z2, pos, dim, n_modes, n_points, out, true, opts);
+}
+
+int gsc_device_status(int32_t device) {
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    GSC_CUDA(cudaEventSynchronize(ctx->scratch_ready));
+    return check_status(*ctx, ctx->stream);
+}
+
+int gsc_summate_structured_f64(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
+                               int64_t z1s, const double *z2, int64_t z2s, int64_t dim,
+                               int64_t n_modes, const double *a0, int64_t n0, int64_t s0,
+                               const double *a1, int64_t n1, int64_t s1, const double *a2,
+                               int64_t n2, int64_t s2, double *out, const gsc_opts *opts) {
+    const double *ax[3] = {a0, a1, a2};
+    const int64_t n[3] = {n0, n1, n2}, sx[3] = {s0, s1, s2};
+    return host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, n_modes, ax, n, sx, out,
+                           false, opts);
+}
+
+int gsc_summate_structured_dev(const double *cov, const double *z1, const double *z2,
+                               int64_t dim, int64_t n_modes, const double *a0, int64_t n0,
+                               const double *a1, int64_t n1, const double *a2, int64_t n2,
+                               double *out, const gsc_opts *opts) {
+    const double *ax[3] = {a0, a1, a2};
+    const int64_t n[3] = {n0, n1, n2};
+    return dev_structured(cov, z1, z2, dim, n_modes, ax, n, out, false, opts);
+}
+
+int gsc_summate_incompr_structured_f64(const double *cov, int64_t cs_d, int64_t cs_n,
+                                       const double *z1, int64_t z1s, const double *z2,
+                                       int64_t z2s, int64_t dim, int64_t n_modes,
+                                       const double *a0, int64_t n0, int64_t s0,
+                                       const double *a1, int64_t n1, int64_t s1,
+                                       const double *a2, int64_t n2, int64_t s2, double *out,
+                                       const gsc_opts *opts) {
+    const double *ax[3] = {a0, a1, a2};
+    const int64_t n[3] = {n0, n1, n2}, sx[3] = {s0, s1, s2};
+    return host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, n_modes, ax, n, sx, out,
+                           true, opts);
+}
+
+int gsc_summate_incompr_structured_dev(const double *cov, const double *z1, const double *z2,
+                                       int64_t dim, int64_t n_modes, const double *a0,
+                                       int64_t n0, const double *a1, int64_t n1,
+                                       const double *a2, int64_t n2, double *out,
+                                       const gsc_opts *opts) {
+    const double *ax[3] = {a0, a1, a2};
+    const int64_t n[3] = {n0, n1, n2};
+    return dev_structured(cov, z1, z2, dim, n_modes, ax, n, out, true, opts);
 }
 
 }  // extern "C"

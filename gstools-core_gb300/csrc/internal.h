@@ -37,6 +37,10 @@ enum KernelId : int32_t {
     K_PLAIN_LIBM = 3,      // FP64 summators on CUDA's sincos()
     K_SPLIT_REDUCE = 4,    // ordered sum of mode-split partials
     K_GENERIC = 5,         // any dimension, one thread per point
+    K_SEP_TABLES = 6,      // per-axis factor tables of the separable form
+    K_SEP_TC_F16 = 7,      // tcgen05 separable contraction, f16 hi/lo split
+    K_SEP_TC_BF16 = 8,     // tcgen05 separable contraction, bf16 hi/lo split
+    K_GRID_EXPAND = 9,     // meshgrid of structured axes (plain form on grids)
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -58,6 +62,8 @@ struct DeviceCtx {
     DevBuf scratch;                  // tables and partial sums
     void *pinned = nullptr;          // pinned host staging
     size_t pinned_bytes = 0;
+    DevBuf grid;                     // expanded meshgrid for plain forms on grids
+    int *status = nullptr;           // sticky kernel status word (device)
 };
 
 // Returns the context of `device` (-1 = current), initialising it once.
@@ -91,5 +97,24 @@ struct PlainArgs {
     int variant;         // 0 table-driven sincos, 1 CUDA sincos()
 };
 int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st);
+
+// ---- separable tensor-core summators on structured grids (separable_tc.cu) --
+struct SepArgs {
+    const double *cov;        // (dim, n_modes) row-major, device
+    const double *z1, *z2;    // (n_modes), device
+    int64_t dim, n_modes;     // dim in {2, 3}
+    const double *axis[3];    // device axes; axis[i] has n[i] points
+    int64_t n[3];
+    bool incompr;
+    int form;                 // GSC_FORM_SEP_F16X3 or GSC_FORM_SEP_BF16X3
+    int chunk_kblocks;        // k-blocks per FP32 accumulation chunk, 0 = default
+    double *out;              // (ncomp, prod n) row-major, device
+    int *status;              // device status word (0 = ok)
+};
+int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);
+
+// meshgrid(axis..., indexing="ij") flattened: pos[d * P + p], device
+int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double *pos,
+                cudaStream_t st);
 
 }  // namespace gsc

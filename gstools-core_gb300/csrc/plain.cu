@@ -324,7 +324,36 @@ int sm_count(int device) {
     return n;
 }
 
+__global__ void grid_expand_kernel(const double *__restrict__ a0, const double *__restrict__ a1,
+                                   const double *__restrict__ a2, int64_t n0, int64_t n1,
+                                   int64_t n2, int dim, double *__restrict__ pos) {
+    const int64_t P = n0 * n1 * n2;
+    const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int64_t i2 = p % n2, i01 = p / n2, i1 = i01 % n1, i0 = i01 / n1;
+    if (dim == 2) {
+        // (n0, n1) grid: p = i0 * n1 + i1 with n2 == 1
+        pos[p] = a0[i0];
+        pos[P + p] = a1[i1];
+    } else {
+        pos[p] = a0[i0];
+        pos[P + p] = a1[i1];
+        pos[2 * P + p] = a2[i2];
+    }
+}
+
 }  // namespace
+
+int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double *pos,
+                cudaStream_t st) {
+    const int64_t n2 = dim == 3 ? n[2] : 1;
+    const int64_t P = n[0] * n[1] * n2;
+    if (P == 0) return GSC_OK;
+    grid_expand_kernel<<<static_cast<unsigned>((P + 255) / 256), 256, 0, st>>>(
+        axis[0], axis[1], dim == 3 ? axis[2] : nullptr, n[0], n[1], n2, static_cast<int>(dim), pos);
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
 
 int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
     constexpr int R = 4;

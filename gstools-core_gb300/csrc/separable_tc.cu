@@ -1,0 +1,608 @@
+// separable_tc.cu -- the randomization-method summator on structured grids,
+// as a complex contraction on tcgen05 tensor cores (sm_103a).
+//
+// On a structured grid x_p = (X_a, Y_b, Z_c) the phase factor separates:
+//   z1 cos(k.x) + z2 sin(k.x) = Re[(z1 - i z2) e^{i kx X_a} e^{i ky Y_b} e^{i kz Z_c}]
+// so the field (reference src/field.rs:37-65 evaluated on the flattened
+// meshgrid) becomes, for every X_a,
+//   u[a, b, c] = sum_j Re[ s_a[j] B[b, j] C[c, j] ],
+//   s_a[j] = (z1_j - i z2_j) e^{i kx_j X_a},  B[b, j] = e^{i ky_j Y_b},
+//   C[c, j] = e^{i kz_j Z_c} (times the projector weight p_i(k_j) for the
+//   incompressible field, reference src/field.rs:138-152),
+// i.e. one real GEMM per X_a with K = 2 * modes:
+//   rows     F[b, 2j] = Re(s_a B),  F[b, 2j+1] = Im(s_a B)     (built on chip)
+//   columns  G[c, 2j] = Re C,       G[c, 2j+1] = -Im C          (static table)
+//   u[a, b, c] = sum_k F[b, k] G[c, k].
+// In 2-D the same GEMM runs once with s = z1 - i z2 and (rows, columns) =
+// (X, Y).
+//
+// Precision.  Both operands are split into two half-precision terms
+// (hi + lo, 22 significant bits); the GEMM sums hi*hi + hi*lo + lo*hi
+// ("f16x3"; "bf16x3" with bfloat16 terms) in FP32 tensor-memory
+// accumulators.  FP32 accumulation over all 2N terms would round at the
+// full field magnitude on every MMA instruction, so the K loop is cut into
+// chunks of KC k-blocks: each chunk accumulates from zero in one TMEM
+// region and the epilogue warps add it into a running total held in a
+// second TMEM region while the next chunk is computed.
+//
+// Kernel structure (one CTA per output tile of 128 rows x 256 columns of
+// one X_a; 10 warps):
+//   warps 0-3  epilogue: drain chunk accumulators, final FP64 store
+//   warps 4-7  producers: build the F tile (hi, lo) for each k-block in
+//              the 128-byte-swizzled K-major layout the MMA reads
+//   warp  8    TMA: loads the G tiles (hi, lo) of each k-block
+//   warp  9    MMA issuer (one thread) and TMEM owner
+// Two pipeline stages of 96 KB (F hi/lo 2 x 16 KB, G hi/lo 2 x 32 KB).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "internal.h"
+#include "sm100.cuh"
+
+namespace gsc {
+namespace {
+using namespace sm100;
+
+constexpr int BM = 128;                         // tile rows (TMEM lanes)
+constexpr int BN = 256;                         // tile columns
+constexpr int BK = 64;                          // K elements per k-block (32 modes)
+constexpr int STAGES = 2;
+constexpr int A_BYTES = BM * BK * 2;            // one F term of one stage
+constexpr int G_BYTES = BN * BK * 2;            // one G term of one stage
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * G_BYTES;
+constexpr int kThreadsTC = 320;
+constexpr int kTmaWarp = 8;
+constexpr int kMmaWarp = 9;
+constexpr uint32_t kTmemCols = 512;             // acc [0, 256), total [256, 512)
+constexpr size_t kSmemBytes = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+
+constexpr double kTwoOverPi = 0.6366197723675814;
+constexpr double kPio2Hi = 1.5707963267948966;      // fl(pi/2)
+constexpr double kPio2Lo = 6.123233995736766e-17;   // fl(pi/2 - kPio2Hi)
+constexpr double kRound = 6755399441055744.0;       // 1.5 * 2^52
+
+// e^{i phi} to about one FP32 ulp: FP64 two-constant Cody-Waite reduction to
+// |r| <= pi/4, FP32 sincos of r with a first-order correction for the FP32
+// rounding of r, quadrant rotation.  |phi| beyond 1e13 uses FP64 sincos.
+__device__ __forceinline__ float2 cis_f32(double phi) {
+    if (!(fabs(phi) < 1.0e13)) {
+        double s, c;
+        sincos(phi, &s, &c);
+        return make_float2(static_cast<float>(c), static_cast<float>(s));
+    }
+    const double t = fma(phi, kTwoOverPi, kRound);
+    const double q = t - kRound;
+    const int quad = __double2loint(t) & 3;
+    double r = fma(-q, kPio2Hi, phi);
+    r = fma(-q, kPio2Lo, r);
+    const float rh = __double2float_rn(r);
+    const float rl = __double2float_rn(r - static_cast<double>(rh));
+    float sn, cs;
+    sincosf(rh, &sn, &cs);
+    const float s1 = fmaf(rl, cs, sn);
+    const float c1 = fmaf(-rl, sn, cs);
+    switch (quad) {
+        case 0: return make_float2(c1, s1);
+        case 1: return make_float2(-s1, c1);
+        case 2: return make_float2(-c1, -s1);
+        default: return make_float2(s1, -c1);
+    }
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+// FP32 -> FP64 with integer operations only (GB300's FP64 pipe is 1/64 of
+// FP32).  FP32 subnormals (< 1.2e-38) become signed zeros.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xFFu, man = u & 0x7FFFFFu;
+    uint32_t hi, lo;
+    if (e == 0u) {
+        hi = sign;
+        lo = 0u;
+    } else if (e == 0xFFu) {
+        hi = sign | 0x7FF00000u | (man >> 3) | (man ? 0x80000u : 0u);
+        lo = man << 29;
+    } else {
+        hi = sign | ((e + 896u) << 20) | (man >> 3);
+        lo = man << 29;
+    }
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+
+template <bool BF16>
+struct Split;
+template <>
+struct Split<false> {
+    // v ~ hi + lo, both IEEE half, packed as (re, im) pairs
+    __device__ __forceinline__ static void run(float re, float im, uint32_t &hi, uint32_t &lo) {
+        const __half2 h = __floats2half2_rn(re, im);
+        const float2 hf = __half22float2(h);
+        const __half2 l = __floats2half2_rn(re - hf.x, im - hf.y);
+        hi = *reinterpret_cast<const uint32_t *>(&h);
+        lo = *reinterpret_cast<const uint32_t *>(&l);
+    }
+};
+template <>
+struct Split<true> {
+    __device__ __forceinline__ static void run(float re, float im, uint32_t &hi, uint32_t &lo) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(re, im);
+        const float2 hf = __bfloat1622float2(h);
+        const __nv_bfloat162 l = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+        hi = *reinterpret_cast<const uint32_t *>(&h);
+        lo = *reinterpret_cast<const uint32_t *>(&l);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// tables
+// ---------------------------------------------------------------------------
+struct TabArgs {
+    const double *cov;          // (dim, n_modes) row-major
+    const double *z1, *z2;
+    int dim, n_modes;
+    const double *ax_b;          // batch axis (X) for 3-D, unused in 2-D
+    const double *ax_m;          // row axis
+    const double *ax_n;          // column axis
+    int kb_dim, km_dim, kn_dim;  // which k component goes with each axis
+    int nb, nm, nn, ncomp, incompr;
+    int k_pad;                   // K elements per G row (multiple of 64)
+    int ncn_pad;                 // G rows (multiple of BN)
+    float2 *svec;                // [nb][n_modes]
+    float2 *btab;                // [n_modes][nm]
+    uint32_t *ghi, *glo;         // [ncn_pad][k_pad/2] packed (re, -im) pairs
+};
+
+__global__ void sep_svec_kernel(TabArgs t) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<int64_t>(t.nb) * t.n_modes) return;
+    const int b = static_cast<int>(i / t.n_modes), j = static_cast<int>(i % t.n_modes);
+    float2 w = make_float2(static_cast<float>(t.z1[j]), static_cast<float>(-t.z2[j]));
+    if (t.dim == 3) {
+        const float2 e = cis_f32(t.cov[t.kb_dim * t.n_modes + j] * t.ax_b[b]);
+        // (z1 - i z2) e, formed in FP64 from the FP32 factor, rounded once
+        const double re = t.z1[j] * e.x + t.z2[j] * e.y;
+        const double im = t.z1[j] * e.y - t.z2[j] * e.x;
+        w = make_float2(static_cast<float>(re), static_cast<float>(im));
+    }
+    t.svec[i] = w;
+}
+
+__global__ void sep_btab_kernel(TabArgs t) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<int64_t>(t.n_modes) * t.nm) return;
+    const int j = static_cast<int>(i / t.nm), m = static_cast<int>(i % t.nm);
+    t.btab[i] = cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m]);
+}
+
+template <bool BF16>
+__global__ void sep_gtab_kernel(TabArgs t) {
+    const int half_k = t.k_pad / 2;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<int64_t>(t.ncn_pad) * half_k) return;
+    const int row = static_cast<int>(i / half_k), j = static_cast<int>(i % half_k);
+    float re = 0.f, im = 0.f;
+    if (row < t.ncomp * t.nn && j < t.n_modes) {
+        const int c = row / t.nn, n = row - c * t.nn;
+        float2 e = cis_f32(t.cov[t.kn_dim * t.n_modes + j] * t.ax_n[n]);
+        double pw = 1.0;
+        if (t.incompr) {
+            // projector weight, as the reference forms it (src/field.rs:138-152)
+            double kk = 0.0;
+            for (int d = 0; d < t.dim; ++d) {
+                const double kd = t.cov[d * t.n_modes + j];
+                kk = __dadd_rn(kk, __dmul_rn(kd, kd));
+            }
+            const double k0 = t.cov[j];
+            const double k_2 = __ddiv_rn(k0, kk);
+            pw = (c == 0) ? __dadd_rn(1.0, -__dmul_rn(k0, k_2))
+                          : -__dmul_rn(t.cov[c * t.n_modes + j], k_2);
+        }
+        re = static_cast<float>(pw * e.x);
+        im = static_cast<float>(-(pw * e.y));
+    }
+    uint32_t hi, lo;
+    Split<BF16>::run(re, im, hi, lo);
+    t.ghi[i] = hi;
+    t.glo[i] = lo;
+}
+
+// ---------------------------------------------------------------------------
+// GEMM kernel
+// ---------------------------------------------------------------------------
+struct TcParams {
+    const float2 *svec;     // [nb][n_modes]
+    const float2 *btab;     // [n_modes][nm]
+    int n_modes, nm, nb, nn, ncn;   // ncn = ncomp * nn valid G rows
+    int kb_total, kc;               // k-blocks, k-blocks per accumulation chunk
+    int m_tiles, n_tiles;
+    double *out;
+    int64_t comp_stride, batch_stride, row_stride;
+    int *status;
+};
+
+template <bool BF16>
+__global__ void __launch_bounds__(kThreadsTC, 1)
+sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
+              const __grid_constant__ CUtensorMap map_glo, const TcParams p) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+    uint64_t *full_a = bars;                  // producers -> MMA   (128 arrivals)
+    uint64_t *full_g = bars + STAGES;         // TMA -> MMA         (1 arrival + bytes)
+    uint64_t *empty = bars + 2 * STAGES;      // MMA commit -> producers, TMA
+    uint64_t *acc_full = bars + 3 * STAGES;   // MMA commit -> epilogue
+    uint64_t *acc_empty = acc_full + 1;       // epilogue -> MMA    (128 arrivals)
+    uint64_t *drain = acc_full + 2;           // MMA commit on abort
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int tile = blockIdx.x;
+    const int nt = tile % p.n_tiles;
+    tile /= p.n_tiles;
+    const int mt = tile % p.m_tiles;
+    const int b = tile / p.m_tiles;
+    const int m0 = mt * BM, n0 = nt * BN;
+    const int KB = p.kb_total, KC = p.kc;
+    const int NC = (KB + KC - 1) / KC;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full_a[s], 128);
+            mbar_init(&full_g[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, 128);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == kMmaWarp) {
+        tmem_alloc(tmem_slot, kTmemCols);
+        tmem_relinquish();
+    }
+    if (warp == kTmaWarp && lane == 0) {
+        tma_prefetch_map(&map_ghi);
+        tma_prefetch_map(&map_glo);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t t_acc = tmem, t_tot = tmem + 256;
+
+    if (warp == kTmaWarp) {
+        // ---- TMA: G tiles --------------------------------------------------
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < KB; ++kb) {
+                const int s = kb % STAGES, n = kb / STAGES;
+                if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status,
+                                        kErrTimeoutEmpty))
+                    break;
+                unsigned char *st = smem + s * STAGE_BYTES;
+                mbar_arrive_expect_tx(&full_g[s], 2 * G_BYTES);
+                tma_load_2d(st + 2 * A_BYTES, &map_ghi, &full_g[s], kb * BK, n0);
+                tma_load_2d(st + 2 * A_BYTES + G_BYTES, &map_glo, &full_g[s], kb * BK, n0);
+                ++issued;
+            }
+            if (*abort_flag) {   // let the copies in flight land before the CTA exits
+                for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb)
+                    mbar_wait_drain(&full_g[kb % STAGES], (kb / STAGES) & 1, p.status);
+            }
+        }
+    } else if (warp == kMmaWarp) {
+        // ---- MMA issue -------------------------------------------------------
+        if (lane == 0) {
+            const uint32_t idesc = idesc_f16(BM, BN, BF16);
+            bool ok = true;
+            for (int kb = 0; kb < KB; ++kb) {
+                const int s = kb % STAGES, n = kb / STAGES;
+                const int c = kb / KC;
+                const bool first = (kb % KC) == 0;
+                const bool last = (kb % KC) == KC - 1 || kb == KB - 1;
+                if (first && c > 0)
+                    ok = mbar_wait(acc_empty, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
+                if (ok) ok = mbar_wait(&full_a[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
+                if (ok) ok = mbar_wait(&full_g[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+                const uint32_t a_hi = sa, a_lo = sa + A_BYTES;
+                const uint32_t g_hi = sa + 2 * A_BYTES, g_lo = g_hi + G_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint32_t off = kk * 32;   // 16 elements of 2 bytes
+                    mma_f16_ss(t_acc, desc_k_sw128(a_hi + off), desc_k_sw128(g_hi + off), idesc,
+                               (first && kk == 0) ? 0u : 1u);
+                    mma_f16_ss(t_acc, desc_k_sw128(a_hi + off), desc_k_sw128(g_lo + off), idesc, 1u);
+                    mma_f16_ss(t_acc, desc_k_sw128(a_lo + off), desc_k_sw128(g_hi + off), idesc, 1u);
+                }
+                mma_commit(&empty[s]);
+                if (last) mma_commit(acc_full);
+            }
+            if (!ok) {   // wait for the MMAs already issued before TMEM is freed
+                mma_commit(drain);
+                mbar_wait_drain(drain, 0, p.status);
+            }
+        }
+    } else if (warp >= 4) {
+        // ---- producers: F tile rows ----------------------------------------------
+        // Thread r builds row m0 + r.  The B-table values of k-block kb + 1
+        // are loaded while k-block kb is converted, hiding the L2 latency.
+        const int r = threadIdx.x - 128;
+        const int m = m0 + r;
+        const bool row_ok = m < p.nm;
+        const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
+        const uint32_t row_off = (r >> 3) * 1024 + (r & 7) * 128;
+        float2 cur[32];
+        auto load_block = [&](int kb, float2 (&dst)[32]) {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                const int j = kb * 32 + q;
+                dst[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm + m)
+                                                   : make_float2(0.f, 0.f);
+            }
+        };
+        load_block(0, cur);
+        for (int kb = 0; kb < KB; ++kb) {
+            const int s = kb % STAGES, n = kb / STAGES;
+            float2 nxt[32];
+            if (kb + 1 < KB) load_block(kb + 1, nxt);
+            if (n > 0 &&
+                !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status, kErrTimeoutEmpty))
+                break;
+            unsigned char *a_hi = smem + s * STAGE_BYTES;
+            unsigned char *a_lo = a_hi + A_BYTES;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {   // 16-byte chunk c: modes 4c .. 4c+3
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int j = kb * 32 + c * 4 + q;
+                    const float2 sj = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
+                    const float2 v = cmulf(cur[c * 4 + q], sj);
+                    Split<BF16>::run(v.x, v.y, hw[q], lw[q]);
+                }
+                const uint32_t phys = row_off + ((c ^ (r & 7)) << 4);
+                *reinterpret_cast<uint4 *>(a_hi + phys) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(a_lo + phys) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+            fence_proxy_async_smem();
+            mbar_arrive(&full_a[s]);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) cur[q] = nxt[q];
+        }
+    } else {
+        // ---- epilogue: warps 0-3, TMEM lanes 32*warp .. +31 ----------------------
+        const uint32_t lane_off = static_cast<uint32_t>(32 * warp) << 16;
+        const int m = m0 + 32 * warp + lane;
+        for (int c = 0; c < NC; ++c) {
+            if (!mbar_wait(acc_full, c & 1, abort_flag, p.status, kErrTimeoutAcc)) break;
+            tc_fence_after();
+            if (c < NC - 1) {
+                for (int g = 0; g < BN / 32; ++g) {
+                    uint32_t a[32], t[32];
+                    __syncwarp();
+                    tmem_ld32(t_acc + lane_off + 32 * g, a);
+                    if (c > 0) tmem_ld32(t_tot + lane_off + 32 * g, t);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int i = 0; i < 32; ++i)
+                        t[i] = c > 0 ? __float_as_uint(__uint_as_float(t[i]) + __uint_as_float(a[i]))
+                                     : a[i];
+                    tmem_st32(t_tot + lane_off + 32 * g, t);
+                }
+                tmem_st_wait();
+                tc_fence_before();
+                mbar_arrive(acc_empty);
+            } else {
+                const bool row_ok = m < p.nm;
+                double *orow = p.out + static_cast<int64_t>(b) * p.batch_stride +
+                               static_cast<int64_t>(row_ok ? m : 0) * p.row_stride;
+                for (int g = 0; g < BN / 32; ++g) {
+                    uint32_t a[32], t[32];
+                    __syncwarp();
+                    tmem_ld32(t_acc + lane_off + 32 * g, a);
+                    if (c > 0) tmem_ld32(t_tot + lane_off + 32 * g, t);
+                    tmem_ld_wait();
+                    const int gn0 = n0 + 32 * g;
+                    if (row_ok && gn0 < p.ncn) {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) {
+                            const int gn = gn0 + i;
+                            if (gn < p.ncn) {
+                                const float v = c > 0 ? __uint_as_float(t[i]) + __uint_as_float(a[i])
+                                                      : __uint_as_float(a[i]);
+                                const int comp = gn / p.nn;
+                                orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(v);
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encode_fn(EncodeTiledFn *out) {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                               cudaEnableDefault, &q);
+        if (err == cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    if (!fn) return set_error(GSC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    *out = fn;
+    return GSC_OK;
+}
+
+int make_map(CUtensorMap *map, void *base, bool bf16, int k_pad, int rows) {
+    EncodeTiledFn fn;
+    GSC_TRY(encode_fn(&fn));
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(k_pad), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(k_pad) * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BN)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                          2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GSC_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return GSC_OK;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+template <bool BF16>
+int configure_tc() {
+    static bool done = false;
+    if (!done) {
+        GSC_CUDA(cudaFuncSetAttribute(sep_tc_kernel<BF16>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(kSmemBytes)));
+        done = true;
+    }
+    return GSC_OK;
+}
+
+}  // namespace
+
+int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
+    const bool bf16 = a.form == GSC_FORM_SEP_BF16X3;
+    const int dim = static_cast<int>(a.dim);
+    const int N = static_cast<int>(a.n_modes);
+    const int ncomp = a.incompr ? dim : 1;
+    const int nb = dim == 3 ? static_cast<int>(a.n[0]) : 1;
+    const int nm = static_cast<int>(dim == 3 ? a.n[1] : a.n[0]);
+    const int nn = static_cast<int>(dim == 3 ? a.n[2] : a.n[1]);
+    const int64_t P = static_cast<int64_t>(nb) * nm * nn;
+    if (P == 0) return GSC_OK;
+    const int KB = std::max(1, (2 * N + BK - 1) / BK);
+    const int k_pad = KB * BK;
+    const int ncn = ncomp * nn;
+    const int n_tiles = (ncn + BN - 1) / BN;
+    const int ncn_pad = n_tiles * BN;
+    const int m_tiles = (nm + BM - 1) / BM;
+
+    // scratch: svec, btab, G hi, G lo
+    const size_t off_svec = 0;
+    const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(N), 1024);
+    const size_t off_ghi = align_up(off_btab + sizeof(float2) * static_cast<size_t>(N) * nm, 1024);
+    const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
+    const size_t off_glo = align_up(off_ghi + g_bytes, 1024);
+    const size_t total = off_glo + g_bytes;
+    GSC_TRY(ensure_dev(ctx, ctx.scratch, total));
+    GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
+    unsigned char *base = static_cast<unsigned char *>(ctx.scratch.ptr);
+    int *status = a.status;
+
+    TabArgs t;
+    t.cov = a.cov;
+    t.z1 = a.z1;
+    t.z2 = a.z2;
+    t.dim = dim;
+    t.n_modes = N;
+    t.ax_b = dim == 3 ? a.axis[0] : nullptr;
+    t.ax_m = dim == 3 ? a.axis[1] : a.axis[0];
+    t.ax_n = dim == 3 ? a.axis[2] : a.axis[1];
+    t.kb_dim = 0;
+    t.km_dim = dim == 3 ? 1 : 0;
+    t.kn_dim = dim == 3 ? 2 : 1;
+    t.nb = nb;
+    t.nm = nm;
+    t.nn = nn;
+    t.ncomp = ncomp;
+    t.incompr = a.incompr ? 1 : 0;
+    t.k_pad = k_pad;
+    t.ncn_pad = ncn_pad;
+    t.svec = reinterpret_cast<float2 *>(base + off_svec);
+    t.btab = reinterpret_cast<float2 *>(base + off_btab);
+    t.ghi = reinterpret_cast<uint32_t *>(base + off_ghi);
+    t.glo = reinterpret_cast<uint32_t *>(base + off_glo);
+
+    {
+        TimedLaunch tl(st);
+        tl.begin(K_SEP_TABLES);
+        const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(N) * nm;
+        const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
+        if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
+        if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
+        if (bf16)
+            sep_gtab_kernel<true><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+        else
+            sep_gtab_kernel<false><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+        tl.end();
+        GSC_CUDA(cudaGetLastError());
+    }
+
+    CUtensorMap mh, ml;
+    GSC_TRY(make_map(&mh, t.ghi, bf16, k_pad, ncn_pad));
+    GSC_TRY(make_map(&ml, t.glo, bf16, k_pad, ncn_pad));
+
+    TcParams p;
+    p.svec = t.svec;
+    p.btab = t.btab;
+    p.n_modes = N;
+    p.nm = nm;
+    p.nb = nb;
+    p.nn = nn;
+    p.ncn = ncn;
+    p.kb_total = KB;
+    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : 4;
+    p.m_tiles = m_tiles;
+    p.n_tiles = n_tiles;
+    p.out = a.out;
+    p.comp_stride = P;
+    p.batch_stride = static_cast<int64_t>(nm) * nn;
+    p.row_stride = nn;
+    p.status = status;
+    const int64_t grid = static_cast<int64_t>(nb) * m_tiles * n_tiles;
+    if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
+    {
+        TimedLaunch tl(st);
+        tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
+        if (bf16) {
+            GSC_TRY(configure_tc<true>());
+            sep_tc_kernel<true><<<static_cast<unsigned>(grid), kThreadsTC, kSmemBytes, st>>>(mh, ml, p);
+        } else {
+            GSC_TRY(configure_tc<false>());
+            sep_tc_kernel<false><<<static_cast<unsigned>(grid), kThreadsTC, kSmemBytes, st>>>(mh, ml, p);
+        }
+        tl.end();
+        GSC_CUDA(cudaGetLastError());
+    }
+    GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+    return GSC_OK;
+}
+
+}  // namespace gsc

@@ -32,6 +32,8 @@ from . import _native
 from ._native import GscError, device_count, last_timings
 
 __all__ = ["summate", "summate_incompr", "summate_device", "summate_incompr_device",
+           "summate_structured", "summate_incompr_structured", "summate_structured_device",
+           "summate_incompr_structured_device", "device_status",
            "device_count", "last_timings", "GscError", "__version__"]
 
 __version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
@@ -192,3 +194,113 @@ def summate_incompr_device(cov_samples, z1, z2, pos, out, *, form="auto", tolera
     _native.check(_native.lib.gsc_summate_incompr_dev(
         *args, dim, n, p, _cuda_view(out, "out", (dim, p)), ctypes.byref(o)))
     return out
+
+
+# ---------------------------------------------------------------------------
+# structured grids (extension: the reference's callers expand the mesh)
+# ---------------------------------------------------------------------------
+def _axes_host(axes, dim):
+    if not isinstance(axes, (list, tuple)) or len(axes) != dim:
+        raise ValueError(f"axes must be a sequence of {dim} 1-D float64 arrays")
+    out = []
+    for i, a in enumerate(axes):
+        out.append(_array(a, f"axes[{i}]", 1))
+    while len(out) < 3:
+        out.append(None)
+    return out
+
+
+def _structured_host(fn, cov_samples, z1, z2, axes, num_threads, form, tolerance, timing,
+                     device, incompr):
+    cov = _array(cov_samples, "cov_samples", 2)
+    z1 = _array(z1, "z1", 1)
+    z2 = _array(z2, "z2", 1)
+    _num_threads(num_threads)
+    dim, n = cov.shape
+    _assert_eq(cov.shape[1], z1.shape[0])
+    _assert_eq(cov.shape[1], z2.shape[0])
+    ax = _axes_host(axes, dim)
+    if incompr and dim not in (2, 3):
+        raise ValueError("Only two- and three-dimensional problems are supported.")
+    npts = 1
+    for a in ax[:dim]:
+        npts *= a.shape[0]
+    out = np.empty((dim, npts) if incompr else npts, dtype=np.float64)
+    args = []
+    for a in ax:
+        if a is None:
+            args += [None, 0, 0]
+        else:
+            args += [a.ctypes.data, a.shape[0], _strides(a)[0]]
+    cs, zs1, zs2 = _strides(cov), _strides(z1), _strides(z2)
+    o = _opts(form, tolerance, timing, device)
+    _native.check(fn(cov.ctypes.data, cs[0], cs[1], z1.ctypes.data, zs1[0], z2.ctypes.data,
+                     zs2[0], dim, n, *args, out.ctypes.data, ctypes.byref(o)))
+    return out
+
+
+def summate_structured(cov_samples, z1, z2, axes, num_threads=None, *, form="auto",
+                       tolerance=None, timing=False, device=-1):
+    """``summate`` on the structured grid ``meshgrid(*axes, indexing="ij")``.
+
+    Equal to ``summate(cov_samples, z1, z2, pos)`` with
+    ``pos = np.array(np.meshgrid(*axes, indexing="ij")).reshape(dim, -1)``
+    (the flattening GSTools uses for structured meshes), but the grid is never
+    expanded: with ``form="sep_f16x3"`` (or ``form="auto"`` and
+    ``tolerance >= 2e-6``) the sum runs as a separable complex contraction on
+    the tensor cores.  Returns a flat (n_points,) array.
+    """
+    return _structured_host(_native.lib.gsc_summate_structured_f64, cov_samples, z1, z2, axes,
+                            num_threads, form, tolerance, timing, device, False)
+
+
+def summate_incompr_structured(cov_samples, z1, z2, axes, num_threads=None, *, form="auto",
+                               tolerance=None, timing=False, device=-1):
+    """``summate_incompr`` on a structured grid; returns (dim, n_points), C order."""
+    return _structured_host(_native.lib.gsc_summate_incompr_structured_f64, cov_samples, z1,
+                            z2, axes, num_threads, form, tolerance, timing, device, True)
+
+
+def _structured_dev(fn, cov_samples, z1, z2, axes, out, form, tolerance, stream, timing,
+                    device, incompr):
+    cs = cov_samples.__cuda_array_interface__["shape"]
+    if len(cs) != 2:
+        raise TypeError("cov_samples must be 2-D")
+    dim, n = cs
+    if not isinstance(axes, (list, tuple)) or len(axes) != dim:
+        raise ValueError(f"axes must be a sequence of {dim} CUDA arrays")
+    args, npts = [], 1
+    for i, a in enumerate(axes):
+        la = a.__cuda_array_interface__["shape"]
+        if len(la) != 1:
+            raise TypeError(f"axes[{i}] must be 1-D")
+        args += [_cuda_view(a, f"axes[{i}]", (la[0],)), la[0]]
+        npts *= la[0]
+    while len(args) < 6:
+        args += [None, 0]
+    shape = (dim, npts) if incompr else (npts,)
+    o = _opts(form, tolerance, timing, device, stream)
+    _native.check(fn(_cuda_view(cov_samples, "cov_samples", (dim, n)), _cuda_view(z1, "z1", (n,)),
+                     _cuda_view(z2, "z2", (n,)), dim, n, *args, _cuda_view(out, "out", shape),
+                     ctypes.byref(o)))
+    return out
+
+
+def summate_structured_device(cov_samples, z1, z2, axes, out, *, form="auto", tolerance=None,
+                              stream=None, timing=False, device=-1):
+    """``summate_structured`` on device arrays; writes ``out`` (n_points,)."""
+    return _structured_dev(_native.lib.gsc_summate_structured_dev, cov_samples, z1, z2, axes,
+                           out, form, tolerance, stream, timing, device, False)
+
+
+def summate_incompr_structured_device(cov_samples, z1, z2, axes, out, *, form="auto",
+                                      tolerance=None, stream=None, timing=False, device=-1):
+    """``summate_incompr_structured`` on device arrays; ``out`` is (dim, n_points)."""
+    return _structured_dev(_native.lib.gsc_summate_incompr_structured_dev, cov_samples, z1, z2,
+                           axes, out, form, tolerance, stream, timing, device, True)
+
+
+def device_status(device=-1) -> None:
+    """Raises GscError if a kernel of an earlier device-array call on ``device``
+    reported a failed pipeline wait (the output of that call is invalid)."""
+    _native.check(_native.lib.gsc_device_status(device))

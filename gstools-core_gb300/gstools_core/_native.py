@@ -25,6 +25,8 @@ FORMS = {
     "auto": 0,
     "plain": 1,
     "plain_libm": 2,
+    "sep_f16x3": 3,
+    "sep_bf16x3": 4,
 }
 
 
@@ -63,6 +65,17 @@ SIGNATURES = {
     "gsc_summate_incompr_f64": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P, _I64, _P, _I64,
                                                _I64, _I64, _I64, _I64, _P, _I64, _I64, _OPTS]),
     "gsc_summate_incompr_dev": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _OPTS]),
+    "gsc_device_status": (ctypes.c_int, [_I32]),
+    "gsc_summate_structured_f64": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P, _I64, _I64, _I64,
+                                                  _P, _I64, _I64, _P, _I64, _I64, _P, _I64, _I64,
+                                                  _P, _OPTS]),
+    "gsc_summate_structured_dev": (ctypes.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _P, _I64,
+                                                  _P, _I64, _P, _OPTS]),
+    "gsc_summate_incompr_structured_f64": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P, _I64,
+                                                          _I64, _I64, _P, _I64, _I64, _P, _I64,
+                                                          _I64, _P, _I64, _I64, _P, _OPTS]),
+    "gsc_summate_incompr_structured_dev": (ctypes.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _P,
+                                                          _I64, _P, _I64, _P, _OPTS]),
 }
 
 

@@ -55,6 +55,11 @@ extern "C" {
 #define GSC_FORM_AUTO       0  /* library choice for the requested tolerance */
 #define GSC_FORM_PLAIN_F64  1  /* FP64 end to end, table-driven FP64 sincos   */
 #define GSC_FORM_PLAIN_F64_LIBM 2  /* FP64 end to end on CUDA's sincos()    */
+#define GSC_FORM_SEP_F16X3  3  /* structured grids: separable contraction on
+                                  tcgen05 tensor cores, both operands split
+                                  into f16 hi + lo, 3 products, FP32
+                                  accumulation drained every 4 k-blocks     */
+#define GSC_FORM_SEP_BF16X3 4  /* as GSC_FORM_SEP_F16X3 with bf16 terms       */
 
 /* ---- flags ----------------------------------------------------------- */
 #define GSC_FLAG_TIMING     1  /* record per-kernel CUDA-event timings      */
@@ -89,6 +94,12 @@ int gsc_device_count(int32_t *count);
  * kernels were recorded.  Names come from gsc_kernel_name(). */
 int gsc_last_timings(int32_t *kernel_ids, double *ms, int32_t cap);
 const char *gsc_kernel_name(int32_t kernel_id);
+
+/* Status of the kernels launched by device-pointer calls on `device`
+ * (-1 = current): waits for them, returns GSC_OK or GSC_ERR_KERNEL (a
+ * pipeline wait gave up; the output of that call is invalid), and clears
+ * the status.  Host-pointer calls check it themselves. */
+int gsc_device_status(int32_t device);
 
 /* ---- scalar randomization method: src/field.rs:37-65 ------------------ */
 /* u[p] = sum_j z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)
@@ -127,6 +138,51 @@ int gsc_summate_incompr_f64(const double *cov, int64_t cov_stride_d, int64_t cov
 int gsc_summate_incompr_dev(const double *cov, const double *z1, const double *z2,
                             const double *pos, int64_t dim, int64_t n_modes,
                             int64_t n_points, double *out, const gsc_opts *opts);
+
+/* ---- structured grids ------------------------------------------------ */
+/* The scalar field of gsc_summate_f64 on the grid
+ * meshgrid(axis0, axis1[, axis2], indexing="ij") flattened in C order, i.e.
+ * the points GSTools passes to summate for a structured mesh:
+ * p = (i0 * n1 + i1) * n2 + i2.  dim in {1, 2, 3}; axis d has n_d points
+ * with element stride s_d (unused axes: NULL, 0, 0).  out[p], p < prod n_d,
+ * contiguous.  Forms: GSC_FORM_SEP_* (tensor cores), GSC_FORM_PLAIN_* (the
+ * plain kernel on the expanded grid) or AUTO.  New entry point: the
+ * reference has no structured variant (its callers expand the grid). */
+int gsc_summate_structured_f64(const double *cov, int64_t cov_stride_d, int64_t cov_stride_n,
+                               const double *z1, int64_t z1_stride,
+                               const double *z2, int64_t z2_stride,
+                               int64_t dim, int64_t n_modes,
+                               const double *axis0, int64_t n0, int64_t s0,
+                               const double *axis1, int64_t n1, int64_t s1,
+                               const double *axis2, int64_t n2, int64_t s2,
+                               double *out, const gsc_opts *opts);
+
+/* Device-pointer form: contiguous axes, out (prod n_d) contiguous. */
+int gsc_summate_structured_dev(const double *cov, const double *z1, const double *z2,
+                               int64_t dim, int64_t n_modes,
+                               const double *axis0, int64_t n0,
+                               const double *axis1, int64_t n1,
+                               const double *axis2, int64_t n2,
+                               double *out, const gsc_opts *opts);
+
+/* Incompressible field on a structured grid (dim in {2, 3}): out is
+ * (dim, prod n_d) row-major (component c at out + c * prod n_d). */
+int gsc_summate_incompr_structured_f64(const double *cov, int64_t cov_stride_d,
+                                       int64_t cov_stride_n,
+                                       const double *z1, int64_t z1_stride,
+                                       const double *z2, int64_t z2_stride,
+                                       int64_t dim, int64_t n_modes,
+                                       const double *axis0, int64_t n0, int64_t s0,
+                                       const double *axis1, int64_t n1, int64_t s1,
+                                       const double *axis2, int64_t n2, int64_t s2,
+                                       double *out, const gsc_opts *opts);
+
+int gsc_summate_incompr_structured_dev(const double *cov, const double *z1, const double *z2,
+                                       int64_t dim, int64_t n_modes,
+                                       const double *axis0, int64_t n0,
+                                       const double *axis1, int64_t n1,
+                                       const double *axis2, int64_t n2,
+                                       double *out, const gsc_opts *opts);
 
 #ifdef __cplusplus
 }
