@@ -38,7 +38,7 @@ const char *kernel_name(int32_t id) {
     static const char *names[K_COUNT] = {
         "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
-        "grid_expand",
+        "grid_expand", "sep_tc_f16x5",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -202,7 +202,7 @@ static int resolve_opts(const gsc_opts *o, Resolved *r) {
     if (!o) return GSC_OK;
     if (o->struct_size < static_cast<int32_t>(sizeof(gsc_opts)))
         return set_error(GSC_ERR_INVALID, "gsc_opts.struct_size is smaller than sizeof(gsc_opts)");
-    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_SEP_BF16X3)
+    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_SEP_F16X5)
         return set_error(GSC_ERR_INVALID, "unknown form");
     r->form = o->form;
     r->device = o->device;
@@ -241,7 +241,9 @@ static int check_device_ptr(const void *p, const char *name) {
 
 static int plain_variant(const Resolved &r) { return r.form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0; }
 
-static bool is_sep(int form) { return form == GSC_FORM_SEP_F16X3 || form == GSC_FORM_SEP_BF16X3; }
+static bool is_sep(int form) {
+    return form == GSC_FORM_SEP_F16X3 || form == GSC_FORM_SEP_BF16X3 || form == GSC_FORM_SEP_F16X5;
+}
 
 static int unstructured_form(const Resolved &r) {
     if (is_sep(r.form))
@@ -253,11 +255,15 @@ static int unstructured_form(const Resolved &r) {
 
 // Largest max|err| / field RMS each form is validated to (tests and bench
 // measure it); AUTO picks the fastest form whose bound fits the tolerance.
-constexpr double kBoundSepF16x3 = 2e-6;
+constexpr double kBoundSepF16x3 = 1e-5;
+constexpr double kBoundSepF16x5 = 1e-6;
 
 static int structured_form(const Resolved &r, int64_t dim) {
     int f = r.form;
-    if (f == GSC_FORM_AUTO) f = r.tolerance >= kBoundSepF16x3 ? GSC_FORM_SEP_F16X3 : GSC_FORM_PLAIN_F64;
+    if (f == GSC_FORM_AUTO)
+        f = r.tolerance >= kBoundSepF16x3   ? GSC_FORM_SEP_F16X3
+            : r.tolerance >= kBoundSepF16x5 ? GSC_FORM_SEP_F16X5
+                                            : GSC_FORM_PLAIN_F64;
     if (is_sep(f) && dim < 2) f = GSC_FORM_PLAIN_F64;   // 1-D: nothing to contract
     return f;
 }

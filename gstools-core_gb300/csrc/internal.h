@@ -41,6 +41,7 @@ enum KernelId : int32_t {
     K_SEP_TC_F16 = 7,      // tcgen05 separable contraction, f16 hi/lo split
     K_SEP_TC_BF16 = 8,     // tcgen05 separable contraction, bf16 hi/lo split
     K_GRID_EXPAND = 9,     // meshgrid of structured axes (plain form on grids)
+    K_SEP_TC_F16X5 = 10,   // tcgen05 separable contraction, exact leading term
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -106,7 +107,7 @@ struct SepArgs {
     const double *axis[3];    // device axes; axis[i] has n[i] points
     int64_t n[3];
     bool incompr;
-    int form;                 // GSC_FORM_SEP_F16X3 or GSC_FORM_SEP_BF16X3
+    int form;                 // GSC_FORM_SEP_F16X3, _BF16X3 or _F16X5
     int chunk_kblocks;        // k-blocks per FP32 accumulation chunk, 0 = default
     double *out;              // (ncomp, prod n) row-major, device
     int *status;              // device status word (0 = ok)

@@ -61,6 +61,12 @@ constexpr int kMmaWarp = 9;
 constexpr uint32_t kTmemCols = 512;             // acc [0, 256), total [256, 512)
 constexpr size_t kSmemBytes = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 
+// Both operands are scaled by 2^10 before the split so that the lo terms of
+// values down to 2^-13 stay normal f16 numbers (the tensor core does not
+// keep f16 subnormals); the epilogue multiplies by 2^-20, exactly.
+constexpr float kOperandScale = 1024.0f;
+constexpr float kProductUnscale = 1.0f / (1024.0f * 1024.0f);
+
 constexpr double kTwoOverPi = 0.6366197723675814;
 constexpr double kPio2Hi = 1.5707963267948966;      // fl(pi/2)
 constexpr double kPio2Lo = 6.123233995736766e-17;   // fl(pi/2 - kPio2Hi)
@@ -158,18 +164,20 @@ struct TabArgs {
     float2 *svec;                // [nb][n_modes]
     float2 *btab;                // [n_modes][nm]
     uint32_t *ghi, *glo;         // [ncn_pad][k_pad/2] packed (re, -im) pairs
+    float *wnorm;                // x5 form: {W, 1/W}, W = 2^ceil(log2 max|z1 - i z2|)
 };
 
 __global__ void sep_svec_kernel(TabArgs t) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= static_cast<int64_t>(t.nb) * t.n_modes) return;
+    const double inv_w = t.wnorm ? static_cast<double>(t.wnorm[1]) : 1.0;
     const int b = static_cast<int>(i / t.n_modes), j = static_cast<int>(i % t.n_modes);
-    float2 w = make_float2(static_cast<float>(t.z1[j]), static_cast<float>(-t.z2[j]));
+    float2 w = make_float2(static_cast<float>(t.z1[j] * inv_w), static_cast<float>(-t.z2[j] * inv_w));
     if (t.dim == 3) {
         const float2 e = cis_f32(t.cov[t.kb_dim * t.n_modes + j] * t.ax_b[b]);
         // (z1 - i z2) e, formed in FP64 from the FP32 factor, rounded once
-        const double re = t.z1[j] * e.x + t.z2[j] * e.y;
-        const double im = t.z1[j] * e.y - t.z2[j] * e.x;
+        const double re = (t.z1[j] * e.x + t.z2[j] * e.y) * inv_w;
+        const double im = (t.z1[j] * e.y - t.z2[j] * e.x) * inv_w;
         w = make_float2(static_cast<float>(re), static_cast<float>(im));
     }
     t.svec[i] = w;
@@ -205,8 +213,8 @@ __global__ void sep_gtab_kernel(TabArgs t) {
             pw = (c == 0) ? __dadd_rn(1.0, -__dmul_rn(k0, k_2))
                           : -__dmul_rn(t.cov[c * t.n_modes + j], k_2);
         }
-        re = static_cast<float>(pw * e.x);
-        im = static_cast<float>(-(pw * e.y));
+        re = static_cast<float>(pw * e.x) * kOperandScale;
+        im = static_cast<float>(-(pw * e.y)) * kOperandScale;
     }
     uint32_t hi, lo;
     Split<BF16>::run(re, im, hi, lo);
@@ -372,7 +380,7 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
                     const int j = kb * 32 + c * 4 + q;
                     const float2 sj = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
                     const float2 v = cmulf(cur[c * 4 + q], sj);
-                    Split<BF16>::run(v.x, v.y, hw[q], lw[q]);
+                    Split<BF16>::run(v.x * kOperandScale, v.y * kOperandScale, hw[q], lw[q]);
                 }
                 const uint32_t phys = row_off + ((c ^ (r & 7)) << 4);
                 *reinterpret_cast<uint4 *>(a_hi + phys) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
@@ -422,8 +430,8 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
                         for (int i = 0; i < 32; ++i) {
                             const int gn = gn0 + i;
                             if (gn < p.ncn) {
-                                const float v = c > 0 ? __uint_as_float(t[i]) + __uint_as_float(a[i])
-                                                      : __uint_as_float(a[i]);
+                                const float v = (c > 0 ? __uint_as_float(t[i]) + __uint_as_float(a[i])
+                                                       : __uint_as_float(a[i])) * kProductUnscale;
                                 const int comp = gn / p.nn;
                                 orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(v);
                             }
@@ -439,6 +447,336 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
     __syncthreads();
     tc_fence_after();
     if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---------------------------------------------------------------------------
+// Exact-leading-term form ("f16x5").
+//
+// The f16x3 form above loses accuracy in the tensor core's FP32 accumulator,
+// which truncates on every MMA instruction at the accumulator's magnitude.
+// This form removes that error from the dominant product:
+//   F (rows, |F| <= 1 after dividing s by W)  = F1 + F2 + F3
+//   G (columns, |G| <= 1)                     = G1 + G2
+// in units of 2^15:  F1 = 2^15 * rint(F * 2^(bF-1)) / 2^(bF-1)  (bF-bit integer grid),
+//                    G1 = 2^15 * rint(G * 2^11) / 2^11           (12-bit integer grid),
+// F2 = f16(F*2^15 - F1), F3 = f16(F*2^15 - F1 - F2), G2 = f16(G*2^15 - G1).
+// Every product F1*G1 is an integer multiple of 2^(15+15-(bF-1)-11); their
+// sum stays far below 2^24 multiples, so the "main" TMEM accumulator adds
+// them EXACTLY whatever the hardware rounding.  The four cross products
+// F2G1 + F1G2 + F2G2 + F3G1 (about 2^-9 of the field) go to a second TMEM
+// accumulator that the epilogue drains every KC k-blocks into FP32 totals
+// held in registers, so their rounding never builds up at full magnitude.
+// Representation: F to 2^-31, G to 2^-23 relative; products F2G3, F3G2 ...
+// below 2^-30 are dropped.
+//
+// Warp roles (16 warps, 512 threads, 128 registers each):
+//   warps 0-7   epilogue: warp w reads TMEM lanes 32*(w%4).., columns
+//               128*(w/4) .. +128 (cross totals live in 128 registers)
+//   warps 8-11  producers: F1, F2, F3 tiles of each k-block
+//   warp 12     TMA: G1, G2 tiles
+//   warp 13     MMA issuer and TMEM owner; warps 14-15 idle
+// Stages: F1/F2/F3 3 x 16 KB + G1/G2 2 x 32 KB = 112 KB, two stages.
+// ---------------------------------------------------------------------------
+constexpr int X5_THREADS = 512;
+constexpr int X5_STAGE = 3 * A_BYTES + 2 * G_BYTES;
+constexpr size_t kSmemX5 = 2 * X5_STAGE + 1024 + 256;
+constexpr float kUnit = 32768.0f;            // 2^15
+
+__global__ void sep_wnorm_kernel(const double *__restrict__ z1, const double *__restrict__ z2,
+                                 int n, float *__restrict__ wnorm) {
+    __shared__ double red[256];
+    double m = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, z1[j] * z1[j] + z2[j] * z2[j]);
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        // W = 2^e >= max |z1 - i z2| (a power of two, so scaling by it is exact)
+        int e = 0;
+        const double mx = sqrt(red[0]);
+        if (mx > 0.0 && isfinite(mx)) {
+            frexp(mx, &e);              // mx in [2^(e-1), 2^e)
+        }
+        wnorm[0] = ldexpf(1.0f, e);
+        wnorm[1] = ldexpf(1.0f, -e);
+    }
+}
+
+__global__ void sep_gtab_x5_kernel(TabArgs t) {
+    const int half_k = t.k_pad / 2;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<int64_t>(t.ncn_pad) * half_k) return;
+    const int row = static_cast<int>(i / half_k), j = static_cast<int>(i % half_k);
+    float re = 0.f, im = 0.f;
+    if (row < t.ncomp * t.nn && j < t.n_modes) {
+        const int c = row / t.nn, n = row - c * t.nn;
+        const float2 e = cis_f32(t.cov[t.kn_dim * t.n_modes + j] * t.ax_n[n]);
+        double pw = 1.0;
+        if (t.incompr) {
+            double kk = 0.0;
+            for (int d = 0; d < t.dim; ++d) {
+                const double kd = t.cov[d * t.n_modes + j];
+                kk = __dadd_rn(kk, __dmul_rn(kd, kd));
+            }
+            const double k0 = t.cov[j];
+            const double k_2 = __ddiv_rn(k0, kk);
+            pw = (c == 0) ? __dadd_rn(1.0, -__dmul_rn(k0, k_2))
+                          : -__dmul_rn(t.cov[c * t.n_modes + j], k_2);
+        }
+        re = static_cast<float>(pw * e.x);
+        im = static_cast<float>(-(pw * e.y));
+    }
+    // G1 on the 12-bit integer grid (in units of 2^15 / 2^11 = 16), G2 the f16 rest
+    const float g1r = rintf(re * 2048.0f) * 16.0f, g1i = rintf(im * 2048.0f) * 16.0f;
+    const __half2 h1 = __floats2half2_rn(g1r, g1i);
+    const __half2 h2 = __floats2half2_rn(re * kUnit - g1r, im * kUnit - g1i);
+    t.ghi[i] = *reinterpret_cast<const uint32_t *>(&h1);
+    t.glo[i] = *reinterpret_cast<const uint32_t *>(&h2);
+}
+
+struct X5Params {
+    TcParams base;
+    float lead_scale;        // 2^(bF-1)
+    float lead_unit;         // 2^15 / 2^(bF-1)
+    const float *wnorm;      // {W, 1/W}
+};
+
+// three-slice split of one component in units of 2^15
+__device__ __forceinline__ void slice3(float x, float lead_scale, float lead_unit, float &s1,
+                                       float &s2, float &s3) {
+    const float xs = x * kUnit;
+    s1 = rintf(x * lead_scale) * lead_unit;
+    const float r = xs - s1;                        // exact
+    s2 = __half2float(__float2half_rn(r));
+    s3 = r - s2;                                    // exact; rounded to f16 by the caller
+}
+
+__global__ void __launch_bounds__(X5_THREADS, 1)
+sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant__ CUtensorMap map_g2,
+              const X5Params xp) {
+    const TcParams &p = xp.base;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * X5_STAGE);
+    uint64_t *full_a = bars;            // [2] producers -> MMA (128 arrivals)
+    uint64_t *full_g = bars + 2;        // [2] TMA -> MMA (1 arrival + bytes)
+    uint64_t *empty = bars + 4;         // [2] MMA commit -> producers, TMA
+    uint64_t *cross_full = bars + 6;    // MMA commit -> epilogue (per chunk)
+    uint64_t *cross_empty = bars + 7;   // epilogue -> MMA (256 arrivals)
+    uint64_t *drain = bars + 8;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 9);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int tile = blockIdx.x;
+    const int nt = tile % p.n_tiles;
+    tile /= p.n_tiles;
+    const int mt = tile % p.m_tiles;
+    const int b = tile / p.m_tiles;
+    const int m0 = mt * BM, n0 = nt * BN;
+    const int KB = p.kb_total, KC = p.kc;
+    const int NC = (KB + KC - 1) / KC;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&full_a[s], 128);
+            mbar_init(&full_g[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(cross_full, 1);
+        mbar_init(cross_empty, 256);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 13) {
+        tmem_alloc(tmem_slot, kTmemCols);
+        tmem_relinquish();
+    }
+    if (warp == 12 && lane == 0) {
+        tma_prefetch_map(&map_g1);
+        tma_prefetch_map(&map_g2);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t t_main = tmem, t_cross = tmem + 256;
+
+    if (warp >= 12) {
+        if (warp == 12 && lane == 0) {
+            // ---- TMA: G1, G2 -------------------------------------------------
+            int issued = 0;
+            for (int kb = 0; kb < KB; ++kb) {
+                const int s = kb & 1, n = kb >> 1;
+                if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status,
+                                        kErrTimeoutEmpty))
+                    break;
+                unsigned char *st = smem + s * X5_STAGE;
+                mbar_arrive_expect_tx(&full_g[s], 2 * G_BYTES);
+                tma_load_2d(st + 3 * A_BYTES, &map_g1, &full_g[s], kb * BK, n0);
+                tma_load_2d(st + 3 * A_BYTES + G_BYTES, &map_g2, &full_g[s], kb * BK, n0);
+                ++issued;
+            }
+            if (*abort_flag)
+                for (int kb = issued > 2 ? issued - 2 : 0; kb < issued; ++kb)
+                    mbar_wait_drain(&full_g[kb & 1], (kb >> 1) & 1, p.status);
+        } else if (warp == 13 && lane == 0) {
+            // ---- MMA ---------------------------------------------------------
+            const uint32_t idesc = idesc_f16(BM, BN, false);
+            bool ok = true;
+            for (int kb = 0; kb < KB; ++kb) {
+                const int s = kb & 1, n = kb >> 1;
+                const int c = kb / KC;
+                const bool first = (kb % KC) == 0;
+                const bool last = (kb % KC) == KC - 1 || kb == KB - 1;
+                ok = mbar_wait(&full_a[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
+                if (ok) ok = mbar_wait(&full_g[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + s * X5_STAGE);
+                const uint32_t f1 = sa, f2 = sa + A_BYTES, f3 = sa + 2 * A_BYTES;
+                const uint32_t g1 = sa + 3 * A_BYTES, g2 = g1 + G_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint32_t o = kk * 32;
+                    mma_f16_ss(t_main, desc_k_sw128(f1 + o), desc_k_sw128(g1 + o), idesc,
+                               (kb > 0 || kk > 0) ? 1u : 0u);
+                }
+                if (first && c > 0) {
+                    ok = mbar_wait(cross_empty, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
+                    if (!ok) break;
+                    tc_fence_after();
+                }
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint32_t o = kk * 32;
+                    mma_f16_ss(t_cross, desc_k_sw128(f2 + o), desc_k_sw128(g1 + o), idesc,
+                               (first && kk == 0) ? 0u : 1u);
+                    mma_f16_ss(t_cross, desc_k_sw128(f1 + o), desc_k_sw128(g2 + o), idesc, 1u);
+                    mma_f16_ss(t_cross, desc_k_sw128(f2 + o), desc_k_sw128(g2 + o), idesc, 1u);
+                    mma_f16_ss(t_cross, desc_k_sw128(f3 + o), desc_k_sw128(g1 + o), idesc, 1u);
+                }
+                mma_commit(&empty[s]);
+                if (last) mma_commit(cross_full);
+            }
+            if (!ok) {
+                mma_commit(drain);
+                mbar_wait_drain(drain, 0, p.status);
+            }
+        }
+    } else if (warp >= 8) {
+        // ---- producers ---------------------------------------------------------
+        const int r = threadIdx.x - 256;
+        const int m = m0 + r;
+        const bool row_ok = m < p.nm;
+        const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
+        const uint32_t row_off = (r >> 3) * 1024 + (r & 7) * 128;
+        const float ls = xp.lead_scale, lu = xp.lead_unit;
+        for (int kb = 0; kb < KB; ++kb) {
+            const int s = kb & 1, n = kb >> 1;
+            float2 cur[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                const int j = kb * 32 + q;
+                cur[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm + m)
+                                                   : make_float2(0.f, 0.f);
+            }
+            if (n > 0 &&
+                !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status, kErrTimeoutEmpty))
+                break;
+            unsigned char *f1 = smem + s * X5_STAGE;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int j = kb * 32 + c * 4 + q;
+                    const float2 sj = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
+                    const float2 v = cmulf(cur[c * 4 + q], sj);
+                    float a1, a2, a3, b1, b2, b3;
+                    slice3(v.x, ls, lu, a1, a2, a3);
+                    slice3(v.y, ls, lu, b1, b2, b3);
+                    const __half2 h1 = __floats2half2_rn(a1, b1);
+                    const __half2 h2 = __floats2half2_rn(a2, b2);
+                    const __half2 h3 = __floats2half2_rn(a3, b3);
+                    w1[q] = *reinterpret_cast<const uint32_t *>(&h1);
+                    w2[q] = *reinterpret_cast<const uint32_t *>(&h2);
+                    w3[q] = *reinterpret_cast<const uint32_t *>(&h3);
+                }
+                const uint32_t phys = row_off + ((c ^ (r & 7)) << 4);
+                *reinterpret_cast<uint4 *>(f1 + phys) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+                *reinterpret_cast<uint4 *>(f1 + A_BYTES + phys) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+                *reinterpret_cast<uint4 *>(f1 + 2 * A_BYTES + phys) =
+                    make_uint4(w3[0], w3[1], w3[2], w3[3]);
+            }
+            fence_proxy_async_smem();
+            mbar_arrive(&full_a[s]);
+        }
+    } else {
+        // ---- epilogue ------------------------------------------------------------
+        const int q = warp & 3, h = warp >> 2;
+        const uint32_t lane_off = static_cast<uint32_t>(32 * q) << 16;
+        const int m = m0 + 32 * q + lane;
+        float tot[128];
+#pragma unroll
+        for (int i = 0; i < 128; ++i) tot[i] = 0.f;
+        bool ok = true;
+        for (int c = 0; c < NC; ++c) {
+            ok = mbar_wait(cross_full, c & 1, abort_flag, p.status, kErrTimeoutAcc);
+            if (!ok) break;
+            tc_fence_after();
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                uint32_t v[16];
+                __syncwarp();
+                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
+            }
+            if (c < NC - 1) {
+                tc_fence_before();
+                mbar_arrive(cross_empty);
+            }
+        }
+        if (ok) {
+            // the last cross commit follows every MMA: main is complete
+            const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
+            const bool row_ok = m < p.nm;
+            double *orow = p.out + static_cast<int64_t>(b) * p.batch_stride +
+                           static_cast<int64_t>(row_ok ? m : 0) * p.row_stride;
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                uint32_t v[16];
+                __syncwarp();
+                tmem_ld16(t_main + lane_off + 128 * h + 16 * g, v);
+                tmem_ld_wait();
+                const int gn0 = n0 + 128 * h + 16 * g;
+                if (row_ok && gn0 < p.ncn) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int gn = gn0 + i;
+                        if (gn < p.ncn) {
+                            const float val = (__uint_as_float(v[i]) + tot[16 * g + i]) * unscale;
+                            const int comp = gn / p.nn;
+                            orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(val);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 13) tmem_dealloc(tmem, kTmemCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -498,6 +836,7 @@ int configure_tc() {
 }  // namespace
 
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
+    const bool x5 = a.form == GSC_FORM_SEP_F16X5;
     const bool bf16 = a.form == GSC_FORM_SEP_BF16X3;
     const int dim = static_cast<int>(a.dim);
     const int N = static_cast<int>(a.n_modes);
@@ -514,8 +853,9 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int ncn_pad = n_tiles * BN;
     const int m_tiles = (nm + BM - 1) / BM;
 
-    // scratch: svec, btab, G hi, G lo
-    const size_t off_svec = 0;
+    // scratch: normaliser, svec, btab, G hi (G1), G lo (G2)
+    const size_t off_wn = 0;
+    const size_t off_svec = 1024;
     const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(N), 1024);
     const size_t off_ghi = align_up(off_btab + sizeof(float2) * static_cast<size_t>(N) * nm, 1024);
     const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
@@ -549,15 +889,19 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.btab = reinterpret_cast<float2 *>(base + off_btab);
     t.ghi = reinterpret_cast<uint32_t *>(base + off_ghi);
     t.glo = reinterpret_cast<uint32_t *>(base + off_glo);
+    t.wnorm = x5 ? reinterpret_cast<float *>(base + off_wn) : nullptr;
 
     {
         TimedLaunch tl(st);
         tl.begin(K_SEP_TABLES);
+        if (x5) sep_wnorm_kernel<<<1, 256, 0, st>>>(a.z1, a.z2, N, t.wnorm);
         const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(N) * nm;
         const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
         if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
         if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
-        if (bf16)
+        if (x5)
+            sep_gtab_x5_kernel<<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+        else if (bf16)
             sep_gtab_kernel<true><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
         else
             sep_gtab_kernel<false><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
@@ -578,7 +922,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.nn = nn;
     p.ncn = ncn;
     p.kb_total = KB;
-    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : 4;
+    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : (x5 ? 8 : 4);
     p.m_tiles = m_tiles;
     p.n_tiles = n_tiles;
     p.out = a.out;
@@ -588,8 +932,28 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.status = status;
     const int64_t grid = static_cast<int64_t>(nb) * m_tiles * n_tiles;
     if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
-    {
-        TimedLaunch tl(st);
+    TimedLaunch tl(st);
+    if (x5) {
+        // leading-slice width: the exact main sum must stay below 2^24 units;
+        // it grows like sqrt(K), so wider K gets a narrower grid
+        int bf = 9;
+        if (N > 4096) bf = 8;
+        if (N > 16384) bf = 7;
+        if (N > 65536) bf = 6;
+        X5Params xp;
+        xp.base = p;
+        xp.lead_scale = static_cast<float>(1 << (bf - 1));
+        xp.lead_unit = kUnit / xp.lead_scale;
+        xp.wnorm = t.wnorm;
+        static bool configured = false;
+        if (!configured) {
+            GSC_CUDA(cudaFuncSetAttribute(sep_x5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(kSmemX5)));
+            configured = true;
+        }
+        tl.begin(K_SEP_TC_F16X5);
+        sep_x5_kernel<<<static_cast<unsigned>(grid), X5_THREADS, kSmemX5, st>>>(mh, ml, xp);
+    } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
         if (bf16) {
             GSC_TRY(configure_tc<true>());
@@ -598,9 +962,9 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             GSC_TRY(configure_tc<false>());
             sep_tc_kernel<false><<<static_cast<unsigned>(grid), kThreadsTC, kSmemBytes, st>>>(mh, ml, p);
         }
-        tl.end();
-        GSC_CUDA(cudaGetLastError());
     }
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
     GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
     return GSC_OK;
 }

@@ -246,9 +246,11 @@ def summate_structured(cov_samples, z1, z2, axes, num_threads=None, *, form="aut
     Equal to ``summate(cov_samples, z1, z2, pos)`` with
     ``pos = np.array(np.meshgrid(*axes, indexing="ij")).reshape(dim, -1)``
     (the flattening GSTools uses for structured meshes), but the grid is never
-    expanded: with ``form="sep_f16x3"`` (or ``form="auto"`` and
-    ``tolerance >= 2e-6``) the sum runs as a separable complex contraction on
-    the tensor cores.  Returns a flat (n_points,) array.
+    expanded: with ``form="sep_f16x5"`` (or ``form="auto"`` and
+    ``tolerance >= 1e-6``) the sum runs as a separable complex contraction on
+    the tensor cores with max error below 1e-6 of the field RMS;
+    ``form="sep_f16x3"`` (``tolerance >= 1e-5``) is faster and less exact.
+    Returns a flat (n_points,) array.
     """
     return _structured_host(_native.lib.gsc_summate_structured_f64, cov_samples, z1, z2, axes,
                             num_threads, form, tolerance, timing, device, False)

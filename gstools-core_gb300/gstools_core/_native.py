@@ -27,6 +27,7 @@ FORMS = {
     "plain_libm": 2,
     "sep_f16x3": 3,
     "sep_bf16x3": 4,
+    "sep_f16x5": 5,
 }
 
 

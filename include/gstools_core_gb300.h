@@ -57,14 +57,23 @@ extern "C" {
 #define GSC_FORM_PLAIN_F64_LIBM 2  /* FP64 end to end on CUDA's sincos()    */
 #define GSC_FORM_SEP_F16X3  3  /* structured grids: separable contraction on
                                   tcgen05 tensor cores, both operands split
-                                  into f16 hi + lo, 3 products, FP32
-                                  accumulation drained every 4 k-blocks     */
-#define GSC_FORM_SEP_BF16X3 4  /* as GSC_FORM_SEP_F16X3 with bf16 terms       */
+                                  into f16 hi + lo, 3 products; max error
+                                  about 5e-6 of the field RMS               */
+#define GSC_FORM_SEP_BF16X3 4  /* as GSC_FORM_SEP_F16X3 with bf16 terms
+                                  (about 5e-5)                                */
+#define GSC_FORM_SEP_F16X5  5  /* structured grids, 5 products: the leading
+                                  product on an integer grid that the FP32
+                                  tensor-memory accumulator sums exactly,
+                                  the rest drained in chunks; max error
+                                  below 1e-6 of the field RMS               */
 
 /* ---- flags ----------------------------------------------------------- */
 #define GSC_FLAG_TIMING     1  /* record per-kernel CUDA-event timings      */
 
-/* Options.  Pass NULL for the defaults (form AUTO at tolerance 1e-12,
+/* AUTO on structured grids picks GSC_FORM_SEP_F16X3 for tolerance >= 1e-5,
+ * GSC_FORM_SEP_F16X5 for tolerance >= 1e-6, else GSC_FORM_PLAIN_F64.
+ *
+ * Options.  Pass NULL for the defaults (form AUTO at tolerance 1e-12,
  * current device, library stream for host-pointer calls and the legacy
  * default stream for device-pointer calls). */
 typedef struct gsc_opts {
