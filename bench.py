@@ -238,6 +238,55 @@ def max_over_ranks(world, value: float) -> float:
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def default_form(w):
+    return "sep_f16x5" if w["axes"] is not None else "plain"
+
+
+def make_device_step(gsc, torch, w, form, dev, stream):
+    """Returns (step(timing) -> None, out_tensor) running the workload on the device."""
+    P = n_points(w)
+    cov_d = torch.from_numpy(np.ascontiguousarray(w["cov"])).to(dev)
+    z1_d = torch.from_numpy(w["z1"]).to(dev)
+    z2_d = torch.from_numpy(w["z2"]).to(dev)
+    nout = w["dim"] if w["incompr"] else 1
+    out_d = torch.empty((nout, P) if w["incompr"] else (P,), dtype=torch.float64, device=dev)
+    if w["axes"] is not None and form.startswith("sep"):
+        axes_d = tuple(torch.from_numpy(a).to(dev) for a in w["axes"])
+        call = gsc.summate_incompr_structured_device if w["incompr"] else gsc.summate_structured_device
+
+        def step(timing=False):
+            call(cov_d, z1_d, z2_d, axes_d, out_d, form=form, stream=stream.cuda_stream,
+                 timing=timing)
+    else:
+        pos_h = w["pos"] if w["pos"] is not None else flat_grid(w["axes"])
+        pos_d = torch.from_numpy(pos_h).to(dev)
+        call = gsc.summate_incompr_device if w["incompr"] else gsc.summate_device
+
+        def step(timing=False):
+            call(cov_d, z1_d, z2_d, pos_d, out_d, form=form, stream=stream.cuda_stream,
+                 timing=timing)
+    return step, out_d
+
+
+def timed_steps(torch, gsc, step, stream, steps, flush):
+    """Per-step CUDA-event times (L2 flushed before each step) and kernel timings."""
+    per_step, kern, launches = [], {}, 0
+    for _ in range(steps):
+        flush.fill_(1)                       # evict L2 (129 MB) between steps
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(timing=True)
+        b.record(stream)
+        b.synchronize()
+        per_step.append(a.elapsed_time(b))
+        tl = gsc.last_timings()
+        launches += len(tl)
+        for name, ms in tl:
+            kern.setdefault(name, []).append(ms)
+    return per_step, kern, launches
+
+
 def run_ours(args, world, rank, local):
     import torch
     import gstools_core as gsc
@@ -247,58 +296,34 @@ def run_ours(args, world, rank, local):
     w = workload(args.workload)
     P, N = n_points(w), w["cov"].shape[1]
     work = float(P) * N
-    form = args.form
+    form = default_form(w) if args.form == "auto" else args.form
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
-    pos_h = w["pos"] if w["pos"] is not None else flat_grid(w["axes"])
-    cov_d = torch.from_numpy(np.ascontiguousarray(w["cov"])).to(dev)
-    z1_d = torch.from_numpy(w["z1"]).to(dev)
-    z2_d = torch.from_numpy(w["z2"]).to(dev)
-    pos_d = torch.from_numpy(pos_h).to(dev)
-    nout = w["dim"] if w["incompr"] else 1
-    out_d = torch.empty((nout, P) if w["incompr"] else (P,), dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    call = gsc.summate_incompr_device if w["incompr"] else gsc.summate_device
-
-    def step(timing=False):
-        call(cov_d, z1_d, z2_d, pos_d, out_d, form=form, stream=stream.cuda_stream,
-             timing=timing)
+    step, out_d = make_device_step(gsc, torch, w, form, dev, stream)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    gsc.device_status()
 
     # ---- timed region ------------------------------------------------------
-    per_step, kern = [], {}
-    launches = 0
     with ClockSampler(local) as clk:
         barrier(world)
         torch.cuda.synchronize()
         t_wall = time.perf_counter()
-        for _ in range(args.steps):
-            flush.fill_(1)                       # evict L2 (129 MB) between steps
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            step(timing=True)
-            b.record(stream)
-            b.synchronize()
-            per_step.append(a.elapsed_time(b))
-            tl = gsc.last_timings()
-            launches += len(tl)
-            for name, ms in tl:
-                kern.setdefault(name, []).append(ms)
+        per_step, kern, launches = timed_steps(torch, gsc, step, stream, args.steps, flush)
         torch.cuda.synchronize()
         barrier(world)
         t_wall = time.perf_counter() - t_wall
+    gsc.device_status()
     ms_step = max_over_ranks(world, float(np.mean(per_step)))
     value = work * world / (ms_step * 1e-3) / 1e9
 
     # ---- dominant kernel roofline ------------------------------------------
     dom = max(kern, key=lambda k: sum(kern[k]))
-    per_launch = kern[dom]
-    launches_per_step = len(per_launch) / args.steps
-    dom_ms = float(np.mean(per_launch))
+    launches_per_step = len(kern[dom]) / args.steps
+    dom_ms = float(np.mean(kern[dom]))
     roof = roofline(args, w, dom, dom_ms, launches_per_step)
 
     # ---- parity spot check of this very output against the oracle ----------
@@ -306,7 +331,7 @@ def run_ours(args, world, rank, local):
     if not args.no_check:
         rng = np.random.default_rng(7)
         idx = np.sort(rng.choice(P, size=min(P, 2048), replace=False))
-        pos_s = sample_points(w, idx) if w["pos"] is None else np.ascontiguousarray(w["pos"][:, idx])
+        pos_s = sample_points(w, idx)
         fn = oracle.summator_incompr if w["incompr"] else oracle.summator
         ref = fn(w["cov"], w["z1"], w["z2"], pos_s, num_threads=host_cores())
         got = out_d.cpu().numpy()
@@ -314,24 +339,47 @@ def run_ours(args, world, rank, local):
         rms = float(np.sqrt(np.mean(ref ** 2)))
         err = {"max_abs_over_rms": float(np.max(np.abs(got - ref)) / rms),
                "rms_over_rms": float(np.sqrt(np.mean((got - ref) ** 2)) / rms),
-               "points_checked": int(len(idx))}
+               "points_checked": int(len(idx)), "reference": "oracle (field.rs restatement), FP64"}
+
+    # ---- the plain FP64 kernel on the same workload (the comparison arm) ---
+    plain = None
+    if form != "plain" and not args.no_plain:
+        pstep, _ = make_device_step(gsc, torch, w, "plain", dev, stream)
+        pstep()
+        torch.cuda.synchronize()
+        pt, pk, _ = timed_steps(torch, gsc, pstep, stream, 1, flush)
+        pms = max_over_ranks(world, float(np.mean(pt)))
+        plain = {"value": work * world / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
+                 "steps": 1, "path": "plain FP64 kernel on the flattened meshgrid"
+                 if w["pos"] is None else "plain FP64 kernel",
+                 "kernels_ms": {k: float(np.mean(v)) for k, v in pk.items()}}
+        plain["speedup_of_chosen_form"] = value / plain["value"]
 
     # ---- e2e through the public host API -----------------------------------
     e2e = None
     if not args.no_e2e:
-        host_call = gsc.summate_incompr if w["incompr"] else gsc.summate
-        host_call(w["cov"], w["z1"], w["z2"], pos_h, form=form)   # warm the staging
+        nout = w["dim"] if w["incompr"] else 1
+        if w["axes"] is not None and form.startswith("sep"):
+            host_call = gsc.summate_incompr_structured if w["incompr"] else gsc.summate_structured
+            host_args = (w["cov"], w["z1"], w["z2"], w["axes"])
+            h2d = (w["cov"].size + 2 * N + sum(len(a) for a in w["axes"])) * 8
+        else:
+            pos_h = w["pos"] if w["pos"] is not None else flat_grid(w["axes"])
+            host_call = gsc.summate_incompr if w["incompr"] else gsc.summate
+            host_args = (w["cov"], w["z1"], w["z2"], pos_h)
+            h2d = (w["cov"].size + 2 * N + pos_h.size) * 8
+        host_call(*host_args, form=form)      # warm the staging buffers
         ts = []
         for _ in range(max(1, min(args.steps, 3))):
             barrier(world)
             t0 = time.perf_counter()
-            host_call(w["cov"], w["z1"], w["z2"], pos_h, form=form)
+            host_call(*host_args, form=form)
             ts.append(time.perf_counter() - t0)
         t_e2e = max_over_ranks(world, float(np.mean(ts)))
-        h2d = (w["cov"].size + 2 * N + pos_h.size) * 8
         e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nout * P * 8),
-               "ms_per_step": t_e2e * 1e3, "api": "gstools_core." + host_call.__name__}
+               "ms_per_step": t_e2e * 1e3, "api": "gstools_core." + host_call.__name__,
+               "timing": "host wall clock around the synchronous call"}
 
     # ---- CPU baseline (rank 0, N=1 only) -----------------------------------
     cpu = None
@@ -346,12 +394,15 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded numpy default_rng)",
+        "dtype": "f16 split operands, f32 accumulation, f64 output" if form.startswith("sep")
+                 else "f64",
+        "data": "synthetic (seeded numpy default_rng)",
         "config": {"workload": args.workload, "desc": w["desc"], "points": P, "modes": N,
-                   "form": form, "path": "flattened meshgrid" if w["pos"] is None else "points",
+                   "form": form,
                    "l2": "flushed by a 256 MiB write before every timed step",
                    "wall_s": t_wall},
         "error_vs_oracle": err,
+        "plain_fp64": plain,
         "kernels_ms_per_step": {k: float(np.sum(v) / args.steps) for k, v in kern.items()},
         "gpu_launches": int(launches),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
@@ -369,13 +420,33 @@ def measured_peaks():
 
 
 def roofline(args, w, dom, dom_ms, launches_per_step):
-    """Roofline entry for the dominant kernel.  The plain summators are bound by
-    the FP64 pipe: algorithmic FLOPs per point*mode = 2d+3 (+1 sincos) for the
-    scalar field and 4d+2 for the incompressible one."""
+    """Roofline entry for the dominant kernel.
+
+    Tensor-core forms (bound "tensor"): FLOPs per launch = products x 2 x
+    points x 2N (the real GEMM has K = 2N per output component; "products" is
+    the number of split products the kernel issues: 5 for sep_f16x5, 3 for
+    sep_f16x3 / sep_bf16x3), against the measured dense 16-bit peak.
+    Plain FP64 (bound "fp64"): 2d+3 (scalar) or 4d+2 (incompr) FLOPs per
+    point*mode plus one sincos, against cuBLAS DGEMM's measured FP64 rate."""
     import torch
     P, N, d = n_points(w), w["cov"].shape[1], w["dim"]
-    flops_pm = (4 * d + 2) if w["incompr"] else (2 * d + 3)
+    nout = d if w["incompr"] else 1
     per_launch_units = P * N / max(launches_per_step, 1)
+    if dom.startswith("sep_tc"):
+        products = {"sep_tc_f16x5": 5, "sep_tc_f16x3": 3, "sep_tc_bf16x3": 3}[dom]
+        flops = products * 2.0 * per_launch_units * 2 * nout
+        achieved = flops / (dom_ms * 1e-3) / 1e12
+        peaks = measured_peaks()
+        peak = peaks.get("bf16_tflops")
+        how = "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS bf16; f16 runs at the same rate)"
+        if peak is None:
+            peak, how = 1900.0, "fallback 1.9 PFLOP/s"
+        return {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": how,
+                "algorithmic_tflops_single_product": achieved / products,
+                "note": f"{products} split products x 2 x points x 2N FLOPs per launch"}
+    flops_pm = (4 * d + 2) if w["incompr"] else (2 * d + 3)
     achieved = flops_pm * per_launch_units / (dom_ms * 1e-3) / 1e12
     peak, how = fp64_peak(torch)
     return {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
@@ -448,6 +519,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -458,16 +458,19 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 //   F (rows, |F| <= 1 after dividing s by W)  = F1 + F2 + F3
 //   G (columns, |G| <= 1)                     = G1 + G2
 // in units of 2^15:  F1 = 2^15 * rint(F * 2^(bF-1)) / 2^(bF-1)  (bF-bit integer grid),
-//                    G1 = 2^15 * rint(G * 2^11) / 2^11           (12-bit integer grid),
+//                    G1 = 2^15 * rint(G * 2^10) / 2^10           (11-bit integer grid),
 // F2 = f16(F*2^15 - F1), F3 = f16(F*2^15 - F1 - F2), G2 = f16(G*2^15 - G1).
-// Every product F1*G1 is an integer multiple of 2^(15+15-(bF-1)-11); their
-// sum stays far below 2^24 multiples, so the "main" TMEM accumulator adds
-// them EXACTLY whatever the hardware rounding.  The four cross products
-// F2G1 + F1G2 + F2G2 + F3G1 (about 2^-9 of the field) go to a second TMEM
-// accumulator that the epilogue drains every KC k-blocks into FP32 totals
-// held in registers, so their rounding never builds up at full magnitude.
-// Representation: F to 2^-31, G to 2^-23 relative; products F2G3, F3G2 ...
-// below 2^-30 are dropped.
+// Every product F1*G1 is an integer multiple of 2^(30-(bF-1)-10) ("counts");
+// bF (3..9) is picked on the device so that six standard deviations of the
+// field stay below 2^23 counts, so the "main" TMEM accumulator adds them
+// EXACTLY whatever the hardware rounding.  (Exactness holds for fields of
+// random modes, as GSTools draws them; a field value beyond ~12 standard
+// deviations would start rounding the main sum.)  The four cross products
+// F2G1 + F1G2 + F2G2 + F3G1 (about 2^-7 of the field) go to a second TMEM
+// accumulator that the epilogue drains every KC = 4 k-blocks into FP32
+// totals held in registers, so their rounding never builds up at full
+// magnitude.  Representation: F to about 2^-29, G to 2^-22 relative; the
+// product F3G2 (below 2^-28) is dropped.
 //
 // Warp roles (16 warps, 512 threads, 128 registers each):
 //   warps 0-7   epilogue: warp w reads TMEM lanes 32*(w%4).., columns
@@ -481,27 +484,46 @@ constexpr int X5_THREADS = 512;
 constexpr int X5_STAGE = 3 * A_BYTES + 2 * G_BYTES;
 constexpr size_t kSmemX5 = 2 * X5_STAGE + 1024 + 256;
 constexpr float kUnit = 32768.0f;            // 2^15
+constexpr int kLeadBitsG = 11;               // G1 grid: 2^15 * rint(G * 2^10) / 2^10
 
+// Normaliser and leading-grid width of the x5 form, written to wnorm[0..3]:
+//   W = 2^e >= max |z1 - i z2|  (so s / W is exact and |F| <= 1),
+//   the leading F grid 2^(bF-1) with bF chosen so that the expected extreme
+//   of the exact main sum, about 6 * sqrt(sum |w|^2 / 2) / W * 2^(bF+bG-2)
+//   counts (6 standard deviations of the field), stays below 2^23 counts
+//   with bG = 11: one bit of headroom under FP32's 2^24.
 __global__ void sep_wnorm_kernel(const double *__restrict__ z1, const double *__restrict__ z2,
                                  int n, float *__restrict__ wnorm) {
-    __shared__ double red[256];
-    double m = 0.0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, z1[j] * z1[j] + z2[j] * z2[j]);
-    red[threadIdx.x] = m;
+    __shared__ double red_max[256], red_sum[256];
+    double m = 0.0, sum = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double a = z1[j] * z1[j] + z2[j] * z2[j];
+        m = fmax(m, a);
+        sum += a;
+    }
+    red_max[threadIdx.x] = m;
+    red_sum[threadIdx.x] = sum;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+        if (threadIdx.x < o) {
+            red_max[threadIdx.x] = fmax(red_max[threadIdx.x], red_max[threadIdx.x + o]);
+            red_sum[threadIdx.x] += red_sum[threadIdx.x + o];
+        }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        // W = 2^e >= max |z1 - i z2| (a power of two, so scaling by it is exact)
         int e = 0;
-        const double mx = sqrt(red[0]);
-        if (mx > 0.0 && isfinite(mx)) {
-            frexp(mx, &e);              // mx in [2^(e-1), 2^e)
-        }
-        wnorm[0] = ldexpf(1.0f, e);
-        wnorm[1] = ldexpf(1.0f, -e);
+        const double mx = sqrt(red_max[0]);
+        if (mx > 0.0 && isfinite(mx)) frexp(mx, &e);           // mx in [2^(e-1), 2^e)
+        const double W = ldexp(1.0, e);
+        const double typ = 6.0 * sqrt(fmax(red_sum[0], 1e-300) * 0.5) / W;
+        // 2^(bF - 1 + kLeadBitsG - 1) * typ <= 2^23
+        int bf = static_cast<int>(floor(23.0 + 2.0 - kLeadBitsG - log2(fmax(typ, 1.0))));
+        bf = bf < 3 ? 3 : (bf > 9 ? 9 : bf);
+        wnorm[0] = static_cast<float>(W);
+        wnorm[1] = static_cast<float>(1.0 / W);
+        wnorm[2] = ldexpf(1.0f, bf - 1);                        // lead_scale
+        wnorm[3] = kUnit / ldexpf(1.0f, bf - 1);                // lead_unit
     }
 }
 
@@ -529,8 +551,9 @@ __global__ void sep_gtab_x5_kernel(TabArgs t) {
         re = static_cast<float>(pw * e.x);
         im = static_cast<float>(-(pw * e.y));
     }
-    // G1 on the 12-bit integer grid (in units of 2^15 / 2^11 = 16), G2 the f16 rest
-    const float g1r = rintf(re * 2048.0f) * 16.0f, g1i = rintf(im * 2048.0f) * 16.0f;
+    // G1 on the 11-bit integer grid (units of 2^15 / 2^10 = 32), G2 the f16 rest
+    const float gs = static_cast<float>(1 << (kLeadBitsG - 1)), gu = kUnit / gs;
+    const float g1r = rintf(re * gs) * gu, g1i = rintf(im * gs) * gu;
     const __half2 h1 = __floats2half2_rn(g1r, g1i);
     const __half2 h2 = __floats2half2_rn(re * kUnit - g1r, im * kUnit - g1i);
     t.ghi[i] = *reinterpret_cast<const uint32_t *>(&h1);
@@ -539,9 +562,7 @@ __global__ void sep_gtab_x5_kernel(TabArgs t) {
 
 struct X5Params {
     TcParams base;
-    float lead_scale;        // 2^(bF-1)
-    float lead_unit;         // 2^15 / 2^(bF-1)
-    const float *wnorm;      // {W, 1/W}
+    const float *wnorm;      // {W, 1/W, 2^(bF-1), 2^15 / 2^(bF-1)}
 };
 
 // three-slice split of one component in units of 2^15
@@ -676,7 +697,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
         const bool row_ok = m < p.nm;
         const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
         const uint32_t row_off = (r >> 3) * 1024 + (r & 7) * 128;
-        const float ls = xp.lead_scale, lu = xp.lead_unit;
+        const float ls = xp.wnorm[2], lu = xp.wnorm[3];
         for (int kb = 0; kb < KB; ++kb) {
             const int s = kb & 1, n = kb >> 1;
             float2 cur[32];
@@ -922,7 +943,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.nn = nn;
     p.ncn = ncn;
     p.kb_total = KB;
-    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : (x5 ? 8 : 4);
+    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : 4;
     p.m_tiles = m_tiles;
     p.n_tiles = n_tiles;
     p.out = a.out;
@@ -934,16 +955,8 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
     TimedLaunch tl(st);
     if (x5) {
-        // leading-slice width: the exact main sum must stay below 2^24 units;
-        // it grows like sqrt(K), so wider K gets a narrower grid
-        int bf = 9;
-        if (N > 4096) bf = 8;
-        if (N > 16384) bf = 7;
-        if (N > 65536) bf = 6;
         X5Params xp;
         xp.base = p;
-        xp.lead_scale = static_cast<float>(1 << (bf - 1));
-        xp.lead_unit = kUnit / xp.lead_scale;
         xp.wnorm = t.wnorm;
         static bool configured = false;
         if (!configured) {
