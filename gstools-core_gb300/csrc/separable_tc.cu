@@ -472,7 +472,8 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 // magnitude.  Representation: F to about 2^-29, G to 2^-22 relative; the
 // product F3G2 (below 2^-28) is dropped.
 //
-// Warp roles (16 warps, 512 threads, 128 registers each):
+// Warp roles (16 warps, 512 threads launched at 128 registers each, then
+// re-split with setmaxnreg: epilogue 160, producers 152, TMA/MMA 40):
 //   warps 0-7   epilogue: warp w reads TMEM lanes 32*(w%4).., columns
 //               128*(w/4) .. +128 (cross totals live in 128 registers)
 //   warps 8-11  producers: F1, F2, F3 tiles of each k-block
@@ -481,6 +482,9 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 // Stages: F1/F2/F3 3 x 16 KB + G1/G2 2 x 32 KB = 112 KB, two stages.
 // ---------------------------------------------------------------------------
 constexpr int X5_THREADS = 512;
+constexpr int X5_EPI_REGS = 160, X5_PROD_REGS = 152, X5_CTRL_REGS = 40;
+static_assert(4 * 32 * (2 * X5_EPI_REGS + X5_PROD_REGS + X5_CTRL_REGS) <= X5_THREADS * 128,
+              "setmaxnreg split exceeds the registers the block is launched with");
 constexpr int X5_STAGE = 3 * A_BYTES + 2 * G_BYTES;
 constexpr size_t kSmemX5 = 2 * X5_STAGE + 1024 + 256;
 constexpr float kUnit = 32768.0f;            // 2^15
@@ -629,6 +633,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
     const uint32_t t_main = tmem, t_cross = tmem + 256;
 
     if (warp >= 12) {
+        regs_dec<X5_CTRL_REGS>();
         if (warp == 12 && lane == 0) {
             // ---- TMA: G1, G2 -------------------------------------------------
             int issued = 0;
@@ -691,22 +696,30 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
             }
         }
     } else if (warp >= 8) {
+        regs_inc<X5_PROD_REGS>();
         // ---- producers ---------------------------------------------------------
+        // B-table values of k-block kb + 1 are loaded while k-block kb is
+        // sliced, so the L2 latency overlaps the conversion work.
         const int r = threadIdx.x - 256;
         const int m = m0 + r;
         const bool row_ok = m < p.nm;
         const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
         const uint32_t row_off = (r >> 3) * 1024 + (r & 7) * 128;
         const float ls = xp.wnorm[2], lu = xp.wnorm[3];
-        for (int kb = 0; kb < KB; ++kb) {
-            const int s = kb & 1, n = kb >> 1;
-            float2 cur[32];
+        float2 cur[32];
+        auto load_block = [&](int kb, float2 (&dst)[32]) {
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
                 const int j = kb * 32 + q;
-                cur[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm + m)
+                dst[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm + m)
                                                    : make_float2(0.f, 0.f);
             }
+        };
+        load_block(0, cur);
+        for (int kb = 0; kb < KB; ++kb) {
+            const int s = kb & 1, n = kb >> 1;
+            float2 nxt[32];
+            if (kb + 1 < KB) load_block(kb + 1, nxt);
             if (n > 0 &&
                 !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status, kErrTimeoutEmpty))
                 break;
@@ -737,8 +750,11 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
             }
             fence_proxy_async_smem();
             mbar_arrive(&full_a[s]);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) cur[q] = nxt[q];
         }
     } else {
+        regs_inc<X5_EPI_REGS>();
         // ---- epilogue ------------------------------------------------------------
         const int q = warp & 3, h = warp >> 2;
         const uint32_t lane_off = static_cast<uint32_t>(32 * q) << 16;
@@ -752,13 +768,13 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
             if (!ok) break;
             tc_fence_after();
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                uint32_t v[16];
+            for (int g = 0; g < 16; ++g) {
+                uint32_t v[8];
                 __syncwarp();
-                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, v);
+                tmem_ld8(t_cross + lane_off + 128 * h + 8 * g, v);
                 tmem_ld_wait();
 #pragma unroll
-                for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
+                for (int i = 0; i < 8; ++i) tot[8 * g + i] += __uint_as_float(v[i]);
             }
             if (c < NC - 1) {
                 tc_fence_before();
@@ -772,18 +788,18 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
             double *orow = p.out + static_cast<int64_t>(b) * p.batch_stride +
                            static_cast<int64_t>(row_ok ? m : 0) * p.row_stride;
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                uint32_t v[16];
+            for (int g = 0; g < 16; ++g) {
+                uint32_t v[8];
                 __syncwarp();
-                tmem_ld16(t_main + lane_off + 128 * h + 16 * g, v);
+                tmem_ld8(t_main + lane_off + 128 * h + 8 * g, v);
                 tmem_ld_wait();
-                const int gn0 = n0 + 128 * h + 16 * g;
+                const int gn0 = n0 + 128 * h + 8 * g;
                 if (row_ok && gn0 < p.ncn) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
+                    for (int i = 0; i < 8; ++i) {
                         const int gn = gn0 + i;
                         if (gn < p.ncn) {
-                            const float val = (__uint_as_float(v[i]) + tot[16 * g + i]) * unscale;
+                            const float val = (__uint_as_float(v[i]) + tot[8 * g + i]) * unscale;
                             const int comp = gn / p.nn;
                             orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(val);
                         }
