@@ -218,6 +218,12 @@ def dist_setup():
     return world, rank, local
 
 
+def shard_range(n_points: int, rank: int, world: int):
+    """Contiguous point range [lo, hi) of `rank`: points are independent, so
+    a multi-GPU run needs no collective on the data path."""
+    return n_points * rank // world, n_points * (rank + 1) // world
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
