@@ -641,6 +641,57 @@ int gsc_summate_incompr_dev(const double *cov, const double *z1, const double *z
     return dev_plain(cov, z1, z2, pos, dim, n_modes, n_points, out, true, opts);
 }
 
+int gsc_summate_dev_noalloc(const double *cov, const double *z1, const double *z2,
+                            const double *pos, int64_t dim, int64_t n_modes, int64_t n_points,
+                            double *out, const gsc_opts *opts) {
+    Resolved ro;
+    GSC_TRY(resolve_opts(opts, &ro));
+    GSC_TRY(check_sizes(dim, n_modes, n_points));
+    if (dim < 1 || dim > 3)
+        return set_error(GSC_ERR_DIM, "gsc_summate_dev_noalloc supports dimensions 1, 2 and 3");
+    if (ro.form != GSC_FORM_AUTO && ro.form != GSC_FORM_PLAIN_F64)
+        return set_error(GSC_ERR_INVALID, "gsc_summate_dev_noalloc runs the plain FP64 form only");
+    if (n_modes > kNoAllocModes)
+        return set_error(GSC_ERR_INVALID, "gsc_summate_dev_noalloc takes at most " +
+                                              std::to_string(kNoAllocModes) + " modes per call");
+    GSC_TRY(need_ptr(cov, dim * n_modes > 0, "cov_samples"));
+    GSC_TRY(need_ptr(z1, n_modes > 0, "z1"));
+    GSC_TRY(need_ptr(z2, n_modes > 0, "z2"));
+    GSC_TRY(need_ptr(pos, dim * n_points > 0, "pos"));
+    GSC_TRY(need_ptr(out, n_points > 0, "out"));
+    if (n_points == 0) return GSC_OK;
+    // no library context here: its creation allocates (stream, status word)
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return set_error(GSC_ERR_NO_DEVICE, "no usable CUDA device; this library has no CPU path");
+    }
+    int device = ro.device;
+    if (device < 0) GSC_CUDA(cudaGetDevice(&device));
+    if (device >= count) return set_error(GSC_ERR_INVALID, "device ordinal out of range");
+    DeviceGuard g;
+    GSC_TRY(g.set(device));
+    GSC_TRY(check_device_ptr(cov, "cov_samples"));
+    GSC_TRY(check_device_ptr(z1, "z1"));
+    GSC_TRY(check_device_ptr(z2, "z2"));
+    GSC_TRY(check_device_ptr(pos, "pos"));
+    GSC_TRY(check_device_ptr(out, "out"));
+    PlainArgs a;
+    a.cov = cov;
+    a.z1 = z1;
+    a.z2 = z2;
+    a.pos = pos;
+    a.dim = dim;
+    a.n_modes = n_modes;
+    a.n_points = n_points;
+    a.incompr = false;
+    a.out = out;
+    a.out_sd = n_points;
+    a.out_sp = 1;
+    a.variant = 0;
+    return plain_noalloc_run(device, a, ro.stream);
+}
+
 int gsc_device_status(int32_t device) {
     DeviceCtx *ctx = nullptr;
     GSC_TRY(get_ctx(device, &ctx));

@@ -99,6 +99,11 @@ struct PlainArgs {
 };
 int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st);
 
+// Allocation-free scalar summator (plain.cu): per-mode tables in a fixed
+// device array of kNoAllocModes modes; `device` must be current.
+constexpr int64_t kNoAllocModes = 1024;
+int plain_noalloc_run(int device, const PlainArgs &a, cudaStream_t st);
+
 // ---- separable tensor-core summators on structured grids (separable_tc.cu) --
 struct SepArgs {
     const double *cov;        // (dim, n_modes) row-major, device

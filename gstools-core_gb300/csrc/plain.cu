@@ -32,6 +32,8 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "internal.h"
 
@@ -458,6 +460,78 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
     }
     GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
     return GSC_OK;
+}
+
+}  // namespace gsc
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the scalar FP64 summator.
+//
+// Some callers must not let a library allocate device memory: a host whose
+// framework allocator already owns the whole device (a cudaMalloc from the
+// library would fail or fragment that pool), a real-time loop that cannot
+// afford to block in the driver's allocator, or a plug-in host that only
+// permits memory from its own arena.  For them the per-mode tables of the
+// plain kernel live in one fixed array compiled into the library, so a call
+// allocates nothing; the caller passes the inputs and the output as usual.
+//
+// The array (4 MiB of tables + 96 KiB of mode records, enough for 1024
+// modes) is held on every GPU that loads the library until the process
+// exits.  All calls share it and it keeps the last call's contents; every
+// call rewrites the part it reads, so nothing has to start at zero.  Calls
+// whose kernels overlap on the GPU (different streams, no ordering between
+// them) race on the array.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char
+    gsc_noalloc_scratch[gsc::kNoAllocModes * 256 * 16 + gsc::kNoAllocModes * 12 * 8];
+
+namespace gsc {
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[64] = {nullptr};
+
+// The device address of the fixed array on the current device, looked up
+// once per device.  Host code cannot use the array's name as a device
+// address: outside device code it names a host-side stand-in.
+static int noalloc_address(int device, void **addr) {
+    if (device < 0 || device >= 64) return set_error(GSC_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, gsc_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(fixed table array)");
+        g_noalloc_addr[device] = p;
+    }
+    *addr = g_noalloc_addr[device];
+    return GSC_OK;
+}
+
+int plain_noalloc_run(int device, const PlainArgs &a, cudaStream_t st) {
+    constexpr int R = 4;
+    const int64_t P = a.n_points, N = a.n_modes;
+    if (N > kNoAllocModes)
+        return set_error(GSC_ERR_INVALID, "gsc_summate_dev_noalloc takes at most " +
+                                              std::to_string(kNoAllocModes) +
+                                              " modes per call (its fixed table array holds "
+                                              "that many); split the modes over several calls "
+                                              "or use gsc_summate_dev");
+    if (P == 0) return GSC_OK;
+    void *scratch = nullptr;
+    GSC_TRY(noalloc_address(device, &scratch));
+    double2 *wtab = static_cast<double2 *>(scratch);
+    double *rec = reinterpret_cast<double *>(static_cast<unsigned char *>(scratch) +
+                                             kNoAllocModes * kM * sizeof(double2));
+    const int64_t bx = (P + kThreads * R - 1) / (kThreads * R);
+    if (bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
+    if (N > 0) {
+        mode_table_kernel<<<static_cast<unsigned>(N), kM, 0, st>>>(a.cov, a.z1, a.z2, a.dim, N, 0,
+                                                                      0, 1, wtab, rec);
+        GSC_CUDA(cudaGetLastError());
+    }
+    const size_t smem = 2 * (kTileModes * kM * 16 + kTileModes * kRec * 8);
+    // one mode split: every point's modes are summed by one thread, in order
+    return dispatch_dim<R, false, false>(a.dim, dim3(static_cast<unsigned>(bx), 1), smem, st,
+                                         a.pos, P, wtab, rec, N, N, 0, a.out, P, a.out_sp, 0);
 }
 
 }  // namespace gsc

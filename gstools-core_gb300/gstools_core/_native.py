@@ -67,6 +67,7 @@ SIGNATURES = {
                                                _I64, _I64, _I64, _I64, _P, _I64, _I64, _OPTS]),
     "gsc_summate_incompr_dev": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _OPTS]),
     "gsc_device_status": (ctypes.c_int, [_I32]),
+    "gsc_summate_dev_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _I64, _P, _OPTS]),
     "gsc_summate_structured_f64": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P, _I64, _I64, _I64,
                                                   _P, _I64, _I64, _P, _I64, _I64, _P, _I64, _I64,
                                                   _P, _OPTS]),

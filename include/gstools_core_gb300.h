@@ -128,6 +128,25 @@ int gsc_summate_dev(const double *cov, const double *z1, const double *z2,
                     const double *pos, int64_t dim, int64_t n_modes,
                     int64_t n_points, double *out, const gsc_opts *opts);
 
+/* Allocation-free form of gsc_summate_dev.  It has no counterpart in the
+ * reference.  It is for callers that may not have a library allocate device
+ * memory -- a host whose own allocator owns the whole GPU, a real-time loop
+ * that cannot block in the driver's allocator, a plug-in host that hands out
+ * memory only from its arena.  The call allocates nothing: the plain FP64
+ * kernel's per-mode tables live in a fixed array inside the library
+ * (4 MiB + 96 KiB, held on every GPU that loads the library until exit), so
+ * a call takes at most 1024 modes and returns GSC_ERR_INVALID beyond that.
+ * Inputs and output are the caller's device arrays, as for gsc_summate_dev;
+ * dim in {1, 2, 3}; forms AUTO or PLAIN_F64 only.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and
+ * configures the kernel; make that first call before any stream capture.
+ * All calls share the array, which keeps the last call's contents; kernels
+ * of calls that overlap on the GPU race on it, so order such calls on one
+ * stream or with events. */
+int gsc_summate_dev_noalloc(const double *cov, const double *z1, const double *z2,
+                            const double *pos, int64_t dim, int64_t n_modes,
+                            int64_t n_points, double *out, const gsc_opts *opts);
+
 /* ---- incompressible vector field: src/field.rs:97-182 ----------------- */
 /* u[i, p] = sum_j p_i(k_j) (z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)),
  * p(k) = e_1 - k k_0 / |k|^2, dim in {2, 3}; out (dim, n_points) written
