@@ -160,6 +160,7 @@ struct TabArgs {
     int kb_dim, km_dim, kn_dim;  // which k component goes with each axis
     int nb, nm, nn, ncomp, incompr;
     int k_pad;                   // K elements per G row (multiple of 64)
+    int nm_ld;                   // B-table row length (nm rounded up to 16)
     int ncn_pad;                 // G rows (multiple of BN)
     float2 *svec;                // [nb][n_modes]
     float2 *btab;                // [n_modes][nm]
@@ -183,11 +184,14 @@ __global__ void sep_svec_kernel(TabArgs t) {
     t.svec[i] = w;
 }
 
+// B table [n_modes][nm_ld]; columns nm .. nm_ld-1 are zero padding (TMA
+// tiles of the x5 form read whole 128-row blocks).
 __global__ void sep_btab_kernel(TabArgs t) {
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= static_cast<int64_t>(t.n_modes) * t.nm) return;
-    const int j = static_cast<int>(i / t.nm), m = static_cast<int>(i % t.nm);
-    t.btab[i] = cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m]);
+    if (i >= static_cast<int64_t>(t.n_modes) * t.nm_ld) return;
+    const int j = static_cast<int>(i / t.nm_ld), m = static_cast<int>(i % t.nm_ld);
+    t.btab[i] = m < t.nm ? cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m])
+                         : make_float2(0.f, 0.f);
 }
 
 template <bool BF16>
@@ -227,8 +231,8 @@ __global__ void sep_gtab_kernel(TabArgs t) {
 // ---------------------------------------------------------------------------
 struct TcParams {
     const float2 *svec;     // [nb][n_modes]
-    const float2 *btab;     // [n_modes][nm]
-    int n_modes, nm, nb, nn, ncn;   // ncn = ncomp * nn valid G rows
+    const float2 *btab;     // [n_modes][nm_ld]
+    int n_modes, nm, nm_ld, nb, nn, ncn;   // ncn = ncomp * nn valid G rows
     int kb_total, kc;               // k-blocks, k-blocks per accumulation chunk
     int m_tiles, n_tiles;
     double *out;
@@ -358,7 +362,7 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
                 const int j = kb * 32 + q;
-                dst[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm + m)
+                dst[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm_ld + m)
                                                    : make_float2(0.f, 0.f);
             }
         };
@@ -485,8 +489,6 @@ constexpr int X5_THREADS = 512;
 constexpr int X5_EPI_REGS = 160, X5_PROD_REGS = 152, X5_CTRL_REGS = 40;
 static_assert(4 * 32 * (2 * X5_EPI_REGS + X5_PROD_REGS + X5_CTRL_REGS) <= X5_THREADS * 128,
               "setmaxnreg split exceeds the registers the block is launched with");
-constexpr int X5_STAGE = 3 * A_BYTES + 2 * G_BYTES;
-constexpr size_t kSmemX5 = 2 * X5_STAGE + 1024 + 256;
 constexpr float kUnit = 32768.0f;            // 2^15
 constexpr int kLeadBitsG = 11;               // G1 grid: 2^15 * rint(G * 2^10) / 2^10
 
@@ -572,28 +574,44 @@ struct X5Params {
 // three-slice split of one component in units of 2^15
 __device__ __forceinline__ void slice3(float x, float lead_scale, float lead_unit, float &s1,
                                        float &s2, float &s3) {
-    const float xs = x * kUnit;
     s1 = rintf(x * lead_scale) * lead_unit;
-    const float r = xs - s1;                        // exact
+    const float r = fmaf(x, kUnit, -s1);            // exact
     s2 = __half2float(__float2half_rn(r));
     s3 = r - s2;                                    // exact; rounded to f16 by the caller
 }
 
+// Pipeline of the x5 kernel: k-blocks of 32 K elements (16 modes), three
+// stages of 72 KB: F1 F2 F3 (128 rows x 64 B each), G1 G2 (256 rows x 64 B,
+// by TMA, 64-byte swizzle) and the B-table tile (16 modes x 128 rows of
+// float2, by TMA) that the producers read instead of going to L2.
+constexpr int X5_BK = 32;
+constexpr int X5_STAGES = 3;
+constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
+constexpr int X5_G_BYTES = BN * X5_BK * 2;          // 16 KB
+constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
+constexpr int X5_OFF_G1 = 3 * X5_F_BYTES;
+constexpr int X5_OFF_G2 = X5_OFF_G1 + X5_G_BYTES;
+constexpr int X5_OFF_BT = X5_OFF_G2 + X5_G_BYTES;
+constexpr int X5_STAGE_V2 = X5_OFF_BT + X5_BT_BYTES;   // 72 KB
+constexpr size_t kSmemX5v2 = X5_STAGES * X5_STAGE_V2 + 1024 + 256;
+constexpr int X5_TMA_BYTES = 2 * X5_G_BYTES + X5_BT_BYTES;
+constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
+
 __global__ void __launch_bounds__(X5_THREADS, 1)
 sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant__ CUtensorMap map_g2,
-              const X5Params xp) {
+              const __grid_constant__ CUtensorMap map_bt, const X5Params xp) {
     const TcParams &p = xp.base;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * X5_STAGE);
-    uint64_t *full_a = bars;            // [2] producers -> MMA (128 arrivals)
-    uint64_t *full_g = bars + 2;        // [2] TMA -> MMA (1 arrival + bytes)
-    uint64_t *empty = bars + 4;         // [2] MMA commit -> producers, TMA
-    uint64_t *cross_full = bars + 6;    // MMA commit -> epilogue (per chunk)
-    uint64_t *cross_empty = bars + 7;   // epilogue -> MMA (256 arrivals)
-    uint64_t *drain = bars + 8;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 9);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + X5_STAGES * X5_STAGE_V2);
+    uint64_t *full_t = bars;                    // [3] TMA -> producers, MMA (1 arrival + bytes)
+    uint64_t *full_a = bars + 3;                // [3] producers -> MMA (128 arrivals)
+    uint64_t *empty = bars + 6;                 // [3] MMA commit -> TMA
+    uint64_t *cross_full = bars + 9;            // MMA commit -> epilogue (per chunk)
+    uint64_t *cross_empty = bars + 10;          // epilogue -> MMA (256 arrivals)
+    uint64_t *drain = bars + 11;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 12);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -607,9 +625,9 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
     const int NC = (KB + KC - 1) / KC;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < X5_STAGES; ++s) {
+            mbar_init(&full_t[s], 1);
             mbar_init(&full_a[s], 128);
-            mbar_init(&full_g[s], 1);
             mbar_init(&empty[s], 1);
         }
         mbar_init(cross_full, 1);
@@ -625,6 +643,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
     if (warp == 12 && lane == 0) {
         tma_prefetch_map(&map_g1);
         tma_prefetch_map(&map_g2);
+        tma_prefetch_map(&map_bt);
     }
     tc_fence_before();
     __syncthreads();
@@ -635,42 +654,43 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
     if (warp >= 12) {
         regs_dec<X5_CTRL_REGS>();
         if (warp == 12 && lane == 0) {
-            // ---- TMA: G1, G2 -------------------------------------------------
+            // ---- TMA: G1, G2, B-table tile --------------------------------------
             int issued = 0;
             for (int kb = 0; kb < KB; ++kb) {
-                const int s = kb & 1, n = kb >> 1;
+                const int s = kb % X5_STAGES, n = kb / X5_STAGES;
                 if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status,
                                         kErrTimeoutEmpty))
                     break;
-                unsigned char *st = smem + s * X5_STAGE;
-                mbar_arrive_expect_tx(&full_g[s], 2 * G_BYTES);
-                tma_load_2d(st + 3 * A_BYTES, &map_g1, &full_g[s], kb * BK, n0);
-                tma_load_2d(st + 3 * A_BYTES + G_BYTES, &map_g2, &full_g[s], kb * BK, n0);
+                unsigned char *st = smem + s * X5_STAGE_V2;
+                mbar_arrive_expect_tx(&full_t[s], X5_TMA_BYTES);
+                tma_load_2d(st + X5_OFF_G1, &map_g1, &full_t[s], kb * X5_BK, n0);
+                tma_load_2d(st + X5_OFF_G2, &map_g2, &full_t[s], kb * X5_BK, n0);
+                tma_load_2d(st + X5_OFF_BT, &map_bt, &full_t[s], m0, kb * 16);
                 ++issued;
             }
             if (*abort_flag)
-                for (int kb = issued > 2 ? issued - 2 : 0; kb < issued; ++kb)
-                    mbar_wait_drain(&full_g[kb & 1], (kb >> 1) & 1, p.status);
+                for (int kb = issued > X5_STAGES ? issued - X5_STAGES : 0; kb < issued; ++kb)
+                    mbar_wait_drain(&full_t[kb % X5_STAGES], (kb / X5_STAGES) & 1, p.status);
         } else if (warp == 13 && lane == 0) {
             // ---- MMA ---------------------------------------------------------
             const uint32_t idesc = idesc_f16(BM, BN, false);
             bool ok = true;
             for (int kb = 0; kb < KB; ++kb) {
-                const int s = kb & 1, n = kb >> 1;
+                const int s = kb % X5_STAGES, n = kb / X5_STAGES;
                 const int c = kb / KC;
                 const bool first = (kb % KC) == 0;
                 const bool last = (kb % KC) == KC - 1 || kb == KB - 1;
-                ok = mbar_wait(&full_a[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
-                if (ok) ok = mbar_wait(&full_g[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
+                ok = mbar_wait(&full_t[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
+                if (ok) ok = mbar_wait(&full_a[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t sa = smem_u32(smem + s * X5_STAGE);
-                const uint32_t f1 = sa, f2 = sa + A_BYTES, f3 = sa + 2 * A_BYTES;
-                const uint32_t g1 = sa + 3 * A_BYTES, g2 = g1 + G_BYTES;
+                const uint32_t sa = smem_u32(smem + s * X5_STAGE_V2);
+                const uint32_t f1 = sa, f2 = sa + X5_F_BYTES, f3 = sa + 2 * X5_F_BYTES;
+                const uint32_t g1 = sa + X5_OFF_G1, g2 = sa + X5_OFF_G2;
 #pragma unroll
-                for (int kk = 0; kk < BK / 16; ++kk) {
+                for (int kk = 0; kk < X5_BK / 16; ++kk) {
                     const uint32_t o = kk * 32;
-                    mma_f16_ss(t_main, desc_k_sw128(f1 + o), desc_k_sw128(g1 + o), idesc,
+                    mma_f16_ss(t_main, desc_k_sw64(f1 + o), desc_k_sw64(g1 + o), idesc,
                                (kb > 0 || kk > 0) ? 1u : 0u);
                 }
                 if (first && c > 0) {
@@ -679,13 +699,13 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
                     tc_fence_after();
                 }
 #pragma unroll
-                for (int kk = 0; kk < BK / 16; ++kk) {
+                for (int kk = 0; kk < X5_BK / 16; ++kk) {
                     const uint32_t o = kk * 32;
-                    mma_f16_ss(t_cross, desc_k_sw128(f2 + o), desc_k_sw128(g1 + o), idesc,
+                    mma_f16_ss(t_cross, desc_k_sw64(f2 + o), desc_k_sw64(g1 + o), idesc,
                                (first && kk == 0) ? 0u : 1u);
-                    mma_f16_ss(t_cross, desc_k_sw128(f1 + o), desc_k_sw128(g2 + o), idesc, 1u);
-                    mma_f16_ss(t_cross, desc_k_sw128(f2 + o), desc_k_sw128(g2 + o), idesc, 1u);
-                    mma_f16_ss(t_cross, desc_k_sw128(f3 + o), desc_k_sw128(g1 + o), idesc, 1u);
+                    mma_f16_ss(t_cross, desc_k_sw64(f1 + o), desc_k_sw64(g2 + o), idesc, 1u);
+                    mma_f16_ss(t_cross, desc_k_sw64(f2 + o), desc_k_sw64(g2 + o), idesc, 1u);
+                    mma_f16_ss(t_cross, desc_k_sw64(f3 + o), desc_k_sw64(g1 + o), idesc, 1u);
                 }
                 mma_commit(&empty[s]);
                 if (last) mma_commit(cross_full);
@@ -697,41 +717,35 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
         }
     } else if (warp >= 8) {
         regs_inc<X5_PROD_REGS>();
-        // ---- producers ---------------------------------------------------------
-        // B-table values of k-block kb + 1 are loaded while k-block kb is
-        // sliced, so the L2 latency overlaps the conversion work.
+        // ---- producers: row r of the F tile, 16 modes per k-block ----------------
         const int r = threadIdx.x - 256;
-        const int m = m0 + r;
-        const bool row_ok = m < p.nm;
         const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
-        const uint32_t row_off = (r >> 3) * 1024 + (r & 7) * 128;
+        const uint32_t row_off = r * 64;                       // 64-byte rows
+        const uint32_t swz = (r >> 1) & 3;                     // 64-byte swizzle phase
         const float ls = xp.wnorm[2], lu = xp.wnorm[3];
-        float2 cur[32];
-        auto load_block = [&](int kb, float2 (&dst)[32]) {
+        float2 sj[16];
+        auto load_s = [&](int kb, float2 (&dst)[16]) {
 #pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                const int j = kb * 32 + q;
-                dst[q] = (row_ok && j < p.n_modes) ? __ldg(p.btab + static_cast<int64_t>(j) * p.nm + m)
-                                                   : make_float2(0.f, 0.f);
+            for (int q = 0; q < 16; ++q) {
+                const int j = kb * 16 + q;
+                dst[q] = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
             }
         };
-        load_block(0, cur);
+        load_s(0, sj);
         for (int kb = 0; kb < KB; ++kb) {
-            const int s = kb & 1, n = kb >> 1;
-            float2 nxt[32];
-            if (kb + 1 < KB) load_block(kb + 1, nxt);
-            if (n > 0 &&
-                !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status, kErrTimeoutEmpty))
-                break;
-            unsigned char *f1 = smem + s * X5_STAGE;
+            const int s = kb % X5_STAGES, n = kb / X5_STAGES;
+            float2 sn[16];
+            if (kb + 1 < KB) load_s(kb + 1, sn);
+            if (!mbar_wait(&full_t[s], n & 1, abort_flag, p.status, kErrTimeoutFull)) break;
+            unsigned char *st = smem + s * X5_STAGE_V2;
+            const float2 *bt = reinterpret_cast<const float2 *>(st + X5_OFF_BT);
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
+            for (int c = 0; c < 4; ++c) {          // 16-byte chunk c: modes 4c .. 4c+3
                 uint32_t w1[4], w2[4], w3[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const int j = kb * 32 + c * 4 + q;
-                    const float2 sj = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
-                    const float2 v = cmulf(cur[c * 4 + q], sj);
+                    const int jl = c * 4 + q;
+                    const float2 v = cmulf(bt[jl * BM + r], sj[jl]);
                     float a1, a2, a3, b1, b2, b3;
                     slice3(v.x, ls, lu, a1, a2, a3);
                     slice3(v.y, ls, lu, b1, b2, b3);
@@ -742,16 +756,17 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
                     w2[q] = *reinterpret_cast<const uint32_t *>(&h2);
                     w3[q] = *reinterpret_cast<const uint32_t *>(&h3);
                 }
-                const uint32_t phys = row_off + ((c ^ (r & 7)) << 4);
-                *reinterpret_cast<uint4 *>(f1 + phys) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-                *reinterpret_cast<uint4 *>(f1 + A_BYTES + phys) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
-                *reinterpret_cast<uint4 *>(f1 + 2 * A_BYTES + phys) =
+                const uint32_t phys = row_off + ((c ^ swz) << 4);
+                *reinterpret_cast<uint4 *>(st + phys) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+                *reinterpret_cast<uint4 *>(st + X5_F_BYTES + phys) =
+                    make_uint4(w2[0], w2[1], w2[2], w2[3]);
+                *reinterpret_cast<uint4 *>(st + 2 * X5_F_BYTES + phys) =
                     make_uint4(w3[0], w3[1], w3[2], w3[3]);
             }
             fence_proxy_async_smem();
             mbar_arrive(&full_a[s]);
 #pragma unroll
-            for (int q = 0; q < 32; ++q) cur[q] = nxt[q];
+            for (int q = 0; q < 16; ++q) sj[q] = sn[q];
         }
     } else {
         regs_inc<X5_EPI_REGS>();
@@ -768,13 +783,13 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
             if (!ok) break;
             tc_fence_after();
 #pragma unroll
-            for (int g = 0; g < 16; ++g) {
-                uint32_t v[8];
+            for (int g = 0; g < 8; ++g) {
+                uint32_t v[16];
                 __syncwarp();
-                tmem_ld8(t_cross + lane_off + 128 * h + 8 * g, v);
+                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, v);
                 tmem_ld_wait();
 #pragma unroll
-                for (int i = 0; i < 8; ++i) tot[8 * g + i] += __uint_as_float(v[i]);
+                for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
             }
             if (c < NC - 1) {
                 tc_fence_before();
@@ -788,18 +803,18 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
             double *orow = p.out + static_cast<int64_t>(b) * p.batch_stride +
                            static_cast<int64_t>(row_ok ? m : 0) * p.row_stride;
 #pragma unroll
-            for (int g = 0; g < 16; ++g) {
-                uint32_t v[8];
+            for (int g = 0; g < 8; ++g) {
+                uint32_t v[16];
                 __syncwarp();
-                tmem_ld8(t_main + lane_off + 128 * h + 8 * g, v);
+                tmem_ld16(t_main + lane_off + 128 * h + 16 * g, v);
                 tmem_ld_wait();
-                const int gn0 = n0 + 128 * h + 8 * g;
+                const int gn0 = n0 + 128 * h + 16 * g;
                 if (row_ok && gn0 < p.ncn) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
+                    for (int i = 0; i < 16; ++i) {
                         const int gn = gn0 + i;
                         if (gn < p.ncn) {
-                            const float val = (__uint_as_float(v[i]) + tot[8 * g + i]) * unscale;
+                            const float val = (__uint_as_float(v[i]) + tot[16 * g + i]) * unscale;
                             const int comp = gn / p.nn;
                             orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(val);
                         }
@@ -841,17 +856,19 @@ int encode_fn(EncodeTiledFn *out) {
     return GSC_OK;
 }
 
-int make_map(CUtensorMap *map, void *base, bool bf16, int k_pad, int rows) {
+// 2-D tiled tensor map: `inner` elements per row (contiguous), `rows` rows,
+// box (box_inner, box_rows).
+int make_map(CUtensorMap *map, void *base, CUtensorMapDataType dtype, int elem_bytes, int inner,
+             int rows, int box_inner, int box_rows, CUtensorMapSwizzle swizzle) {
     EncodeTiledFn fn;
     GSC_TRY(encode_fn(&fn));
-    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(k_pad), static_cast<cuuint64_t>(rows)};
-    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(k_pad) * 2};
-    const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BN)};
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(inner), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(inner) * elem_bytes};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_inner), static_cast<cuuint32_t>(box_rows)};
     const cuuint32_t estr[2] = {1, 1};
-    const CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                          2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r = fn(map, dtype, 2, base, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(GSC_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     return GSC_OK;
 }
@@ -883,9 +900,11 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int nn = static_cast<int>(dim == 3 ? a.n[2] : a.n[1]);
     const int64_t P = static_cast<int64_t>(nb) * nm * nn;
     if (P == 0) return GSC_OK;
-    const int KB = std::max(1, (2 * N + BK - 1) / BK);
-    const int k_pad = KB * BK;
+    const int bk = x5 ? X5_BK : BK;
+    const int KB = std::max(1, (2 * N + bk - 1) / bk);
+    const int k_pad = KB * bk;
     const int ncn = ncomp * nn;
+    const int nm_ld = (nm + 15) / 16 * 16;
     const int n_tiles = (ncn + BN - 1) / BN;
     const int ncn_pad = n_tiles * BN;
     const int m_tiles = (nm + BM - 1) / BM;
@@ -894,7 +913,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const size_t off_wn = 0;
     const size_t off_svec = 1024;
     const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(N), 1024);
-    const size_t off_ghi = align_up(off_btab + sizeof(float2) * static_cast<size_t>(N) * nm, 1024);
+    const size_t off_ghi = align_up(off_btab + sizeof(float2) * static_cast<size_t>(N) * nm_ld, 1024);
     const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
     const size_t off_glo = align_up(off_ghi + g_bytes, 1024);
     const size_t total = off_glo + g_bytes;
@@ -921,6 +940,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.ncomp = ncomp;
     t.incompr = a.incompr ? 1 : 0;
     t.k_pad = k_pad;
+    t.nm_ld = nm_ld;
     t.ncn_pad = ncn_pad;
     t.svec = reinterpret_cast<float2 *>(base + off_svec);
     t.btab = reinterpret_cast<float2 *>(base + off_btab);
@@ -932,7 +952,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         TimedLaunch tl(st);
         tl.begin(K_SEP_TABLES);
         if (x5) sep_wnorm_kernel<<<1, 256, 0, st>>>(a.z1, a.z2, N, t.wnorm);
-        const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(N) * nm;
+        const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(N) * nm_ld;
         const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
         if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
         if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
@@ -946,20 +966,27 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         GSC_CUDA(cudaGetLastError());
     }
 
-    CUtensorMap mh, ml;
-    GSC_TRY(make_map(&mh, t.ghi, bf16, k_pad, ncn_pad));
-    GSC_TRY(make_map(&ml, t.glo, bf16, k_pad, ncn_pad));
+    CUtensorMap mh, ml, mb;
+    const CUtensorMapDataType gtype =
+        bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    const CUtensorMapSwizzle gswz = x5 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
+    GSC_TRY(make_map(&mh, t.ghi, gtype, 2, k_pad, ncn_pad, bk, BN, gswz));
+    GSC_TRY(make_map(&ml, t.glo, gtype, 2, k_pad, ncn_pad, bk, BN, gswz));
+    if (x5)
+        GSC_TRY(make_map(&mb, t.btab, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, nm_ld, N, BM, 16,
+                         CU_TENSOR_MAP_SWIZZLE_NONE));
 
     TcParams p;
     p.svec = t.svec;
     p.btab = t.btab;
     p.n_modes = N;
     p.nm = nm;
+    p.nm_ld = nm_ld;
     p.nb = nb;
     p.nn = nn;
     p.ncn = ncn;
     p.kb_total = KB;
-    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : 4;
+    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : (x5 ? X5_CHUNK : 4);
     p.m_tiles = m_tiles;
     p.n_tiles = n_tiles;
     p.out = a.out;
@@ -977,11 +1004,11 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         static bool configured = false;
         if (!configured) {
             GSC_CUDA(cudaFuncSetAttribute(sep_x5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          static_cast<int>(kSmemX5)));
+                                          static_cast<int>(kSmemX5v2)));
             configured = true;
         }
         tl.begin(K_SEP_TC_F16X5);
-        sep_x5_kernel<<<static_cast<unsigned>(grid), X5_THREADS, kSmemX5, st>>>(mh, ml, xp);
+        sep_x5_kernel<<<static_cast<unsigned>(grid), X5_THREADS, kSmemX5v2, st>>>(mh, ml, mb, xp);
     } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
         if (bf16) {

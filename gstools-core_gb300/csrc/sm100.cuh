@@ -233,6 +233,18 @@ __device__ __forceinline__ uint64_t desc_k_sw128(uint32_t saddr) {
     return d;
 }
 
+// Same for the 64-byte swizzled layout: rows of 64 bytes, 8-row atoms of
+// 512 bytes (stride byte offset 512).
+__device__ __forceinline__ uint64_t desc_k_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);   // start address
+    d |= static_cast<uint64_t>(1) << 16;                     // LBO (unused)
+    d |= static_cast<uint64_t>(512 >> 4) << 32;              // SBO = 512 B
+    d |= static_cast<uint64_t>(1) << 46;                     // descriptor version
+    d |= static_cast<uint64_t>(4) << 61;                     // SWIZZLE_64B
+    return d;
+}
+
 // Instruction descriptor of tcgen05.mma kind::f16 with F32 accumulation,
 // both operands K-major.  ab_bf16 selects BF16 (else F16) inputs.
 __host__ __device__ constexpr uint32_t idesc_f16(int M, int N, bool ab_bf16) {
