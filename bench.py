@@ -245,7 +245,9 @@ def max_over_ranks(world, value: float) -> float:
 # our arm
 # ---------------------------------------------------------------------------
 def default_form(w):
-    return "sep_f16x5" if w["axes"] is not None else "plain"
+    """The chosen form per workload: the exact-leading-term tensor-core
+    contraction on structured grids, the mixed-precision kernel on points."""
+    return "sep_f16x5" if w["axes"] is not None else "mixed"
 
 
 def make_device_step(gsc, torch, w, form, dev, stream):
@@ -400,8 +402,9 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f16 split operands, f32 accumulation, f64 output" if form.startswith("sep")
-                 else "f64",
+        "dtype": ("f16 split operands, f32 accumulation, f64 output" if form.startswith("sep")
+                  else "f32 pairs (phase), f32 (sincos, tile sums), f64 output"
+                  if form.startswith("mixed") else "f64"),
         "data": "synthetic (seeded numpy default_rng)",
         "config": {"workload": args.workload, "desc": w["desc"], "points": P, "modes": N,
                    "form": form,

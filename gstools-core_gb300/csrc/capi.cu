@@ -38,7 +38,8 @@ const char *kernel_name(int32_t id) {
     static const char *names[K_COUNT] = {
         "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
-        "grid_expand", "sep_tc_f16x5",
+        "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
+        "mixed_f64phase",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -202,7 +203,7 @@ static int resolve_opts(const gsc_opts *o, Resolved *r) {
     if (!o) return GSC_OK;
     if (o->struct_size < static_cast<int32_t>(sizeof(gsc_opts)))
         return set_error(GSC_ERR_INVALID, "gsc_opts.struct_size is smaller than sizeof(gsc_opts)");
-    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_SEP_F16X5)
+    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_MIXED_F64PHASE)
         return set_error(GSC_ERR_INVALID, "unknown form");
     r->form = o->form;
     r->device = o->device;
@@ -257,6 +258,21 @@ static int unstructured_form(const Resolved &r) {
 // measure it); AUTO picks the fastest form whose bound fits the tolerance.
 constexpr double kBoundSepF16x3 = 1e-5;
 constexpr double kBoundSepF16x5 = 1e-6;
+constexpr double kBoundMixed = 1e-6;
+
+static bool is_mixed(int form) {
+    return form == GSC_FORM_MIXED || form == GSC_FORM_MIXED_F64PHASE;
+}
+
+// plain or mixed forms on explicit points (device pointers in `a`)
+static int run_points(DeviceCtx &ctx, const Resolved &ro, PlainArgs &a, cudaStream_t st) {
+    int f = ro.form;
+    if (f == GSC_FORM_AUTO) f = ro.tolerance >= kBoundMixed ? GSC_FORM_MIXED : GSC_FORM_PLAIN_F64;
+    const bool mixed_ok = a.dim >= 1 && a.dim <= 3 && !(a.incompr && a.dim == 1);
+    if (is_mixed(f) && mixed_ok) return mixed_run(ctx, a, f == GSC_FORM_MIXED_F64PHASE, st);
+    a.variant = f == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0;
+    return plain_run(ctx, a, st);
+}
 
 static int structured_form(const Resolved &r, int64_t dim) {
     int f = r.form;
@@ -264,7 +280,9 @@ static int structured_form(const Resolved &r, int64_t dim) {
         f = r.tolerance >= kBoundSepF16x3   ? GSC_FORM_SEP_F16X3
             : r.tolerance >= kBoundSepF16x5 ? GSC_FORM_SEP_F16X5
                                             : GSC_FORM_PLAIN_F64;
-    if (is_sep(f) && dim < 2) f = GSC_FORM_PLAIN_F64;   // 1-D: nothing to contract
+    if (is_sep(f) && dim < 2)   // 1-D: nothing to contract
+        f = (r.form == GSC_FORM_AUTO && r.tolerance >= kBoundMixed) ? GSC_FORM_MIXED
+                                                                  : GSC_FORM_PLAIN_F64;
     return f;
 }
 
@@ -353,8 +371,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     a.out = d + n_in;
     a.out_sd = P;
     a.out_sp = 1;
-    a.variant = plain_variant(ro);
-    GSC_TRY(plain_run(*ctx, a, st));
+    GSC_TRY(run_points(*ctx, ro, a, st));
     double *ho = h + n_in;
     GSC_CUDA(cudaMemcpyAsync(ho, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
     GSC_CUDA(cudaStreamSynchronize(st));
@@ -406,8 +423,7 @@ static int dev_plain(const double *cov, const double *z1, const double *z2, cons
     a.out = out;
     a.out_sd = P;
     a.out_sp = 1;
-    a.variant = plain_variant(ro);
-    return plain_run(*ctx, a, ro.stream);
+    return run_points(*ctx, ro, a, ro.stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -482,8 +498,9 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
     a.out = out;
     a.out_sd = P;
     a.out_sp = 1;
-    a.variant = form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0;
-    return plain_run(ctx, a, st);
+    Resolved rp = ro;
+    rp.form = form;
+    return run_points(ctx, rp, a, st);
 }
 
 static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,

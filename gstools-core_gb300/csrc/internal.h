@@ -42,6 +42,10 @@ enum KernelId : int32_t {
     K_SEP_TC_BF16 = 8,     // tcgen05 separable contraction, bf16 hi/lo split
     K_GRID_EXPAND = 9,     // meshgrid of structured axes (plain form on grids)
     K_SEP_TC_F16X5 = 10,   // tcgen05 separable contraction, exact leading term
+    K_MIXED_MODES = 11,    // per-mode records of the mixed form
+    K_MIXED_SCALAR = 12,   // mixed form, double-float phase, scalar field
+    K_MIXED_INCOMPR = 13,  // mixed form, double-float phase, vector field
+    K_MIXED_F64PHASE = 14, // mixed form with the phase in FP64
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -98,6 +102,13 @@ struct PlainArgs {
     int variant;         // 0 table-driven sincos, 1 CUDA sincos()
 };
 int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st);
+
+// out[i*sd + p*sp] = sum over s of part[s][i][p], s ascending (plain.cu)
+int split_reduce(const double *part, int64_t S, int64_t nout, int64_t P, double *out, int64_t sd,
+                 int64_t sp, cudaStream_t st);
+
+// ---- mixed-precision summators (mixed.cu) -----------------------------------
+int mixed_run(DeviceCtx &ctx, const PlainArgs &a, bool f64phase, cudaStream_t st);
 
 // Allocation-free scalar summator (plain.cu): per-mode tables in a fixed
 // device array of kNoAllocModes modes; `device` must be current.

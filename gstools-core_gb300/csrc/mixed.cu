@@ -1,0 +1,335 @@
+// mixed.cu -- mixed-precision summators for unstructured points (sm_103a).
+//
+// Same sums as plain.cu (reference src/field.rs:37-65 and :97-182) for points
+// without grid structure, where no tensor-core factorisation exists and every
+// point*mode needs its own phase and sincos.  GB300 executes FP64 at 1/64 of
+// the FP32 rate (1.89 vs 119 FMA per clock per SM), so this form keeps FP64
+// accuracy only where it is needed and spends FP32 instructions:
+//
+//  * phase in turns, theta = kappa.x with kappa = k / 2pi, in double-float
+//    (FP32 pairs): kappa = kh + kl per mode, x = xh + xl per point (48
+//    significant bits each); per dimension p = kh*xh is split exactly into
+//    p (rounded) and fma(kh, xh, -p), the integer turns rint(p) are dropped
+//    exactly, and the small terms kh*xl + kl*xh are added in FP32.  The
+//    reduced phase keeps about 2^-40 turns of absolute accuracy for |k.x|
+//    up to 1e6, far beyond what FP32 can represent as a plain product
+//    (FP64 would spend 9 FP64 instructions per point*mode here);
+//  * sincos(2 pi theta): quadrant by rounding 4 theta, then sin/cos of
+//    2 pi f, |f| <= 1/8, by polynomials fitted for this kernel (FP32
+//    coefficients, max error 8.5e-8 / 5.7e-8 over the interval), corrected
+//    to first order for the low part of the phase;
+//  * z1 cos + z2 sin accumulated in FP32 over tiles of 32 modes, each tile
+//    folded into a double-float (TwoSum) running total, converted to FP64 at
+//    the end: the compensated sum across tiles is as accurate as FP64.
+//
+// The "mixed_f64phase" variant forms the phase and its reduction in FP64
+// (the literal recipe: 5 FP64 instructions per point*mode) and shares the
+// rest; it exists to measure what the double-float phase buys.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "internal.h"
+
+namespace gsc {
+namespace {
+
+constexpr int kMxThreads = 128;
+constexpr int kMxR = 4;              // points per thread
+constexpr int kMxTile = 32;          // modes per FP32 accumulation tile
+constexpr int kMxRec = 12;           // floats per mode: kh0 kh1 kh2 kl0 kl1 kl2 z1 z2 w0 w1 w2 -
+constexpr int kMxRec64 = 4;          // doubles per mode (FP64-phase variant): kappa0..2, -
+constexpr double kInv2Pi = 0.15915494309189535;   // fl(1 / (2 pi))
+constexpr float kTwoPiF = 6.2831854820251465f;     // fl32(2 pi)
+constexpr float kRoundF = 12582912.0f;             // 1.5 * 2^23: x + kRoundF rounds x
+
+// sin(2 pi f) = f * S(f^2), cos(2 pi f) = C(f^2) on |f| <= 1/8 (fitted here)
+constexpr float kS0 = 6.2831854820251465f, kS1 = -41.34170150756836f, kS2 = 81.60517883300781f,
+                kS3 = -76.6958236694336f, kS4 = 41.41468811035156f;
+constexpr float kC0 = 1.0f, kC1 = -19.739208221435547f, kC2 = 64.93931579589844f,
+                kC3 = -85.44285583496094f, kC4 = 59.220428466796875f;
+
+__global__ void mixed_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+                                  const double *__restrict__ z2, int64_t dim, int64_t n_modes,
+                                  int64_t j0, int64_t nc, int incompr, float *__restrict__ rec,
+                                  double *__restrict__ rec64) {
+    const int64_t jl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (jl >= nc) return;
+    const int64_t j = j0 + jl;
+    double k[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
+    float *r = rec + jl * kMxRec;
+    for (int d = 0; d < 3; ++d) {
+        const double kap = k[d] * kInv2Pi;
+        const float hi = __double2float_rn(kap);
+        r[d] = hi;
+        r[3 + d] = __double2float_rn(kap - static_cast<double>(hi));
+        rec64[jl * kMxRec64 + d] = kap;
+    }
+    rec64[jl * kMxRec64 + 3] = 0.0;
+    r[6] = __double2float_rn(z1[j]);
+    r[7] = __double2float_rn(z2[j]);
+    double w0 = 0.0, w1 = 0.0, w2 = 0.0;
+    if (incompr) {   // projector as the reference forms it (src/field.rs:138-152)
+        double kk = 0.0;
+        for (int d = 0; d < dim; ++d) kk = __dadd_rn(kk, __dmul_rn(k[d], k[d]));
+        const double k_2 = __ddiv_rn(k[0], kk);
+        w0 = __dadd_rn(1.0, -__dmul_rn(k[0], k_2));
+        w1 = -__dmul_rn(k[1], k_2);
+        w2 = -__dmul_rn(k[2], k_2);
+    }
+    r[8] = __double2float_rn(w0);
+    r[9] = __double2float_rn(w1);
+    r[10] = __double2float_rn(w2);
+    r[11] = 0.f;
+}
+
+// (z1 cos + z2 sin)(2 pi (th + tl)), th in [-1/2, 1/2] turns, tl tiny
+__device__ __forceinline__ float mixed_term(float th, float tl, float z1, float z2) {
+    const float qf = fmaf(th, 4.0f, kRoundF);
+    const float q = qf - kRoundF;
+    const int qi = __float_as_int(qf);
+    const float f = fmaf(q, -0.25f, th);                     // exact, |f| <= 1/8
+    const float f2 = f * f;
+    float s = fmaf(fmaf(fmaf(fmaf(kS4, f2, kS3), f2, kS2), f2, kS1), f2, kS0) * f;
+    float c = fmaf(fmaf(fmaf(fmaf(kC4, f2, kC3), f2, kC2), f2, kC1), f2, kC0);
+    const float tw = tl * kTwoPiF;                           // first-order low-part correction
+    const float s1 = fmaf(tw, c, s);
+    const float c1 = fmaf(-tw, s, c);
+    // rotate by q quarter turns
+    const bool swap = qi & 1;
+    float sr = swap ? c1 : s1;
+    float cr = swap ? s1 : c1;
+    sr = __int_as_float(__float_as_int(sr) ^ ((qi & 2) << 30));
+    cr = __int_as_float(__float_as_int(cr) ^ (((qi + 1) & 2) << 30));
+    return fmaf(z1, cr, z2 * sr);
+}
+
+// Knuth's TwoSum: (hi, lo) += a
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float a) {
+    const float s = hi + a;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (a - bb);
+    hi = s;
+    lo += e;
+}
+
+template <int D, bool INC, bool F64P>
+__global__ void __launch_bounds__(kMxThreads)
+mixed_kernel(const double *__restrict__ pos, int64_t P, const float *__restrict__ rec,
+             const double *__restrict__ rec64, int64_t nc, int64_t mps, int accumulate,
+             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    constexpr int NOUT = INC ? D : 1;
+    __shared__ __align__(16) float srec[kMxTile * kMxRec];
+    __shared__ __align__(16) double srec64[F64P ? kMxTile * kMxRec64 : 1];
+    const int tid = threadIdx.x;
+    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * (kMxThreads * kMxR) + tid;
+    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
+    const int64_t je = min(nc, jb + mps);
+
+    float xh[kMxR][D], xl[kMxR][D];
+    double xd[kMxR][D];
+    float hi[kMxR][NOUT], lo[kMxR][NOUT];
+#pragma unroll
+    for (int r = 0; r < kMxR; ++r) {
+        const int64_t p = p0 + r * kMxThreads;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double x = p < P ? pos[d * P + p] : 0.0;
+            xd[r][d] = x;
+            xh[r][d] = __double2float_rn(x);
+            xl[r][d] = __double2float_rn(x - static_cast<double>(xh[r][d]));
+        }
+#pragma unroll
+        for (int i = 0; i < NOUT; ++i) hi[r][i] = lo[r][i] = 0.f;
+    }
+
+    for (int64_t t0 = jb; t0 < je; t0 += kMxTile) {
+        const int tm = static_cast<int>(min(static_cast<int64_t>(kMxTile), je - t0));
+        __syncthreads();
+        for (int i = tid; i < tm * kMxRec; i += kMxThreads) srec[i] = rec[t0 * kMxRec + i];
+        if (F64P)
+            for (int i = tid; i < tm * kMxRec64; i += kMxThreads) srec64[i] = rec64[t0 * kMxRec64 + i];
+        __syncthreads();
+        float acc[kMxR][NOUT];
+#pragma unroll
+        for (int r = 0; r < kMxR; ++r)
+#pragma unroll
+            for (int i = 0; i < NOUT; ++i) acc[r][i] = 0.f;
+        for (int m = 0; m < tm; ++m) {
+            const float *mr = srec + m * kMxRec;
+            const float z1 = mr[6], z2 = mr[7];
+            float w[3] = {mr[8], mr[9], mr[10]};
+#pragma unroll
+            for (int r = 0; r < kMxR; ++r) {
+                float th, tl;
+                if (F64P) {
+                    const double *kr = srec64 + m * kMxRec64;
+                    double t = kr[0] * xd[r][0];
+                    if (D > 1) t = fma(kr[1], xd[r][1], t);
+                    if (D > 2) t = fma(kr[2], xd[r][2], t);
+                    t -= rint(t);
+                    th = __double2float_rn(t);
+                    tl = 0.f;
+                } else {
+                    float a = 0.f, b = 0.f;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        const float kh = mr[d], kl = mr[3 + d];
+                        const float pr = kh * xh[r][d];
+                        const float e = fmaf(kh, xh[r][d], -pr);      // exact
+                        a += pr - rintf(pr);                            // exact
+                        b = fmaf(kh, xl[r][d], fmaf(kl, xh[r][d], e + b));
+                    }
+                    const float a2 = a - rintf(a);
+                    th = a2 + b;
+                    tl = b - (th - a2);
+                }
+                const float z12 = mixed_term(th, tl, z1, z2);
+                if (INC) {
+#pragma unroll
+                    for (int i = 0; i < NOUT; ++i) acc[r][i] = fmaf(w[i], z12, acc[r][i]);
+                } else {
+                    acc[r][0] += z12;
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kMxR; ++r)
+#pragma unroll
+            for (int i = 0; i < NOUT; ++i) two_sum_add(hi[r][i], lo[r][i], acc[r][i]);
+    }
+
+    double *d0 = dst + static_cast<int64_t>(blockIdx.y) * split_stride;
+#pragma unroll
+    for (int r = 0; r < kMxR; ++r) {
+        const int64_t p = p0 + r * kMxThreads;
+        if (p >= P) continue;
+#pragma unroll
+        for (int i = 0; i < NOUT; ++i) {
+            const double v = static_cast<double>(hi[r][i]) + static_cast<double>(lo[r][i]);
+            double *o = d0 + i * sd + p * sp;
+            *o = accumulate ? *o + v : v;
+        }
+    }
+}
+
+template <int D, bool INC, bool F64P>
+int launch_mixed(dim3 grid, cudaStream_t st, const double *pos, int64_t P, const float *rec,
+                 const double *rec64, int64_t nc, int64_t mps, int accumulate, double *dst,
+                 int64_t sd, int64_t sp, int64_t split_stride) {
+    mixed_kernel<D, INC, F64P><<<grid, kMxThreads, 0, st>>>(pos, P, rec, rec64, nc, mps, accumulate,
+                                                             dst, sd, sp, split_stride);
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+template <bool INC, bool F64P>
+int dispatch_mixed(int64_t dim, dim3 grid, cudaStream_t st, const double *pos, int64_t P,
+                   const float *rec, const double *rec64, int64_t nc, int64_t mps, int accumulate,
+                   double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    switch (dim) {
+        case 1:
+            if (!INC)
+                return launch_mixed<1, INC, F64P>(grid, st, pos, P, rec, rec64, nc, mps, accumulate,
+                                                  dst, sd, sp, split_stride);
+            break;
+        case 2:
+            return launch_mixed<2, INC, F64P>(grid, st, pos, P, rec, rec64, nc, mps, accumulate,
+                                              dst, sd, sp, split_stride);
+        case 3:
+            return launch_mixed<3, INC, F64P>(grid, st, pos, P, rec, rec64, nc, mps, accumulate,
+                                              dst, sd, sp, split_stride);
+    }
+    return set_error(GSC_ERR_DIM, "the mixed form supports dimensions 1, 2, 3 (incompressible: 2, 3)");
+}
+
+int mx_sm_count(int device) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0)
+        n = 152;
+    return n;
+}
+
+}  // namespace
+
+int mixed_run(DeviceCtx &ctx, const PlainArgs &a, bool f64phase, cudaStream_t st) {
+    const int64_t P = a.n_points, N = a.n_modes, dim = a.dim;
+    if (P == 0) return GSC_OK;
+    const int64_t nout = a.incompr ? dim : 1;
+    if (dim < 1 || dim > 3 || (a.incompr && dim == 1))
+        return set_error(GSC_ERR_DIM, "the mixed form supports dimensions 1, 2, 3 (incompressible: 2, 3)");
+    constexpr int64_t kChunk = 1 << 20;   // modes per record build
+    const int64_t pts_per_block = static_cast<int64_t>(kMxThreads) * kMxR;
+    const int64_t bx = (P + pts_per_block - 1) / pts_per_block;
+    if (bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
+    const int64_t chunk = std::min<int64_t>(N, kChunk);
+    const int64_t want_blocks = static_cast<int64_t>(mx_sm_count(ctx.device)) * 8;
+    int64_t S = std::max<int64_t>(1, (want_blocks + bx - 1) / bx);
+    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kMxTile)));
+    S = std::min<int64_t>(S, 64);
+    int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
+    mps = (mps + kMxTile - 1) / kMxTile * kMxTile;
+    if (mps > 0) S = std::max<int64_t>(1, (chunk + mps - 1) / mps);
+    if (N == 0) S = 1;
+
+    const size_t rec_bytes = static_cast<size_t>(chunk) * kMxRec * sizeof(float);
+    const size_t rec64_bytes = static_cast<size_t>(chunk) * kMxRec64 * sizeof(double);
+    const size_t part_bytes = S > 1 ? static_cast<size_t>(S) * nout * P * sizeof(double) : 0;
+    const size_t off_rec64 = (rec_bytes + 255) / 256 * 256;
+    const size_t off_part = off_rec64 + (rec64_bytes + 255) / 256 * 256;
+    GSC_TRY(ensure_dev(ctx, ctx.scratch, off_part + part_bytes + 256));
+    GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
+    unsigned char *sbase = static_cast<unsigned char *>(ctx.scratch.ptr);
+    float *rec = reinterpret_cast<float *>(sbase);
+    double *rec64 = reinterpret_cast<double *>(sbase + off_rec64);
+    double *part = reinterpret_cast<double *>(sbase + off_part);
+
+    double *dst = S > 1 ? part : a.out;
+    const int64_t sd = S > 1 ? P : a.out_sd;
+    const int64_t sp = S > 1 ? 1 : a.out_sp;
+    const int64_t split_stride = S > 1 ? nout * P : 0;
+    const dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(S));
+
+    int64_t j0 = 0;
+    int first = 1;
+    do {
+        const int64_t nc = std::min<int64_t>(N - j0, kChunk);
+        if (nc > 0) {
+            TimedLaunch tl(st);
+            tl.begin(K_MIXED_MODES);
+            mixed_mode_kernel<<<static_cast<unsigned>((nc + 127) / 128), 128, 0, st>>>(
+                a.cov, a.z1, a.z2, dim, N, j0, nc, a.incompr ? 1 : 0, rec, rec64);
+            tl.end();
+            GSC_CUDA(cudaGetLastError());
+        }
+        const int64_t mps_c = nc > 0 ? std::min<int64_t>(mps, nc) : 0;
+        const dim3 g(grid.x, static_cast<unsigned>(
+                                 nc > 0 ? std::min<int64_t>(S, (nc + mps_c - 1) / mps_c) : 1));
+        const dim3 gl = first ? grid : g;
+        TimedLaunch tl(st);
+        tl.begin(f64phase ? K_MIXED_F64PHASE : (a.incompr ? K_MIXED_INCOMPR : K_MIXED_SCALAR));
+        int rc;
+        if (a.incompr)
+            rc = f64phase ? dispatch_mixed<true, true>(dim, gl, st, a.pos, P, rec, rec64, nc, mps_c,
+                                                       !first, dst, sd, sp, split_stride)
+                          : dispatch_mixed<true, false>(dim, gl, st, a.pos, P, rec, rec64, nc,
+                                                        mps_c, !first, dst, sd, sp, split_stride);
+        else
+            rc = f64phase ? dispatch_mixed<false, true>(dim, gl, st, a.pos, P, rec, rec64, nc,
+                                                        mps_c, !first, dst, sd, sp, split_stride)
+                          : dispatch_mixed<false, false>(dim, gl, st, a.pos, P, rec, rec64, nc,
+                                                         mps_c, !first, dst, sd, sp, split_stride);
+        tl.end();
+        if (rc != GSC_OK) return rc;
+        first = 0;
+        j0 += nc;
+    } while (j0 < N);
+
+    if (S > 1) GSC_TRY(split_reduce(part, S, nout, P, a.out, a.out_sd, a.out_sp, st));
+    GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+    return GSC_OK;
+}
+
+}  // namespace gsc

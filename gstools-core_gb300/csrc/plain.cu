@@ -346,6 +346,18 @@ __global__ void grid_expand_kernel(const double *__restrict__ a0, const double *
 
 }  // namespace
 
+int split_reduce(const double *part, int64_t S, int64_t nout, int64_t P, double *out, int64_t sd,
+                 int64_t sp, cudaStream_t st) {
+    TimedLaunch tl(st);
+    tl.begin(K_SPLIT_REDUCE);
+    const int64_t tot = nout * P;
+    split_reduce_kernel<<<static_cast<unsigned>((tot + 255) / 256), 256, 0, st>>>(part, S, nout, P,
+                                                                                 out, sd, sp);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
 int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double *pos,
                 cudaStream_t st) {
     const int64_t n2 = dim == 3 ? n[2] : 1;

@@ -28,6 +28,8 @@ FORMS = {
     "sep_f16x3": 3,
     "sep_bf16x3": 4,
     "sep_f16x5": 5,
+    "mixed": 6,
+    "mixed_f64phase": 7,
 }
 
 

@@ -66,12 +66,19 @@ extern "C" {
                                   tensor-memory accumulator sums exactly,
                                   the rest drained in chunks; max error
                                   below 1e-6 of the field RMS               */
+#define GSC_FORM_MIXED      6  /* any points: phase in double-float (FP32
+                                  pairs), FP32 sincos, FP32 sums per 32 modes
+                                  with a compensated total; below 1e-6 of
+                                  the field RMS for |k.x| up to ~1e6        */
+#define GSC_FORM_MIXED_F64PHASE 7 /* as GSC_FORM_MIXED with the phase and its
+                                  reduction in FP64                          */
 
 /* ---- flags ----------------------------------------------------------- */
 #define GSC_FLAG_TIMING     1  /* record per-kernel CUDA-event timings      */
 
 /* AUTO on structured grids picks GSC_FORM_SEP_F16X3 for tolerance >= 1e-5,
- * GSC_FORM_SEP_F16X5 for tolerance >= 1e-6, else GSC_FORM_PLAIN_F64.
+ * GSC_FORM_SEP_F16X5 for tolerance >= 1e-6, else GSC_FORM_PLAIN_F64; on
+ * explicit points GSC_FORM_MIXED for tolerance >= 1e-6, else PLAIN_F64.
  *
  * Options.  Pass NULL for the defaults (form AUTO at tolerance 1e-12,
  * current device, library stream for host-pointer calls and the legacy

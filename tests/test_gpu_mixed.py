@@ -1,0 +1,95 @@
+"""Mixed-precision forms on explicit points against the oracle (GPU tests).
+
+`mixed`: phase in double-float (FP32 pairs), FP32 sincos, FP32 sums per 32
+modes with a compensated total.  `mixed_f64phase`: phase and reduction in
+FP64.  Bar for both: max |err| <= 1e-6 x RMS of the oracle field
+(reference src/field.rs:37-65, :97-182), including the heavy-tailed spectrum
+of the unstructured 3-D benchmark where |k.x| reaches 1e5.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err, rms
+
+pytestmark = pytest.mark.gpu
+NT = os.cpu_count() or 1
+TOL = 1e-6
+
+
+def _case(seed, dim, n, p, kscale=0.5, span=50.0, heavy=False):
+    rng = np.random.default_rng(seed)
+    if heavy:
+        cov = rng.standard_normal((dim, n)) / np.sqrt(rng.chisquare(1, n)) * kscale
+    else:
+        cov = rng.normal(0, kscale, (dim, n))
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(0, span, (dim, p))
+    return cov, z1, z2, pos
+
+
+@pytest.mark.parametrize("form", ["mixed", "mixed_f64phase"])
+@pytest.mark.parametrize("dim,n,p", [(1, 300, 5000), (2, 1000, 20000), (3, 64, 1 << 16),
+                                     (3, 1, 100), (2, 7, 33), (3, 2000, 4000)])
+def test_mixed_scalar(gsc, form, dim, n, p):
+    cov, z1, z2, pos = _case(dim * 100 + n, dim, n, p)
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+    out = gsc.summate(cov, z1, z2, pos, form=form)
+    err = rel_err(out, ref)
+    print(f"{form} d={dim} N={n} P={p}: {err:.3e}")
+    assert err <= TOL
+
+
+@pytest.mark.parametrize("form", ["mixed", "mixed_f64phase"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mixed_incompr(gsc, form, dim):
+    cov, z1, z2, pos = _case(7 + dim, dim, 500, 8000)
+    ref = oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)
+    out = gsc.summate_incompr(cov, z1, z2, pos, form=form)
+    assert out.shape == ref.shape and out.flags.f_contiguous
+    err = rel_err(out, ref)
+    print(f"incompr {form} d={dim}: {err:.3e}")
+    assert err <= TOL
+
+
+def test_mixed_heavy_tailed_unstructured(gsc):
+    """The unstructured 3-D benchmark's spectrum (Student-t, l = 5) on
+    [0, 1000]^3 with 4096 modes: |k.x| reaches 1e5."""
+    cov, z1, z2, pos = _case(3, 3, 4096, 1 << 15, kscale=0.2, span=1000.0, heavy=True)
+    assert np.max(np.abs(cov.T @ pos[:, :256])) > 1e4
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+    for form in ("mixed", "mixed_f64phase"):
+        out = gsc.summate(cov, z1, z2, pos, form=form)
+        err = rel_err(out, ref)
+        e_rms = float(np.sqrt(np.mean((out - ref) ** 2)) / rms(ref))
+        print(f"{form} heavy 3-D 4096 modes: max {err:.3e} rms {e_rms:.3e}")
+        assert err <= TOL
+
+
+def test_mixed_many_modes_chunks_and_splits(gsc):
+    cov, z1, z2, pos = _case(4, 2, 9000, 700)     # few points: modes split across CTAs
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+    assert rel_err(gsc.summate(cov, z1, z2, pos, form="mixed"), ref) <= TOL
+
+
+def test_auto_picks_mixed_within_tolerance(gsc):
+    cov, z1, z2, pos = _case(5, 3, 100, 3000)
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+    out = gsc.summate(cov, z1, z2, pos, tolerance=1e-6, timing=True)
+    assert "mixed_scalar" in [k for k, _ in gsc.last_timings()]
+    assert rel_err(out, ref) <= TOL
+    out = gsc.summate(cov, z1, z2, pos, timing=True)             # default: FP64
+    assert "plain_f64_scalar" in [k for k, _ in gsc.last_timings()]
+    assert rel_err(out, ref) <= 1e-12
+
+
+def test_mixed_on_structured_grid(gsc):
+    rng = np.random.default_rng(6)
+    cov = rng.normal(0, 0.3, (3, 300))
+    z1, z2 = rng.standard_normal(300), rng.standard_normal(300)
+    axes = tuple(np.arange(s, dtype=np.float64) for s in (10, 20, 30))
+    pos = np.array(np.meshgrid(*axes, indexing="ij")).reshape(3, -1)
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+    assert rel_err(gsc.summate_structured(cov, z1, z2, axes, form="mixed"), ref) <= TOL
