@@ -250,6 +250,15 @@ def default_form(w):
     return "sep_f16x5" if w["axes"] is not None else "mixed"
 
 
+def other_forms(w, chosen):
+    """Forms measured beside the chosen one (besides the plain FP64 arm)."""
+    if w["axes"] is not None:
+        cand = ["sep_f64", "sep_f16x3"]
+    else:
+        cand = ["mixed_f64phase"]
+    return [f for f in cand if f != chosen]
+
+
 def make_device_step(gsc, torch, w, form, dev, stream):
     """Returns (step(timing) -> None, out_tensor) running the workload on the device."""
     P = n_points(w)
@@ -335,19 +344,38 @@ def run_ours(args, world, rank, local):
     roof = roofline(args, w, dom, dom_ms, launches_per_step)
 
     # ---- parity spot check of this very output against the oracle ----------
-    err = None
+    err, check = None, None
     if not args.no_check:
         rng = np.random.default_rng(7)
         idx = np.sort(rng.choice(P, size=min(P, 2048), replace=False))
         pos_s = sample_points(w, idx)
         fn = oracle.summator_incompr if w["incompr"] else oracle.summator
         ref = fn(w["cov"], w["z1"], w["z2"], pos_s, num_threads=host_cores())
-        got = out_d.cpu().numpy()
-        got = got[:, idx] if w["incompr"] else got[idx]
         rms = float(np.sqrt(np.mean(ref ** 2)))
-        err = {"max_abs_over_rms": float(np.max(np.abs(got - ref)) / rms),
-               "rms_over_rms": float(np.sqrt(np.mean((got - ref) ** 2)) / rms),
-               "points_checked": int(len(idx)), "reference": "oracle (field.rs restatement), FP64"}
+
+        def check(out_t):
+            got = out_t.cpu().numpy()
+            got = got[:, idx] if w["incompr"] else got[idx]
+            return {"max_abs_over_rms": float(np.max(np.abs(got - ref)) / rms),
+                    "rms_over_rms": float(np.sqrt(np.mean((got - ref) ** 2)) / rms),
+                    "points_checked": int(len(idx)),
+                    "reference": "oracle (field.rs restatement), FP64"}
+        err = check(out_d)
+
+    # ---- the other forms on the same workload (one timed step each) -------
+    others = {}
+    for oform in ([] if args.no_plain else other_forms(w, form)):
+        ostep, oout = make_device_step(gsc, torch, w, oform, dev, stream)
+        ostep()
+        torch.cuda.synchronize()
+        ot, ok_, _ = timed_steps(torch, gsc, ostep, stream, 2, flush)
+        gsc.device_status()
+        oms = max_over_ranks(world, float(np.mean(ot)))
+        others[oform] = {"value": work * world / (oms * 1e-3) / 1e9, "unit": UNIT,
+                         "ms_per_step": oms,
+                         "kernels_ms": {k: float(np.mean(v)) for k, v in ok_.items()},
+                         "error_vs_oracle": check(oout) if check else None}
+        del oout
 
     # ---- the plain FP64 kernel on the same workload (the comparison arm) ---
     plain = None
@@ -412,6 +440,7 @@ def run_ours(args, world, rank, local):
                    "wall_s": t_wall},
         "error_vs_oracle": err,
         "plain_fp64": plain,
+        "other_forms": others,
         "kernels_ms_per_step": {k: float(np.sum(v) / args.steps) for k, v in kern.items()},
         "gpu_launches": int(launches),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),

@@ -39,7 +39,7 @@ const char *kernel_name(int32_t id) {
         "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
-        "mixed_f64phase",
+        "mixed_f64phase", "sep_f64_dmma",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -203,7 +203,7 @@ static int resolve_opts(const gsc_opts *o, Resolved *r) {
     if (!o) return GSC_OK;
     if (o->struct_size < static_cast<int32_t>(sizeof(gsc_opts)))
         return set_error(GSC_ERR_INVALID, "gsc_opts.struct_size is smaller than sizeof(gsc_opts)");
-    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_MIXED_F64PHASE)
+    if (o->form < GSC_FORM_AUTO || o->form > GSC_FORM_SEP_F64)
         return set_error(GSC_ERR_INVALID, "unknown form");
     r->form = o->form;
     r->device = o->device;
@@ -243,7 +243,8 @@ static int check_device_ptr(const void *p, const char *name) {
 static int plain_variant(const Resolved &r) { return r.form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0; }
 
 static bool is_sep(int form) {
-    return form == GSC_FORM_SEP_F16X3 || form == GSC_FORM_SEP_BF16X3 || form == GSC_FORM_SEP_F16X5;
+    return form == GSC_FORM_SEP_F16X3 || form == GSC_FORM_SEP_BF16X3 ||
+           form == GSC_FORM_SEP_F16X5 || form == GSC_FORM_SEP_F64;
 }
 
 static int unstructured_form(const Resolved &r) {
@@ -279,7 +280,7 @@ static int structured_form(const Resolved &r, int64_t dim) {
     if (f == GSC_FORM_AUTO)
         f = r.tolerance >= kBoundSepF16x3   ? GSC_FORM_SEP_F16X3
             : r.tolerance >= kBoundSepF16x5 ? GSC_FORM_SEP_F16X5
-                                            : GSC_FORM_PLAIN_F64;
+                                            : GSC_FORM_SEP_F64;
     if (is_sep(f) && dim < 2)   // 1-D: nothing to contract
         f = (r.form == GSC_FORM_AUTO && r.tolerance >= kBoundMixed) ? GSC_FORM_MIXED
                                                                   : GSC_FORM_PLAIN_F64;
@@ -473,7 +474,7 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
         a.chunk_kblocks = 0;
         a.out = out;
         a.status = ctx.status;
-        return sep_tc_run(ctx, a, st);
+        return form == GSC_FORM_SEP_F64 ? sep_f64_run(ctx, a, st) : sep_tc_run(ctx, a, st);
     }
     // plain FP64 forms on the expanded grid
     const double *pos = axis[0];

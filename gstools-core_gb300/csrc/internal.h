@@ -46,6 +46,7 @@ enum KernelId : int32_t {
     K_MIXED_SCALAR = 12,   // mixed form, double-float phase, scalar field
     K_MIXED_INCOMPR = 13,  // mixed form, double-float phase, vector field
     K_MIXED_F64PHASE = 14, // mixed form with the phase in FP64
+    K_SEP_F64 = 15,        // separable contraction on the FP64 MMA
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -129,6 +130,7 @@ struct SepArgs {
     int *status;              // device status word (0 = ok)
 };
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);
+int sep_f64_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);   // separable_f64.cu
 
 // meshgrid(axis..., indexing="ij") flattened: pos[d * P + p], device
 int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double *pos,

@@ -30,6 +30,7 @@ FORMS = {
     "sep_f16x5": 5,
     "mixed": 6,
     "mixed_f64phase": 7,
+    "sep_f64": 8,
 }
 
 

@@ -72,12 +72,16 @@ extern "C" {
                                   the field RMS for |k.x| up to ~1e6        */
 #define GSC_FORM_MIXED_F64PHASE 7 /* as GSC_FORM_MIXED with the phase and its
                                   reduction in FP64                          */
+#define GSC_FORM_SEP_F64    8  /* structured grids: separable contraction in
+                                  FP64 on the double-precision MMA; FP64
+                                  round-off (below 1e-12 of the field RMS)   */
 
 /* ---- flags ----------------------------------------------------------- */
 #define GSC_FLAG_TIMING     1  /* record per-kernel CUDA-event timings      */
 
-/* AUTO on structured grids picks GSC_FORM_SEP_F16X3 for tolerance >= 1e-5,
- * GSC_FORM_SEP_F16X5 for tolerance >= 1e-6, else GSC_FORM_PLAIN_F64; on
+/* AUTO on structured grids (2-D, 3-D) picks GSC_FORM_SEP_F16X3 for
+ * tolerance >= 1e-5, GSC_FORM_SEP_F16X5 for tolerance >= 1e-6, else
+ * GSC_FORM_SEP_F64; on
  * explicit points GSC_FORM_MIXED for tolerance >= 1e-6, else PLAIN_F64.
  *
  * Options.  Pass NULL for the defaults (form AUTO at tolerance 1e-12,

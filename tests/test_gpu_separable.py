@@ -19,7 +19,8 @@ from conftest import rel_err, rms
 pytestmark = pytest.mark.gpu
 
 NT = os.cpu_count() or 1
-BOUND = {"plain": 1e-12, "sep_f16x5": 1e-6, "sep_f16x3": 1e-5, "sep_bf16x3": 1e-4}
+BOUND = {"plain": 1e-12, "sep_f64": 1e-12, "sep_f16x5": 1e-6, "sep_f16x3": 1e-5,
+         "sep_bf16x3": 1e-4}
 
 
 def _grid_case(seed, shape, n, kscale=0.3, heavy=False, spacing=1.0, origin=0.0):
@@ -42,7 +43,7 @@ def _report(name, err):
     print(f"{name}: max|err|/rms = {err:.3e}")
 
 
-@pytest.mark.parametrize("form", ["plain", "sep_f16x5", "sep_f16x3", "sep_bf16x3"])
+@pytest.mark.parametrize("form", ["plain", "sep_f64", "sep_f16x5", "sep_f16x3", "sep_bf16x3"])
 @pytest.mark.parametrize("shape,n", [
     ((37, 300), 100),          # 2-D: 1 row tile, 2 column tiles
     ((20, 150, 40), 77),       # 3-D: ragged rows, one k-chunk
@@ -59,7 +60,7 @@ def test_structured_scalar(gsc, form, shape, n):
     assert err <= BOUND[form]
 
 
-@pytest.mark.parametrize("form", ["plain", "sep_f16x5", "sep_f16x3"])
+@pytest.mark.parametrize("form", ["plain", "sep_f64", "sep_f16x5", "sep_f16x3"])
 @pytest.mark.parametrize("shape,n", [((30, 70), 150), ((12, 40, 30), 200), ((5, 129, 100), 64)])
 def test_structured_incompr(gsc, form, shape, n):
     cov, z1, z2, axes = _grid_case(3 * sum(shape) + n, shape, n)
@@ -76,7 +77,7 @@ def test_heavy_tailed_c2_like(gsc):
     64^3 grid with 2000 modes: the tensor-core form stays within its bound."""
     cov, z1, z2, axes = _grid_case(2, (64, 64, 64), 2000, kscale=1 / 20, heavy=True)
     ref = oracle.summator(cov, z1, z2, _flat(axes), num_threads=NT)
-    for form in ("sep_f16x5", "sep_f16x3"):
+    for form in ("sep_f64", "sep_f16x5", "sep_f16x3"):
         out = gsc.summate_structured(cov, z1, z2, axes, form=form)
         err = rel_err(out, ref)
         e_rms = float(np.sqrt(np.mean((out - ref) ** 2)) / rms(ref))
@@ -89,7 +90,7 @@ def test_auto_respects_tolerance(gsc):
     ref = oracle.summator(cov, z1, z2, _flat(axes))
     tight = gsc.summate_structured(cov, z1, z2, axes, timing=True)
     assert rel_err(tight, ref) <= 1e-12            # default tolerance: FP64 forms only
-    assert "sep_tc_f16x3" not in [k for k, _ in gsc.last_timings()]
+    assert "sep_f64_dmma" in [k for k, _ in gsc.last_timings()]
     mid = gsc.summate_structured(cov, z1, z2, axes, tolerance=1e-6, timing=True)
     assert "sep_tc_f16x5" in [k for k, _ in gsc.last_timings()]
     assert rel_err(mid, ref) <= BOUND["sep_f16x5"]
