@@ -166,6 +166,8 @@ struct TabArgs {
     float2 *btab;                // [n_modes][nm]
     uint32_t *ghi, *glo;         // [ncn_pad][k_pad/2] packed (re, -im) pairs
     float *wnorm;                // x5 form: {W, 1/W}, W = 2^ceil(log2 max|z1 - i z2|)
+    int tiled;                   // x5 form: B table and G stored as contiguous stage blocks
+    int kbt;                     // x5 form: k-blocks (16 modes each)
 };
 
 __global__ void sep_svec_kernel(TabArgs t) {
@@ -184,14 +186,26 @@ __global__ void sep_svec_kernel(TabArgs t) {
     t.svec[i] = w;
 }
 
-// B table [n_modes][nm_ld]; columns nm .. nm_ld-1 are zero padding (TMA
-// tiles of the x5 form read whole 128-row blocks).
+// B table [n_modes][nm_ld], columns nm .. nm_ld-1 zero.  For the x5 form
+// (tiled) the same values are stored as contiguous 16 KB blocks, one per
+// (128-row tile, k-block of 16 modes): block (mt, kb) holds
+// [16 modes][128 rows] float2, exactly the shared-memory image its stage
+// needs, so one bulk copy moves it.
 __global__ void sep_btab_kernel(TabArgs t) {
+    // the tiled layout also zero-fills the modes past n_modes of the last k-block
+    const int64_t nj = t.tiled ? static_cast<int64_t>(t.kbt) * 16 : t.n_modes;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= static_cast<int64_t>(t.n_modes) * t.nm_ld) return;
+    if (i >= nj * t.nm_ld) return;
     const int j = static_cast<int>(i / t.nm_ld), m = static_cast<int>(i % t.nm_ld);
-    t.btab[i] = m < t.nm ? cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m])
+    const float2 v = (m < t.nm && j < t.n_modes)
+                         ? cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m])
                          : make_float2(0.f, 0.f);
+    if (t.tiled) {
+        const int mt = m / 128, r = m % 128, kb = j / 16, q = j % 16;
+        t.btab[((static_cast<int64_t>(mt) * t.kbt + kb) * 16 + q) * 128 + r] = v;
+    } else {
+        t.btab[i] = v;
+    }
 }
 
 template <bool BF16>
@@ -562,13 +576,21 @@ __global__ void sep_gtab_x5_kernel(TabArgs t) {
     const float g1r = rintf(re * gs) * gu, g1i = rintf(im * gs) * gu;
     const __half2 h1 = __floats2half2_rn(g1r, g1i);
     const __half2 h2 = __floats2half2_rn(re * kUnit - g1r, im * kUnit - g1i);
-    t.ghi[i] = *reinterpret_cast<const uint32_t *>(&h1);
-    t.glo[i] = *reinterpret_cast<const uint32_t *>(&h2);
+    // Stored as contiguous 16 KB stage blocks, one per (256-row tile, k-block
+    // of 16 modes), already in the 64-byte-swizzled K-major layout the MMA
+    // reads: row r at r * 64 bytes, 16-byte chunk c at c ^ ((r >> 1) & 3).
+    const int nt = row / BN, r = row % BN, kb = j / 16, jl = j % 16;
+    const int64_t blk = (static_cast<int64_t>(nt) * t.kbt + kb) * (BN * 64);
+    const int off = r * 64 + (((jl >> 2) ^ ((r >> 1) & 3)) << 4) + (jl & 3) * 4;
+    const int64_t w = (blk + off) / 4;
+    t.ghi[w] = *reinterpret_cast<const uint32_t *>(&h1);
+    t.glo[w] = *reinterpret_cast<const uint32_t *>(&h2);
 }
 
 struct X5Params {
     TcParams base;
     const float *wnorm;      // {W, 1/W, 2^(bF-1), 2^15 / 2^(bF-1)}
+    const unsigned char *g1, *g2, *bt;   // stage blocks (see the table kernels)
 };
 
 // three-slice split of one component in units of 2^15
@@ -598,8 +620,7 @@ constexpr int X5_TMA_BYTES = 2 * X5_G_BYTES + X5_BT_BYTES;
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
 
 __global__ void __launch_bounds__(X5_THREADS, 1)
-sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant__ CUtensorMap map_g2,
-              const __grid_constant__ CUtensorMap map_bt, const X5Params xp) {
+sep_x5_kernel(const X5Params xp) {
     const TcParams &p = xp.base;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -640,11 +661,6 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
         tmem_alloc(tmem_slot, kTmemCols);
         tmem_relinquish();
     }
-    if (warp == 12 && lane == 0) {
-        tma_prefetch_map(&map_g1);
-        tma_prefetch_map(&map_g2);
-        tma_prefetch_map(&map_bt);
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -662,10 +678,12 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap map_g1, const __grid_constant_
                                         kErrTimeoutEmpty))
                     break;
                 unsigned char *st = smem + s * X5_STAGE_V2;
+                const int64_t gblk = (static_cast<int64_t>(nt) * KB + kb) * X5_G_BYTES;
+                const int64_t bblk = (static_cast<int64_t>(mt) * KB + kb) * X5_BT_BYTES;
                 mbar_arrive_expect_tx(&full_t[s], X5_TMA_BYTES);
-                tma_load_2d(st + X5_OFF_G1, &map_g1, &full_t[s], kb * X5_BK, n0);
-                tma_load_2d(st + X5_OFF_G2, &map_g2, &full_t[s], kb * X5_BK, n0);
-                tma_load_2d(st + X5_OFF_BT, &map_bt, &full_t[s], m0, kb * 16);
+                bulk_copy_g2s(st + X5_OFF_G1, xp.g1 + gblk, X5_G_BYTES, &full_t[s]);
+                bulk_copy_g2s(st + X5_OFF_G2, xp.g2 + gblk, X5_G_BYTES, &full_t[s]);
+                bulk_copy_g2s(st + X5_OFF_BT, xp.bt + bblk, X5_BT_BYTES, &full_t[s]);
                 ++issued;
             }
             if (*abort_flag)
@@ -904,7 +922,9 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int KB = std::max(1, (2 * N + bk - 1) / bk);
     const int k_pad = KB * bk;
     const int ncn = ncomp * nn;
-    const int nm_ld = (nm + 15) / 16 * 16;
+    const int m_tiles_ = (nm + BM - 1) / BM;
+    // x5 stores the B table as whole 128-row tiles
+    const int nm_ld = x5 ? m_tiles_ * BM : (nm + 15) / 16 * 16;
     const int n_tiles = (ncn + BN - 1) / BN;
     const int ncn_pad = n_tiles * BN;
     const int m_tiles = (nm + BM - 1) / BM;
@@ -913,7 +933,8 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const size_t off_wn = 0;
     const size_t off_svec = 1024;
     const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(N), 1024);
-    const size_t off_ghi = align_up(off_btab + sizeof(float2) * static_cast<size_t>(N) * nm_ld, 1024);
+    const size_t bt_modes = x5 ? static_cast<size_t>(KB) * 16 : static_cast<size_t>(N);
+    const size_t off_ghi = align_up(off_btab + sizeof(float2) * bt_modes * nm_ld, 1024);
     const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
     const size_t off_glo = align_up(off_ghi + g_bytes, 1024);
     const size_t total = off_glo + g_bytes;
@@ -947,12 +968,14 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.ghi = reinterpret_cast<uint32_t *>(base + off_ghi);
     t.glo = reinterpret_cast<uint32_t *>(base + off_glo);
     t.wnorm = x5 ? reinterpret_cast<float *>(base + off_wn) : nullptr;
+    t.tiled = x5 ? 1 : 0;
+    t.kbt = KB;
 
     {
         TimedLaunch tl(st);
         tl.begin(K_SEP_TABLES);
         if (x5) sep_wnorm_kernel<<<1, 256, 0, st>>>(a.z1, a.z2, N, t.wnorm);
-        const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(N) * nm_ld;
+        const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(bt_modes) * nm_ld;
         const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
         if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
         if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
@@ -966,15 +989,13 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         GSC_CUDA(cudaGetLastError());
     }
 
-    CUtensorMap mh, ml, mb;
-    const CUtensorMapDataType gtype =
-        bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
-    const CUtensorMapSwizzle gswz = x5 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
-    GSC_TRY(make_map(&mh, t.ghi, gtype, 2, k_pad, ncn_pad, bk, BN, gswz));
-    GSC_TRY(make_map(&ml, t.glo, gtype, 2, k_pad, ncn_pad, bk, BN, gswz));
-    if (x5)
-        GSC_TRY(make_map(&mb, t.btab, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, nm_ld, N, BM, 16,
-                         CU_TENSOR_MAP_SWIZZLE_NONE));
+    CUtensorMap mh, ml;
+    if (!x5) {
+        const CUtensorMapDataType gtype =
+            bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+        GSC_TRY(make_map(&mh, t.ghi, gtype, 2, k_pad, ncn_pad, bk, BN, CU_TENSOR_MAP_SWIZZLE_128B));
+        GSC_TRY(make_map(&ml, t.glo, gtype, 2, k_pad, ncn_pad, bk, BN, CU_TENSOR_MAP_SWIZZLE_128B));
+    }
 
     TcParams p;
     p.svec = t.svec;
@@ -1001,6 +1022,9 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         X5Params xp;
         xp.base = p;
         xp.wnorm = t.wnorm;
+        xp.g1 = reinterpret_cast<const unsigned char *>(t.ghi);
+        xp.g2 = reinterpret_cast<const unsigned char *>(t.glo);
+        xp.bt = reinterpret_cast<const unsigned char *>(t.btab);
         static bool configured = false;
         if (!configured) {
             GSC_CUDA(cudaFuncSetAttribute(sep_x5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1008,7 +1032,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             configured = true;
         }
         tl.begin(K_SEP_TC_F16X5);
-        sep_x5_kernel<<<static_cast<unsigned>(grid), X5_THREADS, kSmemX5v2, st>>>(mh, ml, mb, xp);
+        sep_x5_kernel<<<static_cast<unsigned>(grid), X5_THREADS, kSmemX5v2, st>>>(xp);
     } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
         if (bf16) {
