@@ -644,6 +644,12 @@ sep_x5_kernel(const X5Params xp) {
     const int m0 = mt * BM, n0 = nt * BN;
     const int KB = p.kb_total, KC = p.kc;
     const int NC = (KB + KC - 1) / KC;
+    // Every tile walks the k-blocks from its own starting point, so the
+    // CTAs of a wave do not all fetch the same table blocks at the same
+    // moment (which hot-spots a few L2 slices); the sums do not depend on
+    // the order (the main sum is exact, the rest is drained in chunks).
+    const int rot = static_cast<int>((static_cast<int64_t>(blockIdx.x) * 97) % KB);
+    auto kb_of = [&](int i) { const int t = i + rot; return t >= KB ? t - KB : t; };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < X5_STAGES; ++s) {
@@ -672,8 +678,8 @@ sep_x5_kernel(const X5Params xp) {
         if (warp == 12 && lane == 0) {
             // ---- TMA: G1, G2, B-table tile --------------------------------------
             int issued = 0;
-            for (int kb = 0; kb < KB; ++kb) {
-                const int s = kb % X5_STAGES, n = kb / X5_STAGES;
+            for (int i = 0; i < KB; ++i) {
+                const int s = i % X5_STAGES, n = i / X5_STAGES, kb = kb_of(i);
                 if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status,
                                         kErrTimeoutEmpty))
                     break;
@@ -687,17 +693,17 @@ sep_x5_kernel(const X5Params xp) {
                 ++issued;
             }
             if (*abort_flag)
-                for (int kb = issued > X5_STAGES ? issued - X5_STAGES : 0; kb < issued; ++kb)
-                    mbar_wait_drain(&full_t[kb % X5_STAGES], (kb / X5_STAGES) & 1, p.status);
+                for (int i = issued > X5_STAGES ? issued - X5_STAGES : 0; i < issued; ++i)
+                    mbar_wait_drain(&full_t[i % X5_STAGES], (i / X5_STAGES) & 1, p.status);
         } else if (warp == 13 && lane == 0) {
             // ---- MMA ---------------------------------------------------------
             const uint32_t idesc = idesc_f16(BM, BN, false);
             bool ok = true;
-            for (int kb = 0; kb < KB; ++kb) {
-                const int s = kb % X5_STAGES, n = kb / X5_STAGES;
-                const int c = kb / KC;
-                const bool first = (kb % KC) == 0;
-                const bool last = (kb % KC) == KC - 1 || kb == KB - 1;
+            for (int i = 0; i < KB; ++i) {
+                const int s = i % X5_STAGES, n = i / X5_STAGES;
+                const int c = i / KC;
+                const bool first = (i % KC) == 0;
+                const bool last = (i % KC) == KC - 1 || i == KB - 1;
                 ok = mbar_wait(&full_t[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
                 if (ok) ok = mbar_wait(&full_a[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
                 if (!ok) break;
@@ -709,7 +715,7 @@ sep_x5_kernel(const X5Params xp) {
                 for (int kk = 0; kk < X5_BK / 16; ++kk) {
                     const uint32_t o = kk * 32;
                     mma_f16_ss(t_main, desc_k_sw64(f1 + o), desc_k_sw64(g1 + o), idesc,
-                               (kb > 0 || kk > 0) ? 1u : 0u);
+                               (i > 0 || kk > 0) ? 1u : 0u);
                 }
                 if (first && c > 0) {
                     ok = mbar_wait(cross_empty, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
@@ -749,11 +755,11 @@ sep_x5_kernel(const X5Params xp) {
                 dst[q] = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
             }
         };
-        load_s(0, sj);
-        for (int kb = 0; kb < KB; ++kb) {
-            const int s = kb % X5_STAGES, n = kb / X5_STAGES;
+        load_s(kb_of(0), sj);
+        for (int i = 0; i < KB; ++i) {
+            const int s = i % X5_STAGES, n = i / X5_STAGES;
             float2 sn[16];
-            if (kb + 1 < KB) load_s(kb + 1, sn);
+            if (i + 1 < KB) load_s(kb_of(i + 1), sn);
             if (!mbar_wait(&full_t[s], n & 1, abort_flag, p.status, kErrTimeoutFull)) break;
             unsigned char *st = smem + s * X5_STAGE_V2;
             const float2 *bt = reinterpret_cast<const float2 *>(st + X5_OFF_BT);
