@@ -499,9 +499,10 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 //   warp 13     MMA issuer and TMEM owner; warps 14-15 idle
 // Stages: F1/F2/F3 3 x 16 KB + G1/G2 2 x 32 KB = 112 KB, two stages.
 // ---------------------------------------------------------------------------
-constexpr int X5_THREADS = 512;
-constexpr int X5_EPI_REGS = 160, X5_PROD_REGS = 152, X5_CTRL_REGS = 40;
-static_assert(4 * 32 * (2 * X5_EPI_REGS + X5_PROD_REGS + X5_CTRL_REGS) <= X5_THREADS * 128,
+constexpr int X5_THREADS = 384;                 // 8 worker warps + 4 control warps
+constexpr int X5_LAUNCH_REGS = 168;             // 65536 / 384, rounded down to 8
+constexpr int X5_WORK_REGS = 208, X5_CTRL_REGS = 56;
+static_assert(4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS) <= X5_THREADS * X5_LAUNCH_REGS,
               "setmaxnreg split exceeds the registers the block is launched with");
 constexpr float kUnit = 32768.0f;            // 2^15
 constexpr int kLeadBitsG = 11;               // G1 grid: 2^15 * rint(G * 2^10) / 2^10
@@ -593,19 +594,19 @@ struct X5Params {
     const unsigned char *g1, *g2, *bt;   // stage blocks (see the table kernels)
 };
 
-// three-slice split of one component in units of 2^15
-__device__ __forceinline__ void slice3(float x, float lead_scale, float lead_unit, float &s1,
-                                       float &s2, float &s3) {
-    s1 = rintf(x * lead_scale) * lead_unit;
-    const float r = fmaf(x, kUnit, -s1);            // exact
-    s2 = __half2float(__float2half_rn(r));
-    s3 = r - s2;                                    // exact; rounded to f16 by the caller
-}
-
 // Pipeline of the x5 kernel: k-blocks of 32 K elements (16 modes), three
 // stages of 72 KB: F1 F2 F3 (128 rows x 64 B each), G1 G2 (256 rows x 64 B,
-// by TMA, 64-byte swizzle) and the B-table tile (16 modes x 128 rows of
-// float2, by TMA) that the producers read instead of going to L2.
+// 64-byte swizzle) and the B-table tile (16 modes x 128 rows of float2),
+// the last three moved by contiguous bulk copies from pre-tiled tables.
+//
+// Warp roles (12 warps): warps 0-7 are "workers": worker warp w builds, for
+// rows 32*(w%4) .. +31 of the F tile, the modes 8*(w/4) .. +7 of every
+// k-block (two warps per SM sub-partition share the slicing work), and
+// drains TMEM lanes 32*(w%4).., columns 128*(w/4) .. +128 of the cross
+// accumulator into 128 FP32 registers; warp 8 issues the bulk copies,
+// warp 9 the MMAs (and owns TMEM), warps 10-11 idle.  Workers drain a
+// finished cross chunk whenever they find one, also while they wait for
+// copies, so no wait of theirs can block the MMA that would release it.
 constexpr int X5_BK = 32;
 constexpr int X5_STAGES = 3;
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
@@ -618,6 +619,21 @@ constexpr int X5_STAGE_V2 = X5_OFF_BT + X5_BT_BYTES;   // 72 KB
 constexpr size_t kSmemX5v2 = X5_STAGES * X5_STAGE_V2 + 1024 + 256;
 constexpr int X5_TMA_BYTES = 2 * X5_G_BYTES + X5_BT_BYTES;
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
+constexpr int kTmaWarpX5 = 8, kMmaWarpX5 = 9;
+
+// three slices of a (re, im) pair in units of 2^15, packed as half2
+__device__ __forceinline__ void slice3x2(float2 v, float ls, float lu, uint32_t &w1, uint32_t &w2,
+                                         uint32_t &w3) {
+    const float s1x = rintf(v.x * ls) * lu, s1y = rintf(v.y * ls) * lu;
+    const float rx = fmaf(v.x, kUnit, -s1x), ry = fmaf(v.y, kUnit, -s1y);   // exact
+    const __half2 h1 = __floats2half2_rn(s1x, s1y);
+    const __half2 h2 = __floats2half2_rn(rx, ry);
+    const float2 b2 = __half22float2(h2);
+    const __half2 h3 = __floats2half2_rn(rx - b2.x, ry - b2.y);             // exact differences
+    w1 = *reinterpret_cast<const uint32_t *>(&h1);
+    w2 = *reinterpret_cast<const uint32_t *>(&h2);
+    w3 = *reinterpret_cast<const uint32_t *>(&h3);
+}
 
 __global__ void __launch_bounds__(X5_THREADS, 1)
 sep_x5_kernel(const X5Params xp) {
@@ -626,11 +642,11 @@ sep_x5_kernel(const X5Params xp) {
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + X5_STAGES * X5_STAGE_V2);
-    uint64_t *full_t = bars;                    // [3] TMA -> producers, MMA (1 arrival + bytes)
-    uint64_t *full_a = bars + 3;                // [3] producers -> MMA (128 arrivals)
-    uint64_t *empty = bars + 6;                 // [3] MMA commit -> TMA
-    uint64_t *cross_full = bars + 9;            // MMA commit -> epilogue (per chunk)
-    uint64_t *cross_empty = bars + 10;          // epilogue -> MMA (256 arrivals)
+    uint64_t *full_t = bars;                    // [3] copies -> workers, MMA (1 arrival + bytes)
+    uint64_t *full_a = bars + 3;                // [3] workers -> MMA (256 arrivals)
+    uint64_t *empty = bars + 6;                 // [3] MMA commit -> copy warp
+    uint64_t *cross_full = bars + 9;            // MMA commit -> workers (per chunk)
+    uint64_t *cross_empty = bars + 10;          // workers -> MMA (256 arrivals)
     uint64_t *drain = bars + 11;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 12);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
@@ -646,15 +662,15 @@ sep_x5_kernel(const X5Params xp) {
     const int NC = (KB + KC - 1) / KC;
     // Every tile walks the k-blocks from its own starting point, so the
     // CTAs of a wave do not all fetch the same table blocks at the same
-    // moment (which hot-spots a few L2 slices); the sums do not depend on
-    // the order (the main sum is exact, the rest is drained in chunks).
+    // moment; the sums do not depend on the order (the main sum is exact,
+    // the rest is drained in chunks).
     const int rot = static_cast<int>((static_cast<int64_t>(blockIdx.x) * 97) % KB);
     auto kb_of = [&](int i) { const int t = i + rot; return t >= KB ? t - KB : t; };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < X5_STAGES; ++s) {
             mbar_init(&full_t[s], 1);
-            mbar_init(&full_a[s], 128);
+            mbar_init(&full_a[s], 256);
             mbar_init(&empty[s], 1);
         }
         mbar_init(cross_full, 1);
@@ -663,7 +679,7 @@ sep_x5_kernel(const X5Params xp) {
         *abort_flag = 0;
         fence_mbar_init();
     }
-    if (warp == 13) {
+    if (warp == kMmaWarpX5) {
         tmem_alloc(tmem_slot, kTmemCols);
         tmem_relinquish();
     }
@@ -673,10 +689,10 @@ sep_x5_kernel(const X5Params xp) {
     const uint32_t tmem = *tmem_slot;
     const uint32_t t_main = tmem, t_cross = tmem + 256;
 
-    if (warp >= 12) {
+    if (warp >= 8) {
         regs_dec<X5_CTRL_REGS>();
-        if (warp == 12 && lane == 0) {
-            // ---- TMA: G1, G2, B-table tile --------------------------------------
+        if (warp == kTmaWarpX5 && lane == 0) {
+            // ---- bulk copies: G1, G2, B-table block ----------------------------
             int issued = 0;
             for (int i = 0; i < KB; ++i) {
                 const int s = i % X5_STAGES, n = i / X5_STAGES, kb = kb_of(i);
@@ -695,7 +711,7 @@ sep_x5_kernel(const X5Params xp) {
             if (*abort_flag)
                 for (int i = issued > X5_STAGES ? issued - X5_STAGES : 0; i < issued; ++i)
                     mbar_wait_drain(&full_t[i % X5_STAGES], (i / X5_STAGES) & 1, p.status);
-        } else if (warp == 13 && lane == 0) {
+        } else if (warp == kMmaWarpX5 && lane == 0) {
             // ---- MMA ---------------------------------------------------------
             const uint32_t idesc = idesc_f16(BM, BN, false);
             bool ok = true;
@@ -739,46 +755,97 @@ sep_x5_kernel(const X5Params xp) {
                 mbar_wait_drain(drain, 0, p.status);
             }
         }
-    } else if (warp >= 8) {
-        regs_inc<X5_PROD_REGS>();
-        // ---- producers: row r of the F tile, 16 modes per k-block ----------------
-        const int r = threadIdx.x - 256;
+    } else {
+        regs_inc<X5_WORK_REGS>();
+        // ---- workers: F-tile slices, cross drains, final epilogue -----------------
+        const int q = warp & 3, h = warp >> 2;
+        const int r = 32 * q + lane;                            // F row and TMEM lane
+        const uint32_t lane_off = static_cast<uint32_t>(32 * q) << 16;
         const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
-        const uint32_t row_off = r * 64;                       // 64-byte rows
-        const uint32_t swz = (r >> 1) & 3;                     // 64-byte swizzle phase
+        const uint32_t row_off = r * 64;                        // 64-byte rows
+        const uint32_t swz = (r >> 1) & 3;                      // 64-byte swizzle phase
         const float ls = xp.wnorm[2], lu = xp.wnorm[3];
-        float2 sj[16];
-        auto load_s = [&](int kb, float2 (&dst)[16]) {
+        float tot[128];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int j = kb * 16 + q;
-                dst[q] = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
+        for (int i = 0; i < 128; ++i) tot[i] = 0.f;
+        int pend = 0;                                           // next cross chunk to drain
+        auto drain_chunk = [&]() {
+            tc_fence_after();
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                uint32_t v[16];
+                __syncwarp();
+                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
+            }
+            tc_fence_before();
+            mbar_arrive(cross_empty);
+            ++pend;
+        };
+        // Decisions that lead to a warp-collective TMEM load are taken by the
+        // whole warp: a barrier counts as passed once every lane has seen it.
+        auto warp_passed = [&](uint64_t *bar, uint32_t parity) {
+            return __all_sync(0xffffffffu, mbar_try_wait(bar, parity));
+        };
+        // drains every finished, not yet drained chunk except the last one
+        // (a non-blocking probe: most polls find nothing to drain)
+        auto poll_drain = [&]() {
+            while (pend < NC - 1 && __all_sync(0xffffffffu, mbar_test_wait(cross_full, pend & 1)))
+                drain_chunk();
+        };
+        // waits (bounded) for the chunk being drained next or the final commit
+        auto wait_chunk = [&](int c) -> bool {
+            const bool got = mbar_wait(cross_full, c & 1, abort_flag, p.status, kErrTimeoutAcc);
+            return __all_sync(0xffffffffu, got);
+        };
+        // waits for stage s, draining chunks meanwhile; false on timeout/abort
+        auto wait_stage = [&](int s, uint32_t parity) -> bool {
+            if (warp_passed(&full_t[s], parity)) return true;
+            const uint64_t t0 = globaltimer_ns();
+            for (uint32_t it = 1;; ++it) {
+                poll_drain();
+                if (warp_passed(&full_t[s], parity)) return true;
+                if ((it & 63) == 0) {
+                    int stop = *abort_flag ? 1 : (globaltimer_ns() - t0 > kWaitLimitNs ? 2 : 0);
+                    stop = __shfl_sync(0xffffffffu, stop, 0);
+                    if (stop == 2 && lane == 0) {
+                        *abort_flag = 1;
+                        atomicCAS(p.status, 0, kErrTimeoutFull);
+                    }
+                    if (stop) return false;
+                }
             }
         };
+        float2 sj[8];
+        auto load_s = [&](int kb, float2 (&dst)[8]) {
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int j = kb * 16 + 8 * h + t;
+                dst[t] = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
+            }
+        };
+        bool ok = true;
         load_s(kb_of(0), sj);
         for (int i = 0; i < KB; ++i) {
             const int s = i % X5_STAGES, n = i / X5_STAGES;
-            float2 sn[16];
+            float2 sn[8];
             if (i + 1 < KB) load_s(kb_of(i + 1), sn);
-            if (!mbar_wait(&full_t[s], n & 1, abort_flag, p.status, kErrTimeoutFull)) break;
+            if (!wait_stage(s, n & 1)) {
+                ok = false;
+                break;
+            }
             unsigned char *st = smem + s * X5_STAGE_V2;
             const float2 *bt = reinterpret_cast<const float2 *>(st + X5_OFF_BT);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {          // 16-byte chunk c: modes 4c .. 4c+3
+            for (int cc = 0; cc < 2; ++cc) {          // 16-byte chunks 2h, 2h+1: modes 4c .. 4c+3
+                const int c = 2 * h + cc;
                 uint32_t w1[4], w2[4], w3[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int jl = c * 4 + q;
-                    const float2 v = cmulf(bt[jl * BM + r], sj[jl]);
-                    float a1, a2, a3, b1, b2, b3;
-                    slice3(v.x, ls, lu, a1, a2, a3);
-                    slice3(v.y, ls, lu, b1, b2, b3);
-                    const __half2 h1 = __floats2half2_rn(a1, b1);
-                    const __half2 h2 = __floats2half2_rn(a2, b2);
-                    const __half2 h3 = __floats2half2_rn(a3, b3);
-                    w1[q] = *reinterpret_cast<const uint32_t *>(&h1);
-                    w2[q] = *reinterpret_cast<const uint32_t *>(&h2);
-                    w3[q] = *reinterpret_cast<const uint32_t *>(&h3);
+                for (int t = 0; t < 4; ++t) {
+                    const float2 v = cmulf(bt[(4 * c + t) * BM + r], sj[4 * cc + t]);
+                    slice3x2(v, ls, lu, w1[t], w2[t], w3[t]);
                 }
                 const uint32_t phys = row_off + ((c ^ swz) << 4);
                 *reinterpret_cast<uint4 *>(st + phys) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
@@ -790,55 +857,37 @@ sep_x5_kernel(const X5Params xp) {
             fence_proxy_async_smem();
             mbar_arrive(&full_a[s]);
 #pragma unroll
-            for (int q = 0; q < 16; ++q) sj[q] = sn[q];
+            for (int t = 0; t < 8; ++t) sj[t] = sn[t];
+            poll_drain();
         }
-    } else {
-        regs_inc<X5_EPI_REGS>();
-        // ---- epilogue ------------------------------------------------------------
-        const int q = warp & 3, h = warp >> 2;
-        const uint32_t lane_off = static_cast<uint32_t>(32 * q) << 16;
-        const int m = m0 + 32 * q + lane;
-        float tot[128];
-#pragma unroll
-        for (int i = 0; i < 128; ++i) tot[i] = 0.f;
-        bool ok = true;
-        for (int c = 0; c < NC; ++c) {
-            ok = mbar_wait(cross_full, c & 1, abort_flag, p.status, kErrTimeoutAcc);
-            if (!ok) break;
-            tc_fence_after();
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                uint32_t v[16];
-                __syncwarp();
-                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, v);
-                tmem_ld_wait();
-#pragma unroll
-                for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
-            }
-            if (c < NC - 1) {
-                tc_fence_before();
-                mbar_arrive(cross_empty);
-            }
+        // remaining non-final chunks, then the final one (it follows every MMA)
+        while (ok && pend < NC - 1) {
+            ok = wait_chunk(pend);
+            if (ok) drain_chunk();
         }
+        if (ok) ok = wait_chunk(NC - 1);
         if (ok) {
-            // the last cross commit follows every MMA: main is complete
+            tc_fence_after();
             const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
+            const int m = m0 + r;
             const bool row_ok = m < p.nm;
             double *orow = p.out + static_cast<int64_t>(b) * p.batch_stride +
                            static_cast<int64_t>(row_ok ? m : 0) * p.row_stride;
 #pragma unroll
             for (int g = 0; g < 8; ++g) {
-                uint32_t v[16];
+                uint32_t v[16], x[16];
                 __syncwarp();
                 tmem_ld16(t_main + lane_off + 128 * h + 16 * g, v);
+                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, x);
                 tmem_ld_wait();
                 const int gn0 = n0 + 128 * h + 16 * g;
                 if (row_ok && gn0 < p.ncn) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int gn = gn0 + i;
+                    for (int t = 0; t < 16; ++t) {
+                        const int gn = gn0 + t;
                         if (gn < p.ncn) {
-                            const float val = (__uint_as_float(v[i]) + tot[16 * g + i]) * unscale;
+                            const float val = (__uint_as_float(v[t]) +
+                                               (tot[16 * g + t] + __uint_as_float(x[t]))) * unscale;
                             const int comp = gn / p.nn;
                             orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(val);
                         }
@@ -852,7 +901,7 @@ sep_x5_kernel(const X5Params xp) {
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 13) tmem_dealloc(tmem, kTmemCols);
+    if (warp == kMmaWarpX5) tmem_dealloc(tmem, kTmemCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -1033,6 +1082,13 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         xp.bt = reinterpret_cast<const unsigned char *>(t.btab);
         static bool configured = false;
         if (!configured) {
+            // The warps re-balance their registers with setmaxnreg; the
+            // increases can only be served from what the block was launched
+            // with, so a build that launches with fewer registers must not run.
+            cudaFuncAttributes fa{};
+            GSC_CUDA(cudaFuncGetAttributes(&fa, sep_x5_kernel));
+            if (fa.numRegs * X5_THREADS < 4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS))
+                return set_error(GSC_ERR_KERNEL, "x5 kernel built with too few registers per thread");
             GSC_CUDA(cudaFuncSetAttribute(sep_x5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(kSmemX5v2)));
             configured = true;
