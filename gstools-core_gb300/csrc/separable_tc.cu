@@ -501,7 +501,7 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 // ---------------------------------------------------------------------------
 constexpr int X5_THREADS = 384;                 // 8 worker warps + 4 control warps
 constexpr int X5_LAUNCH_REGS = 168;             // 65536 / 384, rounded down to 8
-constexpr int X5_WORK_REGS = 208, X5_CTRL_REGS = 56;
+constexpr int X5_WORK_REGS = 216, X5_CTRL_REGS = 48;
 static_assert(4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS) <= X5_THREADS * X5_LAUNCH_REGS,
               "setmaxnreg split exceeds the registers the block is launched with");
 constexpr float kUnit = 32768.0f;            // 2^15
@@ -867,31 +867,35 @@ sep_x5_kernel(const X5Params xp) {
         }
         if (ok) ok = wait_chunk(NC - 1);
         if (ok) {
+            // Every MMA has completed, so the stage buffers are free: each
+            // warp turns its 32 rows x 32 columns blocks around in shared
+            // memory (pitch 33 doubles) and stores them row by row, 256
+            // contiguous bytes per instruction.
             tc_fence_after();
             const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
-            const int m = m0 + r;
-            const bool row_ok = m < p.nm;
-            double *orow = p.out + static_cast<int64_t>(b) * p.batch_stride +
-                           static_cast<int64_t>(row_ok ? m : 0) * p.row_stride;
+            double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
+            double *ob = p.out + static_cast<int64_t>(b) * p.batch_stride;
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                uint32_t v[16], x[16];
+            for (int g = 0; g < 4; ++g) {
+                uint32_t v[32];
                 __syncwarp();
-                tmem_ld16(t_main + lane_off + 128 * h + 16 * g, v);
-                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, x);
+                tmem_ld32(t_cross + lane_off + 128 * h + 32 * g, v);
                 tmem_ld_wait();
-                const int gn0 = n0 + 128 * h + 16 * g;
-                if (row_ok && gn0 < p.ncn) {
 #pragma unroll
-                    for (int t = 0; t < 16; ++t) {
-                        const int gn = gn0 + t;
-                        if (gn < p.ncn) {
-                            const float val = (__uint_as_float(v[t]) +
-                                               (tot[16 * g + t] + __uint_as_float(x[t]))) * unscale;
-                            const int comp = gn / p.nn;
-                            orow[comp * p.comp_stride + (gn - comp * p.nn)] = f32_to_f64(val);
-                        }
-                    }
+                for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
+                tmem_ld32(t_main + lane_off + 128 * h + 32 * g, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int t = 0; t < 32; ++t)
+                    tr[lane * 33 + t] = f32_to_f64((__uint_as_float(v[t]) + tot[32 * g + t]) * unscale);
+                __syncwarp();
+                const int gn = n0 + 128 * h + 32 * g + lane;
+                if (gn < p.ncn) {
+                    const int comp = gn / p.nn;
+                    double *oc = ob + comp * p.comp_stride + (gn - comp * p.nn);
+                    const int rows = min(32, p.nm - (m0 + 32 * q));
+                    for (int R = 0; R < rows; ++R)
+                        oc[static_cast<int64_t>(m0 + 32 * q + R) * p.row_stride] = tr[R * 33 + lane];
                 }
             }
             __syncwarp();
