@@ -39,7 +39,7 @@ const char *kernel_name(int32_t id) {
         "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
-        "mixed_f64phase", "sep_f64_dmma",
+        "mixed_f64phase", "sep_f64_dmma", "fourier_scale",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -240,8 +240,6 @@ static int check_device_ptr(const void *p, const char *name) {
     return GSC_OK;
 }
 
-static int plain_variant(const Resolved &r) { return r.form == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0; }
-
 static bool is_sep(int form) {
     return form == GSC_FORM_SEP_F16X3 || form == GSC_FORM_SEP_BF16X3 ||
            form == GSC_FORM_SEP_F16X5 || form == GSC_FORM_SEP_F64;
@@ -322,7 +320,8 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
                       int64_t z1s, const double *z2, int64_t z2s, const double *pos,
                       int64_t ps_d, int64_t ps_p, int64_t dim, int64_t N, int64_t P,
                       double *out, int64_t os_d, int64_t os_p, bool incompr,
-                      const gsc_opts *opts) {
+                      const gsc_opts *opts, const double *sf = nullptr, int64_t sfs = 0) {
+    // sf != nullptr: Fourier method, spectrum factor sf[j * sfs] (scalar field)
     Resolved ro;
     GSC_TRY(resolve_opts(opts, &ro));
     GSC_TRY(check_sizes(dim, N, P));
@@ -336,6 +335,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(unstructured_form(ro));
     timing_reset(ro.flags & GSC_FLAG_TIMING);
     if (P == 0) return GSC_OK;
+    const size_t n_sf = sf ? static_cast<size_t>(N) : 0;
 
     DeviceCtx *ctx = nullptr;
     GSC_TRY(get_ctx(ro.device, &ctx));
@@ -346,7 +346,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
 
     const int64_t nout = incompr ? dim : 1;
     const size_t n_cov = static_cast<size_t>(dim * N), n_pos = static_cast<size_t>(dim * P);
-    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_pos;
+    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_pos;
     const size_t n_out = static_cast<size_t>(nout * P);
     const size_t bytes = (n_in + n_out) * sizeof(double);
     GSC_TRY(ensure_pinned(*ctx, bytes));
@@ -356,15 +356,18 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     gather2(cov, cs_d, cs_n, dim, N, h);
     gather2(z1, 0, z1s, 1, N, h + n_cov);
     gather2(z2, 0, z2s, 1, N, h + n_cov + N);
-    gather2(pos, ps_d, ps_p, dim, P, h + n_cov + 2 * N);
+    if (sf) gather2(sf, 0, sfs, 1, N, h + n_cov + 2 * N);
+    gather2(pos, ps_d, ps_p, dim, P, h + n_cov + 2 * N + n_sf);
 
     double *d = static_cast<double *>(ctx->io.ptr);
     GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
+                                  d + n_cov + N, st));
     PlainArgs a;
     a.cov = d;
     a.z1 = d + n_cov;
     a.z2 = d + n_cov + N;
-    a.pos = d + n_cov + 2 * N;
+    a.pos = d + n_cov + 2 * N + n_sf;
     a.dim = dim;
     a.n_modes = N;
     a.n_points = P;
@@ -386,9 +389,23 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     return GSC_OK;
 }
 
+// Spectrum-scaled copies of z1, z2 for device-pointer Fourier calls, in the
+// context's own buffer (the caller's arrays stay untouched).
+static int scaled_modes(DeviceCtx &ctx, const double *sf, const double *&z1, const double *&z2,
+                        int64_t N, cudaStream_t st) {
+    if (N == 0) return GSC_OK;
+    GSC_TRY(ensure_dev(ctx, ctx.zscaled, 2 * static_cast<size_t>(N) * sizeof(double)));
+    GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
+    double *zs = static_cast<double *>(ctx.zscaled.ptr);
+    GSC_TRY(fourier_scale(sf, z1, z2, N, zs, zs + N, st));
+    z1 = zs;
+    z2 = zs + N;
+    return GSC_OK;
+}
+
 static int dev_plain(const double *cov, const double *z1, const double *z2, const double *pos,
                      int64_t dim, int64_t N, int64_t P, double *out, bool incompr,
-                     const gsc_opts *opts) {
+                     const gsc_opts *opts, bool fourier = false, const double *sf = nullptr) {
     Resolved ro;
     GSC_TRY(resolve_opts(opts, &ro));
     GSC_TRY(check_sizes(dim, N, P));
@@ -412,6 +429,11 @@ static int dev_plain(const double *cov, const double *z1, const double *z2, cons
     GSC_TRY(check_device_ptr(z2, "z2"));
     GSC_TRY(check_device_ptr(pos, "pos"));
     GSC_TRY(check_device_ptr(out, "out"));
+    if (fourier) {
+        GSC_TRY(need_ptr(sf, N > 0, "spectrum_factor"));
+        if (N > 0) GSC_TRY(check_device_ptr(sf, "spectrum_factor"));
+        GSC_TRY(scaled_modes(*ctx, sf, z1, z2, N, ro.stream));
+    }
     PlainArgs a;
     a.cov = cov;
     a.z1 = z1;
@@ -507,7 +529,8 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
 static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
                            int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
                            const double *const *ax, const int64_t *n, const int64_t *sx,
-                           double *out, bool incompr, const gsc_opts *opts) {
+                           double *out, bool incompr, const gsc_opts *opts,
+                           const double *sf = nullptr, int64_t sfs = 0) {
     Resolved ro;
     GSC_TRY(resolve_opts(opts, &ro));
     GSC_TRY(check_structured(dim, N, n, incompr));
@@ -532,7 +555,8 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     const size_t n_cov = static_cast<size_t>(dim * N);
     size_t n_ax = 0;
     for (int d = 0; d < dim; ++d) n_ax += static_cast<size_t>(n[d]);
-    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_ax;
+    const size_t n_sf = sf ? static_cast<size_t>(N) : 0;
+    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_ax;
     const size_t n_out = static_cast<size_t>(nout * P);
     GSC_TRY(ensure_pinned(*ctx, n_in * sizeof(double)));
     GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out) * sizeof(double) + 1024));
@@ -540,7 +564,8 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     gather2(cov, cs_d, cs_n, dim, N, h);
     gather2(z1, 0, z1s, 1, N, h + n_cov);
     gather2(z2, 0, z2s, 1, N, h + n_cov + N);
-    size_t off = n_cov + 2 * N;
+    if (sf) gather2(sf, 0, sfs, 1, N, h + n_cov + 2 * N);
+    size_t off = n_cov + 2 * N + n_sf;
     double *d = static_cast<double *>(ctx->io.ptr);
     const double *dax[3] = {nullptr, nullptr, nullptr};
     for (int k = 0; k < dim; ++k) {
@@ -549,6 +574,8 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         off += static_cast<size_t>(n[k]);
     }
     GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
+                                  d + n_cov + N, st));
     // output buffer 128-byte aligned after the inputs
     double *dout = reinterpret_cast<double *>(
         (reinterpret_cast<uintptr_t>(d + n_in) + 127) & ~static_cast<uintptr_t>(127));
@@ -561,7 +588,8 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
 
 static int dev_structured(const double *cov, const double *z1, const double *z2, int64_t dim,
                           int64_t N, const double *const *ax, const int64_t *n, double *out,
-                          bool incompr, const gsc_opts *opts) {
+                          bool incompr, const gsc_opts *opts, bool fourier = false,
+                          const double *sf = nullptr) {
     Resolved ro;
     GSC_TRY(resolve_opts(opts, &ro));
     GSC_TRY(check_structured(dim, N, n, incompr));
@@ -584,6 +612,11 @@ static int dev_structured(const double *cov, const double *z1, const double *z2,
     GSC_TRY(check_device_ptr(z2, "z2"));
     for (int d = 0; d < dim; ++d) GSC_TRY(check_device_ptr(ax[d], "axis"));
     GSC_TRY(check_device_ptr(out, "out"));
+    if (fourier) {
+        GSC_TRY(need_ptr(sf, N > 0, "spectrum_factor"));
+        if (N > 0) GSC_TRY(check_device_ptr(sf, "spectrum_factor"));
+        GSC_TRY(scaled_modes(*ctx, sf, z1, z2, N, ro.stream));
+    }
     return run_structured(*ctx, ro, cov, z1, z2, dim, N, ax, n, incompr, out, ro.stream);
 }
 
@@ -657,6 +690,26 @@ int gsc_summate_incompr_dev(const double *cov, const double *z1, const double *z
                             const double *pos, int64_t dim, int64_t n_modes, int64_t n_points,
                             double *out, const gsc_opts *opts) {
     return dev_plain(cov, z1, z2, pos, dim, n_modes, n_points, out, true, opts);
+}
+
+int gsc_summate_fourier_f64(const double *spectrum_factor, int64_t sf_stride, const double *modes,
+                            int64_t modes_stride_d, int64_t modes_stride_n, const double *z1,
+                            int64_t z1_stride, const double *z2, int64_t z2_stride,
+                            const double *pos, int64_t pos_stride_d, int64_t pos_stride_p,
+                            int64_t dim, int64_t n_modes, int64_t n_points, double *out,
+                            int64_t out_stride, const gsc_opts *opts) {
+    if (!spectrum_factor && n_modes > 0)
+        return set_error(GSC_ERR_INVALID, "spectrum_factor is NULL");
+    return host_plain(modes, modes_stride_d, modes_stride_n, z1, z1_stride, z2, z2_stride, pos,
+                      pos_stride_d, pos_stride_p, dim, n_modes, n_points, out, 0, out_stride,
+                      false, opts, n_modes > 0 ? spectrum_factor : nullptr, sf_stride);
+}
+
+int gsc_summate_fourier_dev(const double *spectrum_factor, const double *modes, const double *z1,
+                            const double *z2, const double *pos, int64_t dim, int64_t n_modes,
+                            int64_t n_points, double *out, const gsc_opts *opts) {
+    return dev_plain(modes, z1, z2, pos, dim, n_modes, n_points, out, false, opts, true,
+                     spectrum_factor);
 }
 
 int gsc_summate_dev_noalloc(const double *cov, const double *z1, const double *z2,
@@ -761,6 +814,33 @@ int gsc_summate_incompr_structured_dev(const double *cov, const double *z1, cons
     const double *ax[3] = {a0, a1, a2};
     const int64_t n[3] = {n0, n1, n2};
     return dev_structured(cov, z1, z2, dim, n_modes, ax, n, out, true, opts);
+}
+
+int gsc_summate_fourier_structured_f64(const double *spectrum_factor, int64_t sf_stride,
+                                       const double *modes, int64_t ms_d, int64_t ms_n,
+                                       const double *z1, int64_t z1s, const double *z2,
+                                       int64_t z2s, int64_t dim, int64_t n_modes,
+                                       const double *a0, int64_t n0, int64_t s0,
+                                       const double *a1, int64_t n1, int64_t s1,
+                                       const double *a2, int64_t n2, int64_t s2, double *out,
+                                       const gsc_opts *opts) {
+    if (!spectrum_factor && n_modes > 0)
+        return set_error(GSC_ERR_INVALID, "spectrum_factor is NULL");
+    const double *ax[3] = {a0, a1, a2};
+    const int64_t n[3] = {n0, n1, n2}, sx[3] = {s0, s1, s2};
+    return host_structured(modes, ms_d, ms_n, z1, z1s, z2, z2s, dim, n_modes, ax, n, sx, out,
+                           false, opts, n_modes > 0 ? spectrum_factor : nullptr, sf_stride);
+}
+
+int gsc_summate_fourier_structured_dev(const double *spectrum_factor, const double *modes,
+                                       const double *z1, const double *z2, int64_t dim,
+                                       int64_t n_modes, const double *a0, int64_t n0,
+                                       const double *a1, int64_t n1, const double *a2,
+                                       int64_t n2, double *out, const gsc_opts *opts) {
+    const double *ax[3] = {a0, a1, a2};
+    const int64_t n[3] = {n0, n1, n2};
+    return dev_structured(modes, z1, z2, dim, n_modes, ax, n, out, false, opts, true,
+                          spectrum_factor);
 }
 
 }  // extern "C"

@@ -47,6 +47,7 @@ enum KernelId : int32_t {
     K_MIXED_INCOMPR = 13,  // mixed form, double-float phase, vector field
     K_MIXED_F64PHASE = 14, // mixed form with the phase in FP64
     K_SEP_F64 = 15,        // separable contraction on the FP64 MMA
+    K_FOURIER_SCALE = 16,  // spectrum factor folded into z1, z2 (Fourier method)
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -69,6 +70,7 @@ struct DeviceCtx {
     void *pinned = nullptr;          // pinned host staging
     size_t pinned_bytes = 0;
     DevBuf grid;                     // expanded meshgrid for plain forms on grids
+    DevBuf zscaled;                  // spectrum-scaled z1, z2 of device-pointer Fourier calls
     int *status = nullptr;           // sticky kernel status word (device)
 };
 
@@ -131,6 +133,11 @@ struct SepArgs {
 };
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);
 int sep_f64_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);   // separable_f64.cu
+
+// Fourier method (src/field.rs:219-249): z1s[j] = sf[j] * z1[j],
+// z2s[j] = sf[j] * z2[j], device pointers; z1s may alias z1 (in place).
+int fourier_scale(const double *sf, const double *z1, const double *z2, int64_t n, double *z1s,
+                  double *z2s, cudaStream_t st);
 
 // meshgrid(axis..., indexing="ij") flattened: pos[d * P + p], device
 int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double *pos,

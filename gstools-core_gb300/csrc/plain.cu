@@ -344,7 +344,31 @@ __global__ void grid_expand_kernel(const double *__restrict__ a0, const double *
     }
 }
 
+// Fourier method: the spectrum factor multiplies z1 cos + z2 sin of its mode
+// (src/field.rs:241-242), so folding it into z1, z2 once per call lets every
+// summator form compute the Fourier field unchanged.
+__global__ void fourier_scale_kernel(const double *__restrict__ sf, const double *z1,
+                                     const double *z2, int64_t n, double *z1s, double *z2s) {
+    const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double f = sf[j], a = z1[j], b = z2[j];
+    z1s[j] = __dmul_rn(f, a);
+    z2s[j] = __dmul_rn(f, b);
+}
+
 }  // namespace
+
+int fourier_scale(const double *sf, const double *z1, const double *z2, int64_t n, double *z1s,
+                  double *z2s, cudaStream_t st) {
+    if (n == 0) return GSC_OK;
+    TimedLaunch tl(st);
+    tl.begin(K_FOURIER_SCALE);
+    fourier_scale_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(sf, z1, z2, n, z1s,
+                                                                                z2s);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
 
 int split_reduce(const double *part, int64_t S, int64_t nout, int64_t P, double *out, int64_t sd,
                  int64_t sp, cudaStream_t st) {

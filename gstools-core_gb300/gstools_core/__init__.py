@@ -6,6 +6,8 @@ Mirrors the Python module that GSTools-Core's PyO3 layer exposes
     summate(cov_samples, z1, z2, pos, num_threads=None) -> ndarray (n_points,)
     summate_incompr(cov_samples, z1, z2, pos, num_threads=None)
         -> ndarray (dim, n_points), Fortran ordered like the reference
+    summate_fourier(spectrum_factor, modes, z1, z2, pos, num_threads=None)
+        -> ndarray (n_points,)                      (src/lib.rs:67-84)
     __version__
 
 Same argument names, dtypes, shapes and return values.  The work runs on the
@@ -31,9 +33,11 @@ import numpy as np
 from . import _native
 from ._native import GscError, device_count, last_timings
 
-__all__ = ["summate", "summate_incompr", "summate_device", "summate_incompr_device",
-           "summate_structured", "summate_incompr_structured", "summate_structured_device",
-           "summate_incompr_structured_device", "device_status",
+__all__ = ["summate", "summate_incompr", "summate_fourier", "summate_device",
+           "summate_incompr_device", "summate_fourier_device",
+           "summate_structured", "summate_incompr_structured", "summate_fourier_structured",
+           "summate_structured_device", "summate_incompr_structured_device",
+           "summate_fourier_structured_device", "device_status",
            "device_count", "last_timings", "GscError", "__version__"]
 
 __version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
@@ -81,8 +85,8 @@ def _opts(form, tolerance, timing, device=-1, stream=None):
                              tolerance=tolerance or 0.0)
 
 
-def _prepare(cov_samples, z1, z2, pos, num_threads):
-    cov = _array(cov_samples, "cov_samples", 2)
+def _prepare(cov_samples, z1, z2, pos, num_threads, cov_name="cov_samples"):
+    cov = _array(cov_samples, cov_name, 2)
     z1 = _array(z1, "z1", 1)
     z2 = _array(z2, "z2", 1)
     pos = _array(pos, "pos", 2)
@@ -137,6 +141,30 @@ def summate_incompr(cov_samples, z1, z2, pos, num_threads=None, *, form="auto", 
         cov.ctypes.data, cs[0], cs[1], z1.ctypes.data, zs1[0], z2.ctypes.data, zs2[0],
         pos.ctypes.data, ps[0], ps[1], dim, n, p, out.ctypes.data, os_[0], os_[1],
         ctypes.byref(o)))
+    return out
+
+
+def summate_fourier(spectrum_factor, modes, z1, z2, pos, num_threads=None, *, form="auto",
+                    tolerance=None, timing=False, device=-1):
+    """Fourier method (reference ``src/field.rs:219-249``).
+
+    u[p] = sum_j sf[j] (z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p))
+    with k_j = modes[:, j] (the equidistant Fourier grid) and sf the spectrum
+    factor sqrt(2 S(k_j dk)).
+    """
+    sf = _array(spectrum_factor, "spectrum_factor", 1)
+    modes, z1, z2, pos = _prepare(modes, z1, z2, pos, num_threads, "modes")
+    dim, n = modes.shape
+    # the reference zips sf with the mode columns, which asserts equal length
+    _assert_eq(sf.shape[0], n)
+    p = pos.shape[1]
+    out = np.empty(p, dtype=np.float64)
+    ms, zs1, zs2, ps = _strides(modes), _strides(z1), _strides(z2), _strides(pos)
+    o = _opts(form, tolerance, timing, device)
+    _native.check(_native.lib.gsc_summate_fourier_f64(
+        sf.ctypes.data, _strides(sf)[0], modes.ctypes.data, ms[0], ms[1], z1.ctypes.data,
+        zs1[0], z2.ctypes.data, zs2[0], pos.ctypes.data, ps[0], ps[1], dim, n, p,
+        out.ctypes.data, 1, ctypes.byref(o)))
     return out
 
 
@@ -211,14 +239,17 @@ def _axes_host(axes, dim):
 
 
 def _structured_host(fn, cov_samples, z1, z2, axes, num_threads, form, tolerance, timing,
-                     device, incompr):
-    cov = _array(cov_samples, "cov_samples", 2)
+                     device, incompr, spectrum_factor=None):
+    sf = None if spectrum_factor is None else _array(spectrum_factor, "spectrum_factor", 1)
+    cov = _array(cov_samples, "cov_samples" if sf is None else "modes", 2)
     z1 = _array(z1, "z1", 1)
     z2 = _array(z2, "z2", 1)
     _num_threads(num_threads)
     dim, n = cov.shape
     _assert_eq(cov.shape[1], z1.shape[0])
     _assert_eq(cov.shape[1], z2.shape[0])
+    if sf is not None:
+        _assert_eq(sf.shape[0], n)
     ax = _axes_host(axes, dim)
     if incompr and dim not in (2, 3):
         raise ValueError("Only two- and three-dimensional problems are supported.")
@@ -234,8 +265,9 @@ def _structured_host(fn, cov_samples, z1, z2, axes, num_threads, form, tolerance
             args += [a.ctypes.data, a.shape[0], _strides(a)[0]]
     cs, zs1, zs2 = _strides(cov), _strides(z1), _strides(z2)
     o = _opts(form, tolerance, timing, device)
-    _native.check(fn(cov.ctypes.data, cs[0], cs[1], z1.ctypes.data, zs1[0], z2.ctypes.data,
-                     zs2[0], dim, n, *args, out.ctypes.data, ctypes.byref(o)))
+    lead = [] if sf is None else [sf.ctypes.data, _strides(sf)[0]]
+    _native.check(fn(*lead, cov.ctypes.data, cs[0], cs[1], z1.ctypes.data, zs1[0],
+                     z2.ctypes.data, zs2[0], dim, n, *args, out.ctypes.data, ctypes.byref(o)))
     return out
 
 
@@ -263,8 +295,16 @@ def summate_incompr_structured(cov_samples, z1, z2, axes, num_threads=None, *, f
                             z2, axes, num_threads, form, tolerance, timing, device, True)
 
 
+def summate_fourier_structured(spectrum_factor, modes, z1, z2, axes, num_threads=None, *,
+                               form="auto", tolerance=None, timing=False, device=-1):
+    """``summate_fourier`` on the structured grid ``meshgrid(*axes, indexing="ij")``
+    (flat (n_points,) result); the forms are those of ``summate_structured``."""
+    return _structured_host(_native.lib.gsc_summate_fourier_structured_f64, modes, z1, z2, axes,
+                            num_threads, form, tolerance, timing, device, False, spectrum_factor)
+
+
 def _structured_dev(fn, cov_samples, z1, z2, axes, out, form, tolerance, stream, timing,
-                    device, incompr):
+                    device, incompr, spectrum_factor=None):
     cs = cov_samples.__cuda_array_interface__["shape"]
     if len(cs) != 2:
         raise TypeError("cov_samples must be 2-D")
@@ -282,7 +322,9 @@ def _structured_dev(fn, cov_samples, z1, z2, axes, out, form, tolerance, stream,
         args += [None, 0]
     shape = (dim, npts) if incompr else (npts,)
     o = _opts(form, tolerance, timing, device, stream)
-    _native.check(fn(_cuda_view(cov_samples, "cov_samples", (dim, n)), _cuda_view(z1, "z1", (n,)),
+    lead = [] if spectrum_factor is None else [_cuda_view(spectrum_factor, "spectrum_factor", (n,))]
+    _native.check(fn(*lead, _cuda_view(cov_samples, "cov_samples", (dim, n)),
+                     _cuda_view(z1, "z1", (n,)),
                      _cuda_view(z2, "z2", (n,)), dim, n, *args, _cuda_view(out, "out", shape),
                      ctypes.byref(o)))
     return out
@@ -300,6 +342,27 @@ def summate_incompr_structured_device(cov_samples, z1, z2, axes, out, *, form="a
     """``summate_incompr_structured`` on device arrays; ``out`` is (dim, n_points)."""
     return _structured_dev(_native.lib.gsc_summate_incompr_structured_dev, cov_samples, z1, z2,
                            axes, out, form, tolerance, stream, timing, device, True)
+
+
+def summate_fourier_device(spectrum_factor, modes, z1, z2, pos, out, *, form="auto",
+                           tolerance=None, stream=None, timing=False, device=-1):
+    """``summate_fourier`` on device arrays; writes ``out`` (n_points,)."""
+    dim, n, p = _dev_shapes(modes, pos)
+    args = [_cuda_view(spectrum_factor, "spectrum_factor", (n,)),
+            _cuda_view(modes, "modes", (dim, n)), _cuda_view(z1, "z1", (n,)),
+            _cuda_view(z2, "z2", (n,)), _cuda_view(pos, "pos", (dim, p))]
+    o = _opts(form, tolerance, timing, device, stream)
+    _native.check(_native.lib.gsc_summate_fourier_dev(*args, dim, n, p,
+                                                      _cuda_view(out, "out", (p,)),
+                                                      ctypes.byref(o)))
+    return out
+
+
+def summate_fourier_structured_device(spectrum_factor, modes, z1, z2, axes, out, *, form="auto",
+                                      tolerance=None, stream=None, timing=False, device=-1):
+    """``summate_fourier_structured`` on device arrays; writes ``out`` (n_points,)."""
+    return _structured_dev(_native.lib.gsc_summate_fourier_structured_dev, modes, z1, z2, axes,
+                           out, form, tolerance, stream, timing, device, False, spectrum_factor)
 
 
 def device_status(device=-1) -> None:

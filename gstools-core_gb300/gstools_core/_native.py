@@ -81,6 +81,16 @@ SIGNATURES = {
                                                           _I64, _P, _I64, _I64, _P, _OPTS]),
     "gsc_summate_incompr_structured_dev": (ctypes.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _P,
                                                           _I64, _P, _I64, _P, _OPTS]),
+    "gsc_summate_fourier_f64": (ctypes.c_int, [_P, _I64, _P, _I64, _I64, _P, _I64, _P, _I64,
+                                               _P, _I64, _I64, _I64, _I64, _I64, _P, _I64,
+                                               _OPTS]),
+    "gsc_summate_fourier_dev": (ctypes.c_int, [_P, _P, _P, _P, _P, _I64, _I64, _I64, _P, _OPTS]),
+    "gsc_summate_fourier_structured_f64": (ctypes.c_int, [_P, _I64, _P, _I64, _I64, _P, _I64,
+                                                          _P, _I64, _I64, _I64, _P, _I64, _I64,
+                                                          _P, _I64, _I64, _P, _I64, _I64, _P,
+                                                          _OPTS]),
+    "gsc_summate_fourier_structured_dev": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _I64,
+                                                          _P, _I64, _P, _I64, _P, _OPTS]),
 }
 
 

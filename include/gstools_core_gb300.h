@@ -8,9 +8,11 @@
  *            src/field.rs:37-43            -> gsc_summate_f64
  *          pub fn field::summator_incompr(...)
  *            src/field.rs:97-103           -> gsc_summate_incompr_f64
- *   Python gstools_core.summate / summate_incompr (PyO3)
- *            src/lib.rs:33-48, 50-65       -> same two entry points, bound by
- *                                             the package gstools_core
+ *          pub fn field::summator_fourier(...)
+ *            src/field.rs:219-226          -> gsc_summate_fourier_f64
+ *   Python gstools_core.summate / summate_incompr / summate_fourier (PyO3)
+ *            src/lib.rs:33-48, 50-65, 67-84 -> same three entry points, bound
+ *                                             by the package gstools_core
  *
  * Conventions
  *  - Arrays are float64.  Strides are in ELEMENTS (ndarray / numpy strides
@@ -158,6 +160,29 @@ int gsc_summate_dev_noalloc(const double *cov, const double *z1, const double *z
                             const double *pos, int64_t dim, int64_t n_modes,
                             int64_t n_points, double *out, const gsc_opts *opts);
 
+/* ---- Fourier method: src/field.rs:219-249 ----------------------------- */
+/* u[p] = sum_j sf[j] (z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)) with k_j
+ * the columns of `modes` (dim, n_modes) -- the equidistant Fourier grid --
+ * and sf the spectrum factor sqrt(2 S(k_j dk)) (n_modes).  The factor is
+ * folded into z1, z2 on the GPU (one rounding each), after which every form
+ * of gsc_summate_f64 applies.  Replaces field::summator_fourier
+ * (src/field.rs:219) / PyO3 summate_fourier (src/lib.rs:67-84). */
+int gsc_summate_fourier_f64(const double *spectrum_factor, int64_t sf_stride,
+                            const double *modes, int64_t modes_stride_d, int64_t modes_stride_n,
+                            const double *z1, int64_t z1_stride,
+                            const double *z2, int64_t z2_stride,
+                            const double *pos, int64_t pos_stride_d, int64_t pos_stride_p,
+                            int64_t dim, int64_t n_modes, int64_t n_points,
+                            double *out, int64_t out_stride,
+                            const gsc_opts *opts);
+
+/* Device-pointer form: modes (dim, n_modes) and pos (dim, n_points)
+ * row-major; spectrum_factor, z1, z2 (n_modes); out (n_points). */
+int gsc_summate_fourier_dev(const double *spectrum_factor, const double *modes,
+                            const double *z1, const double *z2, const double *pos,
+                            int64_t dim, int64_t n_modes, int64_t n_points,
+                            double *out, const gsc_opts *opts);
+
 /* ---- incompressible vector field: src/field.rs:97-182 ----------------- */
 /* u[i, p] = sum_j p_i(k_j) (z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)),
  * p(k) = e_1 - k k_0 / |k|^2, dim in {2, 3}; out (dim, n_points) written
@@ -217,6 +242,30 @@ int gsc_summate_incompr_structured_f64(const double *cov, int64_t cov_stride_d,
                                        double *out, const gsc_opts *opts);
 
 int gsc_summate_incompr_structured_dev(const double *cov, const double *z1, const double *z2,
+                                       int64_t dim, int64_t n_modes,
+                                       const double *axis0, int64_t n0,
+                                       const double *axis1, int64_t n1,
+                                       const double *axis2, int64_t n2,
+                                       double *out, const gsc_opts *opts);
+
+/* Fourier-method field on a structured grid (the Fourier modes of a periodic
+ * field lie on an equidistant grid, so the separable forms apply): as
+ * gsc_summate_structured_f64 with the spectrum factor of
+ * gsc_summate_fourier_f64.  No reference counterpart (callers of
+ * summator_fourier expand the grid). */
+int gsc_summate_fourier_structured_f64(const double *spectrum_factor, int64_t sf_stride,
+                                       const double *modes, int64_t modes_stride_d,
+                                       int64_t modes_stride_n,
+                                       const double *z1, int64_t z1_stride,
+                                       const double *z2, int64_t z2_stride,
+                                       int64_t dim, int64_t n_modes,
+                                       const double *axis0, int64_t n0, int64_t s0,
+                                       const double *axis1, int64_t n1, int64_t s1,
+                                       const double *axis2, int64_t n2, int64_t s2,
+                                       double *out, const gsc_opts *opts);
+
+int gsc_summate_fourier_structured_dev(const double *spectrum_factor, const double *modes,
+                                       const double *z1, const double *z2,
                                        int64_t dim, int64_t n_modes,
                                        const double *axis0, int64_t n0,
                                        const double *axis1, int64_t n1,
