@@ -39,7 +39,8 @@ const char *kernel_name(int32_t id) {
         "mode_table", "plain_f64_scalar", "plain_f64_incompr", "plain_f64_libm",
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
-        "mixed_f64phase", "sep_f64_dmma", "fourier_scale",
+        "mixed_f64phase", "sep_f64_dmma", "fourier_scale", "batch_tables", "batch_plain",
+        "batch_mixed",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -102,21 +103,6 @@ void TimedLaunch::end() {
 static std::mutex g_ctx_mu;
 static DeviceCtx *g_ctx[64] = {nullptr};
 
-struct DeviceGuard {
-    int prev = -1;
-    bool changed = false;
-    int set(int dev) {
-        GSC_CUDA(cudaGetDevice(&prev));
-        if (prev != dev) {
-            GSC_CUDA(cudaSetDevice(dev));
-            changed = true;
-        }
-        return GSC_OK;
-    }
-    ~DeviceGuard() {
-        if (changed) cudaSetDevice(prev);
-    }
-};
 
 int get_ctx(int device, DeviceCtx **out) {
     int count = 0;
@@ -191,15 +177,8 @@ int ensure_pinned(DeviceCtx &ctx, size_t bytes) {
 // ---------------------------------------------------------------------------
 // options and validation
 // ---------------------------------------------------------------------------
-struct Resolved {
-    int form = GSC_FORM_AUTO;
-    int device = -1;
-    int flags = 0;
-    cudaStream_t stream = nullptr;
-    double tolerance = 1e-12;
-};
 
-static int resolve_opts(const gsc_opts *o, Resolved *r) {
+int resolve_opts(const gsc_opts *o, Resolved *r) {
     if (!o) return GSC_OK;
     if (o->struct_size < static_cast<int32_t>(sizeof(gsc_opts)))
         return set_error(GSC_ERR_INVALID, "gsc_opts.struct_size is smaller than sizeof(gsc_opts)");
@@ -225,7 +204,7 @@ static int need_ptr(const void *p, bool needed, const char *name) {
     return GSC_OK;
 }
 
-static int check_device_ptr(const void *p, const char *name) {
+int check_device_ptr(const void *p, const char *name) {
     if (!p) return GSC_OK;
     cudaPointerAttributes at;
     cudaError_t e = cudaPointerGetAttributes(&at, p);

@@ -8,6 +8,7 @@
 
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "gstools_core_gb300.h"
 
@@ -48,6 +49,9 @@ enum KernelId : int32_t {
     K_MIXED_F64PHASE = 14, // mixed form with the phase in FP64
     K_SEP_F64 = 15,        // separable contraction on the FP64 MMA
     K_FOURIER_SCALE = 16,  // spectrum factor folded into z1, z2 (Fourier method)
+    K_BATCH_TABLES = 17,   // per-mode tables of every item of a batch
+    K_BATCH_PLAIN = 18,    // persistent FP64 batch kernel (device work queue)
+    K_BATCH_MIXED = 19,    // persistent mixed-precision batch kernel
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -72,7 +76,38 @@ struct DeviceCtx {
     DevBuf grid;                     // expanded meshgrid for plain forms on grids
     DevBuf zscaled;                  // spectrum-scaled z1, z2 of device-pointer Fourier calls
     int *status = nullptr;           // sticky kernel status word (device)
+    gsc_batch *batch = nullptr;      // plan of the last host-pointer batch call
+    std::vector<int64_t> batch_sig;  // its shape signature (reused when equal)
 };
+
+// Makes `dev` current for the guard's lifetime.
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    int set(int dev) {
+        GSC_CUDA(cudaGetDevice(&prev));
+        if (prev != dev) {
+            GSC_CUDA(cudaSetDevice(dev));
+            changed = true;
+        }
+        return GSC_OK;
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+// Options after defaults are applied (capi.cu).
+struct Resolved {
+    int form = GSC_FORM_AUTO;
+    int device = -1;
+    int flags = 0;
+    cudaStream_t stream = nullptr;
+    double tolerance = 1e-12;
+};
+int resolve_opts(const gsc_opts *o, Resolved *r);
+// GSC_OK for NULL or device-accessible memory, else GSC_ERR_INVALID naming `name`.
+int check_device_ptr(const void *p, const char *name);
 
 // Returns the context of `device` (-1 = current), initialising it once.
 int get_ctx(int device, DeviceCtx **out);
@@ -133,6 +168,48 @@ struct SepArgs {
 };
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);
 int sep_f64_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);   // separable_f64.cu
+
+// ---- batched ensembles (batch.cu, with kernels in plain.cu / mixed.cu) ------
+// One realization of an ensemble as the device kernels see it.
+struct BatchItem {
+    const double *cov, *z1, *z2, *sf;   // sf: Fourier spectrum factor or nullptr
+    const double *pos;                  // (dim, n_points) row-major
+    double *out;                        // (nout, n_points) row-major
+    double *part;                       // splits > 1: splits slots of nout * n_points
+    int64_t n_modes, n_points, mode_off;   // mode_off: first row of the shared mode tables
+    int32_t dim, incompr, splits, pad;
+};
+// One entry of the device work queue: a block of points of one item and one
+// mode range (split) of it.
+struct BatchUnit {
+    int32_t item, split;
+    int64_t p_first, jb, je;
+};
+constexpr int kBatchThreads = 128;   // threads per block of the batch kernels
+
+// Per-mode tables of every item, one launch (plain.cu / mixed.cu).  mode_prefix
+// has n_items + 1 entries (exclusive prefix sums of n_modes).
+int batch_plain_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,
+                       int64_t total_modes, void *wtab, double *rec, cudaStream_t st);
+int batch_mixed_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,
+                       int64_t total_modes, float *rec, double *rec64, cudaStream_t st);
+// Persistent kernels fed from the work queue `units` through `counter`
+// (zero before the launch).  Shared-memory bytes and occupancy per config:
+size_t batch_plain_smem(int tile);
+int batch_plain_occupancy(int R, int tile, int device);
+int batch_mixed_occupancy(int R, bool f64phase, int device);
+bool batch_plain_config_ok(int R, int tile);
+bool batch_mixed_config_ok(int R);
+int batch_plain_launch(int R, int tile, int blocks, const BatchItem *items,
+                       const BatchUnit *units, int64_t n_units, int *counter, const void *wtab,
+                       const double *rec, cudaStream_t st);
+int batch_mixed_launch(int R, bool f64phase, int blocks, const BatchItem *items,
+                       const BatchUnit *units, int64_t n_units, int *counter, const float *rec,
+                       const double *rec64, cudaStream_t st);
+constexpr int64_t kPlainTableBytesPerMode = 256 * 16;   // W_j[a], a < 256, double2
+constexpr int64_t kPlainRecBytesPerMode = 12 * 8;
+constexpr int64_t kMixedRecBytesPerMode = 12 * 4;
+constexpr int64_t kMixedRec64BytesPerMode = 4 * 8;
 
 // Fourier method (src/field.rs:219-249): z1s[j] = sf[j] * z1[j],
 // z2s[j] = sf[j] * z2[j], device pointers; z1s may alias z1 (in place).

@@ -38,6 +38,7 @@ namespace gsc {
 namespace {
 
 constexpr int kMxThreads = 128;
+static_assert(kMxThreads == kBatchThreads, "batch units assume the mixed block size");
 constexpr int kMxR = 4;              // points per thread
 constexpr int kMxTile = 32;          // modes per FP32 accumulation tile
 constexpr int kMxRec = 12;           // floats per mode: kh0 kh1 kh2 kl0 kl1 kl2 z1 z2 w0 w1 w2 -
@@ -52,26 +53,22 @@ constexpr float kS0 = 6.2831854820251465f, kS1 = -41.34170150756836f, kS2 = 81.6
 constexpr float kC0 = 1.0f, kC1 = -19.739208221435547f, kC2 = 64.93931579589844f,
                 kC3 = -85.44285583496094f, kC4 = 59.220428466796875f;
 
-__global__ void mixed_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
-                                  const double *__restrict__ z2, int64_t dim, int64_t n_modes,
-                                  int64_t j0, int64_t nc, int incompr, float *__restrict__ rec,
-                                  double *__restrict__ rec64) {
-    const int64_t jl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (jl >= nc) return;
-    const int64_t j = j0 + jl;
+__device__ __forceinline__ void mixed_mode_entry(const double *__restrict__ cov, double z1j,
+                                                 double z2j, int64_t dim, int64_t n_modes,
+                                                 int64_t j, int incompr, float *__restrict__ r,
+                                                 double *__restrict__ r64) {
     double k[3] = {0.0, 0.0, 0.0};
     for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
-    float *r = rec + jl * kMxRec;
     for (int d = 0; d < 3; ++d) {
         const double kap = k[d] * kInv2Pi;
         const float hi = __double2float_rn(kap);
         r[d] = hi;
         r[3 + d] = __double2float_rn(kap - static_cast<double>(hi));
-        rec64[jl * kMxRec64 + d] = kap;
+        r64[d] = kap;
     }
-    rec64[jl * kMxRec64 + 3] = 0.0;
-    r[6] = __double2float_rn(z1[j]);
-    r[7] = __double2float_rn(z2[j]);
+    r64[3] = 0.0;
+    r[6] = __double2float_rn(z1j);
+    r[7] = __double2float_rn(z2j);
     double w0 = 0.0, w1 = 0.0, w2 = 0.0;
     if (incompr) {   // projector as the reference forms it (src/field.rs:138-152)
         double kk = 0.0;
@@ -85,6 +82,42 @@ __global__ void mixed_mode_kernel(const double *__restrict__ cov, const double *
     r[9] = __double2float_rn(w1);
     r[10] = __double2float_rn(w2);
     r[11] = 0.f;
+}
+
+__global__ void mixed_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+                                  const double *__restrict__ z2, int64_t dim, int64_t n_modes,
+                                  int64_t j0, int64_t nc, int incompr, float *__restrict__ rec,
+                                  double *__restrict__ rec64) {
+    const int64_t jl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (jl >= nc) return;
+    const int64_t j = j0 + jl;
+    mixed_mode_entry(cov, z1[j], z2[j], dim, n_modes, j, incompr, rec + jl * kMxRec,
+                     rec64 + jl * kMxRec64);
+}
+
+// Records of every item of a batch, one thread per mode (Fourier factor
+// folded into z1, z2 first).
+__global__ void batch_mixed_table_kernel(const BatchItem *__restrict__ items,
+                                         const int64_t *__restrict__ prefix, int64_t n_items,
+                                         int64_t total, float *__restrict__ rec,
+                                         double *__restrict__ rec64) {
+    const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int64_t lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const BatchItem &it = items[lo];
+    const int64_t j = g - it.mode_off;
+    double z1j = it.z1[j], z2j = it.z2[j];
+    if (it.sf) {
+        const double f = it.sf[j];
+        z1j = __dmul_rn(f, z1j);
+        z2j = __dmul_rn(f, z2j);
+    }
+    mixed_mode_entry(it.cov, z1j, z2j, it.dim, it.n_modes, j, it.incompr, rec + g * kMxRec,
+                     rec64 + g * kMxRec64);
 }
 
 // (z1 cos + z2 sin)(2 pi (th + tl)), th in [-1/2, 1/2] turns, tl tiny
@@ -125,18 +158,20 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float a) {
     lo += e;
 }
 
-template <int D, bool INC, bool F64P>
-__global__ void __launch_bounds__(kMxThreads)
-mixed_kernel(const double *__restrict__ pos, int64_t P, const float *__restrict__ rec,
-             const double *__restrict__ rec64, int64_t nc, int64_t mps, int accumulate,
-             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+// One block's work: the kMxThreads*R points from p_first (thread t owns
+// p_first + t + r*kMxThreads), modes [jb, je) of the records `rec`, `rec64`;
+// sums written (accumulate=0) or added at dst + i*sd + p*sp.  srec / srec64
+// are shared-memory staging areas of kMxTile records.
+template <int D, int R, bool INC, bool F64P>
+__device__ __forceinline__ void mixed_block(const double *__restrict__ pos, int64_t P,
+                                            int64_t p_first, const float *__restrict__ rec,
+                                            const double *__restrict__ rec64, int64_t jb,
+                                            int64_t je, int accumulate, double *__restrict__ dst,
+                                            int64_t sd, int64_t sp, float *srec, double *srec64) {
     constexpr int NOUT = INC ? D : 1;
-    __shared__ __align__(16) float srec[kMxTile * kMxRec];
-    __shared__ __align__(16) double srec64[F64P ? kMxTile * kMxRec64 : 1];
+    constexpr int kMxR = R;
     const int tid = threadIdx.x;
-    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * (kMxThreads * kMxR) + tid;
-    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
-    const int64_t je = min(nc, jb + mps);
+    const int64_t p0 = p_first + tid;
 
     float xh[kMxR][D], xl[kMxR][D];
     double xd[kMxR][D];
@@ -214,7 +249,7 @@ mixed_kernel(const double *__restrict__ pos, int64_t P, const float *__restrict_
             }
     }
 
-    double *d0 = dst + static_cast<int64_t>(blockIdx.y) * split_stride;
+    double *d0 = dst;
 #pragma unroll
     for (int r = 0; r < kMxR; ++r) {
         const int64_t p = p0 + r * kMxThreads;
@@ -224,6 +259,70 @@ mixed_kernel(const double *__restrict__ pos, int64_t P, const float *__restrict_
             const double v = static_cast<double>(hi[r][i]) + static_cast<double>(lo[r][i]);
             double *o = d0 + i * sd + p * sp;
             *o = accumulate ? *o + v : v;
+        }
+    }
+}
+
+template <int D, bool INC, bool F64P>
+__global__ void __launch_bounds__(kMxThreads)
+mixed_kernel(const double *__restrict__ pos, int64_t P, const float *__restrict__ rec,
+             const double *__restrict__ rec64, int64_t nc, int64_t mps, int accumulate,
+             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    __shared__ __align__(16) float srec[kMxTile * kMxRec];
+    __shared__ __align__(16) double srec64[F64P ? kMxTile * kMxRec64 : 1];
+    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
+    const int64_t je = min(nc, jb + mps);
+    mixed_block<D, kMxR, INC, F64P>(pos, P, static_cast<int64_t>(blockIdx.x) * (kMxThreads * kMxR),
+                                    rec, rec64, jb, je, accumulate,
+                                    dst + static_cast<int64_t>(blockIdx.y) * split_stride, sd, sp,
+                                    srec, srec64);
+}
+
+// Persistent batch kernel (see batch_plain_kernel in plain.cu).
+template <int R, bool F64P>
+__global__ void __launch_bounds__(kMxThreads)
+batch_mixed_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict__ units,
+                   int64_t n_units, int *__restrict__ counter, const float *__restrict__ rec,
+                   const double *__restrict__ rec64) {
+    __shared__ __align__(16) float srec[kMxTile * kMxRec];
+    __shared__ __align__(16) double srec64[F64P ? kMxTile * kMxRec64 : 1];
+    __shared__ int s_unit;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1);
+        __syncthreads();
+        const int64_t u = s_unit;
+        if (u >= n_units) break;
+        const BatchUnit w = units[u];
+        const BatchItem &it = items[w.item];
+        const int64_t P = it.n_points;
+        const int64_t nout = it.incompr ? it.dim : 1;
+        double *dst = it.splits > 1 ? it.part + static_cast<int64_t>(w.split) * nout * P : it.out;
+        const float *rc = rec + it.mode_off * kMxRec;
+        const double *rc64 = rec64 + it.mode_off * kMxRec64;
+        switch (it.dim * 2 + it.incompr) {
+            case 2:
+                mixed_block<1, R, false, F64P>(it.pos, P, w.p_first, rc, rc64, w.jb, w.je, 0, dst,
+                                               P, 1, srec, srec64);
+                break;
+            case 4:
+                mixed_block<2, R, false, F64P>(it.pos, P, w.p_first, rc, rc64, w.jb, w.je, 0, dst,
+                                               P, 1, srec, srec64);
+                break;
+            case 5:
+                mixed_block<2, R, true, F64P>(it.pos, P, w.p_first, rc, rc64, w.jb, w.je, 0, dst,
+                                              P, 1, srec, srec64);
+                break;
+            case 6:
+                mixed_block<3, R, false, F64P>(it.pos, P, w.p_first, rc, rc64, w.jb, w.je, 0, dst,
+                                               P, 1, srec, srec64);
+                break;
+            case 7:
+                mixed_block<3, R, true, F64P>(it.pos, P, w.p_first, rc, rc64, w.jb, w.je, 0, dst,
+                                              P, 1, srec, srec64);
+                break;
+            default:
+                break;
         }
     }
 }
@@ -342,6 +441,63 @@ int mixed_run(DeviceCtx &ctx, const PlainArgs &a, bool f64phase, cudaStream_t st
 
     if (S > 1) GSC_TRY(split_reduce(part, S, nout, P, a.out, a.out_sd, a.out_sp, st));
     GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+    return GSC_OK;
+}
+
+// ---- batched ensembles ----------------------------------------------------------
+int batch_mixed_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,
+                       int64_t total_modes, float *rec, double *rec64, cudaStream_t st) {
+    if (total_modes == 0) return GSC_OK;
+    TimedLaunch tl(st);
+    tl.begin(K_BATCH_TABLES);
+    batch_mixed_table_kernel<<<static_cast<unsigned>((total_modes + 127) / 128), 128, 0, st>>>(
+        items, mode_prefix, n_items, total_modes, rec, rec64);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+namespace {
+using BatchMixedFn = void (*)(const BatchItem *, const BatchUnit *, int64_t, int *, const float *,
+                              const double *);
+BatchMixedFn batch_mixed_fn(int R, bool f64p) {
+    if (f64p) {
+        if (R == 2) return batch_mixed_kernel<2, true>;
+        if (R == 4) return batch_mixed_kernel<4, true>;
+        if (R == 8) return batch_mixed_kernel<8, true>;
+    } else {
+        if (R == 2) return batch_mixed_kernel<2, false>;
+        if (R == 4) return batch_mixed_kernel<4, false>;
+        if (R == 8) return batch_mixed_kernel<8, false>;
+    }
+    return nullptr;
+}
+}  // namespace
+
+bool batch_mixed_config_ok(int R) { return batch_mixed_fn(R, false) != nullptr; }
+
+int batch_mixed_occupancy(int R, bool f64phase, int device) {
+    BatchMixedFn fn = batch_mixed_fn(R, f64phase);
+    if (!fn) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kMxThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    (void)device;
+    return n;
+}
+
+int batch_mixed_launch(int R, bool f64phase, int blocks, const BatchItem *items,
+                       const BatchUnit *units, int64_t n_units, int *counter, const float *rec,
+                       const double *rec64, cudaStream_t st) {
+    BatchMixedFn fn = batch_mixed_fn(R, f64phase);
+    if (!fn) return set_error(GSC_ERR_INVALID, "unsupported batch configuration");
+    TimedLaunch tl(st);
+    tl.begin(K_BATCH_MIXED);
+    fn<<<blocks, kMxThreads, 0, st>>>(items, units, n_units, counter, rec, rec64);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
     return GSC_OK;
 }
 

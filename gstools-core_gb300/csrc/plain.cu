@@ -50,6 +50,7 @@ constexpr int kRec = 12;                            // doubles per mode record
 constexpr int kThreads = 128;                       // threads per block
 constexpr int kTileModes = 8;                       // modes per staged tile
 constexpr int64_t kChunkModes = 16384;              // modes per table build
+static_assert(kThreads == kBatchThreads, "batch units assume the plain block size");
 
 // Mode record layout (doubles): k0 k1 k2 | sum|k| | z1 z2 | w0 w1 w2 | pad
 enum { R_K0 = 0, R_KABS = 3, R_Z1 = 4, R_Z2 = 5, R_W0 = 6 };
@@ -66,24 +67,20 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // Per-mode tables: W_j[a] = (z1 - i z2) e^{i 2 pi a / M} and the mode record.
 // grid (nc), block (kM)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kM)
-mode_table_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
-                  const double *__restrict__ z2, int64_t dim, int64_t n_modes, int64_t j0,
-                  int incompr, int want_table, double2 *__restrict__ wtab,
-                  double *__restrict__ rec) {
-    const int64_t jl = blockIdx.x;
-    const int64_t j = j0 + jl;
+// Table row a (thread) and, for a == 0, the record of mode j.
+__device__ __forceinline__ void mode_entry(const double *__restrict__ cov, double z1j, double z2j,
+                                           int64_t dim, int64_t n_modes, int64_t j, int incompr,
+                                           int want_table, double2 *__restrict__ wrow,
+                                           double *__restrict__ r) {
     const int a = threadIdx.x;
-    const double z1j = z1[j], z2j = z2[j];
     if (want_table) {
         double s, c;
         sincospi(a * (1.0 / (kM / 2)), &s, &c);       // angle 2 pi a / M
-        wtab[jl * kM + a] = make_double2(z1j * c + z2j * s, z1j * s - z2j * c);
+        wrow[a] = make_double2(z1j * c + z2j * s, z1j * s - z2j * c);
     }
     if (a == 0) {
         double k[3] = {0.0, 0.0, 0.0};
         for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
-        double *r = rec + jl * kRec;
         r[R_K0 + 0] = k[0];
         r[R_K0 + 1] = k[1];
         r[R_K0 + 2] = k[2];
@@ -105,6 +102,46 @@ mode_table_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
         r[R_W0 + 2] = w2;
         r[9] = r[10] = r[11] = 0.0;
     }
+}
+
+__global__ void __launch_bounds__(kM)
+mode_table_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+                  const double *__restrict__ z2, int64_t dim, int64_t n_modes, int64_t j0,
+                  int incompr, int want_table, double2 *__restrict__ wtab,
+                  double *__restrict__ rec) {
+    const int64_t jl = blockIdx.x;
+    const int64_t j = j0 + jl;
+    mode_entry(cov, z1[j], z2[j], dim, n_modes, j, incompr, want_table, wtab + jl * kM,
+               rec + jl * kRec);
+}
+
+// item owning global row g: the last i with prefix[i] <= g
+__device__ __forceinline__ int64_t owner_of(const int64_t *__restrict__ prefix, int64_t n,
+                                            int64_t g) {
+    int64_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Tables of every item of a batch: grid (total modes), block (kM).  The
+// Fourier factor, where present, multiplies z1 and z2 first.
+__global__ void __launch_bounds__(kM)
+batch_table_kernel(const BatchItem *__restrict__ items, const int64_t *__restrict__ prefix,
+                   int64_t n_items, double2 *__restrict__ wtab, double *__restrict__ rec) {
+    const int64_t g = blockIdx.x;
+    const BatchItem &it = items[owner_of(prefix, n_items, g)];
+    const int64_t j = g - it.mode_off;
+    double z1j = it.z1[j], z2j = it.z2[j];
+    if (it.sf) {
+        const double f = it.sf[j];
+        z1j = __dmul_rn(f, z1j);
+        z2j = __dmul_rn(f, z2j);
+    }
+    mode_entry(it.cov, z1j, z2j, it.dim, it.n_modes, j, it.incompr, 1, wtab + g * kM,
+               rec + g * kRec);
 }
 
 // phase = k.x in the reference's order (ndarray dot on strided columns)
@@ -131,26 +168,25 @@ __device__ __forceinline__ double table_term(double ph, const double2 *__restric
 }
 
 // ---------------------------------------------------------------------------
-// Main kernel.  grid (ceil(P / (T*R)), splits), block T.
-// Split s handles modes [s*mps, min(nc, (s+1)*mps)) of the current chunk and
-// writes (accumulate=0) or adds (accumulate=1) its sums at
-// dst + s*split_stride + i*sd + p*sp.
+// One block's work: the kThreads*R points starting at p_first (thread t owns
+// p_first + t + r*kThreads), modes [jb, je) of the staged tables `wtab`,
+// `rec` (indices relative to them), TILE modes per staged tile.  The sums are
+// written (accumulate=0) or added (accumulate=1) at dst + i*sd + p*sp.
+// Shared memory: 2 * TILE * (kM*16 [table] + kRec*8) bytes at `smem`.
 // ---------------------------------------------------------------------------
-template <int D, int R, bool INC, bool LIBM>
-__global__ void __launch_bounds__(kThreads)
-plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restrict__ wtab,
-             const double *__restrict__ rec, int64_t nc, int64_t mps, int accumulate,
-             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+template <int D, int R, bool INC, bool LIBM, int TILE>
+__device__ __forceinline__ void plain_block(const double *__restrict__ pos, int64_t P,
+                                            int64_t p_first, const double2 *__restrict__ wtab,
+                                            const double *__restrict__ rec, int64_t jb,
+                                            int64_t je, int accumulate, double *__restrict__ dst,
+                                            int64_t sd, int64_t sp, unsigned char *smem) {
     constexpr int NOUT = INC ? D : 1;
-    constexpr int TAB_BYTES = LIBM ? 0 : kTileModes * kM * 16;
-    constexpr int REC_BYTES = kTileModes * kRec * 8;
+    constexpr int TAB_BYTES = LIBM ? 0 : TILE * kM * 16;
+    constexpr int REC_BYTES = TILE * kRec * 8;
     constexpr int STAGE = TAB_BYTES + REC_BYTES;
-    extern __shared__ __align__(16) unsigned char smem[];
 
     const int tid = threadIdx.x;
-    const int64_t p0 = static_cast<int64_t>(blockIdx.x) * (kThreads * R) + tid;
-    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
-    const int64_t je = min(nc, jb + mps);
+    const int64_t p0 = p_first + tid;
 
     double x[R][D];
     double acc[R][NOUT];
@@ -173,7 +209,7 @@ plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restric
     for (int o = 16; o > 0; o >>= 1) xabs = fmax(xabs, __shfl_xor_sync(0xffffffffu, xabs, o));
 
     auto stage_tile = [&](int buf, int64_t t0) {
-        const int tm = static_cast<int>(min(static_cast<int64_t>(kTileModes), je - t0));
+        const int tm = static_cast<int>(min(static_cast<int64_t>(TILE), je - t0));
         unsigned char *base = smem + buf * STAGE;
         if (!LIBM) {
             const int chunks = tm * kM;                      // 16-byte chunks
@@ -189,10 +225,10 @@ plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restric
 
     if (jb < je) stage_tile(0, jb);
     int buf = 0;
-    for (int64_t t0 = jb; t0 < je; t0 += kTileModes, buf ^= 1) {
-        const int tm = static_cast<int>(min(static_cast<int64_t>(kTileModes), je - t0));
-        if (t0 + kTileModes < je) {
-            stage_tile(buf ^ 1, t0 + kTileModes);
+    for (int64_t t0 = jb; t0 < je; t0 += TILE, buf ^= 1) {
+        const int tm = static_cast<int>(min(static_cast<int64_t>(TILE), je - t0));
+        if (t0 + TILE < je) {
+            stage_tile(buf ^ 1, t0 + TILE);
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
@@ -237,15 +273,86 @@ plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restric
         __syncthreads();   // buffer `buf` is refilled two tiles later
     }
 
-    double *d0 = dst + static_cast<int64_t>(blockIdx.y) * split_stride;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int64_t p = p0 + r * kThreads;
         if (p >= P) continue;
 #pragma unroll
         for (int i = 0; i < NOUT; ++i) {
-            double *o = d0 + i * sd + p * sp;
+            double *o = dst + i * sd + p * sp;
             *o = accumulate ? *o + acc[r][i] : acc[r][i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Main kernel.  grid (ceil(P / (T*R)), splits), block T.
+// Split s handles modes [s*mps, min(nc, (s+1)*mps)) of the current chunk and
+// writes (accumulate=0) or adds (accumulate=1) its sums at
+// dst + s*split_stride + i*sd + p*sp.
+// ---------------------------------------------------------------------------
+template <int D, int R, bool INC, bool LIBM>
+__global__ void __launch_bounds__(kThreads)
+plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restrict__ wtab,
+             const double *__restrict__ rec, int64_t nc, int64_t mps, int accumulate,
+             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
+    const int64_t je = min(nc, jb + mps);
+    plain_block<D, R, INC, LIBM, kTileModes>(
+        pos, P, static_cast<int64_t>(blockIdx.x) * (kThreads * R), wtab, rec, jb, je, accumulate,
+        dst + static_cast<int64_t>(blockIdx.y) * split_stride, sd, sp, smem);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent batch kernel: each block takes the next unit of the device work
+// queue (atomic counter) until the queue is empty.  A unit is one point block
+// of one item and one of its mode ranges; its sums go to the item's output,
+// or to its split slot when the item's modes are split.
+// ---------------------------------------------------------------------------
+template <int R, int TILE>
+__global__ void __launch_bounds__(kThreads)
+batch_plain_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict__ units,
+                   int64_t n_units, int *__restrict__ counter, const double2 *__restrict__ wtab,
+                   const double *__restrict__ rec) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_unit;
+    for (;;) {
+        __syncthreads();                     // s_unit of the previous unit is consumed
+        if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1);
+        __syncthreads();
+        const int64_t u = s_unit;
+        if (u >= n_units) break;
+        const BatchUnit w = units[u];
+        const BatchItem &it = items[w.item];
+        const int64_t P = it.n_points;
+        const int64_t nout = it.incompr ? it.dim : 1;
+        double *dst = it.splits > 1 ? it.part + static_cast<int64_t>(w.split) * nout * P : it.out;
+        const double2 *wt = wtab + it.mode_off * kM;
+        const double *rc = rec + it.mode_off * kRec;
+        switch (it.dim * 2 + it.incompr) {
+            case 2:
+                plain_block<1, R, false, false, TILE>(it.pos, P, w.p_first, wt, rc, w.jb, w.je, 0,
+                                                      dst, P, 1, smem);
+                break;
+            case 4:
+                plain_block<2, R, false, false, TILE>(it.pos, P, w.p_first, wt, rc, w.jb, w.je, 0,
+                                                      dst, P, 1, smem);
+                break;
+            case 5:
+                plain_block<2, R, true, false, TILE>(it.pos, P, w.p_first, wt, rc, w.jb, w.je, 0,
+                                                     dst, P, 1, smem);
+                break;
+            case 6:
+                plain_block<3, R, false, false, TILE>(it.pos, P, w.p_first, wt, rc, w.jb, w.je, 0,
+                                                      dst, P, 1, smem);
+                break;
+            case 7:
+                plain_block<3, R, true, false, TILE>(it.pos, P, w.p_first, wt, rc, w.jb, w.je, 0,
+                                                     dst, P, 1, smem);
+                break;
+            default:
+                break;                       // rejected on the host
         }
     }
 }
@@ -495,6 +602,84 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
         GSC_CUDA(cudaGetLastError());
     }
     GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+    return GSC_OK;
+}
+
+// ---- batched ensembles: tables and the persistent kernel ---------------------
+int batch_plain_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,
+                       int64_t total_modes, void *wtab, double *rec, cudaStream_t st) {
+    if (total_modes == 0) return GSC_OK;
+    if (total_modes > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many modes in the batch");
+    TimedLaunch tl(st);
+    tl.begin(K_BATCH_TABLES);
+    batch_table_kernel<<<static_cast<unsigned>(total_modes), kM, 0, st>>>(
+        items, mode_prefix, n_items, static_cast<double2 *>(wtab), rec);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+size_t batch_plain_smem(int tile) { return 2 * static_cast<size_t>(tile) * (kM * 16 + kRec * 8); }
+
+namespace {
+using BatchPlainFn = void (*)(const BatchItem *, const BatchUnit *, int64_t, int *,
+                              const double2 *, const double *);
+BatchPlainFn batch_plain_fn(int R, int tile) {
+    if (tile == 8) {
+        if (R == 2) return batch_plain_kernel<2, 8>;
+        if (R == 4) return batch_plain_kernel<4, 8>;
+        if (R == 8) return batch_plain_kernel<8, 8>;
+    } else if (tile == 16) {
+        if (R == 2) return batch_plain_kernel<2, 16>;
+        if (R == 4) return batch_plain_kernel<4, 16>;
+    }
+    return nullptr;
+}
+int configure_batch_plain(BatchPlainFn fn, int tile) {
+    static std::mutex mu;
+    static BatchPlainFn done[8] = {nullptr};
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto f : done)
+        if (f == fn) return GSC_OK;
+    GSC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(batch_plain_smem(tile))));
+    for (auto &f : done)
+        if (!f) {
+            f = fn;
+            break;
+        }
+    return GSC_OK;
+}
+}  // namespace
+
+bool batch_plain_config_ok(int R, int tile) { return batch_plain_fn(R, tile) != nullptr; }
+
+int batch_plain_occupancy(int R, int tile, int device) {
+    BatchPlainFn fn = batch_plain_fn(R, tile);
+    if (!fn) return 0;
+    if (configure_batch_plain(fn, tile) != GSC_OK) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kThreads, batch_plain_smem(tile)) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    (void)device;
+    return n;
+}
+
+int batch_plain_launch(int R, int tile, int blocks, const BatchItem *items,
+                       const BatchUnit *units, int64_t n_units, int *counter, const void *wtab,
+                       const double *rec, cudaStream_t st) {
+    BatchPlainFn fn = batch_plain_fn(R, tile);
+    if (!fn) return set_error(GSC_ERR_INVALID, "unsupported batch configuration");
+    GSC_TRY(configure_batch_plain(fn, tile));
+    TimedLaunch tl(st);
+    tl.begin(K_BATCH_PLAIN);
+    fn<<<blocks, kThreads, batch_plain_smem(tile), st>>>(items, units, n_units, counter,
+                                                         static_cast<const double2 *>(wtab), rec);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
     return GSC_OK;
 }
 

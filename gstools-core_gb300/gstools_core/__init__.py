@@ -37,7 +37,8 @@ __all__ = ["summate", "summate_incompr", "summate_fourier", "summate_device",
            "summate_incompr_device", "summate_fourier_device",
            "summate_structured", "summate_incompr_structured", "summate_fourier_structured",
            "summate_structured_device", "summate_incompr_structured_device",
-           "summate_fourier_structured_device", "device_status",
+           "summate_fourier_structured_device", "Batch", "summate_batch", "last_batch_config",
+           "device_status",
            "device_count", "last_timings", "GscError", "__version__"]
 
 __version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
@@ -363,6 +364,151 @@ def summate_fourier_structured_device(spectrum_factor, modes, z1, z2, axes, out,
     """``summate_fourier_structured`` on device arrays; writes ``out`` (n_points,)."""
     return _structured_dev(_native.lib.gsc_summate_fourier_structured_dev, modes, z1, z2, axes,
                            out, form, tolerance, stream, timing, device, False, spectrum_factor)
+
+
+# ---------------------------------------------------------------------------
+# batched ensembles (extension: GSTools calls summate once per realization)
+# ---------------------------------------------------------------------------
+def _config_dict(c) -> dict:
+    names = {v: k for k, v in _native.FORMS.items()}
+    return {"form": names.get(c.form, c.form), "points_per_thread": c.points_per_thread,
+            "tile_modes": c.tile_modes, "units_per_block": c.units_per_block,
+            "blocks": c.blocks, "units": c.units, "max_splits": c.max_splits,
+            "tuned": bool(c.tuned), "tune_ms": c.tune_ms, "work": c.work}
+
+
+def _batch_kind(item) -> str:
+    kind = item.get("kind", "scalar")
+    if kind not in _native.BATCH_KINDS:
+        raise ValueError(f"unknown item kind {kind!r}; choose from {sorted(_native.BATCH_KINDS)}")
+    return kind
+
+
+class Batch:
+    """An ensemble of realizations planned for one persistent launch.
+
+    ``items`` is a sequence of dicts of device arrays (``__cuda_array_interface__``,
+    C-contiguous float64): ``cov`` (dim, n_modes) -- the mode grid ``modes``
+    for Fourier items --, ``z1``, ``z2`` (n_modes), ``pos`` (dim, n_points),
+    ``out`` ((n_points,) or (dim, n_points) for ``kind="incompr"``), optional
+    ``kind`` ("scalar", "incompr", "fourier") and ``spectrum_factor``
+    (n_modes, Fourier).  Each item computes what ``summate`` /
+    ``summate_incompr`` / ``summate_fourier`` computes for it.
+
+    Construction tunes the launch configuration on the ensemble's own data
+    (writing scratch values into the outputs) unless ``points_per_thread``,
+    ``tile_modes`` (FP64 form) and ``units_per_block`` are all given or an
+    ensemble of the same shape was tuned before.  ``run`` enqueues one run;
+    ``run_graph`` replays a CUDA graph of it.  The arrays stay bound to the
+    plan: update their contents in place between runs.
+    """
+
+    def __init__(self, items, *, form="auto", tolerance=None, device=-1, timing=False,
+                 points_per_thread=0, tile_modes=0, units_per_block=0):
+        self._handle = None
+        self._keep = list(items)
+        arr = (_native.GscBatchItem * max(1, len(self._keep)))()
+        for i, it in enumerate(self._keep):
+            kind = _batch_kind(it)
+            cov = it["modes"] if kind == "fourier" and "modes" in it else it["cov"]
+            cs = cov.__cuda_array_interface__["shape"]
+            ps = it["pos"].__cuda_array_interface__["shape"]
+            if len(cs) != 2 or len(ps) != 2:
+                raise TypeError(f"item {i}: cov and pos must be 2-D")
+            dim, n = cs
+            _assert_eq(dim, ps[0])
+            p = ps[1]
+            shape = (dim, p) if kind == "incompr" else (p,)
+            sf = None
+            if kind == "fourier":
+                sf = _cuda_view(it["spectrum_factor"], "spectrum_factor", (n,))
+            arr[i] = _native.GscBatchItem(
+                dim, _native.BATCH_KINDS[kind], n, p, _cuda_view(cov, "cov", (dim, n)),
+                _cuda_view(it["z1"], "z1", (n,)), _cuda_view(it["z2"], "z2", (n,)), sf,
+                _cuda_view(it["pos"], "pos", (dim, p)), _cuda_view(it["out"], "out", shape))
+        o = _opts(form, tolerance, timing, device)
+        cfg = _native.make_batch_config(points_per_thread, tile_modes, units_per_block)
+        h = ctypes.c_void_p()
+        _native.check(_native.lib.gsc_batch_create(arr, len(self._keep), ctypes.byref(o),
+                                                    ctypes.byref(cfg), ctypes.byref(h)))
+        self._handle = h
+
+    def run(self, stream=None):
+        """Enqueues one run on ``stream`` (an int CUDA stream handle; None =
+        the legacy default stream); does not synchronise."""
+        _native.check(_native.lib.gsc_batch_run(self._handle, stream or None))
+
+    def run_graph(self, stream=None):
+        """As ``run``, by replaying a CUDA graph captured on the first call."""
+        _native.check(_native.lib.gsc_batch_run_graph(self._handle, stream or None))
+
+    @property
+    def config(self) -> dict:
+        c = _native.make_batch_config()
+        _native.check(_native.lib.gsc_batch_get_config(self._handle, ctypes.byref(c)))
+        return _config_dict(c)
+
+    def close(self):
+        if self._handle:
+            _native.lib.gsc_batch_destroy(self._handle)
+            self._handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def summate_batch(items, *, form="auto", tolerance=None, device=-1, timing=False,
+                  points_per_thread=0, tile_modes=0, units_per_block=0):
+    """Host-array ensemble: ``items`` as for ``Batch`` but numpy float64
+    arrays (any layout; copied dense), without ``out``.  Returns the list of
+    fields: (n_points,) per scalar or Fourier item, (dim, n_points) C order
+    per incompressible item."""
+    keep, outs = [], []
+    arr = (_native.GscBatchItem * max(1, len(items)))()
+    for i, it in enumerate(items):
+        kind = _batch_kind(it)
+        cov = np.ascontiguousarray(_array(it["modes"] if kind == "fourier" and "modes" in it
+                                          else it["cov"], "cov", 2))
+        z1 = np.ascontiguousarray(_array(it["z1"], "z1", 1))
+        z2 = np.ascontiguousarray(_array(it["z2"], "z2", 1))
+        pos = np.ascontiguousarray(_array(it["pos"], "pos", 2))
+        dim, n = cov.shape
+        _assert_eq(dim, pos.shape[0])
+        _assert_eq(n, z1.shape[0])
+        _assert_eq(n, z2.shape[0])
+        p = pos.shape[1]
+        sf = None
+        if kind == "fourier":
+            sf = np.ascontiguousarray(_array(it["spectrum_factor"], "spectrum_factor", 1))
+            _assert_eq(sf.shape[0], n)
+        out = np.empty((dim, p) if kind == "incompr" else p, dtype=np.float64)
+        keep += [cov, z1, z2, pos, sf, out]
+        outs.append(out)
+        arr[i] = _native.GscBatchItem(dim, _native.BATCH_KINDS[kind], n, p, cov.ctypes.data,
+                                      z1.ctypes.data, z2.ctypes.data,
+                                      None if sf is None else sf.ctypes.data, pos.ctypes.data,
+                                      out.ctypes.data)
+    o = _opts(form, tolerance, timing, device)
+    cfg = _native.make_batch_config(points_per_thread, tile_modes, units_per_block)
+    _native.check(_native.lib.gsc_summate_batch_f64(arr, len(items), ctypes.byref(o),
+                                                    ctypes.byref(cfg)))
+    return outs
+
+
+def last_batch_config(device=-1) -> dict:
+    """Configuration of the plan that the last ``summate_batch`` call used."""
+    c = _native.make_batch_config()
+    _native.check(_native.lib.gsc_last_batch_config(device, ctypes.byref(c)))
+    return _config_dict(c)
 
 
 def device_status(device=-1) -> None:

@@ -54,6 +54,45 @@ def make_opts(form="auto", device=-1, flags=0, stream=None, tolerance=0.0) -> Gs
                    ctypes.c_void_p(stream or 0), float(tolerance))
 
 
+class GscBatchItem(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("kind", ctypes.c_int32),
+        ("n_modes", ctypes.c_int64),
+        ("n_points", ctypes.c_int64),
+        ("cov", ctypes.c_void_p),
+        ("z1", ctypes.c_void_p),
+        ("z2", ctypes.c_void_p),
+        ("spectrum_factor", ctypes.c_void_p),
+        ("pos", ctypes.c_void_p),
+        ("out", ctypes.c_void_p),
+    ]
+
+
+class GscBatchConfig(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_int32),
+        ("points_per_thread", ctypes.c_int32),
+        ("tile_modes", ctypes.c_int32),
+        ("units_per_block", ctypes.c_int32),
+        ("form", ctypes.c_int32),
+        ("blocks", ctypes.c_int32),
+        ("units", ctypes.c_int64),
+        ("max_splits", ctypes.c_int32),
+        ("tuned", ctypes.c_int32),
+        ("tune_ms", ctypes.c_double),
+        ("work", ctypes.c_double),
+    ]
+
+
+BATCH_KINDS = {"scalar": 0, "incompr": 1, "fourier": 2}
+
+
+def make_batch_config(points_per_thread=0, tile_modes=0, units_per_block=0) -> GscBatchConfig:
+    return GscBatchConfig(ctypes.sizeof(GscBatchConfig), int(points_per_thread), int(tile_modes),
+                          int(units_per_block))
+
+
 # name -> (restype, argtypes); every symbol declared in the public header
 _P, _I64, _I32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
 _OPTS = ctypes.POINTER(GscOpts)
@@ -91,6 +130,16 @@ SIGNATURES = {
                                                           _OPTS]),
     "gsc_summate_fourier_structured_dev": (ctypes.c_int, [_P, _P, _P, _P, _I64, _I64, _P, _I64,
                                                           _P, _I64, _P, _I64, _P, _OPTS]),
+    "gsc_batch_create": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _OPTS,
+                                        ctypes.POINTER(GscBatchConfig),
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "gsc_batch_run": (ctypes.c_int, [_P, _P]),
+    "gsc_batch_run_graph": (ctypes.c_int, [_P, _P]),
+    "gsc_batch_get_config": (ctypes.c_int, [_P, ctypes.POINTER(GscBatchConfig)]),
+    "gsc_batch_destroy": (ctypes.c_int, [_P]),
+    "gsc_summate_batch_f64": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _OPTS,
+                                             ctypes.POINTER(GscBatchConfig)]),
+    "gsc_last_batch_config": (ctypes.c_int, [_I32, ctypes.POINTER(GscBatchConfig)]),
 }
 
 

@@ -272,6 +272,87 @@ int gsc_summate_fourier_structured_dev(const double *spectrum_factor, const doub
                                        const double *axis2, int64_t n2,
                                        double *out, const gsc_opts *opts);
 
+/* ---- batched ensembles ------------------------------------------------ */
+/* Many realizations (items) with their own dimension, mode and point counts
+ * summed by one persistent kernel fed from a device work queue, replayable
+ * as a CUDA graph.  No reference counterpart: GSTools calls summate once per
+ * realization; each item computes exactly what that call computes.  All
+ * pointers are device pointers to dense row-major arrays: cov (dim, n_modes)
+ * (Fourier: the mode grid), z1, z2, spectrum_factor (n_modes), pos
+ * (dim, n_points), out (n_points), or (dim, n_points) for INCOMPR items. */
+#define GSC_BATCH_SCALAR   0   /* field::summator           src/field.rs:37   */
+#define GSC_BATCH_INCOMPR  1   /* field::summator_incompr   src/field.rs:97   */
+#define GSC_BATCH_FOURIER  2   /* field::summator_fourier   src/field.rs:219  */
+
+typedef struct gsc_batch_item {
+    int32_t dim;                    /* 1, 2, 3 (INCOMPR: 2, 3)               */
+    int32_t kind;                   /* GSC_BATCH_*                           */
+    int64_t n_modes, n_points;
+    const double *cov, *z1, *z2;
+    const double *spectrum_factor;  /* FOURIER items only                    */
+    const double *pos;
+    double *out;
+} gsc_batch_item;
+
+/* Configuration of a plan.  Inputs (0 = let the autotuner choose):
+ * points_per_thread (2, 4, 8), tile_modes (FP64 form: 8 or 16, with 2 or 4
+ * points per thread), units_per_block (target work units per resident
+ * block: how finely item modes are split).  gsc_batch_get_config fills all
+ * fields with what the plan uses. */
+typedef struct gsc_batch_config {
+    int32_t struct_size;            /* sizeof(gsc_batch_config)              */
+    int32_t points_per_thread;
+    int32_t tile_modes;
+    int32_t units_per_block;
+    int32_t form;                   /* out: GSC_FORM_PLAIN_F64 / MIXED / ..   */
+    int32_t blocks;                 /* out: persistent blocks launched       */
+    int64_t units;                  /* out: work units in the queue          */
+    int32_t max_splits;             /* out: largest mode split of an item    */
+    int32_t tuned;                  /* out: 1 if this plan ran the autotuner */
+    double  tune_ms;                /* out: GPU time spent tuning            */
+    double  work;                   /* out: point*modes (x components)       */
+} gsc_batch_config;
+
+typedef struct gsc_batch gsc_batch;
+
+/* Builds a plan on opts->device (forms AUTO, PLAIN_F64, MIXED,
+ * MIXED_F64PHASE; AUTO is MIXED for tolerance >= 1e-6, else PLAIN_F64).  It
+ * allocates the plan's device memory (tables, queue, split partials) and,
+ * unless `config` fixes every choice or an ensemble of the same shape was
+ * tuned before in this process, times the candidate configurations on this
+ * ensemble's own data -- writing scratch values into the items' outputs --
+ * and returns when done.  The item pointers are bound to the plan: change
+ * the data in place between runs, not the pointers. */
+int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
+                     const gsc_batch_config *config, gsc_batch **plan);
+
+/* Enqueues one run of the whole ensemble on `stream` (cudaStream_t, NULL =
+ * legacy default stream): tables, the persistent kernel, the split
+ * reduction.  Allocates nothing and does not synchronise.  Runs of one plan
+ * must not overlap each other on the GPU. */
+int gsc_batch_run(gsc_batch *plan, void *stream);
+
+/* As gsc_batch_run, through a CUDA graph of the run captured on the first
+ * call (on a stream of the plan) and launched on `stream` afterwards. */
+int gsc_batch_run_graph(gsc_batch *plan, void *stream);
+
+int gsc_batch_get_config(const gsc_batch *plan, gsc_batch_config *config);
+
+/* Frees the plan; its runs must have completed. */
+int gsc_batch_destroy(gsc_batch *plan);
+
+/* Host-pointer ensemble: items as for gsc_batch_create but with HOST
+ * pointers to dense row-major arrays.  Copies all inputs to the GPU in one
+ * transfer, runs the ensemble (the plan of the previous call on the device
+ * is reused when the shapes match), and copies every output back before
+ * returning. */
+int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
+                          const gsc_batch_config *config);
+
+/* Configuration of the plan used by the last gsc_summate_batch_f64 call on
+ * `device` (-1 = current). */
+int gsc_last_batch_config(int32_t device, gsc_batch_config *config);
+
 #ifdef __cplusplus
 }
 #endif

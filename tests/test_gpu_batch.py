@@ -1,0 +1,171 @@
+"""Batched ensembles: one persistent launch over many realizations (GPU tests).
+
+Each item of a batch computes what one call of the reference's summator,
+summator_incompr or summator_fourier computes for it (src/field.rs:37-65,
+:97-182, :219-249), so every output is checked against the oracle on the
+same inputs, at the bar of its form (max |err| / field RMS): 1e-12 for the
+FP64 form, 1e-6 for the mixed form.  Cases: items of every kind and
+dimension with uneven point and mode counts (including no points and no
+modes), split modes, the CUDA-graph replay after the inputs change in place,
+deterministic repeats, the autotuner's report, fixed configurations, and
+the host-array entry point.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 1
+BOUND = {"plain": 1e-12, "mixed": 1e-6}
+
+
+def _items(seed, specs):
+    """specs: (kind, dim, n_modes, n_points) -> host item dicts."""
+    rng = np.random.default_rng(seed)
+    items = []
+    for kind, dim, n, p in specs:
+        ell = rng.uniform(2.0, 50.0)
+        if kind == "fourier":
+            cov = rng.integers(-20, 21, (dim, n)) * (2.0 * np.pi / 500.0)
+        elif rng.random() < 0.5:
+            cov = rng.normal(0.0, np.sqrt(2.0) / ell, (dim, n))
+        else:
+            cov = rng.standard_normal((dim, n)) / np.sqrt(rng.chisquare(1, n)) / ell
+        it = {"kind": kind, "cov": np.ascontiguousarray(cov), "z1": rng.standard_normal(n),
+              "z2": rng.standard_normal(n), "pos": rng.uniform(0.0, 500.0, (dim, p))}
+        if kind == "fourier":
+            it["spectrum_factor"] = rng.uniform(0.1, 1.0, n)
+        items.append(it)
+    return items
+
+
+def _oracle(it):
+    if it["kind"] == "incompr":
+        return oracle.summator_incompr(it["cov"], it["z1"], it["z2"], it["pos"], num_threads=NT)
+    if it["kind"] == "fourier":
+        return oracle.summator_fourier(it["spectrum_factor"], it["cov"], it["z1"], it["z2"],
+                                       it["pos"], num_threads=NT)
+    return oracle.summator(it["cov"], it["z1"], it["z2"], it["pos"], num_threads=NT)
+
+
+SPECS = [("scalar", 2, 300, 70000), ("scalar", 3, 2000, 5000), ("incompr", 3, 257, 12345),
+         ("incompr", 2, 64, 1), ("fourier", 2, 500, 3000), ("scalar", 1, 37, 999),
+         ("scalar", 3, 0, 100), ("scalar", 2, 10, 0), ("fourier", 3, 129, 4096),
+         ("scalar", 3, 4096, 600), ("incompr", 3, 1500, 40000)]
+
+
+def _device(torch, items):
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dev = []
+    for it in items:
+        p = it["pos"].shape[1]
+        dim = it["pos"].shape[0]
+        x = {k: d(v) for k, v in it.items() if k != "kind"}
+        x["kind"] = it["kind"]
+        shape = (dim, p) if it["kind"] == "incompr" else (p,)
+        x["out"] = torch.full(shape, float("nan"), dtype=torch.float64, device="cuda")
+        dev.append(x)
+    return dev
+
+
+def _check(items, outs, form):
+    for i, (it, out) in enumerate(zip(items, outs)):
+        ref = _oracle(it)
+        assert out.shape == ref.shape, i
+        if ref.size == 0:
+            continue
+        if not np.any(ref):
+            assert np.array_equal(out, ref), i
+            continue
+        err = rel_err(out, ref)
+        assert err <= BOUND[form], f"item {i} {it['kind']} {it['pos'].shape} x {it['z1'].size}: {err:.3e}"
+
+
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_batch_matches_oracle_run_and_graph(gsc, form):
+    torch = pytest.importorskip("torch")
+    items = _items(1, SPECS)
+    dev = _device(torch, items)
+    with gsc.Batch(dev, form=form) as b:
+        cfg = b.config
+        assert cfg["form"] == form and cfg["units"] > 0 and cfg["blocks"] > 0
+        b.run()
+        torch.cuda.synchronize()
+        first = [x["out"].cpu().numpy().copy() for x in dev]
+        _check(items, first, form)
+        # graph replay: same results, bit for bit (deterministic split order)
+        for x in dev:
+            x["out"].fill_(float("nan"))
+        b.run_graph()
+        b.run_graph()
+        torch.cuda.synchronize()
+        for a, x in zip(first, dev):
+            assert np.array_equal(a, x["out"].cpu().numpy())
+        # new data in the same arrays: the replayed graph sees it
+        items2 = _items(2, SPECS)
+        for x, it in zip(dev, items2):
+            for k in ("cov", "z1", "z2", "pos", "spectrum_factor"):
+                if k in it:
+                    x[k].copy_(torch.from_numpy(np.ascontiguousarray(it[k])))
+        b.run_graph()
+        torch.cuda.synchronize()
+        _check(items2, [x["out"].cpu().numpy() for x in dev], form)
+
+
+def test_batch_split_modes(gsc):
+    """Few points and many modes with a fine unit target: modes are split
+    over units and reduced in split order."""
+    torch = pytest.importorskip("torch")
+    items = _items(3, [("scalar", 3, 6000, 700), ("incompr", 2, 3000, 300), ("scalar", 2, 50, 50)])
+    dev = _device(torch, items)
+    with gsc.Batch(dev, form="plain", points_per_thread=4, tile_modes=8,
+                   units_per_block=64) as b:
+        assert b.config["max_splits"] > 1 and not b.config["tuned"]
+        b.run()
+        torch.cuda.synchronize()
+        _check(items, [x["out"].cpu().numpy() for x in dev], "plain")
+
+
+@pytest.mark.parametrize("R,tile", [(2, 8), (4, 16), (8, 8)])
+def test_batch_fixed_configs(gsc, R, tile):
+    torch = pytest.importorskip("torch")
+    items = _items(4, SPECS[:5])
+    dev = _device(torch, items)
+    with gsc.Batch(dev, form="plain", points_per_thread=R, tile_modes=tile,
+                   units_per_block=4) as b:
+        c = b.config
+        assert (c["points_per_thread"], c["tile_modes"]) == (R, tile)
+        b.run()
+        torch.cuda.synchronize()
+        _check(items, [x["out"].cpu().numpy() for x in dev], "plain")
+
+
+def test_batch_rejects_bad_input(gsc):
+    torch = pytest.importorskip("torch")
+    items = _items(5, [("scalar", 2, 10, 10)])
+    dev = _device(torch, items)
+    with pytest.raises(ValueError):
+        gsc.Batch(dev, form="plain", points_per_thread=3, tile_modes=8, units_per_block=4)
+    with pytest.raises(ValueError):
+        gsc.Batch(dev, form="sep_f16x5")
+    bad = _device(torch, _items(6, [("incompr", 2, 10, 10)]))
+    bad[0]["kind"] = "nope"
+    with pytest.raises(ValueError):
+        gsc.Batch(bad)
+
+
+def test_summate_batch_host_api(gsc):
+    items = _items(7, SPECS)
+    host = [{k: v for k, v in it.items()} for it in items]
+    outs = gsc.summate_batch(host, form="mixed", tolerance=1e-6)
+    _check(items, outs, "mixed")
+    cfg = gsc.last_batch_config()
+    assert cfg["form"] == "mixed"
+    # the same shapes again reuse the plan; plain FP64 bar on a second ensemble
+    outs = gsc.summate_batch(_items(8, SPECS), form="plain")
+    _check(_items(8, SPECS), outs, "plain")
