@@ -13,6 +13,10 @@ benchmark data):
   c3  unstructured 3-D: 16,777,216 points in [0,1000]^3, 4096 modes,
       exponential spectrum l = 5
   c4  incompressible 3-D: 192^3 grid, 2048 modes, Gaussian spectrum l = 8
+  c5  batched ensemble: 512 realizations (seed r each; 2-D for r < 256, else
+      3-D; points log-uniform 1e3..1e6 in [0,500]^d; modes log-uniform
+      256..8192; Gaussian spectrum for even r, exponential for odd r,
+      l uniform in [2, 50]) in one persistent launch replayed as a CUDA graph
 
 One step = one full summation of the workload.  `value` is timed with CUDA
 events on the launch stream, inputs resident in HBM, L2 flushed (a 256 MiB
@@ -79,6 +83,26 @@ def workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
+def ensemble(count=512):
+    """The c5 ensemble: per realization r, rng = default_rng(r), draws in the
+    order P, N, l, pos, cov, z1, z2."""
+    items = []
+    for r in range(count):
+        rng = np.random.default_rng(r)
+        d = 2 if r < count // 2 else 3
+        P = int(round(10 ** rng.uniform(3, 6)))
+        N = int(round(2 ** rng.uniform(8, 13)))
+        ell = rng.uniform(2, 50)
+        pos = rng.uniform(0, 500, (d, P))
+        if r % 2 == 0:
+            cov = rng.normal(0, np.sqrt(2) / ell, (d, N))
+        else:
+            cov = student_t(rng, d, N, ell)
+        z1, z2 = rng.standard_normal(N), rng.standard_normal(N)
+        items.append({"kind": "scalar", "cov": cov, "z1": z1, "z2": z2, "pos": pos})
+    return items
+
+
 def flat_grid(axes):
     return np.ascontiguousarray(
         np.array(np.meshgrid(*axes, indexing="ij")).reshape(len(axes), -1))
@@ -109,7 +133,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -304,6 +328,18 @@ def timed_steps(torch, gsc, step, stream, steps, flush):
     return per_step, kern, launches
 
 
+def warm_up(torch, step, w, min_s=0.5):
+    """At least w untimed steps, continued until min_s seconds have passed so
+    that the clock sampler (50 ms period) sees the GPU under this load before
+    the timed steps, which can be shorter than one sampling period."""
+    n, t0 = 0, time.perf_counter()
+    while n < w or time.perf_counter() - t0 < min_s:
+        step()
+        torch.cuda.synchronize()
+        n += 1
+    return n
+
+
 def run_ours(args, world, rank, local):
     import torch
     import gstools_core as gsc
@@ -319,13 +355,10 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     step, out_d = make_device_step(gsc, torch, w, form, dev, stream)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    gsc.device_status()
-
-    # ---- timed region ------------------------------------------------------
+    # ---- warm-up and timed region, clocks sampled throughout -----------------
     with ClockSampler(local) as clk:
+        warm = warm_up(torch, step, args.warmup)
+        gsc.device_status()
         barrier(world)
         torch.cuda.synchronize()
         t_wall = time.perf_counter()
@@ -437,12 +470,204 @@ def run_ours(args, world, rank, local):
         "config": {"workload": args.workload, "desc": w["desc"], "points": P, "modes": N,
                    "form": form,
                    "l2": "flushed by a 256 MiB write before every timed step",
+                   "warmup_steps_run": warm,
+                   "clocks_window": "nvidia-smi every 50 ms over warm-up and timed steps",
                    "wall_s": t_wall},
         "error_vs_oracle": err,
         "plain_fp64": plain,
         "other_forms": others,
         "kernels_ms_per_step": {k: float(np.sum(v) / args.steps) for k, v in kern.items()},
         "gpu_launches": int(launches),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# c5: the batched ensemble
+# ---------------------------------------------------------------------------
+def ensemble_cpu_rate(items, target_s, steps=1):
+    """Oracle throughput on a bounded sample of the ensemble: every 32nd
+    realization, a seeded subset of its points, all its modes; the subset is
+    sized so one pass takes about target_s on all host threads."""
+    import oracle
+    cores = host_cores()
+    rng = np.random.default_rng(99)
+    picked = items[::32]
+
+    def sample(m):
+        out = []
+        for it in picked:
+            P = it["pos"].shape[1]
+            idx = np.sort(rng.choice(P, size=min(P, m), replace=False))
+            out.append((it, np.ascontiguousarray(it["pos"][:, idx])))
+        return out
+
+    def run(smp):
+        t0 = time.perf_counter()
+        for it, pos in smp:
+            oracle.summator(it["cov"], it["z1"], it["z2"], pos, num_threads=cores)
+        return time.perf_counter() - t0
+
+    probe = sample(4 * cores)
+    dt = max(run(probe), 1e-6)
+    m = int(max(4 * cores, 4 * cores * target_s / dt))
+    smp = sample(m)
+    times = [run(smp) for _ in range(steps)]
+    work = sum(pos.shape[1] * it["cov"].shape[1] for it, pos in smp)
+    t = float(np.mean(times))
+    desc = (f"realizations 0, 32, ..., 480 ({len(smp)} of {len(items)}), up to {m} seeded "
+            f"points each x all their modes ({work:.3g} point*modes), {t:.1f} s on {cores} "
+            f"threads (oracle/field_oracle.c, a restatement of src/field.rs)")
+    return work / t / 1e9, cores, desc, t
+
+
+def run_ours_batch(args, world, rank, local):
+    import torch
+    import gstools_core as gsc
+    import oracle
+
+    torch.cuda.set_device(local)
+    items = ensemble()
+    work = float(sum(it["pos"].shape[1] * it["cov"].shape[1] for it in items))
+    dims = {}
+    for it in items:
+        k = (it["pos"].shape[0], False)
+        dims[k] = dims.get(k, 0.0) + it["pos"].shape[1] * it["cov"].shape[1] / work
+    form = "mixed" if args.form == "auto" else args.form
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    dput = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    dev_items = [{"kind": "scalar", "cov": dput(it["cov"]), "z1": dput(it["z1"]),
+                  "z2": dput(it["z2"]), "pos": dput(it["pos"]),
+                  "out": torch.empty(it["pos"].shape[1], dtype=torch.float64, device=dev)}
+                 for it in items]
+    in_bytes = sum((it["cov"].size + 2 * it["cov"].shape[1] + it["pos"].size) * 8 for it in items)
+    out_bytes = sum(it["pos"].shape[1] * 8 for it in items)
+
+    t0 = time.perf_counter()
+    plan = gsc.Batch(dev_items, form=form, timing=True)
+    t_plan = time.perf_counter() - t0
+    cfg = plan.config
+
+    def step():
+        plan.run_graph(stream.cuda_stream)
+
+    with ClockSampler(local) as clk:
+        warm = warm_up(torch, step, args.warmup)
+        barrier(world)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter()
+        per_step = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            b.synchronize()
+            per_step.append(a.elapsed_time(b))
+        torch.cuda.synchronize()
+        barrier(world)
+        t_wall = time.perf_counter() - t_wall
+    ms_step = max_over_ranks(world, float(np.mean(per_step)))
+    value = work * world / (ms_step * 1e-3) / 1e9
+
+    # per-kernel times of the same run sequence outside the graph
+    flush.fill_(1)
+    plan.run(stream.cuda_stream)
+    torch.cuda.synchronize()
+    kt = gsc.last_timings()
+    kern = {}
+    for name, ms in kt:
+        kern[name] = kern.get(name, 0.0) + ms
+    dom = max(kern, key=kern.get)
+    roof = roofline(args, None, dom, kern[dom], 1, units=work, op_mix=dims)
+
+    # parity on a spread of realizations
+    err = None
+    if not args.no_check:
+        rng = np.random.default_rng(7)
+        worst, worst_rms = 0.0, 0.0
+        for r in (0, 1, 100, 255, 256, 301, 511):
+            it = items[r]
+            P = it["pos"].shape[1]
+            idx = np.sort(rng.choice(P, size=min(P, 512), replace=False))
+            ref = oracle.summator(it["cov"], it["z1"], it["z2"],
+                                  np.ascontiguousarray(it["pos"][:, idx]), num_threads=host_cores())
+            got = dev_items[r]["out"].cpu().numpy()[idx]
+            rms = float(np.sqrt(np.mean(ref ** 2)))
+            worst = max(worst, float(np.max(np.abs(got - ref)) / rms))
+            worst_rms = max(worst_rms, float(np.sqrt(np.mean((got - ref) ** 2)) / rms))
+        err = {"max_abs_over_rms": worst, "rms_over_rms": worst_rms,
+               "points_checked": "512 per realization of 0, 1, 100, 255, 256, 301, 511",
+               "reference": "oracle (field.rs restatement), FP64"}
+
+    # the plain FP64 form of the same ensemble (one graph step)
+    plain = None
+    if not args.no_plain and form != "plain":
+        pplan = gsc.Batch(dev_items, form="plain", timing=True)
+        pplan.run_graph(stream.cuda_stream)
+        torch.cuda.synchronize()
+        flush.fill_(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        pplan.run_graph(stream.cuda_stream)
+        b.record(stream)
+        b.synchronize()
+        pms = max_over_ranks(world, a.elapsed_time(b))
+        plain = {"value": work * world / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
+                 "steps": 1, "path": "persistent FP64 batch kernel", "config": pplan.config}
+        plain["speedup_of_chosen_form"] = value / plain["value"]
+        pplan.close()
+
+    # e2e through the host-array API
+    e2e = None
+    if not args.no_e2e:
+        host = [{"kind": "scalar", "cov": it["cov"], "z1": it["z1"], "z2": it["z2"],
+                 "pos": it["pos"]} for it in items]
+        gsc.summate_batch(host, form=form)          # plan + tuning + staging buffers
+        ts = []
+        for _ in range(max(1, min(args.steps, 3))):
+            barrier(world)
+            t0 = time.perf_counter()
+            gsc.summate_batch(host, form=form)
+            ts.append(time.perf_counter() - t0)
+        t_e2e = max_over_ranks(world, float(np.mean(ts)))
+        e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes),
+               "ms_per_step": t_e2e * 1e3, "api": "gstools_core.summate_batch",
+               "timing": "host wall clock around the synchronous call"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, cores, desc, _ = ensemble_cpu_rate(items, args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": ("f32 pairs (phase), f32 (sincos, tile sums), f64 output"
+                  if form.startswith("mixed") else "f64"),
+        "data": "synthetic (seeded numpy default_rng, one seed per realization)",
+        "config": {"workload": "c5", "desc": "batched ensemble, 512 realizations, "
+                   f"{sum(it['pos'].shape[1] for it in items)} points, "
+                   f"{sum(it['cov'].shape[1] for it in items)} modes in total",
+                   "point_modes": work, "form": form, "plan": cfg, "plan_s": t_plan,
+                   "step": "one CUDA-graph replay: tables, persistent kernel, split reduction",
+                   "l2": "flushed by a 256 MiB write before every timed step",
+                   "warmup_steps_run": warm,
+                   "clocks_window": "nvidia-smi every 50 ms over warm-up and timed steps",
+                   "wall_s": t_wall},
+        "error_vs_oracle": err,
+        "plain_fp64": plain,
+        "kernels_ms_per_step": kern,
+        "gpu_launches": int(len(kt) * args.steps),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
     }
     if rank == 0:
@@ -457,20 +682,34 @@ def measured_peaks():
         return {}
 
 
-def roofline(args, w, dom, dom_ms, launches_per_step):
+# FP64 pipe instructions per point*mode of the plain kernel's table path
+# (phase 2d-1, reduction + polynomials + table combine 12, accumulate 1 or d)
+PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17, (3, True): 20}
+# FP32 FMA-pipe instructions per point*mode of the mixed kernel (double-float
+# phase 8 per dimension + 5, sincos and combine 18, Kahan 4); integer and
+# select instructions run on the ALU pipe and are not counted
+MIXED_FP32_OPS = {1: 35, 2: 43, 3: 51}
+
+
+def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None):
     """Roofline entry for the dominant kernel.
 
     Tensor-core forms (bound "tensor"): FLOPs per launch = products x 2 x
     points x 2N (the real GEMM has K = 2N per output component; "products" is
     the number of split products the kernel issues: 5 for sep_f16x5, 3 for
     sep_f16x3 / sep_bf16x3), against the measured dense 16-bit peak.
-    Plain FP64 (bound "fp64"): 2d+3 (scalar) or 4d+2 (incompr) FLOPs per
-    point*mode plus one sincos, against cuBLAS DGEMM's measured FP64 rate."""
+    FP64 and FP32 forms (bounds "fp64" / "fp32"): the pipe instructions the
+    kernel issues per point*mode (PLAIN_FP64_OPS / MIXED_FP32_OPS), each
+    counted as one fused multiply-add (2 FLOPs, the unit of the peak), against
+    cuBLAS DGEMM / SGEMM (TF32 off) measured on this GPU."""
     import torch
-    P, N, d = n_points(w), w["cov"].shape[1], w["dim"]
-    nout = d if w["incompr"] else 1
-    per_launch_units = P * N / max(launches_per_step, 1)
+    if units is None:
+        P, N = n_points(w), w["cov"].shape[1]
+        units = P * N
+    per_launch_units = units / max(launches_per_step, 1)
     if dom.startswith("sep_tc"):
+        d = w["dim"]
+        nout = d if w["incompr"] else 1
         products = {"sep_tc_f16x5": 5, "sep_tc_f16x3": 3, "sep_tc_bf16x3": 3}[dom]
         flops = products * 2.0 * per_launch_units * 2 * nout
         achieved = flops / (dom_ms * 1e-3) / 1e12
@@ -484,27 +723,34 @@ def roofline(args, w, dom, dom_ms, launches_per_step):
                 "peak_source": how,
                 "algorithmic_tflops_single_product": achieved / products,
                 "note": f"{products} split products x 2 x points x 2N FLOPs per launch"}
-    flops_pm = (4 * d + 2) if w["incompr"] else (2 * d + 3)
-    achieved = flops_pm * per_launch_units / (dom_ms * 1e-3) / 1e12
-    peak, how = fp64_peak(torch)
-    return {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
-            "peak_source": how,
-            "note": f"{flops_pm} algorithmic FLOPs per point*mode plus one sincos; the "
-                    f"sincos cost is not counted"}
+    mixed = "mixed" in dom
+    if op_mix is None:
+        op_mix = {(w["dim"], bool(w["incompr"])): 1.0}
+    if mixed:
+        ops = sum(f * MIXED_FP32_OPS[k[0]] * (k[0] if k[1] else 1) for k, f in op_mix.items())
+    else:
+        ops = sum(f * PLAIN_FP64_OPS[k] for k, f in op_mix.items())
+    achieved = 2.0 * ops * per_launch_units / (dom_ms * 1e-3) / 1e12
+    peak, how = (fp32_peak(torch) if mixed else fp64_peak(torch))
+    return {"bound": "fp32" if mixed else "fp64", "kernel": dom, "achieved": achieved,
+            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+            "traffic": None, "peak_source": how,
+            "pipe_ops_per_point_mode": ops,
+            "note": f"{ops:.1f} {'FP32' if mixed else 'FP64'} pipe instructions per point*mode "
+                    f"(from the kernel source), each counted as one FMA = 2 FLOPs"}
 
 
-_FP64_PEAK = None
+_PEAKS = {}
 
 
-def fp64_peak(torch):
-    """FP64 peak as delivered by cuBLAS DGEMM on this GPU (measured here, best
-    of 5, 8192^3), since MEASURED_PEAKS.json carries no FP64 figure."""
-    global _FP64_PEAK
-    if _FP64_PEAK is None:
+def _gemm_peak(torch, dtype, name):
+    """Best of 5 cuBLAS GEMMs 8192^3 (TF32 off), TFLOP/s."""
+    if name not in _PEAKS:
         n = 8192
-        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        a = torch.randn(n, n, dtype=dtype, device="cuda")
+        b = torch.randn(n, n, dtype=dtype, device="cuda")
         torch.matmul(a, b)
         torch.cuda.synchronize()
         best = 1e9
@@ -515,15 +761,44 @@ def fp64_peak(torch):
             e1.record()
             e1.synchronize()
             best = min(best, e0.elapsed_time(e1))
-        _FP64_PEAK = 2 * n ** 3 / (best * 1e-3) / 1e12
+        torch.backends.cuda.matmul.allow_tf32 = prev
+        _PEAKS[name] = 2 * n ** 3 / (best * 1e-3) / 1e12
         del a, b
-    return _FP64_PEAK, "measured: cuBLAS DGEMM 8192^3, best of 5"
+    return _PEAKS[name]
+
+
+def fp64_peak(torch):
+    """FP64 peak as delivered by cuBLAS DGEMM on this GPU (measured here);
+    MEASURED_PEAKS.json carries no FP64 figure."""
+    return _gemm_peak(torch, torch.float64, "fp64"), "measured: cuBLAS DGEMM 8192^3, best of 5"
+
+
+def fp32_peak(torch):
+    """FP32 (CUDA-core) peak as delivered by cuBLAS SGEMM with TF32 off."""
+    return (_gemm_peak(torch, torch.float32, "fp32"),
+            "measured: cuBLAS SGEMM 8192^3 (TF32 off), best of 5")
 
 
 # ---------------------------------------------------------------------------
 def run_reference(args, world, rank):
     """The reference's CPU algorithm (oracle restatement) on the host cores."""
     if rank != 0:
+        return
+    if args.workload == "c5":
+        items = ensemble()
+        v, cores, desc, t = ensemble_cpu_rate(items, args.cpu_seconds, max(1, args.steps))
+        line = {
+            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded numpy default_rng, one seed per realization)",
+            "config": {"workload": "c5", "desc": "batched ensemble, 512 realizations",
+                       "form": "reference CPU (rayon-equivalent restatement)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
         return
     w = workload(args.workload)
     N = w["cov"].shape[1]
@@ -551,7 +826,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--form", default="auto")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -562,6 +837,8 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "c5":
+        run_ours_batch(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:
