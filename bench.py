@@ -13,6 +13,11 @@ benchmark data):
   c3  unstructured 3-D: 16,777,216 points in [0,1000]^3, 4096 modes,
       exponential spectrum l = 5
   c4  incompressible 3-D: 192^3 grid, 2048 modes, Gaussian spectrum l = 8
+  field  the reference's criterion field benchmarks (benches/main.rs:51-133):
+      summate 2-D and 3-D, summate_incompr 2-D and 3-D, summate_fourier 2-D
+      on 10,000 points x 1000 modes, inputs read from the reference's
+      benches/input text format (--input-dir; synthesized stand-ins when
+      absent); one step = the five calls
   c5  batched ensemble: 512 realizations (seed r each; 2-D for r < 256, else
       3-D; points log-uniform 1e3..1e6 in [0,500]^d; modes log-uniform
       256..8192; Gaussian spectrum for even r, exponential for odd r,
@@ -674,6 +679,194 @@ def run_ours_batch(args, world, rank, local):
         print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# field: the reference's criterion field benchmarks, file inputs
+# ---------------------------------------------------------------------------
+def field_calls(args):
+    """[(name, kind, dim, arrays...)] of benches/main.rs:76-132 from the input files."""
+    from gstools_core import bench_inputs
+    import tempfile
+    d = args.input_dir
+    if not d or not all(os.path.exists(os.path.join(d, f))
+                        for f in bench_inputs.FILES_1D + bench_inputs.FILES_2D):
+        d = tempfile.mkdtemp(prefix="gsc_field_inputs_")
+        bench_inputs.synthesize_field_inputs(d)
+        source = "synthesized stand-ins in the benches/input text format"
+    else:
+        source = f"files in {d}"
+    a = bench_inputs.field_inputs(d)
+    calls = [
+        ("field summate 2d", "scalar", (a["cov_samples_2d"], a["z_1"], a["z_2"], a["pos_2d"])),
+        ("field summate 3d", "scalar", (a["cov_samples_3d"], a["z_1"], a["z_2"], a["pos_3d"])),
+        ("field summate incompr 2d", "incompr",
+         (a["cov_samples_2d"], a["z_1"], a["z_2"], a["pos_2d"])),
+        ("field summate incompr 3d", "incompr",
+         (a["cov_samples_3d"], a["z_1"], a["z_2"], a["pos_3d"])),
+        ("field summate Fourier 2d", "fourier",
+         (a["spectrum_factor_2d"], a["modes_2d"], a["z_1_fourier"], a["z_2_fourier"],
+          a["pos_2d"])),
+    ]
+    return calls, source
+
+
+def field_work(calls):
+    w = 0.0
+    for _, kind, arrs in calls:
+        pos = arrs[-1]
+        n = arrs[1].shape[1] if kind == "fourier" else arrs[0].shape[1]
+        w += float(pos.shape[1]) * n
+    return w
+
+
+def field_oracle(kind, arrs, cores):
+    import oracle
+    if kind == "fourier":
+        return oracle.summator_fourier(*arrs, num_threads=cores)
+    if kind == "incompr":
+        return oracle.summator_incompr(*arrs, num_threads=cores)
+    return oracle.summator(*arrs, num_threads=cores)
+
+
+def run_ours_field(args, world, rank, local):
+    import torch
+    import gstools_core as gsc
+
+    torch.cuda.set_device(local)
+    calls, source = field_calls(args)
+    work = field_work(calls)
+    form = "plain" if args.form == "auto" else args.form
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    dput = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    dev_calls = []
+    for name, kind, arrs in calls:
+        darrs = [dput(x) for x in arrs]
+        pos = arrs[-1]
+        shape = (pos.shape[0], pos.shape[1]) if kind == "incompr" else (pos.shape[1],)
+        out = torch.empty(shape, dtype=torch.float64, device=dev)
+        fn = {"scalar": gsc.summate_device, "incompr": gsc.summate_incompr_device,
+              "fourier": gsc.summate_fourier_device}[kind]
+        dev_calls.append((name, kind, fn, darrs, out))
+
+    def step(timing=False):
+        for _, _, fn, darrs, out in dev_calls:
+            fn(*darrs, out, form=form, stream=stream.cuda_stream, timing=timing)
+
+    with ClockSampler(local) as clk:
+        warm = warm_up(torch, step, args.warmup)
+        barrier(world)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter()
+        per_step, kern, launches = [], {}, 0
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _, _, fn, darrs, out in dev_calls:
+                fn(*darrs, out, form=form, stream=stream.cuda_stream, timing=True)
+                for kname, ms in gsc.last_timings():
+                    kern.setdefault(kname, []).append(ms)
+                    launches += 1
+            b.record(stream)
+            b.synchronize()
+            per_step.append(a.elapsed_time(b))
+        barrier(world)
+        t_wall = time.perf_counter() - t_wall
+    gsc.device_status()
+    ms_step = max_over_ranks(world, float(np.mean(per_step)))
+    value = work * world / (ms_step * 1e-3) / 1e9
+    tot = {k: float(np.sum(v)) / args.steps for k, v in kern.items()}
+    dom = max(tot, key=tot.get)
+    # units and dimension mix of the calls that ran the dominant kernel
+    inc = "incompr" in dom
+    mix, units = {}, 0.0
+    for _, kind, arrs in calls:
+        if (kind == "incompr") != inc:
+            continue
+        n = arrs[1].shape[1] if kind == "fourier" else arrs[0].shape[1]
+        u = float(arrs[-1].shape[1]) * n
+        key = (arrs[-1].shape[0], inc)
+        mix[key] = mix.get(key, 0.0) + u
+        units += u
+    mix = {k: v / units for k, v in mix.items()}
+    roof = roofline(args, None, dom, tot[dom], 1, units=units, op_mix=mix)
+
+    cores = host_cores()
+    per_call, err = {}, {}
+    for (name, kind, arrs), (_, _, fn, darrs, out) in zip(calls, dev_calls):
+        ref = field_oracle(kind, arrs, cores)
+        got = out.cpu().numpy()
+        rms = float(np.sqrt(np.mean(ref ** 2)))
+        err[name] = float(np.max(np.abs(got - ref)) / rms)
+    # per call, device-resident, like criterion's per-function report
+    for name, kind, fn, darrs, out in dev_calls:
+        fn(*darrs, out, form=form, stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(5):
+            fn(*darrs, out, form=form, stream=stream.cuda_stream)
+        b.record(stream)
+        b.synchronize()
+        per_call[name] = a.elapsed_time(b) / 5
+
+    e2e = None
+    if not args.no_e2e:
+        host = {"scalar": gsc.summate, "incompr": gsc.summate_incompr,
+                "fourier": gsc.summate_fourier}
+        h2d = sum(sum(x.size for x in arrs) * 8 for _, _, arrs in calls)
+        d2h = sum((arrs[-1].shape[0] if k == "incompr" else 1) * arrs[-1].shape[1] * 8
+                  for _, k, arrs in calls)
+        for _, kind, arrs in calls:
+            host[kind](*arrs, form=form)
+        ts = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            for _, kind, arrs in calls:
+                host[kind](*arrs, form=form)
+            ts.append(time.perf_counter() - t0)
+        t_e2e = max_over_ranks(world, float(np.mean(ts)))
+        e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": t_e2e * 1e3,
+               "api": "gstools_core.summate / summate_incompr / summate_fourier",
+               "timing": "host wall clock around the five synchronous calls"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        t0 = time.perf_counter()
+        for _, kind, arrs in calls:
+            field_oracle(kind, arrs, cores)
+        t = time.perf_counter() - t0
+        cpu = {"value": work / t / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"the full five calls ({work:.3g} point*modes), {t:.2f} s on {cores} "
+                         f"threads (oracle/field_oracle.c)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if form.startswith("plain") else
+                 "f32 pairs (phase), f32 (sincos, tile sums), f64 output",
+        "data": source,
+        "config": {"workload": "field", "desc": "benches/main.rs field benchmarks: summate "
+                   "2d/3d, summate_incompr 2d/3d, summate_fourier 2d, 1e4 points x 1000 modes",
+                   "form": form, "point_modes": work,
+                   "l2": "flushed by a 256 MiB write before every timed step",
+                   "warmup_steps_run": warm, "wall_s": t_wall},
+        "per_call_ms": per_call,
+        "error_vs_oracle": {"max_abs_over_rms": err,
+                            "reference": "oracle (field.rs restatement), FP64"},
+        "kernels_ms_per_step": tot,
+        "gpu_launches": int(launches),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -784,6 +977,30 @@ def run_reference(args, world, rank):
     """The reference's CPU algorithm (oracle restatement) on the host cores."""
     if rank != 0:
         return
+    if args.workload == "field":
+        calls, source = field_calls(args)
+        work = field_work(calls)
+        cores = host_cores()
+        ts = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            for _, kind, arrs in calls:
+                field_oracle(kind, arrs, cores)
+            ts.append(time.perf_counter() - t0)
+        t = float(np.mean(ts))
+        v = work / t / 1e9
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": source,
+            "config": {"workload": "field", "desc": "benches/main.rs field benchmarks",
+                       "form": "reference CPU (rayon-equivalent restatement)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "the full five calls per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
     if args.workload == "c5":
         items = ensemble()
         v, cores, desc, t = ensemble_cpu_rate(items, args.cpu_seconds, max(1, args.steps))
@@ -826,7 +1043,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "field"])
+    ap.add_argument("--input-dir", default=None,
+                    help="benches/input directory of the reference (workload field)")
     ap.add_argument("--form", default="auto")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -839,6 +1058,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "c5":
         run_ours_batch(args, world, rank, local)
+    elif args.workload == "field":
+        run_ours_field(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

@@ -147,3 +147,37 @@ def test_separable_rejected_for_unstructured(gsc):
     cov, z1, z2, axes = _grid_case(8, (4, 4), 10)
     with pytest.raises(ValueError, match="structured grid"):
         gsc.summate(cov, z1, z2, _flat(axes), form="sep_f16x3")
+
+
+def _spectral_divergence(u, L):
+    """max_k |k . u_hat(k)| / max_k |k| |u_hat(k)| of a periodic vector field
+    u (d, n, n[, n]) on [0, L)^d."""
+    d = u.shape[0]
+    n = u.shape[1:]
+    uh = [np.fft.fftn(u[i]) for i in range(d)]
+    ks = np.meshgrid(*[2.0 * np.pi * np.fft.fftfreq(m, d=L / m) for m in n], indexing="ij")
+    div = sum(ks[i] * uh[i] for i in range(d))
+    kmag = np.sqrt(sum(k ** 2 for k in ks))
+    umag = np.sqrt(sum(np.abs(x) ** 2 for x in uh))
+    return float(np.max(np.abs(div)) / np.max(kmag * umag))
+
+
+@pytest.mark.parametrize("form,bound", [("plain", 1e-12), ("sep_f64", 1e-12), ("sep_f16x5", 1e-5)])
+@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 48)])
+def test_incompr_divergence_free_in_spectral_space(gsc, form, bound, shape):
+    """Modes on the FFT grid of a periodic box: the field's Fourier
+    coefficients satisfy k . u_hat(k) = 0 (the projector of src/field.rs:138-152
+    removes the longitudinal part), to round-off of the form."""
+    dim = len(shape)
+    L = 8.0 * np.pi
+    rng = np.random.default_rng(11 + dim)
+    m = rng.integers(-min(shape) // 2 + 1, min(shape) // 2, (dim, 300))
+    m = m[:, np.any(m != 0, axis=0)]
+    cov = m * (2.0 * np.pi / L)
+    n = cov.shape[1]
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    axes = tuple(np.arange(s) * (L / s) for s in shape)
+    u = gsc.summate_incompr_structured(cov, z1, z2, axes, form=form)
+    div = _spectral_divergence(u.reshape((dim,) + shape), L)
+    print(f"divergence {form} {shape}: {div:.3e}")
+    assert div <= bound
