@@ -362,7 +362,7 @@ def run_ours(args, world, rank, local):
 
     # ---- warm-up and timed region, clocks sampled throughout -----------------
     with ClockSampler(local) as clk:
-        warm = warm_up(torch, step, args.warmup)
+        warm = warm_up(torch, step, args.warmup, args.min_warmup_s)
         gsc.device_status()
         barrier(world)
         torch.cuda.synchronize()
@@ -561,7 +561,7 @@ def run_ours_batch(args, world, rank, local):
         plan.run_graph(stream.cuda_stream)
 
     with ClockSampler(local) as clk:
-        warm = warm_up(torch, step, args.warmup)
+        warm = warm_up(torch, step, args.warmup, args.min_warmup_s)
         barrier(world)
         torch.cuda.synchronize()
         t_wall = time.perf_counter()
@@ -754,7 +754,7 @@ def run_ours_field(args, world, rank, local):
             fn(*darrs, out, form=form, stream=stream.cuda_stream, timing=timing)
 
     with ClockSampler(local) as clk:
-        warm = warm_up(torch, step, args.warmup)
+        warm = warm_up(torch, step, args.warmup, args.min_warmup_s)
         barrier(world)
         torch.cuda.synchronize()
         t_wall = time.perf_counter()
@@ -1052,6 +1052,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--min-warmup-s", type=float, default=0.5,
+                    help="keep warming up until this many seconds passed (clock sampling)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
