@@ -884,6 +884,15 @@ PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17,
 MIXED_FP32_OPS = {1: 35, 2: 43, 3: 51}
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture each (summaries in profiles/); None where no capture exists
+PROFILED_TRAFFIC = {
+    ("sep_tc_f16x5", "c2"): (12.4e6 + 73.2e6, "profiles/sep_tc_f16x5_c2.md"),
+    ("mixed_scalar", "c1"): (1.66e6, "profiles/mixed_scalar_c1.md"),
+    ("plain_f64_scalar", "c1"): (5.8e6, "profiles/plain_f64_scalar_c1.md"),
+}
+
+
 def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None):
     """Roofline entry for the dominant kernel.
 
@@ -900,6 +909,15 @@ def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None):
         P, N = n_points(w), w["cov"].shape[1]
         units = P * N
     per_launch_units = units / max(launches_per_step, 1)
+    traffic, tsrc = PROFILED_TRAFFIC.get((dom, getattr(args, "workload", None)), (None, None))
+    entry = _roofline_entry(args, w, dom, dom_ms, per_launch_units, op_mix, torch)
+    entry["traffic"] = traffic
+    if tsrc:
+        entry["traffic_source"] = f"ncu dram__bytes_read.sum + dram__bytes_write.sum, {tsrc}"
+    return entry
+
+
+def _roofline_entry(args, w, dom, dom_ms, per_launch_units, op_mix, torch):
     if dom.startswith("sep_tc"):
         d = w["dim"]
         nout = d if w["incompr"] else 1
