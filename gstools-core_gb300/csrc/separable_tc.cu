@@ -40,6 +40,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "internal.h"
 #include "sm100.cuh"
@@ -168,6 +169,7 @@ struct TabArgs {
     float *wnorm;                // x5 form: {W, 1/W}, W = 2^ceil(log2 max|z1 - i z2|)
     int tiled;                   // x5 form: B table and G stored as contiguous stage blocks
     int kbt;                     // x5 form: k-blocks (16 modes each)
+    int bn;                      // x5 form: G rows per stage block (tile width)
 };
 
 __global__ void sep_svec_kernel(TabArgs t) {
@@ -580,8 +582,8 @@ __global__ void sep_gtab_x5_kernel(TabArgs t) {
     // Stored as contiguous 16 KB stage blocks, one per (256-row tile, k-block
     // of 16 modes), already in the 64-byte-swizzled K-major layout the MMA
     // reads: row r at r * 64 bytes, 16-byte chunk c at c ^ ((r >> 1) & 3).
-    const int nt = row / BN, r = row % BN, kb = j / 16, jl = j % 16;
-    const int64_t blk = (static_cast<int64_t>(nt) * t.kbt + kb) * (BN * 64);
+    const int nt = row / t.bn, r = row % t.bn, kb = j / 16, jl = j % 16;
+    const int64_t blk = (static_cast<int64_t>(nt) * t.kbt + kb) * (t.bn * 64);
     const int off = r * 64 + (((jl >> 2) ^ ((r >> 1) & 3)) << 4) + (jl & 3) * 4;
     const int64_t w = (blk + off) / 4;
     t.ghi[w] = *reinterpret_cast<const uint32_t *>(&h1);
@@ -610,15 +612,26 @@ struct X5Params {
 constexpr int X5_BK = 32;
 constexpr int X5_STAGES = 3;
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
-constexpr int X5_G_BYTES = BN * X5_BK * 2;          // 16 KB
 constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
-constexpr int X5_OFF_G1 = 3 * X5_F_BYTES;
-constexpr int X5_OFF_G2 = X5_OFF_G1 + X5_G_BYTES;
-constexpr int X5_OFF_BT = X5_OFF_G2 + X5_G_BYTES;
-constexpr int X5_STAGE_V2 = X5_OFF_BT + X5_BT_BYTES;   // 72 KB
-constexpr size_t kSmemX5v2 = X5_STAGES * X5_STAGE_V2 + 1024 + 256;
-constexpr int X5_TMA_BYTES = 2 * X5_G_BYTES + X5_BT_BYTES;
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
+
+// Stage layout for tiles of BNX output columns (256, or 192 where that pads
+// the columns less, e.g. 3 x 192 components): every operand starts on a
+// 1024-byte boundary, as the 64-byte swizzle and the bulk copies need.
+template <int BNX>
+struct X5Layout {
+    static constexpr int G_BYTES = BNX * X5_BK * 2;      // 16 KB / 12 KB
+    static constexpr int OFF_G1 = 3 * X5_F_BYTES;
+    static constexpr int OFF_G2 = OFF_G1 + G_BYTES;
+    static constexpr int OFF_BT = OFF_G2 + G_BYTES;
+    static constexpr int STAGE = OFF_BT + X5_BT_BYTES;   // 72 KB / 64 KB
+    static constexpr size_t SMEM = X5_STAGES * STAGE + 1024 + 256;
+    static constexpr int TMA_BYTES = 2 * G_BYTES + X5_BT_BYTES;
+    static constexpr int HC = BNX / 2;                   // columns per worker half
+    static_assert(OFF_G2 % 1024 == 0 && OFF_BT % 1024 == 0 && STAGE % 1024 == 0,
+                  "stage operands must be 1024-byte aligned");
+    static_assert(HC % 32 == 0 && BNX % 16 == 0 && BNX <= 256, "tile width");
+};
 constexpr int kTmaWarpX5 = 8, kMmaWarpX5 = 9;
 
 // three slices of a (re, im) pair in units of 2^15, packed as half2
@@ -635,13 +648,15 @@ __device__ __forceinline__ void slice3x2(float2 v, float ls, float lu, uint32_t 
     w3 = *reinterpret_cast<const uint32_t *>(&h3);
 }
 
+template <int BNX>
 __global__ void __launch_bounds__(X5_THREADS, 1)
 sep_x5_kernel(const X5Params xp) {
+    using L = X5Layout<BNX>;
     const TcParams &p = xp.base;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + X5_STAGES * X5_STAGE_V2);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + X5_STAGES * L::STAGE);
     uint64_t *full_t = bars;                    // [3] copies -> workers, MMA (1 arrival + bytes)
     uint64_t *full_a = bars + 3;                // [3] workers -> MMA (256 arrivals)
     uint64_t *empty = bars + 6;                 // [3] MMA commit -> copy warp
@@ -657,7 +672,7 @@ sep_x5_kernel(const X5Params xp) {
     tile /= p.n_tiles;
     const int mt = tile % p.m_tiles;
     const int b = tile / p.m_tiles;
-    const int m0 = mt * BM, n0 = nt * BN;
+    const int m0 = mt * BM, n0 = nt * BNX;
     const int KB = p.kb_total, KC = p.kc;
     const int NC = (KB + KC - 1) / KC;
     // Every tile walks the k-blocks from its own starting point, so the
@@ -699,13 +714,13 @@ sep_x5_kernel(const X5Params xp) {
                 if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status,
                                         kErrTimeoutEmpty))
                     break;
-                unsigned char *st = smem + s * X5_STAGE_V2;
-                const int64_t gblk = (static_cast<int64_t>(nt) * KB + kb) * X5_G_BYTES;
+                unsigned char *st = smem + s * L::STAGE;
+                const int64_t gblk = (static_cast<int64_t>(nt) * KB + kb) * L::G_BYTES;
                 const int64_t bblk = (static_cast<int64_t>(mt) * KB + kb) * X5_BT_BYTES;
-                mbar_arrive_expect_tx(&full_t[s], X5_TMA_BYTES);
-                bulk_copy_g2s(st + X5_OFF_G1, xp.g1 + gblk, X5_G_BYTES, &full_t[s]);
-                bulk_copy_g2s(st + X5_OFF_G2, xp.g2 + gblk, X5_G_BYTES, &full_t[s]);
-                bulk_copy_g2s(st + X5_OFF_BT, xp.bt + bblk, X5_BT_BYTES, &full_t[s]);
+                mbar_arrive_expect_tx(&full_t[s], L::TMA_BYTES);
+                bulk_copy_g2s(st + L::OFF_G1, xp.g1 + gblk, L::G_BYTES, &full_t[s]);
+                bulk_copy_g2s(st + L::OFF_G2, xp.g2 + gblk, L::G_BYTES, &full_t[s]);
+                bulk_copy_g2s(st + L::OFF_BT, xp.bt + bblk, X5_BT_BYTES, &full_t[s]);
                 ++issued;
             }
             if (*abort_flag)
@@ -713,7 +728,7 @@ sep_x5_kernel(const X5Params xp) {
                     mbar_wait_drain(&full_t[i % X5_STAGES], (i / X5_STAGES) & 1, p.status);
         } else if (warp == kMmaWarpX5 && lane == 0) {
             // ---- MMA ---------------------------------------------------------
-            const uint32_t idesc = idesc_f16(BM, BN, false);
+            const uint32_t idesc = idesc_f16(BM, BNX, false);
             bool ok = true;
             for (int i = 0; i < KB; ++i) {
                 const int s = i % X5_STAGES, n = i / X5_STAGES;
@@ -724,9 +739,9 @@ sep_x5_kernel(const X5Params xp) {
                 if (ok) ok = mbar_wait(&full_a[s], n & 1, abort_flag, p.status, kErrTimeoutFull);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t sa = smem_u32(smem + s * X5_STAGE_V2);
+                const uint32_t sa = smem_u32(smem + s * L::STAGE);
                 const uint32_t f1 = sa, f2 = sa + X5_F_BYTES, f3 = sa + 2 * X5_F_BYTES;
-                const uint32_t g1 = sa + X5_OFF_G1, g2 = sa + X5_OFF_G2;
+                const uint32_t g1 = sa + L::OFF_G1, g2 = sa + L::OFF_G2;
 #pragma unroll
                 for (int kk = 0; kk < X5_BK / 16; ++kk) {
                     const uint32_t o = kk * 32;
@@ -765,17 +780,17 @@ sep_x5_kernel(const X5Params xp) {
         const uint32_t row_off = r * 64;                        // 64-byte rows
         const uint32_t swz = (r >> 1) & 3;                      // 64-byte swizzle phase
         const float ls = xp.wnorm[2], lu = xp.wnorm[3];
-        float tot[128];
+        float tot[L::HC];
 #pragma unroll
-        for (int i = 0; i < 128; ++i) tot[i] = 0.f;
+        for (int i = 0; i < L::HC; ++i) tot[i] = 0.f;
         int pend = 0;                                           // next cross chunk to drain
         auto drain_chunk = [&]() {
             tc_fence_after();
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
+            for (int g = 0; g < L::HC / 16; ++g) {
                 uint32_t v[16];
                 __syncwarp();
-                tmem_ld16(t_cross + lane_off + 128 * h + 16 * g, v);
+                tmem_ld16(t_cross + lane_off + L::HC * h + 16 * g, v);
                 tmem_ld_wait();
 #pragma unroll
                 for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
@@ -836,8 +851,8 @@ sep_x5_kernel(const X5Params xp) {
                 ok = false;
                 break;
             }
-            unsigned char *st = smem + s * X5_STAGE_V2;
-            const float2 *bt = reinterpret_cast<const float2 *>(st + X5_OFF_BT);
+            unsigned char *st = smem + s * L::STAGE;
+            const float2 *bt = reinterpret_cast<const float2 *>(st + L::OFF_BT);
 #pragma unroll
             for (int cc = 0; cc < 2; ++cc) {          // 16-byte chunks 2h, 2h+1: modes 4c .. 4c+3
                 const int c = 2 * h + cc;
@@ -876,20 +891,20 @@ sep_x5_kernel(const X5Params xp) {
             double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
             double *ob = p.out + static_cast<int64_t>(b) * p.batch_stride;
 #pragma unroll
-            for (int g = 0; g < 4; ++g) {
+            for (int g = 0; g < L::HC / 32; ++g) {
                 uint32_t v[32];
                 __syncwarp();
-                tmem_ld32(t_cross + lane_off + 128 * h + 32 * g, v);
+                tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
                 tmem_ld_wait();
 #pragma unroll
                 for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
-                tmem_ld32(t_main + lane_off + 128 * h + 32 * g, v);
+                tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
                 tmem_ld_wait();
 #pragma unroll
                 for (int t = 0; t < 32; ++t)
                     tr[lane * 33 + t] = f32_to_f64((__uint_as_float(v[t]) + tot[32 * g + t]) * unscale);
                 __syncwarp();
-                const int gn = n0 + 128 * h + 32 * g + lane;
+                const int gn = n0 + L::HC * h + 32 * g + lane;
                 if (gn < p.ncn) {
                     const int comp = gn / p.nn;
                     double *oc = ob + comp * p.comp_stride + (gn - comp * p.nn);
@@ -966,6 +981,34 @@ int configure_tc() {
 
 }  // namespace
 
+namespace {
+// One-time set-up of an x5 instantiation.  The warps re-balance their
+// registers with setmaxnreg; the increases can only be served from what the
+// block was launched with, so a build that launches with fewer registers
+// must not run.
+template <int BNX>
+int configure_x5() {
+    static std::once_flag once;
+    static int rc = GSC_OK;
+    std::call_once(once, [] {
+        cudaFuncAttributes fa{};
+        cudaError_t e = cudaFuncGetAttributes(&fa, sep_x5_kernel<BNX>);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "cudaFuncGetAttributes (x5)");
+            return;
+        }
+        if (fa.numRegs * X5_THREADS < 4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS)) {
+            rc = set_error(GSC_ERR_KERNEL, "x5 kernel built with too few registers per thread");
+            return;
+        }
+        e = cudaFuncSetAttribute(sep_x5_kernel<BNX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(X5Layout<BNX>::SMEM));
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaFuncSetAttribute (x5)");
+    });
+    return rc;
+}
+}  // namespace
+
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const bool x5 = a.form == GSC_FORM_SEP_F16X5;
     const bool bf16 = a.form == GSC_FORM_SEP_BF16X3;
@@ -984,8 +1027,11 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int m_tiles_ = (nm + BM - 1) / BM;
     // x5 stores the B table as whole 128-row tiles
     const int nm_ld = x5 ? m_tiles_ * BM : (nm + 15) / 16 * 16;
-    const int n_tiles = (ncn + BN - 1) / BN;
-    const int ncn_pad = n_tiles * BN;
+    // x5 tile width: 256 columns, or 192 where that pads the columns less
+    // (e.g. three 192-point components: 576 columns in 3 tiles, not 768)
+    const int bnx = (x5 && (ncn + 191) / 192 * 192 < (ncn + 255) / 256 * 256) ? 192 : BN;
+    const int n_tiles = (ncn + bnx - 1) / bnx;
+    const int ncn_pad = n_tiles * bnx;
     const int m_tiles = (nm + BM - 1) / BM;
 
     // scratch: normaliser, svec, btab, G hi (G1), G lo (G2)
@@ -1029,6 +1075,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.wnorm = x5 ? reinterpret_cast<float *>(base + off_wn) : nullptr;
     t.tiled = x5 ? 1 : 0;
     t.kbt = KB;
+    t.bn = bnx;
 
     {
         TimedLaunch tl(st);
@@ -1084,21 +1131,14 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         xp.g1 = reinterpret_cast<const unsigned char *>(t.ghi);
         xp.g2 = reinterpret_cast<const unsigned char *>(t.glo);
         xp.bt = reinterpret_cast<const unsigned char *>(t.btab);
-        static bool configured = false;
-        if (!configured) {
-            // The warps re-balance their registers with setmaxnreg; the
-            // increases can only be served from what the block was launched
-            // with, so a build that launches with fewer registers must not run.
-            cudaFuncAttributes fa{};
-            GSC_CUDA(cudaFuncGetAttributes(&fa, sep_x5_kernel));
-            if (fa.numRegs * X5_THREADS < 4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS))
-                return set_error(GSC_ERR_KERNEL, "x5 kernel built with too few registers per thread");
-            GSC_CUDA(cudaFuncSetAttribute(sep_x5_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          static_cast<int>(kSmemX5v2)));
-            configured = true;
-        }
         tl.begin(K_SEP_TC_F16X5);
-        sep_x5_kernel<<<static_cast<unsigned>(grid), X5_THREADS, kSmemX5v2, st>>>(xp);
+        if (bnx == 192) {
+            GSC_TRY(configure_x5<192>());
+            sep_x5_kernel<192><<<static_cast<unsigned>(grid), X5_THREADS, X5Layout<192>::SMEM, st>>>(xp);
+        } else {
+            GSC_TRY(configure_x5<256>());
+            sep_x5_kernel<256><<<static_cast<unsigned>(grid), X5_THREADS, X5Layout<256>::SMEM, st>>>(xp);
+        }
     } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
         if (bf16) {
