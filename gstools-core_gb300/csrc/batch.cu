@@ -629,12 +629,35 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     double *d = static_cast<double *>(ctx->io.ptr);
     double *dout = d + n_in;
     std::vector<gsc_batch_item> dev(static_cast<size_t>(count));
-    size_t off = 0, oo = 0;
+    // Large arrays move by DMA straight from the caller's memory; runs of
+    // small ones are packed into the pinned buffer and moved together.
+    constexpr size_t kDirect = size_t(1) << 20;
+    size_t off = 0, oo = 0, run = 0;
+    int rc = GSC_OK;
+    auto flush = [&]() {
+        if (off > run && rc == GSC_OK) {
+            const cudaError_t e = cudaMemcpyAsync(d + run, h + run, (off - run) * sizeof(double),
+                                                  cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync (batch inputs)");
+        }
+        run = off;
+    };
     auto put = [&](const double *src, int64_t n) -> const double * {
         if (n <= 0) return nullptr;
-        memcpy(h + off, src, static_cast<size_t>(n) * sizeof(double));
+        const size_t bytes = static_cast<size_t>(n) * sizeof(double);
         const double *r = d + off;
-        off += static_cast<size_t>(n);
+        if (bytes >= kDirect) {
+            flush();
+            if (rc == GSC_OK) {
+                const cudaError_t e = cudaMemcpyAsync(d + off, src, bytes, cudaMemcpyHostToDevice, st);
+                if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync (batch inputs)");
+            }
+            off += static_cast<size_t>(n);
+            run = off;
+        } else {
+            parallel_copy(h + off, src, bytes);
+            off += static_cast<size_t>(n);
+        }
         return r;
     };
     for (int64_t i = 0; i < count; ++i) {
@@ -649,8 +672,8 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         y.out = x.n_points > 0 ? dout + oo : nullptr;
         oo += static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
     }
-    if (n_in > 0)
-        GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    flush();
+    GSC_TRY(rc);
     // the plan of the previous call is reused when the shapes match
     std::vector<int64_t> sig = {reinterpret_cast<int64_t>(ctx->io.ptr), ro.form,
                                 static_cast<int64_t>(ro.tolerance * 1e15), count};
@@ -676,16 +699,25 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         timing_reset(ro.flags & GSC_FLAG_TIMING);
     }
     GSC_TRY(gsc_batch_run(ctx->batch, st));
-    if (n_out > 0)
-        GSC_CUDA(cudaMemcpyAsync(h, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
-    GSC_CUDA(cudaStreamSynchronize(st));
-    oo = 0;
+    // fault in the output pages while the GPU computes, then DMA straight
+    // into the caller's arrays
+    std::vector<HostSeg> segs;
     for (int64_t i = 0; i < count; ++i) {
         const gsc_batch_item &x = items[i];
         const size_t n = static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
-        if (n > 0) memcpy(x.out, h + oo, n * sizeof(double));
-        oo += n;
+        segs.push_back(HostSeg{x.out, n * sizeof(double)});
     }
+    Prefault pf;
+    pf.start_many(segs);
+    pf.join();
+    oo = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const size_t n = segs[static_cast<size_t>(i)].bytes;
+        if (n > 0)
+            GSC_CUDA(cudaMemcpyAsync(items[i].out, dout + oo, n, cudaMemcpyDeviceToHost, st));
+        oo += n / sizeof(double);
+    }
+    GSC_CUDA(cudaStreamSynchronize(st));
     return GSC_OK;
 }
 

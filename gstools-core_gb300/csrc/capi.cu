@@ -5,9 +5,11 @@
 #include <stddef.h>
 #include <stdint.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -278,14 +280,165 @@ static int check_status(DeviceCtx &ctx, cudaStream_t st) {
     return GSC_OK;
 }
 
+void parallel_copy(void *dst, const void *src, size_t n) {
+    constexpr size_t kMinPart = size_t(4) << 20;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t T = std::min<size_t>(std::min<size_t>(8, hw ? hw : 1), n / kMinPart);
+    if (T <= 1) {
+        memcpy(dst, src, n);
+        return;
+    }
+    const size_t part = (n + T - 1) / T;
+    std::vector<std::thread> th;
+    th.reserve(T - 1);
+    for (size_t t = 1; t < T; ++t) {
+        const size_t o = t * part;
+        if (o >= n) break;
+        const size_t len = std::min(part, n - o);
+        th.emplace_back([=] {
+            memcpy(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, len);
+        });
+    }
+    memcpy(dst, src, std::min(part, n));
+    for (auto &x : th) x.join();
+}
+
+int d2h_scatter(DeviceCtx &ctx, cudaStream_t st, const void *src, size_t n,
+                const std::vector<HostSeg> &segs) {
+    constexpr size_t kChunk = size_t(32) << 20;
+    if (n == 0) return GSC_OK;
+    // copies bytes [o, o + len) of the device range, staged at `stage`, to
+    // the host segments they belong to
+    size_t seg = 0, seg_start = 0;
+    auto scatter = [&](const char *stage, size_t o, size_t len) {
+        while (len > 0) {
+            while (seg < segs.size() && o >= seg_start + segs[seg].bytes) {
+                seg_start += segs[seg].bytes;
+                ++seg;
+            }
+            if (seg >= segs.size()) return;
+            const size_t in_seg = o - seg_start;
+            const size_t take = std::min(len, segs[seg].bytes - in_seg);
+            parallel_copy(static_cast<char *>(segs[seg].dst) + in_seg, stage, take);
+            stage += take;
+            o += take;
+            len -= take;
+        }
+    };
+    if (n <= kChunk) {
+        GSC_TRY(ensure_pinned(ctx, n));
+        GSC_CUDA(cudaMemcpyAsync(ctx.pinned, src, n, cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        scatter(static_cast<const char *>(ctx.pinned), 0, n);
+        return GSC_OK;
+    }
+    GSC_TRY(ensure_pinned(ctx, 2 * kChunk));
+    for (auto &e : ctx.stage_ev)
+        if (!e) GSC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    char *pin[2] = {static_cast<char *>(ctx.pinned), static_cast<char *>(ctx.pinned) + kChunk};
+    const size_t chunks = (n + kChunk - 1) / kChunk;
+    for (size_t k = 0; k <= chunks; ++k) {
+        if (k < chunks) {
+            const size_t o = k * kChunk, len = std::min(kChunk, n - o);
+            GSC_CUDA(cudaMemcpyAsync(pin[k & 1], static_cast<const char *>(src) + o, len,
+                                     cudaMemcpyDeviceToHost, st));
+            GSC_CUDA(cudaEventRecord(ctx.stage_ev[k & 1], st));
+        }
+        if (k > 0) {   // chunk k-1 is copied out while chunk k is in flight
+            const size_t j = k - 1, o = j * kChunk, len = std::min(kChunk, n - o);
+            GSC_CUDA(cudaEventSynchronize(ctx.stage_ev[j & 1]));
+            scatter(pin[j & 1], o, len);
+        }
+    }
+    return GSC_OK;
+}
+
+int d2h_staged(DeviceCtx &ctx, cudaStream_t st, void *dst, const void *src, size_t n) {
+    return d2h_scatter(ctx, st, src, n, {HostSeg{dst, n}});
+}
+
+// Host memory the GPU reads or writes directly (pageable memory on a
+// coherent host link moves at DMA speed once its pages exist): first-touch
+// faults of fresh output arrays are the cost, so they are taken on host
+// threads while the GPU computes.
+void Prefault::start(void *p, size_t n) {
+    if (p && n) start_many({HostSeg{p, n}});
+}
+
+void Prefault::start_many(const std::vector<HostSeg> &segs) {
+    static const size_t kPage = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? static_cast<size_t>(v) : size_t(4096);
+    }();
+    const size_t page = kPage;
+    // (segment, first page, end page) pieces, then an equal share per thread
+    size_t total = 0;
+    for (auto &sg : segs) total += sg.dst && sg.bytes ? (sg.bytes + page - 1) / page : 0;
+    if (total == 0) return;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t T = std::max<size_t>(1, std::min<size_t>(std::min<size_t>(8, hw ? hw : 1),
+                                                          (total + 255) / 256));
+    const size_t per = (total + T - 1) / T;
+    auto touch_range = [segs, page](size_t a, size_t b) {   // global page indices [a, b)
+        size_t first = 0;
+        for (auto &sg : segs) {
+            if (!sg.dst || !sg.bytes) continue;
+            const size_t np = (sg.bytes + page - 1) / page;
+            const size_t lo = std::max(a, first), hi = std::min(b, first + np);
+            for (size_t i = lo; i < hi; ++i) {
+                volatile char *c = static_cast<char *>(sg.dst) + std::min((i - first) * page, sg.bytes - 1);
+                *c = 0;
+            }
+            first += np;
+            if (first >= b) break;
+        }
+    };
+    if (T == 1) {
+        touch_range(0, total);
+        return;
+    }
+    for (size_t t = 0; t < T; ++t) {
+        const size_t a = t * per, b = std::min(total, a + per);
+        if (a < b) th.emplace_back(touch_range, a, b);
+    }
+}
+
+void Prefault::join() {
+    for (auto &x : th) x.join();
+    th.clear();
+}
+
+// Uploads a (rows, cols) host view to dense row-major device memory at
+// d + off: large contiguous arrays go directly, others through the pinned
+// buffer `h` at the same offset.
+static int upload2(cudaStream_t st, double *d, double *h, size_t off, const double *src,
+                   int64_t s0, int64_t s1, int64_t rows, int64_t cols);
+
 // gathers a strided (rows, cols) host view into dense row-major dst
+static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int64_t cols,
+                    double *dst);
+
+static int upload2(cudaStream_t st, double *d, double *h, size_t off, const double *src,
+                   int64_t s0, int64_t s1, int64_t rows, int64_t cols) {
+    const size_t n = static_cast<size_t>(rows * cols);
+    if (n == 0) return GSC_OK;
+    const bool contiguous = s1 == 1 && (rows == 1 || s0 == cols);
+    if (contiguous && n * sizeof(double) >= (size_t(1) << 20)) {
+        GSC_CUDA(cudaMemcpyAsync(d + off, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    } else {
+        gather2(src, s0, s1, rows, cols, h + off);
+        GSC_CUDA(cudaMemcpyAsync(d + off, h + off, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    return GSC_OK;
+}
+
 static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int64_t cols,
                     double *dst) {
     for (int64_t i = 0; i < rows; ++i) {
         const double *row = src + i * s0;
         double *o = dst + i * cols;
         if (s1 == 1) {
-            memcpy(o, row, sizeof(double) * static_cast<size_t>(cols));
+            parallel_copy(o, row, sizeof(double) * static_cast<size_t>(cols));
         } else {
             for (int64_t j = 0; j < cols; ++j) o[j] = row[j * s1];
         }
@@ -332,14 +485,12 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(ensure_dev(*ctx, ctx->io, bytes));
 
     double *h = static_cast<double *>(ctx->pinned);
-    gather2(cov, cs_d, cs_n, dim, N, h);
-    gather2(z1, 0, z1s, 1, N, h + n_cov);
-    gather2(z2, 0, z2s, 1, N, h + n_cov + N);
-    if (sf) gather2(sf, 0, sfs, 1, N, h + n_cov + 2 * N);
-    gather2(pos, ps_d, ps_p, dim, P, h + n_cov + 2 * N + n_sf);
-
     double *d = static_cast<double *>(ctx->io.ptr);
-    GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    GSC_TRY(upload2(st, d, h, 0, cov, cs_d, cs_n, dim, N));
+    GSC_TRY(upload2(st, d, h, n_cov, z1, 0, z1s, 1, N));
+    GSC_TRY(upload2(st, d, h, n_cov + N, z2, 0, z2s, 1, N));
+    if (sf) GSC_TRY(upload2(st, d, h, n_cov + 2 * N, sf, 0, sfs, 1, N));
+    GSC_TRY(upload2(st, d, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P));
     if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
                                   d + n_cov + N, st));
     PlainArgs a;
@@ -355,12 +506,20 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     a.out_sd = P;
     a.out_sp = 1;
     GSC_TRY(run_points(*ctx, ro, a, st));
+    if (os_p == 1 && (nout == 1 || os_d == P)) {
+        Prefault pf;
+        pf.start(out, n_out * sizeof(double));
+        pf.join();
+        GSC_CUDA(cudaMemcpyAsync(out, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        return GSC_OK;
+    }
     double *ho = h + n_in;
     GSC_CUDA(cudaMemcpyAsync(ho, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
     GSC_CUDA(cudaStreamSynchronize(st));
     for (int64_t i = 0; i < nout; ++i) {
         if (os_p == 1 && (nout == 1 || os_d == P)) {
-            memcpy(out + i * os_d, ho + i * P, sizeof(double) * static_cast<size_t>(P));
+            parallel_copy(out + i * os_d, ho + i * P, sizeof(double) * static_cast<size_t>(P));
         } else {
             for (int64_t p = 0; p < P; ++p) out[i * os_d + p * os_p] = ho[i * P + p];
         }
@@ -537,22 +696,23 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     const size_t n_sf = sf ? static_cast<size_t>(N) : 0;
     const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_ax;
     const size_t n_out = static_cast<size_t>(nout * P);
-    GSC_TRY(ensure_pinned(*ctx, n_in * sizeof(double)));
+    // inputs, and the two 32 MiB stages of the output copy
+    GSC_TRY(ensure_pinned(*ctx, std::max(n_in * sizeof(double),
+                                         std::min(n_out * sizeof(double), size_t(64) << 20))));
     GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out) * sizeof(double) + 1024));
     double *h = static_cast<double *>(ctx->pinned);
-    gather2(cov, cs_d, cs_n, dim, N, h);
-    gather2(z1, 0, z1s, 1, N, h + n_cov);
-    gather2(z2, 0, z2s, 1, N, h + n_cov + N);
-    if (sf) gather2(sf, 0, sfs, 1, N, h + n_cov + 2 * N);
-    size_t off = n_cov + 2 * N + n_sf;
     double *d = static_cast<double *>(ctx->io.ptr);
+    GSC_TRY(upload2(st, d, h, 0, cov, cs_d, cs_n, dim, N));
+    GSC_TRY(upload2(st, d, h, n_cov, z1, 0, z1s, 1, N));
+    GSC_TRY(upload2(st, d, h, n_cov + N, z2, 0, z2s, 1, N));
+    if (sf) GSC_TRY(upload2(st, d, h, n_cov + 2 * N, sf, 0, sfs, 1, N));
+    size_t off = n_cov + 2 * N + n_sf;
     const double *dax[3] = {nullptr, nullptr, nullptr};
     for (int k = 0; k < dim; ++k) {
-        gather2(ax[k], 0, sx[k], 1, n[k], h + off);
+        GSC_TRY(upload2(st, d, h, off, ax[k], 0, sx[k], 1, n[k]));
         dax[k] = d + off;
         off += static_cast<size_t>(n[k]);
     }
-    GSC_CUDA(cudaMemcpyAsync(d, h, n_in * sizeof(double), cudaMemcpyHostToDevice, st));
     if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
                                   d + n_cov + N, st));
     // output buffer 128-byte aligned after the inputs
@@ -560,6 +720,11 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         (reinterpret_cast<uintptr_t>(d + n_in) + 127) & ~static_cast<uintptr_t>(127));
     GSC_TRY(run_structured(*ctx, ro, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr, dout,
                            st));
+    // output pages are faulted in on host threads while the GPU computes;
+    // the result then moves by DMA straight into the caller's array
+    Prefault pf;
+    pf.start(out, n_out * sizeof(double));
+    pf.join();
     GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
     GSC_TRY(check_status(*ctx, st));
     return GSC_OK;

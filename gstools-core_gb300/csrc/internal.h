@@ -8,6 +8,7 @@
 
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gstools_core_gb300.h"
@@ -76,6 +77,7 @@ struct DeviceCtx {
     DevBuf grid;                     // expanded meshgrid for plain forms on grids
     DevBuf zscaled;                  // spectrum-scaled z1, z2 of device-pointer Fourier calls
     int *status = nullptr;           // sticky kernel status word (device)
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};   // pipelined device-to-host staging
     gsc_batch *batch = nullptr;      // plan of the last host-pointer batch call
     std::vector<int64_t> batch_sig;  // its shape signature (reused when equal)
 };
@@ -114,6 +116,29 @@ int get_ctx(int device, DeviceCtx **out);
 // Makes `buf` hold at least `bytes`; waits for in-flight users before growing.
 int ensure_dev(DeviceCtx &ctx, DevBuf &buf, size_t bytes);
 int ensure_pinned(DeviceCtx &ctx, size_t bytes);
+// memcpy with up to 8 host threads for large blocks
+void parallel_copy(void *dst, const void *src, size_t bytes);
+// Device -> pageable host through the pinned buffer in 32 MiB chunks, the DMA
+// of one chunk overlapping the host copy of the previous one; returns after
+// the data is in `dst` (synchronises `st`).
+int d2h_staged(DeviceCtx &ctx, cudaStream_t st, void *dst, const void *src, size_t bytes);
+// As d2h_staged for a device range whose consecutive pieces go to separate
+// host arrays (segments in order, sizes summing to `bytes`).
+struct HostSeg {
+    void *dst;
+    size_t bytes;
+};
+int d2h_scatter(DeviceCtx &ctx, cudaStream_t st, const void *src, size_t bytes,
+                const std::vector<HostSeg> &segs);
+// Faults in the pages of a host range on worker threads (start), so that a
+// later device-to-host copy into it runs at DMA speed; join() waits.
+struct Prefault {
+    std::vector<std::thread> th;
+    void start(void *p, size_t bytes);
+    void start_many(const std::vector<HostSeg> &segs);
+    void join();
+    ~Prefault() { join(); }
+};
 
 // ---- timing ---------------------------------------------------------------
 struct TimedLaunch {
