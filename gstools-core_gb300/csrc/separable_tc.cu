@@ -189,25 +189,32 @@ __global__ void sep_svec_kernel(TabArgs t) {
 }
 
 // B table [n_modes][nm_ld], columns nm .. nm_ld-1 zero.  For the x5 form
-// (tiled) the same values are stored as contiguous 16 KB blocks, one per
-// (128-row tile, k-block of 16 modes): block (mt, kb) holds
-// [16 modes][128 rows] float2, exactly the shared-memory image its stage
-// needs, so one bulk copy moves it.
+// (tiled) the values are stored per k-block of 16 modes as [nm rows][16
+// modes] float2, 128 bytes per row with the row's 16-byte chunk c (modes 2c,
+// 2c+1) at position c ^ (m & 7): any run of consecutive rows is one
+// contiguous block that a bulk copy moves into a stage unchanged, and
+// eight consecutive rows read the same logical chunk from eight different
+// bank groups.
 __global__ void sep_btab_kernel(TabArgs t) {
     // the tiled layout also zero-fills the modes past n_modes of the last k-block
     const int64_t nj = t.tiled ? static_cast<int64_t>(t.kbt) * 16 : t.n_modes;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= nj * t.nm_ld) return;
-    const int j = static_cast<int>(i / t.nm_ld), m = static_cast<int>(i % t.nm_ld);
+    int j, m;
+    if (t.tiled) {   // i walks the stored layout, so the stores are contiguous
+        const int e = static_cast<int>(i & 15);
+        const int64_t row = i >> 4;                      // kb * nm + m
+        m = static_cast<int>(row % t.nm_ld);
+        const int kb = static_cast<int>(row / t.nm_ld);
+        j = kb * 16 + ((((e >> 1) ^ (m & 7)) << 1) | (e & 1));
+    } else {
+        j = static_cast<int>(i / t.nm_ld);
+        m = static_cast<int>(i % t.nm_ld);
+    }
     const float2 v = (m < t.nm && j < t.n_modes)
                          ? cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m])
                          : make_float2(0.f, 0.f);
-    if (t.tiled) {
-        const int mt = m / 128, r = m % 128, kb = j / 16, q = j % 16;
-        t.btab[((static_cast<int64_t>(mt) * t.kbt + kb) * 16 + q) * 128 + r] = v;
-    } else {
-        t.btab[i] = v;
-    }
+    t.btab[i] = v;
 }
 
 template <bool BF16>
@@ -251,6 +258,7 @@ struct TcParams {
     int n_modes, nm, nm_ld, nb, nn, ncn;   // ncn = ncomp * nn valid G rows
     int kb_total, kc;               // k-blocks, k-blocks per accumulation chunk
     int m_tiles, n_tiles;
+    int64_t rows_total;             // x5: nb * nm rows, tiled across slices
     double *out;
     int64_t comp_stride, batch_stride, row_stride;
     int *status;
@@ -626,7 +634,6 @@ struct X5Layout {
     static constexpr int OFF_BT = OFF_G2 + G_BYTES;
     static constexpr int STAGE = OFF_BT + X5_BT_BYTES;   // 72 KB / 64 KB
     static constexpr size_t SMEM = X5_STAGES * STAGE + 1024 + 256;
-    static constexpr int TMA_BYTES = 2 * G_BYTES + X5_BT_BYTES;
     static constexpr int HC = BNX / 2;                   // columns per worker half
     static_assert(OFF_G2 % 1024 == 0 && OFF_BT % 1024 == 0 && STAGE % 1024 == 0,
                   "stage operands must be 1024-byte aligned");
@@ -667,12 +674,12 @@ sep_x5_kernel(const X5Params xp) {
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int tile = blockIdx.x;
-    const int nt = tile % p.n_tiles;
-    tile /= p.n_tiles;
-    const int mt = tile % p.m_tiles;
-    const int b = tile / p.m_tiles;
-    const int m0 = mt * BM, n0 = nt * BNX;
+    // Rows are the nb * nm (x-slice, y) pairs taken in order, so a 128-row
+    // tile may span two or more slices and no slice pads a partial tile.
+    const int nt = blockIdx.x % p.n_tiles;
+    const int64_t r0 = static_cast<int64_t>(blockIdx.x / p.n_tiles) * BM;
+    const int n0 = nt * BNX;
+    const int rows_valid = static_cast<int>(min(static_cast<int64_t>(BM), p.rows_total - r0));
     const int KB = p.kb_total, KC = p.kc;
     const int NC = (KB + KC - 1) / KC;
     // Every tile walks the k-blocks from its own starting point, so the
@@ -708,6 +715,23 @@ sep_x5_kernel(const X5Params xp) {
         regs_dec<X5_CTRL_REGS>();
         if (warp == kTmaWarpX5 && lane == 0) {
             // ---- bulk copies: G1, G2, B-table block ----------------------------
+            // the tile's runs of consecutive y rows (a run ends where the tile
+            // crosses into the next x-slice) are the same for every k-block
+            constexpr int kMaxRuns = 4;
+            int run_r[kMaxRuns], run_m[kMaxRuns], run_len[kMaxRuns], n_runs = 0;
+            {
+                int r = 0, m = static_cast<int>(r0 % p.nm);
+                while (r < rows_valid && n_runs < kMaxRuns) {
+                    const int len = min(rows_valid - r, p.nm - m);
+                    run_r[n_runs] = r;
+                    run_m[n_runs] = m;
+                    run_len[n_runs] = len;
+                    ++n_runs;
+                    r += len;
+                    m = 0;
+                }
+                if (r < rows_valid) n_runs = -1;   // more runs (short y axis): computed per copy
+            }
             int issued = 0;
             for (int i = 0; i < KB; ++i) {
                 const int s = i % X5_STAGES, n = i / X5_STAGES, kb = kb_of(i);
@@ -716,11 +740,26 @@ sep_x5_kernel(const X5Params xp) {
                     break;
                 unsigned char *st = smem + s * L::STAGE;
                 const int64_t gblk = (static_cast<int64_t>(nt) * KB + kb) * L::G_BYTES;
-                const int64_t bblk = (static_cast<int64_t>(mt) * KB + kb) * X5_BT_BYTES;
-                mbar_arrive_expect_tx(&full_t[s], L::TMA_BYTES);
+                mbar_arrive_expect_tx(&full_t[s], 2 * L::G_BYTES + rows_valid * 128);
                 bulk_copy_g2s(st + L::OFF_G1, xp.g1 + gblk, L::G_BYTES, &full_t[s]);
                 bulk_copy_g2s(st + L::OFF_G2, xp.g2 + gblk, L::G_BYTES, &full_t[s]);
-                bulk_copy_g2s(st + L::OFF_BT, xp.bt + bblk, X5_BT_BYTES, &full_t[s]);
+                // B rows of the tile: one copy per run
+                const unsigned char *bk = xp.bt + static_cast<int64_t>(kb) * p.nm * 128;
+                if (n_runs >= 0) {
+#pragma unroll
+                    for (int k = 0; k < kMaxRuns; ++k)
+                        if (k < n_runs)
+                            bulk_copy_g2s(st + L::OFF_BT + run_r[k] * 128,
+                                          bk + static_cast<int64_t>(run_m[k]) * 128,
+                                          run_len[k] * 128, &full_t[s]);
+                } else {
+                    for (int r = 0, m = static_cast<int>(r0 % p.nm); r < rows_valid; m = 0) {
+                        const int len = min(rows_valid - r, p.nm - m);
+                        bulk_copy_g2s(st + L::OFF_BT + r * 128, bk + static_cast<int64_t>(m) * 128,
+                                      len * 128, &full_t[s]);
+                        r += len;
+                    }
+                }
                 ++issued;
             }
             if (*abort_flag)
@@ -776,7 +815,15 @@ sep_x5_kernel(const X5Params xp) {
         const int q = warp & 3, h = warp >> 2;
         const int r = 32 * q + lane;                            // F row and TMEM lane
         const uint32_t lane_off = static_cast<uint32_t>(32 * q) << 16;
-        const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
+        const bool row_ok = r < rows_valid;
+        const int64_t grow = row_ok ? r0 + r : 0;               // (x-slice, y) of the row
+        const int bsl = static_cast<int>(grow / p.nm), mrow = static_cast<int>(grow % p.nm);
+        const float2 *sv = p.svec + static_cast<int64_t>(bsl) * p.n_modes;
+        // byte offsets, in this row's 128-byte B line, of the four 16-byte
+        // chunks (modes 8h .. 8h+7) the thread reads: chunk c sits at c ^ (m & 7)
+        const uint32_t bswz = static_cast<uint32_t>(mrow & 7);
+        const uint32_t boff[4] = {((4 * h + 0) ^ bswz) << 4, ((4 * h + 1) ^ bswz) << 4,
+                                  ((4 * h + 2) ^ bswz) << 4, ((4 * h + 3) ^ bswz) << 4};
         const uint32_t row_off = r * 64;                        // 64-byte rows
         const uint32_t swz = (r >> 1) & 3;                      // 64-byte swizzle phase
         const float ls = xp.wnorm[2], lu = xp.wnorm[3];
@@ -838,7 +885,7 @@ sep_x5_kernel(const X5Params xp) {
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
                 const int j = kb * 16 + 8 * h + t;
-                dst[t] = j < p.n_modes ? __ldg(sv + j) : make_float2(0.f, 0.f);
+                dst[t] = (row_ok && j < p.n_modes) ? __ldg(sv + j) : make_float2(0.f, 0.f);
             }
         };
         bool ok = true;
@@ -852,14 +899,21 @@ sep_x5_kernel(const X5Params xp) {
                 break;
             }
             unsigned char *st = smem + s * L::STAGE;
-            const float2 *bt = reinterpret_cast<const float2 *>(st + L::OFF_BT);
+            const unsigned char *brow = st + L::OFF_BT + r * 128;
 #pragma unroll
             for (int cc = 0; cc < 2; ++cc) {          // 16-byte chunks 2h, 2h+1: modes 4c .. 4c+3
                 const int c = 2 * h + cc;
                 uint32_t w1[4], w2[4], w3[4];
+                // B modes 4c .. 4c+3 of this row: table chunks 2c and 2c+1
+                const float4 b01 = *reinterpret_cast<const float4 *>(brow + boff[2 * cc]);
+                const float4 b23 = *reinterpret_cast<const float4 *>(brow + boff[2 * cc + 1]);
+                const float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w),
+                                      make_float2(b23.x, b23.y), make_float2(b23.z, b23.w)};
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
-                    const float2 v = cmulf(bt[(4 * c + t) * BM + r], sj[4 * cc + t]);
+                    // rows past the grid hold stale B data; their s factors are
+                    // zero and their output rows are never stored
+                    const float2 v = cmulf(bv[t], sj[4 * cc + t]);
                     slice3x2(v, ls, lu, w1[t], w2[t], w3[t]);
                 }
                 const uint32_t phys = row_off + ((c ^ swz) << 4);
@@ -889,7 +943,7 @@ sep_x5_kernel(const X5Params xp) {
             tc_fence_after();
             const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
             double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
-            double *ob = p.out + static_cast<int64_t>(b) * p.batch_stride;
+            const int rows = max(0, min(32, rows_valid - 32 * q));
 #pragma unroll
             for (int g = 0; g < L::HC / 32; ++g) {
                 uint32_t v[32];
@@ -907,10 +961,17 @@ sep_x5_kernel(const X5Params xp) {
                 const int gn = n0 + L::HC * h + 32 * g + lane;
                 if (gn < p.ncn) {
                     const int comp = gn / p.nn;
-                    double *oc = ob + comp * p.comp_stride + (gn - comp * p.nn);
-                    const int rows = min(32, p.nm - (m0 + 32 * q));
-                    for (int R = 0; R < rows; ++R)
-                        oc[static_cast<int64_t>(m0 + 32 * q + R) * p.row_stride] = tr[R * 33 + lane];
+                    double *oc = p.out + comp * p.comp_stride + (gn - comp * p.nn);
+                    int64_t rr = r0 + 32 * q;
+                    int bs = static_cast<int>(rr / p.nm), ms = static_cast<int>(rr % p.nm);
+                    for (int R = 0; R < rows; ++R) {
+                        oc[bs * p.batch_stride + static_cast<int64_t>(ms) * p.row_stride] =
+                            tr[R * 33 + lane];
+                        if (++ms == p.nm) {
+                            ms = 0;
+                            ++bs;
+                        }
+                    }
                 }
             }
             __syncwarp();
@@ -1024,15 +1085,15 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int KB = std::max(1, (2 * N + bk - 1) / bk);
     const int k_pad = KB * bk;
     const int ncn = ncomp * nn;
-    const int m_tiles_ = (nm + BM - 1) / BM;
-    // x5 stores the B table as whole 128-row tiles
-    const int nm_ld = x5 ? m_tiles_ * BM : (nm + 15) / 16 * 16;
+    const int nm_ld = x5 ? nm : (nm + 15) / 16 * 16;
     // x5 tile width: 256 columns, or 192 where that pads the columns less
     // (e.g. three 192-point components: 576 columns in 3 tiles, not 768)
     const int bnx = (x5 && (ncn + 191) / 192 * 192 < (ncn + 255) / 256 * 256) ? 192 : BN;
     const int n_tiles = (ncn + bnx - 1) / bnx;
     const int ncn_pad = n_tiles * bnx;
-    const int m_tiles = (nm + BM - 1) / BM;
+    // x5 tiles the nb * nm (slice, row) pairs as one row range
+    const int64_t rows_total = static_cast<int64_t>(nb) * nm;
+    const int m_tiles = x5 ? static_cast<int>((rows_total + BM - 1) / BM) : (nm + BM - 1) / BM;
 
     // scratch: normaliser, svec, btab, G hi (G1), G lo (G2)
     const size_t off_wn = 0;
@@ -1115,13 +1176,14 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.kb_total = KB;
     p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : (x5 ? X5_CHUNK : 4);
     p.m_tiles = m_tiles;
+    p.rows_total = rows_total;
     p.n_tiles = n_tiles;
     p.out = a.out;
     p.comp_stride = P;
     p.batch_stride = static_cast<int64_t>(nm) * nn;
     p.row_stride = nn;
     p.status = status;
-    const int64_t grid = static_cast<int64_t>(nb) * m_tiles * n_tiles;
+    const int64_t grid = static_cast<int64_t>(x5 ? 1 : nb) * m_tiles * n_tiles;
     if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
     TimedLaunch tl(st);
     if (x5) {
