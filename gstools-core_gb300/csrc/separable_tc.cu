@@ -172,10 +172,9 @@ struct TabArgs {
     int bn;                      // x5 form: G rows per stage block (tile width)
 };
 
-__global__ void sep_svec_kernel(TabArgs t) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= static_cast<int64_t>(t.nb) * t.n_modes) return;
-    const double inv_w = t.wnorm ? static_cast<double>(t.wnorm[1]) : 1.0;
+// s_a[j] = (z1_j - i z2_j) e^{i k_x,j X_a} (3-D) or z1_j - i z2_j (2-D), times
+// inv_w (1 unless the caller normalises here)
+__device__ __forceinline__ void svec_entry(const TabArgs &t, int64_t i, double inv_w) {
     const int b = static_cast<int>(i / t.n_modes), j = static_cast<int>(i % t.n_modes);
     float2 w = make_float2(static_cast<float>(t.z1[j] * inv_w), static_cast<float>(-t.z2[j] * inv_w));
     if (t.dim == 3) {
@@ -188,6 +187,12 @@ __global__ void sep_svec_kernel(TabArgs t) {
     t.svec[i] = w;
 }
 
+__global__ void sep_svec_kernel(TabArgs t) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<int64_t>(t.nb) * t.n_modes) return;
+    svec_entry(t, i, t.wnorm ? static_cast<double>(t.wnorm[1]) : 1.0);
+}
+
 // B table [n_modes][nm_ld], columns nm .. nm_ld-1 zero.  For the x5 form
 // (tiled) the values are stored per k-block of 16 modes as [nm rows][16
 // modes] float2, 128 bytes per row with the row's 16-byte chunk c (modes 2c,
@@ -195,11 +200,7 @@ __global__ void sep_svec_kernel(TabArgs t) {
 // contiguous block that a bulk copy moves into a stage unchanged, and
 // eight consecutive rows read the same logical chunk from eight different
 // bank groups.
-__global__ void sep_btab_kernel(TabArgs t) {
-    // the tiled layout also zero-fills the modes past n_modes of the last k-block
-    const int64_t nj = t.tiled ? static_cast<int64_t>(t.kbt) * 16 : t.n_modes;
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= nj * t.nm_ld) return;
+__device__ __forceinline__ void btab_entry(const TabArgs &t, int64_t i) {
     int j, m;
     if (t.tiled) {   // i walks the stored layout, so the stores are contiguous
         const int e = static_cast<int>(i & 15);
@@ -215,6 +216,14 @@ __global__ void sep_btab_kernel(TabArgs t) {
                          ? cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m])
                          : make_float2(0.f, 0.f);
     t.btab[i] = v;
+}
+
+__global__ void sep_btab_kernel(TabArgs t) {
+    // the tiled layout also zero-fills the modes past n_modes of the last k-block
+    const int64_t nj = t.tiled ? static_cast<int64_t>(t.kbt) * 16 : t.n_modes;
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nj * t.nm_ld) return;
+    btab_entry(t, i);
 }
 
 template <bool BF16>
@@ -517,14 +526,17 @@ static_assert(4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS) <= X5_THREADS * X5_LAUN
 constexpr float kUnit = 32768.0f;            // 2^15
 constexpr int kLeadBitsG = 11;               // G1 grid: 2^15 * rint(G * 2^10) / 2^10
 
-// Normaliser and leading-grid width of the x5 form, written to wnorm[0..3]:
-//   W = 2^e >= max |z1 - i z2|  (so s / W is exact and |F| <= 1),
-//   the leading F grid 2^(bF-1) with bF chosen so that the expected extreme
-//   of the exact main sum, about 6 * sqrt(sum |w|^2 / 2) / W * 2^(bF+bG-2)
-//   counts (6 standard deviations of the field), stays below 2^23 counts
-//   with bG = 11: one bit of headroom under FP32's 2^24.
-__global__ void sep_wnorm_kernel(const double *__restrict__ z1, const double *__restrict__ z2,
-                                 int n, float *__restrict__ wnorm) {
+// Normaliser and leading-grid width of the x5 form, one block of 256 threads:
+//   W = 2^e >= max |z1 - i z2|  (so |s / W| <= 1 and |F| <= 1),
+//   the leading F grid 2^(bF-1) with bF (3..9) chosen so that the expected
+//   extreme of the exact main sum, about 6 * sqrt(sum |w|^2 / 2) / W *
+//   2^(bF+bG-2) counts (6 standard deviations of the field), stays below
+//   2^23 counts with bG = 11: one bit of headroom under FP32's 2^24.
+// The s vector is stored unnormalised; the slicing constants absorb 1/W (a
+// power of two, so the slices are those of s / W bit for bit):
+//   wnorm = {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W}
+__device__ void wnorm_block(const double *__restrict__ z1, const double *__restrict__ z2, int n,
+                            float *__restrict__ wnorm) {
     __shared__ double red_max[256], red_sum[256];
     double m = 0.0, sum = 0.0;
     for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -553,49 +565,101 @@ __global__ void sep_wnorm_kernel(const double *__restrict__ z1, const double *__
         bf = bf < 3 ? 3 : (bf > 9 ? 9 : bf);
         wnorm[0] = static_cast<float>(W);
         wnorm[1] = static_cast<float>(1.0 / W);
-        wnorm[2] = ldexpf(1.0f, bf - 1);                        // lead_scale
-        wnorm[3] = kUnit / ldexpf(1.0f, bf - 1);                // lead_unit
+        wnorm[2] = static_cast<float>(ldexp(1.0, bf - 1) / W);      // lead scale of s
+        wnorm[3] = kUnit / ldexpf(1.0f, bf - 1);                     // lead unit
+        wnorm[4] = static_cast<float>(kUnit / W);                    // slice unit of s
     }
 }
 
-__global__ void sep_gtab_x5_kernel(TabArgs t) {
+// G table of the x5 form.  Element (component c, rows 8g .. 8g+7 of the
+// column axis, mode j): the projector weight is formed once for the 8 rows.
+// G1 on the 11-bit integer grid (units of 2^15 / 2^10 = 32), G2 the f16 rest;
+// stored as contiguous stage blocks, one per (tile of t.bn rows, k-block of
+// 16 modes), already in the 64-byte-swizzled K-major layout the MMA reads:
+// row r at r * 64 bytes, 16-byte chunk c at c ^ ((r >> 1) & 3).
+constexpr int kGtabRows = 8;
+// groups of kGtabRows rows: ncomp * ceil(nn / 8) real ones, then the zero
+// padding rows [ncomp * nn, ncn_pad)
+__host__ __device__ __forceinline__ int64_t gtab_x5_groups(int ncomp, int nn, int ncn_pad) {
+    const int64_t real = static_cast<int64_t>(ncomp) * ((nn + kGtabRows - 1) / kGtabRows);
+    const int64_t pad = (ncn_pad - static_cast<int64_t>(ncomp) * nn + kGtabRows - 1) / kGtabRows;
+    return real + (pad > 0 ? pad : 0);
+}
+__device__ __forceinline__ void gtab_x5_entry(const TabArgs &t, int64_t i) {
     const int half_k = t.k_pad / 2;
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= static_cast<int64_t>(t.ncn_pad) * half_k) return;
-    const int row = static_cast<int>(i / half_k), j = static_cast<int>(i % half_k);
-    float re = 0.f, im = 0.f;
-    if (row < t.ncomp * t.nn && j < t.n_modes) {
-        const int c = row / t.nn, n = row - c * t.nn;
-        const float2 e = cis_f32(t.cov[t.kn_dim * t.n_modes + j] * t.ax_n[n]);
-        double pw = 1.0;
-        if (t.incompr) {
-            double kk = 0.0;
-            for (int d = 0; d < t.dim; ++d) {
-                const double kd = t.cov[d * t.n_modes + j];
-                kk = __dadd_rn(kk, __dmul_rn(kd, kd));
-            }
-            const double k0 = t.cov[j];
-            const double k_2 = __ddiv_rn(k0, kk);
-            pw = (c == 0) ? __dadd_rn(1.0, -__dmul_rn(k0, k_2))
-                          : -__dmul_rn(t.cov[c * t.n_modes + j], k_2);
-        }
-        re = static_cast<float>(pw * e.x);
-        im = static_cast<float>(-(pw * e.y));
+    const int ngrp = (t.nn + kGtabRows - 1) / kGtabRows;
+    const int j = static_cast<int>(i % half_k);
+    const int64_t gg = i / half_k;
+    const int64_t nreal = static_cast<int64_t>(t.ncomp) * ngrp;
+    int c, row0, nrows;
+    if (gg < nreal) {
+        c = static_cast<int>(gg / ngrp);
+        const int n0 = static_cast<int>(gg % ngrp) * kGtabRows;
+        row0 = c * t.nn + n0;
+        nrows = min(kGtabRows, t.nn - n0);
+    } else {
+        c = t.ncomp;                                        // padding: zeros
+        row0 = t.ncomp * t.nn + static_cast<int>(gg - nreal) * kGtabRows;
+        nrows = min(kGtabRows, t.ncn_pad - row0);
     }
-    // G1 on the 11-bit integer grid (units of 2^15 / 2^10 = 32), G2 the f16 rest
+    const bool live = c < t.ncomp && j < t.n_modes;
+    double pw = 1.0;
+    if (live && t.incompr) {
+        // projector weight, as the reference forms it (src/field.rs:138-152)
+        double kk = 0.0;
+        for (int d = 0; d < t.dim; ++d) {
+            const double kd = t.cov[d * t.n_modes + j];
+            kk = __dadd_rn(kk, __dmul_rn(kd, kd));
+        }
+        const double k0 = t.cov[j];
+        const double k_2 = __ddiv_rn(k0, kk);
+        pw = (c == 0) ? __dadd_rn(1.0, -__dmul_rn(k0, k_2))
+                      : -__dmul_rn(t.cov[c * t.n_modes + j], k_2);
+    }
+    const double kn = live ? t.cov[t.kn_dim * t.n_modes + j] : 0.0;
     const float gs = static_cast<float>(1 << (kLeadBitsG - 1)), gu = kUnit / gs;
-    const float g1r = rintf(re * gs) * gu, g1i = rintf(im * gs) * gu;
-    const __half2 h1 = __floats2half2_rn(g1r, g1i);
-    const __half2 h2 = __floats2half2_rn(re * kUnit - g1r, im * kUnit - g1i);
-    // Stored as contiguous 16 KB stage blocks, one per (256-row tile, k-block
-    // of 16 modes), already in the 64-byte-swizzled K-major layout the MMA
-    // reads: row r at r * 64 bytes, 16-byte chunk c at c ^ ((r >> 1) & 3).
-    const int nt = row / t.bn, r = row % t.bn, kb = j / 16, jl = j % 16;
-    const int64_t blk = (static_cast<int64_t>(nt) * t.kbt + kb) * (t.bn * 64);
-    const int off = r * 64 + (((jl >> 2) ^ ((r >> 1) & 3)) << 4) + (jl & 3) * 4;
-    const int64_t w = (blk + off) / 4;
-    t.ghi[w] = *reinterpret_cast<const uint32_t *>(&h1);
-    t.glo[w] = *reinterpret_cast<const uint32_t *>(&h2);
+    const int kb = j / 16, jl = j % 16;
+    for (int u = 0; u < nrows; ++u) {
+        const int row = row0 + u;
+        float re = 0.f, im = 0.f;
+        if (live) {
+            const float2 e = cis_f32(kn * t.ax_n[row - c * t.nn]);
+            re = static_cast<float>(pw * e.x);
+            im = static_cast<float>(-(pw * e.y));
+        }
+        const float g1r = rintf(re * gs) * gu, g1i = rintf(im * gs) * gu;
+        const __half2 h1 = __floats2half2_rn(g1r, g1i);
+        const __half2 h2 = __floats2half2_rn(re * kUnit - g1r, im * kUnit - g1i);
+        const int nt = row / t.bn, r = row % t.bn;
+        const int64_t blk = (static_cast<int64_t>(nt) * t.kbt + kb) * (t.bn * 64);
+        const int off = r * 64 + (((jl >> 2) ^ ((r >> 1) & 3)) << 4) + (jl & 3) * 4;
+        const int64_t w = (blk + off) / 4;
+        t.ghi[w] = *reinterpret_cast<const uint32_t *>(&h1);
+        t.glo[w] = *reinterpret_cast<const uint32_t *>(&h2);
+    }
+}
+
+// All tables of the x5 form in one launch: block 0 the normaliser, then
+// blocks of s-vector, B-table and G-table elements.
+__global__ void __launch_bounds__(256)
+sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) {
+    if (blockIdx.x == 0) {
+        wnorm_block(t.z1, t.z2, t.n_modes, t.wnorm);
+        return;
+    }
+    int64_t i = static_cast<int64_t>(blockIdx.x - 1) * 256 + threadIdx.x;
+    const int64_t b_svec = (n_svec + 255) / 256 * 256, b_btab = (n_btab + 255) / 256 * 256;
+    if (i < b_svec) {
+        if (i < n_svec) svec_entry(t, i, 1.0);
+        return;
+    }
+    i -= b_svec;
+    if (i < b_btab) {
+        if (i < n_btab) btab_entry(t, i);
+        return;
+    }
+    i -= b_btab;
+    if (i < n_gtab) gtab_x5_entry(t, i);
 }
 
 struct X5Params {
@@ -641,11 +705,12 @@ struct X5Layout {
 };
 constexpr int kTmaWarpX5 = 8, kMmaWarpX5 = 9;
 
-// three slices of a (re, im) pair in units of 2^15, packed as half2
-__device__ __forceinline__ void slice3x2(float2 v, float ls, float lu, uint32_t &w1, uint32_t &w2,
-                                         uint32_t &w3) {
+// three slices of a (re, im) pair in units of 2^15 (of v * ku / 2^15: the
+// scales absorb the normaliser), packed as half2
+__device__ __forceinline__ void slice3x2(float2 v, float ls, float lu, float ku, uint32_t &w1,
+                                         uint32_t &w2, uint32_t &w3) {
     const float s1x = rintf(v.x * ls) * lu, s1y = rintf(v.y * ls) * lu;
-    const float rx = fmaf(v.x, kUnit, -s1x), ry = fmaf(v.y, kUnit, -s1y);   // exact
+    const float rx = fmaf(v.x, ku, -s1x), ry = fmaf(v.y, ku, -s1y);   // exact
     const __half2 h1 = __floats2half2_rn(s1x, s1y);
     const __half2 h2 = __floats2half2_rn(rx, ry);
     const float2 b2 = __half22float2(h2);
@@ -826,7 +891,7 @@ sep_x5_kernel(const X5Params xp) {
                                   ((4 * h + 2) ^ bswz) << 4, ((4 * h + 3) ^ bswz) << 4};
         const uint32_t row_off = r * 64;                        // 64-byte rows
         const uint32_t swz = (r >> 1) & 3;                      // 64-byte swizzle phase
-        const float ls = xp.wnorm[2], lu = xp.wnorm[3];
+        const float ls = xp.wnorm[2], lu = xp.wnorm[3], ku = xp.wnorm[4];
         float tot[L::HC];
 #pragma unroll
         for (int i = 0; i < L::HC; ++i) tot[i] = 0.f;
@@ -914,7 +979,7 @@ sep_x5_kernel(const X5Params xp) {
                     // rows past the grid hold stale B data; their s factors are
                     // zero and their output rows are never stored
                     const float2 v = cmulf(bv[t], sj[4 * cc + t]);
-                    slice3x2(v, ls, lu, w1[t], w2[t], w3[t]);
+                    slice3x2(v, ls, lu, ku, w1[t], w2[t], w3[t]);
                 }
                 const uint32_t phys = row_off + ((c ^ swz) << 4);
                 *reinterpret_cast<uint4 *>(st + phys) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
@@ -1141,17 +1206,21 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     {
         TimedLaunch tl(st);
         tl.begin(K_SEP_TABLES);
-        if (x5) sep_wnorm_kernel<<<1, 256, 0, st>>>(a.z1, a.z2, N, t.wnorm);
         const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(bt_modes) * nm_ld;
         const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
-        if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
-        if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
-        if (x5)
-            sep_gtab_x5_kernel<<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
-        else if (bf16)
-            sep_gtab_kernel<true><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
-        else
-            sep_gtab_kernel<false><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+        if (x5) {
+            const int64_t ng = gtab_x5_groups(ncomp, nn, ncn_pad) * (k_pad / 2);
+            const int64_t blocks = 1 + (n1 + 255) / 256 + (n2 + 255) / 256 + (ng + 255) / 256;
+            if (blocks > 0x7fffffff) return set_error(GSC_ERR_INVALID, "tables too large");
+            sep_x5_tables_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(t, n1, n2, ng);
+        } else {
+            if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
+            if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
+            if (bf16)
+                sep_gtab_kernel<true><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+            else
+                sep_gtab_kernel<false><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+        }
         tl.end();
         GSC_CUDA(cudaGetLastError());
     }
