@@ -40,6 +40,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "internal.h"
@@ -520,9 +521,6 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 // ---------------------------------------------------------------------------
 constexpr int X5_THREADS = 384;                 // 8 worker warps + 4 control warps
 constexpr int X5_LAUNCH_REGS = 168;             // 65536 / 384, rounded down to 8
-constexpr int X5_WORK_REGS = 216, X5_CTRL_REGS = 48;
-static_assert(4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS) <= X5_THREADS * X5_LAUNCH_REGS,
-              "setmaxnreg split exceeds the registers the block is launched with");
 constexpr float kUnit = 32768.0f;            // 2^15
 constexpr int kLeadBitsG = 11;               // G1 grid: 2^15 * rint(G * 2^10) / 2^10
 
@@ -664,8 +662,15 @@ sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) 
 
 struct X5Params {
     TcParams base;
-    const float *wnorm;      // {W, 1/W, 2^(bF-1), 2^15 / 2^(bF-1)}
+    const float *wnorm;      // {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W}
     const unsigned char *g1, *g2, *bt;   // stage blocks (see the table kernels)
+    // Tail split: tiles [0, full_tiles) run whole, one per CTA; each later
+    // tile runs as ksplit CTAs over consecutive parts of its k-blocks, whose
+    // FP32 partials meet in `ws` ([slot][part][column][row]); the last part
+    // to finish (counted in ws_cnt[slot]) adds them in part order and stores.
+    int full_tiles, ksplit;
+    float *ws;
+    int *ws_cnt;
 };
 
 // Pipeline of the x5 kernel: k-blocks of 32 K elements (16 modes), three
@@ -686,6 +691,7 @@ constexpr int X5_STAGES = 3;
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
 constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
+constexpr int kMaxSplit = 4;                         // most parts a tail tile is split into
 
 // Stage layout for tiles of BNX output columns (256, or 192 where that pads
 // the columns less, e.g. 3 x 192 components): every operand starts on a
@@ -699,6 +705,12 @@ struct X5Layout {
     static constexpr int STAGE = OFF_BT + X5_BT_BYTES;   // 72 KB / 64 KB
     static constexpr size_t SMEM = X5_STAGES * STAGE + 1024 + 256;
     static constexpr int HC = BNX / 2;                   // columns per worker half
+    // setmaxnreg split: workers hold HC FP32 totals; the narrower tile leaves
+    // the control warps room (chosen where ptxas reports no spills)
+    static constexpr int WORK_REGS = BNX == 256 ? 216 : 200;
+    static constexpr int CTRL_REGS = BNX == 256 ? 48 : 80;
+    static_assert(4 * 32 * (2 * WORK_REGS + CTRL_REGS) <= X5_THREADS * X5_LAUNCH_REGS,
+                  "setmaxnreg split exceeds the registers the block is launched with");
     static_assert(OFF_G2 % 1024 == 0 && OFF_BT % 1024 == 0 && STAGE % 1024 == 0,
                   "stage operands must be 1024-byte aligned");
     static_assert(HC % 32 == 0 && BNX % 16 == 0 && BNX <= 256, "tile width");
@@ -720,7 +732,7 @@ __device__ __forceinline__ void slice3x2(float2 v, float ls, float lu, float ku,
     w3 = *reinterpret_cast<const uint32_t *>(&h3);
 }
 
-template <int BNX>
+template <int BNX, bool SPLIT>
 __global__ void __launch_bounds__(X5_THREADS, 1)
 sep_x5_kernel(const X5Params xp) {
     using L = X5Layout<BNX>;
@@ -737,22 +749,31 @@ sep_x5_kernel(const X5Params xp) {
     uint64_t *drain = bars + 11;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 12);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    volatile int *last_part = reinterpret_cast<volatile int *>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Rows are the nb * nm (x-slice, y) pairs taken in order, so a 128-row
     // tile may span two or more slices and no slice pads a partial tile.
-    const int nt = blockIdx.x % p.n_tiles;
-    const int64_t r0 = static_cast<int64_t>(blockIdx.x / p.n_tiles) * BM;
+    // a launch without split tiles compiles the split path out
+    const int u = static_cast<int>(blockIdx.x) - xp.full_tiles;
+    const bool split = SPLIT && u >= 0;
+    const int tile = split ? xp.full_tiles + u / xp.ksplit : static_cast<int>(blockIdx.x);
+    const int part = split ? u % xp.ksplit : 0;
+    const int kbeg = split ? static_cast<int>(static_cast<int64_t>(part) * p.kb_total / xp.ksplit) : 0;
+    const int KB = split ? static_cast<int>(static_cast<int64_t>(part + 1) * p.kb_total / xp.ksplit) - kbeg
+                         : p.kb_total;          // k-blocks of this CTA
+    const int nt = tile % p.n_tiles;
+    const int64_t r0 = static_cast<int64_t>(tile / p.n_tiles) * BM;
     const int n0 = nt * BNX;
     const int rows_valid = static_cast<int>(min(static_cast<int64_t>(BM), p.rows_total - r0));
-    const int KB = p.kb_total, KC = p.kc;
+    const int KC = p.kc;
     const int NC = (KB + KC - 1) / KC;
     // Every tile walks the k-blocks from its own starting point, so the
     // CTAs of a wave do not all fetch the same table blocks at the same
     // moment; the sums do not depend on the order (the main sum is exact,
     // the rest is drained in chunks).
     const int rot = static_cast<int>((static_cast<int64_t>(blockIdx.x) * 97) % KB);
-    auto kb_of = [&](int i) { const int t = i + rot; return t >= KB ? t - KB : t; };
+    auto kb_of = [&](int i) { const int t = i + rot; return kbeg + (t >= KB ? t - KB : t); };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < X5_STAGES; ++s) {
@@ -777,7 +798,7 @@ sep_x5_kernel(const X5Params xp) {
     const uint32_t t_main = tmem, t_cross = tmem + 256;
 
     if (warp >= 8) {
-        regs_dec<X5_CTRL_REGS>();
+        regs_dec<L::CTRL_REGS>();
         if (warp == kTmaWarpX5 && lane == 0) {
             // ---- bulk copies: G1, G2, B-table block ----------------------------
             // the tile's runs of consecutive y rows (a run ends where the tile
@@ -804,7 +825,7 @@ sep_x5_kernel(const X5Params xp) {
                                         kErrTimeoutEmpty))
                     break;
                 unsigned char *st = smem + s * L::STAGE;
-                const int64_t gblk = (static_cast<int64_t>(nt) * KB + kb) * L::G_BYTES;
+                const int64_t gblk = (static_cast<int64_t>(nt) * p.kb_total + kb) * L::G_BYTES;
                 mbar_arrive_expect_tx(&full_t[s], 2 * L::G_BYTES + rows_valid * 128);
                 bulk_copy_g2s(st + L::OFF_G1, xp.g1 + gblk, L::G_BYTES, &full_t[s]);
                 bulk_copy_g2s(st + L::OFF_G2, xp.g2 + gblk, L::G_BYTES, &full_t[s]);
@@ -875,7 +896,7 @@ sep_x5_kernel(const X5Params xp) {
             }
         }
     } else {
-        regs_inc<X5_WORK_REGS>();
+        regs_inc<L::WORK_REGS>();
         // ---- workers: F-tile slices, cross drains, final epilogue -----------------
         const int q = warp & 3, h = warp >> 2;
         const int r = 32 * q + lane;                            // F row and TMEM lane
@@ -1000,17 +1021,56 @@ sep_x5_kernel(const X5Params xp) {
             if (ok) drain_chunk();
         }
         if (ok) ok = wait_chunk(NC - 1);
-        if (ok) {
-            // Every MMA has completed, so the stage buffers are free: each
-            // warp turns its 32 rows x 32 columns blocks around in shared
-            // memory (pitch 33 doubles) and stores them row by row, 256
-            // contiguous bytes per instruction.
-            tc_fence_after();
+        if (!split) {
+            if (ok) {
+                // Every MMA has completed, so the stage buffers are free: each
+                // warp turns its 32 rows x 32 columns blocks around in shared
+                // memory (pitch 33 doubles) and stores them row by row, 256
+                // contiguous bytes per instruction.
+                tc_fence_after();
+                const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
+                double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
+                const int rows = max(0, min(32, rows_valid - 32 * q));
+#pragma unroll
+                for (int g = 0; g < L::HC / 32; ++g) {
+                    uint32_t v[32];
+                    __syncwarp();
+                    tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
+                    tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int t = 0; t < 32; ++t)
+                        tr[lane * 33 + t] = f32_to_f64((__uint_as_float(v[t]) + tot[32 * g + t]) * unscale);
+                    __syncwarp();
+                    const int gn = n0 + L::HC * h + 32 * g + lane;
+                    if (gn < p.ncn) {
+                        const int comp = gn / p.nn;
+                        double *oc = p.out + comp * p.comp_stride + (gn - comp * p.nn);
+                        int64_t rr = r0 + 32 * q;
+                        int bs = static_cast<int>(rr / p.nm), ms = static_cast<int>(rr % p.nm);
+                        for (int R = 0; R < rows; ++R) {
+                            oc[bs * p.batch_stride + static_cast<int64_t>(ms) * p.row_stride] =
+                                tr[R * 33 + lane];
+                            if (++ms == p.nm) {
+                                ms = 0;
+                                ++bs;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        } else if (SPLIT) {
+            // a split tile: write this part's sums, count the parts, and the
+            // last part adds all of them in part order (the result does not
+            // depend on which part finishes last), then stores as above
             const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
             double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
             const int rows = max(0, min(32, rows_valid - 32 * q));
-#pragma unroll
-            for (int g = 0; g < L::HC / 32; ++g) {
+            auto read_group = [&](int g) {
                 uint32_t v[32];
                 __syncwarp();
                 tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
@@ -1020,8 +1080,12 @@ sep_x5_kernel(const X5Params xp) {
                 tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
                 tmem_ld_wait();
 #pragma unroll
-                for (int t = 0; t < 32; ++t)
-                    tr[lane * 33 + t] = f32_to_f64((__uint_as_float(v[t]) + tot[32 * g + t]) * unscale);
+                for (int t = 0; t < 32; ++t) tot[32 * g + t] = __uint_as_float(v[t]) + tot[32 * g + t];
+            };
+            auto store_group = [&](int g) {
+                __syncwarp();
+#pragma unroll
+                for (int t = 0; t < 32; ++t) tr[lane * 33 + t] = f32_to_f64(tot[32 * g + t] * unscale);
                 __syncwarp();
                 const int gn = n0 + L::HC * h + 32 * g + lane;
                 if (gn < p.ncn) {
@@ -1038,8 +1102,43 @@ sep_x5_kernel(const X5Params xp) {
                         }
                     }
                 }
+            };
+            if (ok) {
+                tc_fence_after();
+#pragma unroll
+                for (int g = 0; g < L::HC / 32; ++g) read_group(g);
             }
-            __syncwarp();
+            const int slot = tile - xp.full_tiles, ks = xp.ksplit;
+            float *wsl = xp.ws + static_cast<int64_t>(slot) * ks * BNX * BM;
+            // this thread's column c of part k sits at col0[(k * BNX + c) * BM]
+            float *col0 = wsl + static_cast<int64_t>(L::HC * h) * BM + r;
+            if (ok) {
+                float *wp = col0 + static_cast<int64_t>(part) * BNX * BM;
+#pragma unroll
+                for (int c = 0; c < L::HC; ++c) wp[c * BM] = tot[c];
+            }
+            __threadfence();
+            asm volatile("bar.sync 1, 256;" ::: "memory");      // the 256 worker threads
+            if (threadIdx.x == 0)
+                *last_part = (!*abort_flag && atomicAdd(xp.ws_cnt + slot, 1) == ks - 1) ? 1 : 0;
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            if (ok && *last_part) {
+                __threadfence();
+                if (threadIdx.x == 0) xp.ws_cnt[slot] = 0;          // ready for the next launch
+                // every part (this one included) is read back from the
+                // workspace, so the sums need no second register array
+#pragma unroll
+                for (int c = 0; c < L::HC; ++c) {
+                    float a = __ldcg(col0 + c * BM);
+#pragma unroll
+                    for (int k = 1; k < kMaxSplit; ++k)
+                        if (k < ks) a += __ldcg(col0 + (k * BNX + c) * BM);
+                    tot[c] = a;
+                }
+#pragma unroll
+                for (int g = 0; g < L::HC / 32; ++g) store_group(g);
+                __syncwarp();
+            }
         }
     }
 
@@ -1112,22 +1211,23 @@ namespace {
 // registers with setmaxnreg; the increases can only be served from what the
 // block was launched with, so a build that launches with fewer registers
 // must not run.
-template <int BNX>
+template <int BNX, bool SPLIT>
 int configure_x5() {
     static std::once_flag once;
     static int rc = GSC_OK;
     std::call_once(once, [] {
         cudaFuncAttributes fa{};
-        cudaError_t e = cudaFuncGetAttributes(&fa, sep_x5_kernel<BNX>);
+        cudaError_t e = cudaFuncGetAttributes(&fa, sep_x5_kernel<BNX, SPLIT>);
         if (e != cudaSuccess) {
             rc = cuda_fail(e, "cudaFuncGetAttributes (x5)");
             return;
         }
-        if (fa.numRegs * X5_THREADS < 4 * 32 * (2 * X5_WORK_REGS + X5_CTRL_REGS)) {
+        if (fa.numRegs * X5_THREADS <
+            4 * 32 * (2 * X5Layout<BNX>::WORK_REGS + X5Layout<BNX>::CTRL_REGS)) {
             rc = set_error(GSC_ERR_KERNEL, "x5 kernel built with too few registers per thread");
             return;
         }
-        e = cudaFuncSetAttribute(sep_x5_kernel<BNX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(sep_x5_kernel<BNX, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(X5Layout<BNX>::SMEM));
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaFuncSetAttribute (x5)");
     });
@@ -1160,7 +1260,35 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int64_t rows_total = static_cast<int64_t>(nb) * nm;
     const int m_tiles = x5 ? static_cast<int>((rows_total + BM - 1) / BM) : (nm + BM - 1) / BM;
 
-    // scratch: normaliser, svec, btab, G hi (G1), G lo (G2)
+    // x5 tail split: the tiles of an incomplete last wave run as ksplit CTAs
+    // each over a share of the k-blocks, when that shortens the schedule
+    const int64_t tiles = static_cast<int64_t>(m_tiles) * n_tiles;
+    int64_t full_tiles = tiles, n_split = 0;
+    int ksplit = 1;
+    if (x5) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device) != cudaSuccess ||
+            sms <= 0) {
+            cudaGetLastError();
+            sms = 152;
+        }
+        const int64_t waves = tiles / sms, rem = tiles % sms;
+        double best = static_cast<double>(waves + (rem > 0 ? 1 : 0));
+        for (int k = 2; k <= kMaxSplit && rem > 0 && KB / k >= 8; ++k) {
+            // a part costs 1/k of a tile plus ~5 % for its partial traffic
+            const double span = waves + std::ceil(static_cast<double>(rem * k) / sms) / k * 1.05;
+            if (span < best - 1e-9) {
+                best = span;
+                ksplit = k;
+            }
+        }
+        if (ksplit > 1) {
+            full_tiles = tiles - rem;
+            n_split = rem;
+        }
+    }
+
+    // scratch: normaliser, svec, btab, G hi (G1), G lo (G2), split partials
     const size_t off_wn = 0;
     const size_t off_svec = 1024;
     const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(N), 1024);
@@ -1168,7 +1296,10 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const size_t off_ghi = align_up(off_btab + sizeof(float2) * bt_modes * nm_ld, 1024);
     const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
     const size_t off_glo = align_up(off_ghi + g_bytes, 1024);
-    const size_t total = off_glo + g_bytes;
+    const size_t off_ws = align_up(off_glo + g_bytes, 1024);
+    const size_t ws_bytes = static_cast<size_t>(n_split) * ksplit * bnx * BM * sizeof(float);
+    const size_t off_cnt = align_up(off_ws + ws_bytes, 1024);
+    const size_t total = off_cnt + static_cast<size_t>(n_split) * sizeof(int) + 256;
     GSC_TRY(ensure_dev(ctx, ctx.scratch, total));
     GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
     unsigned char *base = static_cast<unsigned char *>(ctx.scratch.ptr);
@@ -1252,7 +1383,8 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.batch_stride = static_cast<int64_t>(nm) * nn;
     p.row_stride = nn;
     p.status = status;
-    const int64_t grid = static_cast<int64_t>(x5 ? 1 : nb) * m_tiles * n_tiles;
+    const int64_t grid = x5 ? full_tiles + n_split * ksplit
+                            : static_cast<int64_t>(nb) * m_tiles * n_tiles;
     if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
     TimedLaunch tl(st);
     if (x5) {
@@ -1262,13 +1394,26 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         xp.g1 = reinterpret_cast<const unsigned char *>(t.ghi);
         xp.g2 = reinterpret_cast<const unsigned char *>(t.glo);
         xp.bt = reinterpret_cast<const unsigned char *>(t.btab);
+        xp.full_tiles = static_cast<int>(full_tiles);
+        xp.ksplit = ksplit;
+        xp.ws = reinterpret_cast<float *>(base + off_ws);
+        xp.ws_cnt = reinterpret_cast<int *>(base + off_cnt);
+        if (n_split > 0)
+            GSC_CUDA(cudaMemsetAsync(xp.ws_cnt, 0, static_cast<size_t>(n_split) * sizeof(int), st));
         tl.begin(K_SEP_TC_F16X5);
-        if (bnx == 192) {
-            GSC_TRY(configure_x5<192>());
-            sep_x5_kernel<192><<<static_cast<unsigned>(grid), X5_THREADS, X5Layout<192>::SMEM, st>>>(xp);
+        const unsigned g = static_cast<unsigned>(grid);
+        if (bnx == 192 && n_split > 0) {
+            GSC_TRY((configure_x5<192, true>()));
+            sep_x5_kernel<192, true><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(xp);
+        } else if (bnx == 192) {
+            GSC_TRY((configure_x5<192, false>()));
+            sep_x5_kernel<192, false><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(xp);
+        } else if (n_split > 0) {
+            GSC_TRY((configure_x5<256, true>()));
+            sep_x5_kernel<256, true><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(xp);
         } else {
-            GSC_TRY(configure_x5<256>());
-            sep_x5_kernel<256><<<static_cast<unsigned>(grid), X5_THREADS, X5Layout<256>::SMEM, st>>>(xp);
+            GSC_TRY((configure_x5<256, false>()));
+            sep_x5_kernel<256, false><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(xp);
         }
     } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
