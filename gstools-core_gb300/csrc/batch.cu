@@ -529,6 +529,8 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
             }
         }
         if (!hit) {
+            // the tuner reads the inputs: let pending work on them finish
+            GSC_CUDA(cudaDeviceSynchronize());
             timing_reset(false);
             GSC_TRY(autotune(*b, b->cap_stream));
             GSC_CUDA(cudaStreamSynchronize(b->cap_stream));

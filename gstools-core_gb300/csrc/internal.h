@@ -53,6 +53,7 @@ enum KernelId : int32_t {
     K_BATCH_TABLES = 17,   // per-mode tables of every item of a batch
     K_BATCH_PLAIN = 18,    // persistent FP64 batch kernel (device work queue)
     K_BATCH_MIXED = 19,    // persistent mixed-precision batch kernel
+    K_SAMPLE_MODES = 20,   // on-device spectral sampling (Philox4x32-10)
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -76,6 +77,10 @@ struct DeviceCtx {
     size_t pinned_bytes = 0;
     DevBuf grid;                     // expanded meshgrid for plain forms on grids
     DevBuf zscaled;                  // spectrum-scaled z1, z2 of device-pointer Fourier calls
+    DevBuf sampling;                 // item table of on-device sampling calls
+    void *sampling_pinned = nullptr; // its pinned staging, reused once its copy is done
+    size_t sampling_pinned_bytes = 0;
+    cudaEvent_t sampling_ev = nullptr;
     int *status = nullptr;           // sticky kernel status word (device)
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};   // pipelined device-to-host staging
     gsc_batch *batch = nullptr;      // plan of the last host-pointer batch call

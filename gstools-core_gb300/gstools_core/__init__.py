@@ -38,6 +38,7 @@ __all__ = ["summate", "summate_incompr", "summate_fourier", "summate_device",
            "summate_structured", "summate_incompr_structured", "summate_fourier_structured",
            "summate_structured_device", "summate_incompr_structured_device",
            "summate_fourier_structured_device", "Batch", "summate_batch", "last_batch_config",
+           "sample_modes", "sample_modes_batch_device",
            "device_status",
            "device_count", "last_timings", "GscError", "__version__"]
 
@@ -509,6 +510,52 @@ def last_batch_config(device=-1) -> dict:
     c = _native.make_batch_config()
     _native.check(_native.lib.gsc_last_batch_config(device, ctypes.byref(c)))
     return _config_dict(c)
+
+
+# ---------------------------------------------------------------------------
+# on-device spectral sampling (extension: GSTools draws these on the host)
+# ---------------------------------------------------------------------------
+def _spectrum(name) -> int:
+    if name not in _native.SPECTRA:
+        raise ValueError(f"unknown spectrum {name!r}; choose from {sorted(_native.SPECTRA)}")
+    return _native.SPECTRA[name]
+
+
+def sample_modes(spectrum, dim, n_modes, len_scale, seed, realization=0, *, device=-1):
+    """Draws (cov_samples, z1, z2) for one realization on the GPU.
+
+    spectrum "gaussian": k ~ N(0, 2 / len_scale^2) per component;
+    "exponential": k = g / |n| / len_scale (multivariate Student-t, one
+    degree of freedom).  z1, z2 ~ N(0, 1).  Values depend only on (seed,
+    realization, mode): Philox4x32-10 counters.  Returns host arrays
+    (dim, n_modes), (n_modes,), (n_modes,)."""
+    cov = np.empty((int(dim), int(n_modes)), dtype=np.float64)
+    z1 = np.empty(int(n_modes), dtype=np.float64)
+    z2 = np.empty(int(n_modes), dtype=np.float64)
+    o = _opts("auto", None, False, device)
+    _native.check(_native.lib.gsc_sample_modes_f64(
+        _spectrum(spectrum), int(dim), int(n_modes), float(len_scale), int(seed) & (2**64 - 1),
+        int(realization), cov.ctypes.data, z1.ctypes.data, z2.ctypes.data, ctypes.byref(o)))
+    return cov, z1, z2
+
+
+def sample_modes_batch_device(items, seed, *, stream=None, device=-1, timing=False):
+    """Draws many realizations in one launch into device arrays: each item a
+    dict with "spectrum", "len_scale", "realization" and CUDA arrays "cov"
+    (dim, n_modes), "z1", "z2" (n_modes,).  Does not synchronise."""
+    arr = (_native.GscSampleItem * max(1, len(items)))()
+    for i, it in enumerate(items):
+        shape = it["cov"].__cuda_array_interface__["shape"]
+        if len(shape) != 2:
+            raise TypeError(f"item {i}: cov must be 2-D")
+        dim, n = shape
+        arr[i] = _native.GscSampleItem(
+            _spectrum(it["spectrum"]), dim, n, float(it["len_scale"]), int(it.get("realization", i)),
+            _cuda_view(it["cov"], "cov", (dim, n)), _cuda_view(it["z1"], "z1", (n,)),
+            _cuda_view(it["z2"], "z2", (n,)))
+    o = _opts("auto", None, timing, device, stream)
+    _native.check(_native.lib.gsc_sample_modes_batch_dev(arr, len(items),
+                                                         int(seed) & (2**64 - 1), ctypes.byref(o)))
 
 
 def device_status(device=-1) -> None:

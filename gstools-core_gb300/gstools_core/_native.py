@@ -86,6 +86,20 @@ class GscBatchConfig(ctypes.Structure):
 
 
 BATCH_KINDS = {"scalar": 0, "incompr": 1, "fourier": 2}
+SPECTRA = {"gaussian": 0, "exponential": 1}
+
+
+class GscSampleItem(ctypes.Structure):
+    _fields_ = [
+        ("spectrum", ctypes.c_int32),
+        ("dim", ctypes.c_int32),
+        ("n_modes", ctypes.c_int64),
+        ("len_scale", ctypes.c_double),
+        ("realization", ctypes.c_int64),
+        ("cov", ctypes.c_void_p),
+        ("z1", ctypes.c_void_p),
+        ("z2", ctypes.c_void_p),
+    ]
 
 
 def make_batch_config(points_per_thread=0, tile_modes=0, units_per_block=0) -> GscBatchConfig:
@@ -140,6 +154,12 @@ SIGNATURES = {
     "gsc_summate_batch_f64": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _OPTS,
                                              ctypes.POINTER(GscBatchConfig)]),
     "gsc_last_batch_config": (ctypes.c_int, [_I32, ctypes.POINTER(GscBatchConfig)]),
+    "gsc_sample_modes_batch_dev": (ctypes.c_int, [ctypes.POINTER(GscSampleItem), _I64,
+                                                  ctypes.c_uint64, _OPTS]),
+    "gsc_sample_modes_dev": (ctypes.c_int, [_I32, _I32, _I64, ctypes.c_double, ctypes.c_uint64,
+                                            _I64, _P, _P, _P, _OPTS]),
+    "gsc_sample_modes_f64": (ctypes.c_int, [_I32, _I32, _I64, ctypes.c_double, ctypes.c_uint64,
+                                            _I64, _P, _P, _P, _OPTS]),
 }
 
 

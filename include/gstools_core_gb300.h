@@ -353,6 +353,42 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
  * `device` (-1 = current). */
 int gsc_last_batch_config(int32_t device, gsc_batch_config *config);
 
+/* ---- on-device spectral sampling ---------------------------------------- */
+/* The randomization method's inputs drawn on the GPU: wave vectors
+ * cov (dim, n_modes) from a covariance model's spectral density and the
+ * weights z1, z2 ~ N(0, 1).  No reference counterpart: GSTools draws them on
+ * the host (RandMeth).  Every value is a function of (seed, realization,
+ * mode) only (Philox4x32-10 counters), so realizations and modes can be
+ * drawn in any order or subset with identical results.
+ *   GAUSSIAN     k ~ N(0, 2 / len_scale^2) per component
+ *   EXPONENTIAL  k = g / |n| / len_scale, g ~ N(0, I), n ~ N(0, 1)
+ *                (multivariate Student-t, one degree of freedom) */
+#define GSC_SPECTRUM_GAUSSIAN     0
+#define GSC_SPECTRUM_EXPONENTIAL  1
+
+typedef struct gsc_sample_item {
+    int32_t spectrum;               /* GSC_SPECTRUM_*                        */
+    int32_t dim;                    /* 1, 2, 3                               */
+    int64_t n_modes;
+    double  len_scale;              /* > 0                                   */
+    int64_t realization;            /* counter word: one stream per value    */
+    double *cov, *z1, *z2;          /* device outputs, (dim, n_modes), (n)   */
+} gsc_sample_item;
+
+/* All items in one launch on opts->stream (no synchronisation). */
+int gsc_sample_modes_batch_dev(const gsc_sample_item *items, int64_t count, uint64_t seed,
+                               const gsc_opts *opts);
+
+/* One realization, device outputs. */
+int gsc_sample_modes_dev(int32_t spectrum, int32_t dim, int64_t n_modes, double len_scale,
+                         uint64_t seed, int64_t realization, double *cov, double *z1,
+                         double *z2, const gsc_opts *opts);
+
+/* One realization, host outputs (returns when they are written). */
+int gsc_sample_modes_f64(int32_t spectrum, int32_t dim, int64_t n_modes, double len_scale,
+                         uint64_t seed, int64_t realization, double *cov, double *z1,
+                         double *z2, const gsc_opts *opts);
+
 #ifdef __cplusplus
 }
 #endif
