@@ -238,7 +238,7 @@ int batch_mixed_launch(int R, bool f64phase, int blocks, const BatchItem *items,
                        const double *rec64, cudaStream_t st);
 constexpr int64_t kPlainTableBytesPerMode = 256 * 16;   // W_j[a], a < 256, double2
 constexpr int64_t kPlainRecBytesPerMode = 12 * 8;
-constexpr int64_t kMixedRecBytesPerMode = 12 * 4;
+constexpr int64_t kMixedRecBytesPerMode = 20 * 4;
 constexpr int64_t kMixedRec64BytesPerMode = 4 * 8;
 
 // Fourier method (src/field.rs:219-249): z1s[j] = sf[j] * z1[j],

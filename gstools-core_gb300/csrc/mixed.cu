@@ -41,7 +41,11 @@ constexpr int kMxThreads = 128;
 static_assert(kMxThreads == kBatchThreads, "batch units assume the mixed block size");
 constexpr int kMxR = 4;              // points per thread
 constexpr int kMxTile = 32;          // modes per FP32 accumulation tile
-constexpr int kMxRec = 12;           // floats per mode: kh0 kh1 kh2 kl0 kl1 kl2 z1 z2 w0 w1 w2 -
+// floats per mode: kh0 kh1 kh2 kl0 kl1 kl2 z1 z2 w0 w1 w2 - | (a_q, b_q), q = 0..3:
+// the weights rotated by q quarter turns, z1 cos(t + q pi/2) + z2 sin(t + q pi/2)
+// = a_q cos t + b_q sin t: (z1, z2), (z2, -z1), (-z1, -z2), (-z2, z1)
+constexpr int kMxRec = 20;
+constexpr int kMxRot = 12;           // offset of the rotated pairs
 constexpr int kMxRec64 = 4;          // doubles per mode (FP64-phase variant): kappa0..2, -
 constexpr double kInv2Pi = 0.15915494309189535;   // fl(1 / (2 pi))
 constexpr float kTwoPiF = 6.2831854820251465f;     // fl32(2 pi)
@@ -67,8 +71,17 @@ __device__ __forceinline__ void mixed_mode_entry(const double *__restrict__ cov,
         r64[d] = kap;
     }
     r64[3] = 0.0;
-    r[6] = __double2float_rn(z1j);
-    r[7] = __double2float_rn(z2j);
+    const float z1f = __double2float_rn(z1j), z2f = __double2float_rn(z2j);
+    r[6] = z1f;
+    r[7] = z2f;
+    r[kMxRot + 0] = z1f;
+    r[kMxRot + 1] = z2f;
+    r[kMxRot + 2] = z2f;
+    r[kMxRot + 3] = -z1f;
+    r[kMxRot + 4] = -z1f;
+    r[kMxRot + 5] = -z2f;
+    r[kMxRot + 6] = -z2f;
+    r[kMxRot + 7] = z1f;
     double w0 = 0.0, w1 = 0.0, w2 = 0.0;
     if (incompr) {   // projector as the reference forms it (src/field.rs:138-152)
         double kk = 0.0;
@@ -120,11 +133,15 @@ __global__ void batch_mixed_table_kernel(const BatchItem *__restrict__ items,
                      rec64 + g * kMxRec64);
 }
 
-// (z1 cos + z2 sin)(2 pi (th + tl)), th in [-1/2, 1/2] turns, tl tiny
-__device__ __forceinline__ float mixed_term(float th, float tl, float z1, float z2) {
+// (z1 cos + z2 sin)(2 pi (th + tl)), th in [-1/2, 1/2] turns, tl tiny:
+// quadrant q by rounding 4 th, f = th - q/4 (exact, |f| <= 1/8), sin(2 pi f)
+// = f S(f^2), cos(2 pi f) = C(f^2), first-order correction for tl; the
+// rotation by q quarter turns is taken from the mode's rotated weight pairs
+// `ab` (indexed by q mod 4) instead of permuting and negating sin and cos.
+__device__ __forceinline__ float mixed_term(float th, float tl, const float2 *ab) {
     const float qf = fmaf(th, 4.0f, kRoundF);
     const float q = qf - kRoundF;
-    const int qi = __float_as_int(qf);
+    const int qi = __float_as_int(qf);                       // low bits: q mod 4
     const float f = fmaf(q, -0.25f, th);                     // exact, |f| <= 1/8
     const float f2 = f * f;
     float s = fmaf(fmaf(fmaf(fmaf(kS4, f2, kS3), f2, kS2), f2, kS1), f2, kS0) * f;
@@ -132,13 +149,8 @@ __device__ __forceinline__ float mixed_term(float th, float tl, float z1, float 
     const float tw = tl * kTwoPiF;                           // first-order low-part correction
     const float s1 = fmaf(tw, c, s);
     const float c1 = fmaf(-tw, s, c);
-    // rotate by q quarter turns
-    const bool swap = qi & 1;
-    float sr = swap ? c1 : s1;
-    float cr = swap ? s1 : c1;
-    sr = __int_as_float(__float_as_int(sr) ^ ((qi & 2) << 30));
-    cr = __int_as_float(__float_as_int(cr) ^ (((qi + 1) & 2) << 30));
-    return fmaf(z1, cr, z2 * sr);
+    const float2 w = ab[qi & 3];
+    return fmaf(w.x, c1, w.y * s1);
 }
 
 // Kahan step: (sum, cmp) += a, cmp holding minus the lost low-order part
@@ -204,7 +216,7 @@ __device__ __forceinline__ void mixed_block(const double *__restrict__ pos, int6
             for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
         for (int m = 0; m < tm; ++m) {
             const float *mr = srec + m * kMxRec;
-            const float z1 = mr[6], z2 = mr[7];
+            const float2 *ab = reinterpret_cast<const float2 *>(mr + kMxRot);
             float w[3] = {mr[8], mr[9], mr[10]};
 #pragma unroll
             for (int r = 0; r < kMxR; ++r) {
@@ -231,7 +243,7 @@ __device__ __forceinline__ void mixed_block(const double *__restrict__ pos, int6
                     th = a2 + b;
                     tl = b - (th - a2);
                 }
-                const float z12 = mixed_term(th, tl, z1, z2);
+                const float z12 = mixed_term(th, tl, ab);
                 if (INC) {
 #pragma unroll
                     for (int i = 0; i < NOUT; ++i) kahan_add(acc[r][i], cmp[r][i], w[i] * z12);
