@@ -79,14 +79,15 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s: a healthy wait is mic
 // (after recording `code` and raising *abort) on timeout or when another
 // warp has already aborted.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
-                                          int *status, int code) {
+                                          int *status, int code,
+                                          uint64_t limit_ns = kWaitLimitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((i & 63) == 0) {
             if (*abort) return false;
-            if (globaltimer_ns() - t0 > kWaitLimitNs) {
+            if (globaltimer_ns() - t0 > limit_ns) {
                 *abort = 1;
                 atomicCAS(status, 0, code);
                 return false;

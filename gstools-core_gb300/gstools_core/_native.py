@@ -160,6 +160,7 @@ SIGNATURES = {
                                             _I64, _P, _P, _P, _OPTS]),
     "gsc_sample_modes_f64": (ctypes.c_int, [_I32, _I32, _I64, ctypes.c_double, ctypes.c_uint64,
                                             _I64, _P, _P, _P, _OPTS]),
+    "gsc_selftest_wait_timeout": (ctypes.c_int, [_I32, _I64]),
 }
 
 

@@ -353,6 +353,15 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
  * `device` (-1 = current). */
 int gsc_last_batch_config(int32_t device, gsc_batch_config *config);
 
+/* ---- self-test of the failure path -------------------------------------- */
+/* Runs one CTA that waits, with the bounded wait of the tensor-core
+ * pipelines, on a barrier nothing completes; the wait gives up after
+ * limit_us microseconds (1e3 .. 2e6), records its code in the device status
+ * word and the kernel returns.  Returns what gsc_device_status returns:
+ * GSC_ERR_KERNEL with the recorded code, after which the status is clear
+ * and the device remains usable.  No reference counterpart. */
+int gsc_selftest_wait_timeout(int32_t device, int64_t limit_us);
+
 /* ---- on-device spectral sampling ---------------------------------------- */
 /* The randomization method's inputs drawn on the GPU: wave vectors
  * cov (dim, n_modes) from a covariance model's spectral density and the
