@@ -8,6 +8,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -446,6 +447,80 @@ static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int
 }
 
 // ---------------------------------------------------------------------------
+// structured points passed as a list
+// ---------------------------------------------------------------------------
+constexpr int64_t kGridMinPoints = 4096;   // smaller grids are not worth routing
+
+// Runs f(begin, end) over [0, n) on up to 8 host threads (one for small n).
+template <class F>
+static void parallel_ranges(int64_t n, int64_t min_per_thread, F f) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int64_t T = std::max<int64_t>(
+        1, std::min<int64_t>(std::min<int64_t>(8, hw ? hw : 1), n / std::max<int64_t>(1, min_per_thread)));
+    if (T <= 1) {
+        f(int64_t(0), n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int64_t per = (n + T - 1) / T;
+    for (int64_t t = 1; t < T; ++t) {
+        const int64_t a = t * per, b = std::min(n, a + per);
+        if (a < b) th.emplace_back(f, a, b);
+    }
+    f(int64_t(0), std::min(n, per));
+    for (auto &x : th) x.join();
+}
+
+// If pos (dim, P) holds meshgrid(axes, indexing="ij") flattened in C order --
+// how GSTools lays out the points of a structured mesh before it calls
+// summate -- returns true with the axes (every point checked, bit for bit).
+static bool detect_grid(const double *pos, int64_t sd, int64_t sp, int64_t dim, int64_t P,
+                        std::vector<double> ax[3], int64_t n[3]) {
+    if ((dim != 2 && dim != 3) || P < kGridMinPoints) return false;
+    auto at = [=](int64_t d, int64_t i) { return pos[d * sd + i * sp]; };
+    // axis 0 is constant over runs of L0 = n1 (* n2) points, axis 1 (3-D) over L1 = n2
+    int64_t L0 = 1;
+    while (L0 < P && at(0, L0) == at(0, 0)) ++L0;
+    if (P % L0 != 0) return false;
+    int64_t L1 = 1;
+    if (dim == 3) {
+        while (L1 < L0 && at(1, L1) == at(1, 0)) ++L1;
+        if (L0 % L1 != 0) return false;
+    }
+    n[0] = P / L0;
+    n[1] = dim == 3 ? L0 / L1 : L0;
+    n[2] = dim == 3 ? L1 : 1;
+    for (int d = 0; d < dim; ++d)
+        if (n[d] < 2) return false;
+    ax[0].resize(static_cast<size_t>(n[0]));
+    ax[1].resize(static_cast<size_t>(n[1]));
+    for (int64_t a = 0; a < n[0]; ++a) ax[0][a] = at(0, a * L0);
+    for (int64_t b = 0; b < n[1]; ++b) ax[1][b] = at(1, b * L1);
+    if (dim == 3) {
+        ax[2].resize(static_cast<size_t>(n[2]));
+        for (int64_t c = 0; c < n[2]; ++c) ax[2][c] = at(2, c);
+    }
+    std::atomic<bool> ok(true);
+    parallel_ranges(P, int64_t(1) << 20, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e && ok.load(std::memory_order_relaxed); ++i) {
+            bool good = at(0, i) == ax[0][i / L0];
+            if (dim == 3)
+                good = good && at(1, i) == ax[1][(i / L1) % n[1]] && at(2, i) == ax[2][i % n[2]];
+            else
+                good = good && at(1, i) == ax[1][i % n[1]];
+            if (!good) ok.store(false, std::memory_order_relaxed);
+        }
+    });
+    return ok.load();
+}
+
+static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
+                           int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
+                           const double *const *ax, const int64_t *n, const int64_t *sx,
+                           double *out, bool incompr, const gsc_opts *opts,
+                           const double *sf, int64_t sfs);
+
+// ---------------------------------------------------------------------------
 // host-pointer path shared by the scalar and incompressible summators
 // ---------------------------------------------------------------------------
 static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
@@ -468,6 +543,29 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     timing_reset(ro.flags & GSC_FLAG_TIMING);
     if (P == 0) return GSC_OK;
     const size_t n_sf = sf ? static_cast<size_t>(N) : 0;
+    const int64_t nout = incompr ? dim : 1;
+
+    // AUTO on a flattened structured mesh: the separable forms on its axes
+    // (FP64 DMMA at the default tolerance, within the same 1e-12 bar)
+    if (ro.form == GSC_FORM_AUTO) {
+        std::vector<double> axv[3];
+        int64_t n[3] = {1, 1, 1};
+        if (detect_grid(pos, ps_d, ps_p, dim, P, axv, n)) {
+            const double *axp[3] = {axv[0].data(), axv[1].data(), dim == 3 ? axv[2].data() : nullptr};
+            const int64_t sx[3] = {1, 1, 1};
+            if (os_p == 1 && (nout == 1 || os_d == P))
+                return host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx, out,
+                                       incompr, opts, sf, sfs);
+            std::vector<double> tmp(static_cast<size_t>(nout * P));
+            GSC_TRY(host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx,
+                                    tmp.data(), incompr, opts, sf, sfs));
+            parallel_ranges(P, int64_t(1) << 18, [&](int64_t b, int64_t e) {
+                for (int64_t i = 0; i < nout; ++i)
+                    for (int64_t p = b; p < e; ++p) out[i * os_d + p * os_p] = tmp[i * P + p];
+            });
+            return GSC_OK;
+        }
+    }
 
     DeviceCtx *ctx = nullptr;
     GSC_TRY(get_ctx(ro.device, &ctx));
@@ -476,7 +574,6 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(g.set(ctx->device));
     cudaStream_t st = ctx->stream;
 
-    const int64_t nout = incompr ? dim : 1;
     const size_t n_cov = static_cast<size_t>(dim * N), n_pos = static_cast<size_t>(dim * P);
     const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_pos;
     const size_t n_out = static_cast<size_t>(nout * P);
@@ -668,7 +765,7 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
                            int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
                            const double *const *ax, const int64_t *n, const int64_t *sx,
                            double *out, bool incompr, const gsc_opts *opts,
-                           const double *sf = nullptr, int64_t sfs = 0) {
+                           const double *sf, int64_t sfs) {
     Resolved ro;
     GSC_TRY(resolve_opts(opts, &ro));
     GSC_TRY(check_structured(dim, N, n, incompr));
@@ -925,7 +1022,7 @@ int gsc_summate_structured_f64(const double *cov, int64_t cs_d, int64_t cs_n, co
     const double *ax[3] = {a0, a1, a2};
     const int64_t n[3] = {n0, n1, n2}, sx[3] = {s0, s1, s2};
     return host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, n_modes, ax, n, sx, out,
-                           false, opts);
+                           false, opts, nullptr, 0);
 }
 
 int gsc_summate_structured_dev(const double *cov, const double *z1, const double *z2,
@@ -947,7 +1044,7 @@ int gsc_summate_incompr_structured_f64(const double *cov, int64_t cs_d, int64_t 
     const double *ax[3] = {a0, a1, a2};
     const int64_t n[3] = {n0, n1, n2}, sx[3] = {s0, s1, s2};
     return host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, n_modes, ax, n, sx, out,
-                           true, opts);
+                           true, opts, nullptr, 0);
 }
 
 int gsc_summate_incompr_structured_dev(const double *cov, const double *z1, const double *z2,

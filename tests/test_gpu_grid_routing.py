@@ -1,0 +1,98 @@
+"""Flattened structured meshes passed to the point API (GPU tests).
+
+GSTools lays out the points of a structured mesh as
+meshgrid(*axes, indexing="ij") flattened in C order before it calls
+summate / summate_incompr / summate_fourier.  With form "auto" the library
+recognises that layout (every point checked) and computes on the axes with
+the separable FP64 form, within the same 1e-12 bar as the plain kernel;
+anything else -- a perturbed point, repeated axis values, an explicit form --
+takes the point kernels.  Checked against the oracle in every case.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 1
+
+
+def _flat(axes):
+    return np.ascontiguousarray(np.array(np.meshgrid(*axes, indexing="ij")).reshape(len(axes), -1))
+
+
+def _kernels(gsc):
+    return {name for name, _ in gsc.last_timings()}
+
+
+def _case(seed, shape, n):
+    rng = np.random.default_rng(seed)
+    dim = len(shape)
+    cov = rng.normal(0.0, 0.3, (dim, n))
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    axes = tuple(np.sort(rng.uniform(-20, 20, s)) for s in shape)
+    return cov, z1, z2, axes
+
+
+@pytest.mark.parametrize("shape", [(20, 30, 40), (100, 90)])
+def test_scalar_grid_is_routed(gsc, shape):
+    cov, z1, z2, axes = _case(1, shape, 300)
+    pos = _flat(axes)
+    out = gsc.summate(cov, z1, z2, pos, timing=True)
+    assert "sep_f64_dmma" in _kernels(gsc)
+    assert rel_err(out, oracle.summator(cov, z1, z2, pos, num_threads=NT)) <= 1e-12
+
+
+def test_incompr_grid_fortran_output(gsc):
+    cov, z1, z2, axes = _case(2, (16, 24, 32), 200)
+    pos = _flat(axes)
+    out = gsc.summate_incompr(cov, z1, z2, pos, timing=True)
+    assert "sep_f64_dmma" in _kernels(gsc)
+    assert out.flags.f_contiguous and out.shape == (3, pos.shape[1])
+    assert rel_err(out, oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)) <= 1e-12
+
+
+def test_fourier_grid_is_routed(gsc):
+    rng = np.random.default_rng(3)
+    m = np.array(np.meshgrid(*[np.arange(-6, 7)] * 2, indexing="ij")).reshape(2, -1)
+    modes = np.ascontiguousarray(m[:, np.any(m != 0, axis=0)] * (2 * np.pi / 50.0))
+    n = modes.shape[1]
+    sf = rng.uniform(0.1, 1.0, n)
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = _flat((np.arange(80) * 0.625, np.arange(60) * 0.625))
+    out = gsc.summate_fourier(sf, modes, z1, z2, pos, timing=True)
+    assert "sep_f64_dmma" in _kernels(gsc)
+    assert rel_err(out, oracle.summator_fourier(sf, modes, z1, z2, pos, num_threads=NT)) <= 1e-12
+
+
+def test_strided_grid_view_is_routed(gsc):
+    cov, z1, z2, axes = _case(4, (20, 25, 30), 150)
+    pos_f = np.asfortranarray(_flat(axes))
+    out = gsc.summate(cov, z1, z2, pos_f, timing=True)
+    assert "sep_f64_dmma" in _kernels(gsc)
+    assert rel_err(out, oracle.summator(cov, z1, z2, pos_f, num_threads=NT)) <= 1e-12
+
+
+def test_not_a_grid_takes_the_point_kernel(gsc):
+    cov, z1, z2, axes = _case(5, (20, 30, 40), 120)
+    pos = _flat(axes)
+    pos[2, 12345] += 1e-9                                   # one point off the grid
+    out = gsc.summate(cov, z1, z2, pos, timing=True)
+    assert "sep_f64_dmma" not in _kernels(gsc)
+    assert rel_err(out, oracle.summator(cov, z1, z2, pos, num_threads=NT)) <= 1e-12
+    # repeated values on an axis: not separable as detected, still correct
+    ax = (np.array([0.0, 0.0, 1.0, 2.0] * 10), np.arange(50.0), np.arange(40.0))
+    pos = _flat(ax)
+    out = gsc.summate(cov, z1, z2, pos)
+    assert rel_err(out, oracle.summator(cov, z1, z2, pos, num_threads=NT)) <= 1e-12
+
+
+def test_explicit_form_is_not_routed(gsc):
+    cov, z1, z2, axes = _case(6, (20, 30, 40), 100)
+    pos = _flat(axes)
+    gsc.summate(cov, z1, z2, pos, form="plain", timing=True)
+    assert "sep_f64_dmma" not in _kernels(gsc)
