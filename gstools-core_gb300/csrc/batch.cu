@@ -700,6 +700,7 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         ctx->batch_sig = sig;
         timing_reset(ro.flags & GSC_FLAG_TIMING);
     }
+    ctx->batch->flags = ro.flags;               // this call's timing request
     GSC_TRY(gsc_batch_run(ctx->batch, st));
     // fault in the output pages while the GPU computes, then DMA straight
     // into the caller's arrays
