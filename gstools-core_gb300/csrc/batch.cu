@@ -317,6 +317,8 @@ int apply_config(gsc_batch &b, const Cfg &c) {
     const int blocks = occ * batch_sm_count(b.device);
     std::vector<BatchUnit> units;
     GSC_TRY(make_units(b, c, blocks, units));
+    if (units.size() > 0x7fffffff)   // the queue counter is a 32-bit integer
+        return set_error(GSC_ERR_INVALID, "batch too large: more than 2^31 work units");
     GSC_TRY(prepare_items(b));
     GSC_TRY(upload_units(b, units));
     b.cfg = c;
