@@ -153,9 +153,7 @@ namespace {
 
 int dmalloc(void **p, size_t bytes) {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (batch plan)");
-    return GSC_OK;
+    return alloc_device(p, bytes, "cudaMalloc (batch plan)");
 }
 
 bool is_plain(const gsc_batch &b) { return b.form == GSC_FORM_PLAIN_F64; }
@@ -163,6 +161,63 @@ bool is_plain(const gsc_batch &b) { return b.form == GSC_FORM_PLAIN_F64; }
 int occupancy(const gsc_batch &b, const Cfg &c) {
     return is_plain(b) ? batch_plain_occupancy(c.R, c.tile, b.device)
                        : batch_mixed_occupancy(c.R, b.form == GSC_FORM_MIXED_F64PHASE, b.device);
+}
+
+// Item table, mode prefix and total work of a plan from the caller's item
+// descriptors, after their shapes, kinds and pointers are checked
+// (pointers only when check_ptrs: the host-only queue check has none).
+int fill_items(gsc_batch &b, const gsc_batch_item *items, int64_t count, bool check_ptrs) {
+    b.items.resize(static_cast<size_t>(count));
+    b.mode_prefix.assign(static_cast<size_t>(count) + 1, 0);
+    for (int64_t i = 0; i < count; ++i) {
+        const gsc_batch_item &x = items[i];
+        const std::string tag = "item " + std::to_string(i) + ": ";
+        if (x.n_modes < 0 || x.n_points < 0)
+            return set_error(GSC_ERR_INVALID, tag + "negative mode or point count");
+        if (x.n_modes > (int64_t(1) << 30) || x.n_points > (int64_t(1) << 40))
+            return set_error(GSC_ERR_INVALID, tag + "too many modes or points");
+        if (x.kind < GSC_BATCH_SCALAR || x.kind > GSC_BATCH_FOURIER)
+            return set_error(GSC_ERR_INVALID, tag + "unknown kind");
+        const bool inc = x.kind == GSC_BATCH_INCOMPR;
+        if (x.dim < 1 || x.dim > 3 || (inc && x.dim == 1))
+            return set_error(GSC_ERR_DIM, tag + (inc ? "Only two- and three-dimensional problems are supported."
+                                                     : "batches support dimensions 1, 2 and 3"));
+        const char *need[5] = {"cov", "z1", "z2", "pos", "out"};
+        const void *ptrs[5] = {x.cov, x.z1, x.z2, x.pos, x.out};
+        const bool needed[5] = {x.n_modes > 0, x.n_modes > 0, x.n_modes > 0, x.n_points > 0,
+                                x.n_points > 0};
+        for (int k = 0; k < 5; ++k) {
+            if (!check_ptrs) continue;
+            if (needed[k] && !ptrs[k]) return set_error(GSC_ERR_INVALID, tag + need[k] + " is NULL");
+            GSC_TRY(check_device_ptr(ptrs[k], need[k]));
+        }
+        if (x.kind == GSC_BATCH_FOURIER && check_ptrs) {
+            if (x.n_modes > 0 && !x.spectrum_factor)
+                return set_error(GSC_ERR_INVALID, tag + "spectrum_factor is NULL");
+            GSC_TRY(check_device_ptr(x.spectrum_factor, "spectrum_factor"));
+        }
+        BatchItem &it = b.items[static_cast<size_t>(i)];
+        it.cov = x.cov;
+        it.z1 = x.z1;
+        it.z2 = x.z2;
+        it.sf = x.kind == GSC_BATCH_FOURIER ? x.spectrum_factor : nullptr;
+        it.pos = x.pos;
+        it.out = x.out;
+        it.part = nullptr;
+        it.n_modes = x.n_modes;
+        it.n_points = x.n_points;
+        it.mode_off = b.mode_prefix[static_cast<size_t>(i)];
+        it.dim = x.dim;
+        it.incompr = inc ? 1 : 0;
+        it.splits = 1;
+        it.pad = 0;
+        b.mode_prefix[static_cast<size_t>(i) + 1] = it.mode_off + x.n_modes;
+        b.total_work += static_cast<double>(x.n_points) * static_cast<double>(x.n_modes) *
+                         (inc ? x.dim : 1);
+    }
+    b.total_modes = b.mode_prefix.back();
+    if (b.total_modes > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many modes in the batch");
+    return GSC_OK;
 }
 
 // Work units of configuration c, cost-sorted (largest first), and the split
@@ -210,6 +265,69 @@ int make_units(gsc_batch &b, const Cfg &c, int blocks, std::vector<BatchUnit> &u
     std::vector<BatchUnit> sorted(units.size());
     for (size_t k = 0; k < order.size(); ++k) sorted[k] = units[order[k]];
     units.swap(sorted);
+    return GSC_OK;
+}
+
+// Validates a work queue before it is uploaded: every unit names an item and
+// a split that exist, starts on a point-block boundary inside its item and
+// covers a mode range inside it; every (point block, split) of every item
+// appears exactly once, and the splits of a block tile [0, n_modes) in order.
+// A queue that fails would make the persistent kernels skip or double-count
+// points, so the plan refuses it.
+int check_units(const std::vector<BatchItem> &items, int64_t ppb,
+                const std::vector<BatchUnit> &units) {
+    std::vector<int64_t> first(items.size() + 1, 0);
+    for (size_t i = 0; i < items.size(); ++i) {
+        const int64_t nblk = (items[i].n_points + ppb - 1) / ppb;
+        first[i + 1] = first[i] + nblk * std::max<int32_t>(1, items[i].splits);
+    }
+    const int64_t n_slots = first.back();
+    auto bad = [](size_t k, const std::string &why) {
+        return set_error(GSC_ERR_INVALID, "corrupt batch work queue: unit " + std::to_string(k) +
+                                              " " + why);
+    };
+    if (static_cast<int64_t>(units.size()) != n_slots)
+        return set_error(GSC_ERR_INVALID, "corrupt batch work queue: " +
+                                              std::to_string(units.size()) + " units for " +
+                                              std::to_string(n_slots) + " (point block, split) pairs");
+    std::vector<int64_t> jb(static_cast<size_t>(n_slots), -1), je(static_cast<size_t>(n_slots), -1);
+    for (size_t k = 0; k < units.size(); ++k) {
+        const BatchUnit &u = units[k];
+        if (u.item < 0 || static_cast<size_t>(u.item) >= items.size())
+            return bad(k, "names item " + std::to_string(u.item));
+        const BatchItem &it = items[static_cast<size_t>(u.item)];
+        if (u.split < 0 || u.split >= std::max<int32_t>(1, it.splits))
+            return bad(k, "names split " + std::to_string(u.split));
+        if (u.p_first < 0 || u.p_first >= it.n_points || u.p_first % ppb != 0)
+            return bad(k, "starts at point " + std::to_string(u.p_first));
+        if (u.jb < 0 || u.jb > u.je || u.je > it.n_modes)
+            return bad(k, "covers modes [" + std::to_string(u.jb) + ", " + std::to_string(u.je) + ")");
+        const size_t slot = static_cast<size_t>(first[static_cast<size_t>(u.item)] +
+                                                u.p_first / ppb * std::max<int32_t>(1, it.splits) +
+                                                u.split);
+        if (jb[slot] >= 0) return bad(k, "repeats an earlier unit");
+        jb[slot] = u.jb;
+        je[slot] = u.je;
+    }
+    for (size_t i = 0; i < items.size(); ++i) {
+        const int64_t S = std::max<int32_t>(1, items[i].splits);
+        for (int64_t q = first[i]; q < first[i + 1]; q += S) {
+            int64_t at = 0;
+            for (int64_t s = 0; s < S; ++s) {
+                if (jb[static_cast<size_t>(q + s)] != at)
+                    return set_error(GSC_ERR_INVALID,
+                                     "corrupt batch work queue: item " + std::to_string(i) +
+                                         ": split " + std::to_string(s) + " of point block " +
+                                         std::to_string((q - first[i]) / S) +
+                                         " does not start where the previous split ends");
+                at = je[static_cast<size_t>(q + s)];
+            }
+            if (at != items[i].n_modes)
+                return set_error(GSC_ERR_INVALID, "corrupt batch work queue: item " +
+                                                      std::to_string(i) +
+                                                      ": the splits do not reach the last mode");
+        }
+    }
     return GSC_OK;
 }
 
@@ -319,6 +437,7 @@ int apply_config(gsc_batch &b, const Cfg &c) {
     GSC_TRY(make_units(b, c, blocks, units));
     if (units.size() > 0x7fffffff)   // the queue counter is a 32-bit integer
         return set_error(GSC_ERR_INVALID, "batch too large: more than 2^31 work units");
+    GSC_TRY(check_units(b.items, static_cast<int64_t>(kBatchThreads) * c.R, units));
     GSC_TRY(prepare_items(b));
     GSC_TRY(upload_units(b, units));
     b.cfg = c;
@@ -433,55 +552,7 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
     b->device = device;
     b->form = form;
     b->flags = ro.flags;
-    b->items.resize(static_cast<size_t>(count));
-    b->mode_prefix.assign(static_cast<size_t>(count) + 1, 0);
-    for (int64_t i = 0; i < count; ++i) {
-        const gsc_batch_item &x = items[i];
-        const std::string tag = "item " + std::to_string(i) + ": ";
-        if (x.n_modes < 0 || x.n_points < 0)
-            return set_error(GSC_ERR_INVALID, tag + "negative mode or point count");
-        if (x.n_modes > (int64_t(1) << 30) || x.n_points > (int64_t(1) << 40))
-            return set_error(GSC_ERR_INVALID, tag + "too many modes or points");
-        if (x.kind < GSC_BATCH_SCALAR || x.kind > GSC_BATCH_FOURIER)
-            return set_error(GSC_ERR_INVALID, tag + "unknown kind");
-        const bool inc = x.kind == GSC_BATCH_INCOMPR;
-        if (x.dim < 1 || x.dim > 3 || (inc && x.dim == 1))
-            return set_error(GSC_ERR_DIM, tag + (inc ? "Only two- and three-dimensional problems are supported."
-                                                     : "batches support dimensions 1, 2 and 3"));
-        const char *need[5] = {"cov", "z1", "z2", "pos", "out"};
-        const void *ptrs[5] = {x.cov, x.z1, x.z2, x.pos, x.out};
-        const bool needed[5] = {x.n_modes > 0, x.n_modes > 0, x.n_modes > 0, x.n_points > 0,
-                                x.n_points > 0};
-        for (int k = 0; k < 5; ++k) {
-            if (needed[k] && !ptrs[k]) return set_error(GSC_ERR_INVALID, tag + need[k] + " is NULL");
-            GSC_TRY(check_device_ptr(ptrs[k], need[k]));
-        }
-        if (x.kind == GSC_BATCH_FOURIER) {
-            if (x.n_modes > 0 && !x.spectrum_factor)
-                return set_error(GSC_ERR_INVALID, tag + "spectrum_factor is NULL");
-            GSC_TRY(check_device_ptr(x.spectrum_factor, "spectrum_factor"));
-        }
-        BatchItem &it = b->items[static_cast<size_t>(i)];
-        it.cov = x.cov;
-        it.z1 = x.z1;
-        it.z2 = x.z2;
-        it.sf = x.kind == GSC_BATCH_FOURIER ? x.spectrum_factor : nullptr;
-        it.pos = x.pos;
-        it.out = x.out;
-        it.part = nullptr;
-        it.n_modes = x.n_modes;
-        it.n_points = x.n_points;
-        it.mode_off = b->mode_prefix[static_cast<size_t>(i)];
-        it.dim = x.dim;
-        it.incompr = inc ? 1 : 0;
-        it.splits = 1;
-        it.pad = 0;
-        b->mode_prefix[static_cast<size_t>(i) + 1] = it.mode_off + x.n_modes;
-        b->total_work += static_cast<double>(x.n_points) * static_cast<double>(x.n_modes) *
-                         (inc ? x.dim : 1);
-    }
-    b->total_modes = b->mode_prefix.back();
-    if (b->total_modes > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many modes in the batch");
+    GSC_TRY(fill_items(*b, items, count, true));
 
     // device memory of the plan
     GSC_CUDA(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
@@ -724,6 +795,47 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     }
     GSC_CUDA(cudaStreamSynchronize(st));
     return GSC_OK;
+}
+
+int gsc_selftest_batch_queue(const gsc_batch_item *items, int64_t count, int32_t form,
+                             const gsc_batch_config *config, int32_t blocks, int32_t corruption) {
+    if (count < 0 || (count > 0 && !items)) return set_error(GSC_ERR_INVALID, "bad item list");
+    if (count > (int64_t(1) << 20)) return set_error(GSC_ERR_INVALID, "too many items");
+    if (!config || config->struct_size < static_cast<int32_t>(sizeof(gsc_batch_config)))
+        return set_error(GSC_ERR_INVALID, "config is NULL or its struct_size is too small");
+    if (form != GSC_FORM_PLAIN_F64 && form != GSC_FORM_MIXED && form != GSC_FORM_MIXED_F64PHASE)
+        return set_error(GSC_ERR_INVALID, "batches run the point forms PLAIN_F64, MIXED or MIXED_F64PHASE");
+    if (blocks < 1 || blocks > (1 << 20)) return set_error(GSC_ERR_INVALID, "blocks out of range");
+    if (corruption < 0 || corruption > 6) return set_error(GSC_ERR_INVALID, "unknown corruption");
+    gsc_batch b;   // host fields only: no device memory is made
+    b.form = form;
+    GSC_TRY(fill_items(b, items, count, false));
+    Cfg c;
+    c.R = config->points_per_thread;
+    c.tile = is_plain(b) ? config->tile_modes : 32;
+    c.upb = config->units_per_block;
+    const bool ok = c.upb > 0 && (is_plain(b) ? batch_plain_config_ok(c.R, c.tile)
+                                              : batch_mixed_config_ok(c.R));
+    if (!ok) return set_error(GSC_ERR_INVALID, "unsupported batch configuration");
+    std::vector<BatchUnit> units;
+    GSC_TRY(make_units(b, c, blocks, units));
+    if (units.size() > (size_t(1) << 26)) return set_error(GSC_ERR_INVALID, "queue too large for the check");
+    if (corruption > 0) {
+        if (units.empty()) return set_error(GSC_ERR_INVALID, "no units to corrupt");
+        const size_t k = units.size() / 2;
+        switch (corruption) {
+        case 1: units.erase(units.begin() + static_cast<std::ptrdiff_t>(k)); break;
+        case 2:
+            if (units.size() > 1) units[(k + 1) % units.size()] = units[k];
+            else units.push_back(units[k]);
+            break;
+        case 3: units[k].item = static_cast<int32_t>(count); break;
+        case 4: units[k].jb += 1; break;
+        case 5: units[k].p_first += 1; break;
+        case 6: units[k].split = b.items[static_cast<size_t>(units[k].item)].splits; break;
+        }
+    }
+    return check_units(b.items, static_cast<int64_t>(kBatchThreads) * c.R, units);
 }
 
 int gsc_last_batch_config(int32_t device, gsc_batch_config *config) {

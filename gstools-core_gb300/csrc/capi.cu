@@ -126,14 +126,58 @@ int get_ctx(int device, DeviceCtx **out) {
         GSC_TRY(g.set(device));
         auto *c = new DeviceCtx();
         c->device = device;
-        GSC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-        GSC_CUDA(cudaEventCreateWithFlags(&c->scratch_ready, cudaEventDisableTiming));
-        GSC_CUDA(cudaEventRecord(c->scratch_ready, c->stream));
-        GSC_CUDA(cudaMalloc(&c->status, 256));
-        GSC_CUDA(cudaMemset(c->status, 0, 256));
+        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->scratch_ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(c->scratch_ready, c->stream);
+        if (e == cudaSuccess) e = cudaMalloc(&c->status, 256);
+        if (e == cudaSuccess) e = cudaMemset(c->status, 0, 256);
+        if (e != cudaSuccess) {
+            // a context that failed half-way is released; the next call retries
+            if (c->status) cudaFree(c->status);
+            if (c->scratch_ready) cudaEventDestroy(c->scratch_ready);
+            if (c->stream) cudaStreamDestroy(c->stream);
+            delete c;
+            return cuda_fail(e, "device context");
+        }
         g_ctx[device] = c;
     }
     *out = g_ctx[device];
+    return GSC_OK;
+}
+
+// Allocation-failure injection (gsc_selftest_fail_alloc): -1 = off, k >= 0 =
+// the k-th next allocation of a library buffer fails as out of memory.
+static std::atomic<int> g_fail_alloc{-1};
+
+static bool alloc_injected() {
+    int v = g_fail_alloc.load();
+    while (v >= 0) {
+        if (g_fail_alloc.compare_exchange_weak(v, v - 1)) return v == 0;
+    }
+    return false;
+}
+
+int alloc_device(void **p, size_t bytes, const char *what) {
+    *p = nullptr;
+    if (alloc_injected())
+        return set_error(GSC_ERR_NOMEM, std::string(what) + ": injected allocation failure");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, what);
+    }
+    return GSC_OK;
+}
+
+int alloc_pinned(void **p, size_t bytes, const char *what) {
+    *p = nullptr;
+    if (alloc_injected())
+        return set_error(GSC_ERR_NOMEM, std::string(what) + ": injected allocation failure");
+    cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, what);
+    }
     return GSC_OK;
 }
 
@@ -155,7 +199,7 @@ int ensure_dev(DeviceCtx &ctx, DevBuf &buf, size_t bytes) {
     }
     const size_t n = grow_size(bytes);
     void *p = nullptr;
-    GSC_CUDA(cudaMalloc(&p, n));
+    GSC_TRY(alloc_device(&p, n, "cudaMalloc (scratch)"));
     buf.ptr = p;
     buf.bytes = n;
     return GSC_OK;
@@ -171,7 +215,7 @@ int ensure_pinned(DeviceCtx &ctx, size_t bytes) {
     }
     const size_t n = grow_size(bytes);
     void *p = nullptr;
-    GSC_CUDA(cudaHostAlloc(&p, n, cudaHostAllocDefault));
+    GSC_TRY(alloc_pinned(&p, n, "cudaHostAlloc (staging)"));
     ctx.pinned = p;
     ctx.pinned_bytes = n;
     return GSC_OK;
@@ -1012,6 +1056,40 @@ int gsc_device_status(int32_t device) {
     GSC_TRY(g.set(ctx->device));
     GSC_CUDA(cudaEventSynchronize(ctx->scratch_ready));
     return check_status(*ctx, ctx->stream);
+}
+
+int gsc_release_buffers(int32_t device) {
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    // every user of the buffers records scratch_ready (device-pointer calls)
+    // or runs on the context stream (host-pointer calls) before it returns
+    GSC_CUDA(cudaEventSynchronize(ctx->scratch_ready));
+    GSC_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->sampling_ev) GSC_CUDA(cudaEventSynchronize(ctx->sampling_ev));
+    for (DevBuf *b : {&ctx->io, &ctx->scratch, &ctx->grid, &ctx->zscaled, &ctx->sampling}) {
+        if (b->ptr) GSC_CUDA(cudaFree(b->ptr));
+        b->ptr = nullptr;
+        b->bytes = 0;
+    }
+    if (ctx->pinned) GSC_CUDA(cudaFreeHost(ctx->pinned));
+    ctx->pinned = nullptr;
+    ctx->pinned_bytes = 0;
+    if (ctx->sampling_pinned) GSC_CUDA(cudaFreeHost(ctx->sampling_pinned));
+    ctx->sampling_pinned = nullptr;
+    ctx->sampling_pinned_bytes = 0;
+    if (ctx->batch) gsc_batch_destroy(ctx->batch);
+    ctx->batch = nullptr;
+    ctx->batch_sig.clear();
+    return GSC_OK;
+}
+
+int gsc_selftest_fail_alloc(int32_t countdown) {
+    if (countdown < -1) return set_error(GSC_ERR_INVALID, "countdown must be -1 or >= 0");
+    g_fail_alloc.store(countdown);
+    return GSC_OK;
 }
 
 int gsc_summate_structured_f64(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,

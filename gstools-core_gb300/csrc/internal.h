@@ -119,6 +119,10 @@ int check_device_ptr(const void *p, const char *name);
 // Returns the context of `device` (-1 = current), initialising it once.
 int get_ctx(int device, DeviceCtx **out);
 // Makes `buf` hold at least `bytes`; waits for in-flight users before growing.
+// cudaMalloc / cudaHostAlloc with the allocation-failure injection of
+// gsc_selftest_fail_alloc; GSC_ERR_NOMEM on failure, *p = nullptr.
+int alloc_device(void **p, size_t bytes, const char *what);
+int alloc_pinned(void **p, size_t bytes, const char *what);
 int ensure_dev(DeviceCtx &ctx, DevBuf &buf, size_t bytes);
 int ensure_pinned(DeviceCtx &ctx, size_t bytes);
 // memcpy with up to 8 host threads for large blocks

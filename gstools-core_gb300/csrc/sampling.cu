@@ -157,7 +157,7 @@ int gsc_sample_modes_batch_dev(const gsc_sample_item *items, int64_t count, uint
         if (ctx->sampling_pinned) GSC_CUDA(cudaFreeHost(ctx->sampling_pinned));
         ctx->sampling_pinned = nullptr;
         ctx->sampling_pinned_bytes = 0;
-        GSC_CUDA(cudaHostAlloc(&ctx->sampling_pinned, bytes, cudaHostAllocDefault));
+        GSC_TRY(alloc_pinned(&ctx->sampling_pinned, bytes, "cudaHostAlloc (sampling staging)"));
         ctx->sampling_pinned_bytes = bytes;
     }
     unsigned char *h = static_cast<unsigned char *>(ctx->sampling_pinned);

@@ -39,7 +39,7 @@ __all__ = ["summate", "summate_incompr", "summate_fourier", "summate_device",
            "summate_structured_device", "summate_incompr_structured_device",
            "summate_fourier_structured_device", "Batch", "summate_batch", "last_batch_config",
            "sample_modes", "sample_modes_batch_device",
-           "device_status",
+           "device_status", "release_buffers",
            "device_count", "last_timings", "GscError", "__version__"]
 
 __version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
@@ -556,6 +556,13 @@ def sample_modes_batch_device(items, seed, *, stream=None, device=-1, timing=Fal
     o = _opts("auto", None, timing, device, stream)
     _native.check(_native.lib.gsc_sample_modes_batch_dev(arr, len(items),
                                                          int(seed) & (2**64 - 1), ctypes.byref(o)))
+
+
+def release_buffers(device=-1) -> None:
+    """Frees the scratch and staging memory the library keeps on ``device``
+    between calls (and the cached plan of ``summate_batch``); the next call
+    allocates again.  Plans held as ``Batch`` objects stay."""
+    _native.check(_native.lib.gsc_release_buffers(device))
 
 
 def device_status(device=-1) -> None:

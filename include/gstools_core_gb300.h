@@ -123,6 +123,15 @@ const char *gsc_kernel_name(int32_t kernel_id);
  * the status.  Host-pointer calls check it themselves. */
 int gsc_device_status(int32_t device);
 
+/* Frees the scratch memory the library keeps on `device` (-1 = current)
+ * between calls: the input/output, table and staging buffers of host- and
+ * device-pointer calls, their pinned host staging, and the cached plan of
+ * gsc_summate_batch_f64.  Waits for the library's queued work first; the
+ * next call allocates again.  Plans made with gsc_batch_create are the
+ * caller's and stay.  No reference counterpart (the reference allocates per
+ * call). */
+int gsc_release_buffers(int32_t device);
+
 /* ---- scalar randomization method: src/field.rs:37-65 ------------------ */
 /* u[p] = sum_j z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)
  * cov (dim, n_modes), z1/z2 (n_modes), pos (dim, n_points), out (n_points).
@@ -361,6 +370,32 @@ int gsc_last_batch_config(int32_t device, gsc_batch_config *config);
  * GSC_ERR_KERNEL with the recorded code, after which the status is clear
  * and the device remains usable.  No reference counterpart. */
 int gsc_selftest_wait_timeout(int32_t device, int64_t limit_us);
+
+/* Allocation-failure injection: the `countdown`-th next allocation of a
+ * library buffer (0 = the next one; device scratch, pinned staging, batch
+ * plan memory) fails as GSC_ERR_NOMEM with "injected allocation failure" in
+ * the message, exactly as a real out-of-memory does, after which injection
+ * is off again.  -1 switches it off.  Process-wide.  No reference
+ * counterpart. */
+int gsc_selftest_fail_alloc(int32_t countdown);
+
+/* Work-queue check of the batch planner, on the host only (no device is
+ * touched; the items' pointers are ignored): builds the cost-sorted work
+ * queue that gsc_batch_create would build for `items` with configuration
+ * `config` (points_per_thread, tile_modes, units_per_block) and `blocks`
+ * resident blocks, applies `corruption` to it, and validates it the way
+ * every plan's queue is validated before it is uploaded: each unit names an
+ * item and split that exist, starts on a point-block boundary inside the
+ * item and covers a mode range inside it, and every (point block, split) of
+ * every item appears exactly once with the splits tiling [0, n_modes) in
+ * order.  Returns GSC_OK for a valid queue, GSC_ERR_INVALID (with the
+ * failing unit in the message) for a corrupt one.
+ *   corruption 0 none, 1 drop a unit, 2 duplicate a unit, 3 item index out
+ *   of range, 4 shift a unit's mode range, 5 misalign a unit's point block,
+ *   6 split index out of range */
+int gsc_selftest_batch_queue(const gsc_batch_item *items, int64_t count, int32_t form,
+                             const gsc_batch_config *config, int32_t blocks,
+                             int32_t corruption);
 
 /* ---- on-device spectral sampling ---------------------------------------- */
 /* The randomization method's inputs drawn on the GPU: wave vectors

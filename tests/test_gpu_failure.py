@@ -44,3 +44,78 @@ def test_selftest_rejects_limits_out_of_range(gsc):
     from gstools_core import _native
     assert _native.lib.gsc_selftest_wait_timeout(-1, 10) == _native.GSC_ERR_INVALID
     assert _native.lib.gsc_selftest_wait_timeout(-1, 10 ** 9) == _native.GSC_ERR_INVALID
+
+
+def _scalar_case(seed, dim=3, n=200, p=5000):
+    rng = np.random.default_rng(seed)
+    cov = rng.normal(0.0, 0.3, (dim, n))
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(-20.0, 20.0, (dim, p))
+    return cov, z1, z2, pos
+
+
+@pytest.mark.parametrize("countdown", [0, 1])
+def test_allocation_failure_is_reported_and_recovered(gsc, countdown):
+    """An out-of-memory in any of a call's buffer allocations (injected on
+    the host, the same path a failing cudaMalloc takes) raises MemoryError;
+    the next call allocates again and computes the right field."""
+    from gstools_core import _native
+    lib = _native.lib
+    cov, z1, z2, pos = _scalar_case(11)
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=os.cpu_count() or 1)
+    gsc.release_buffers()                      # the next call must allocate
+    assert lib.gsc_selftest_fail_alloc(countdown) == 0
+    try:
+        with pytest.raises(MemoryError, match="injected allocation failure"):
+            gsc.summate(cov, z1, z2, pos, form="plain")
+    finally:
+        lib.gsc_selftest_fail_alloc(-1)
+    out = gsc.summate(cov, z1, z2, pos, form="plain")
+    assert rel_err(out, ref) <= 1e-12
+
+
+def test_batch_plan_allocation_failure(gsc):
+    """A plan whose device memory cannot be had is not made (no partial plan
+    leaks); the same items then make a working plan."""
+    torch = pytest.importorskip("torch")
+    from gstools_core import _native
+    lib = _native.lib
+    items = []
+    for s in range(3):
+        cov, z1, z2, pos = _scalar_case(20 + s, n=100 + s, p=3000 + s)
+        items.append({"cov": cov, "z1": z1, "z2": z2, "pos": pos})
+    dev = [{k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in it.items()}
+           for it in items]
+    for d in dev:
+        d["out"] = torch.empty(d["pos"].shape[1], dtype=torch.float64, device="cuda")
+    for countdown in (0, 2):
+        assert lib.gsc_selftest_fail_alloc(countdown) == 0
+        try:
+            with pytest.raises(MemoryError, match="injected allocation failure"):
+                gsc.Batch(dev, form="plain", points_per_thread=4, tile_modes=8, units_per_block=4)
+        finally:
+            lib.gsc_selftest_fail_alloc(-1)
+    with gsc.Batch(dev, form="plain", points_per_thread=4, tile_modes=8, units_per_block=4) as b:
+        b.run()
+        torch.cuda.synchronize()
+    for it, d in zip(items, dev):
+        ref = oracle.summator(it["cov"], it["z1"], it["z2"], it["pos"])
+        assert rel_err(d["out"].cpu().numpy(), ref) <= 1e-12
+
+
+def test_release_buffers_keeps_results(gsc):
+    """Released between calls of every host-array path, the library
+    reallocates and gives bit-identical results."""
+    cov, z1, z2, pos = _scalar_case(31, dim=2, n=300, p=20000)
+    a = gsc.summate(cov, z1, z2, pos, form="mixed")
+    ai = gsc.summate_incompr(cov, z1, z2, pos, form="plain")
+    gsc.release_buffers()
+    assert np.array_equal(a, gsc.summate(cov, z1, z2, pos, form="mixed"))
+    gsc.release_buffers()
+    assert np.array_equal(ai, gsc.summate_incompr(cov, z1, z2, pos, form="plain"))
+    axes = (np.arange(64.0), np.arange(96.0))
+    s = gsc.summate_structured(cov, z1, z2, axes, form="sep_f16x5")
+    gsc.release_buffers()
+    assert np.array_equal(s, gsc.summate_structured(cov, z1, z2, axes, form="sep_f16x5"))
+    gsc.release_buffers()
+    gsc.release_buffers()                     # twice in a row is harmless
