@@ -111,17 +111,12 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
 __device__ __forceinline__ double f32_to_f64(float f) {
     const uint32_t u = __float_as_uint(f);
     const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xFFu, man = u & 0x7FFFFFu;
-    uint32_t hi, lo;
-    if (e == 0u) {
-        hi = sign;
-        lo = 0u;
-    } else if (e == 0xFFu) {
-        hi = sign | 0x7FF00000u | (man >> 3) | (man ? 0x80000u : 0u);
-        lo = man << 29;
-    } else {
-        hi = sign | ((e + 896u) << 20) | (man >> 3);
-        lo = man << 29;
-    }
+    // selects, not branches, so that independent conversions interleave
+    const uint32_t hi_norm = sign | ((e + 896u) << 20) | (man >> 3);
+    const uint32_t hi_spec = sign | 0x7FF00000u | (man >> 3) | (man ? 0x80000u : 0u);
+    uint32_t hi = e == 0xFFu ? hi_spec : hi_norm;
+    hi = e == 0u ? sign : hi;
+    const uint32_t lo = e == 0u ? 0u : man << 29;
     return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
@@ -671,6 +666,10 @@ struct X5Params {
     int full_tiles, ksplit;
     float *ws;
     int *ws_cnt;
+    // 2 or 3: the output is written by tiled bulk stores through the kernel's
+    // tensor map of that rank ((nn, rows) or (nn, rows, components));
+    // 0: by plain stores
+    int out_rank;
 };
 
 // Pipeline of the x5 kernel: k-blocks of 32 K elements (16 modes), three
@@ -688,6 +687,7 @@ struct X5Params {
 // copies, so no wait of theirs can block the MMA that would release it.
 constexpr int X5_BK = 32;
 constexpr int X5_STAGES = 3;
+constexpr int X5_BOX_OFF = 65536;   // epilogue: FP64 output boxes (2 x 8 warps x 8 KB)
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
 constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
@@ -714,6 +714,8 @@ struct X5Layout {
     static_assert(OFF_G2 % 1024 == 0 && OFF_BT % 1024 == 0 && STAGE % 1024 == 0,
                   "stage operands must be 1024-byte aligned");
     static_assert(HC % 32 == 0 && BNX % 16 == 0 && BNX <= 256, "tile width");
+    static_assert(8 * 32 * 33 * 4 <= X5_BOX_OFF && X5_BOX_OFF + 2 * 8 * 32 * 32 * 8 <= X5_STAGES * STAGE,
+                  "epilogue buffers must fit in the stage memory");
 };
 constexpr int kTmaWarpX5 = 8, kMmaWarpX5 = 9;
 
@@ -734,7 +736,7 @@ __device__ __forceinline__ void slice3x2(float2 v, float ls, float lu, float ku,
 
 template <int BNX, bool SPLIT>
 __global__ void __launch_bounds__(X5_THREADS, 1)
-sep_x5_kernel(const X5Params xp) {
+sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     using L = X5Layout<BNX>;
     const TcParams &p = xp.base;
     extern __shared__ unsigned char smem_raw[];
@@ -1021,45 +1023,85 @@ sep_x5_kernel(const X5Params xp) {
             if (ok) drain_chunk();
         }
         if (ok) ok = wait_chunk(NC - 1);
+        // ---- epilogue ------------------------------------------------------
+        // Every MMA has completed, so the stage buffers are free.  A warp's
+        // 32 rows x 32 columns of FP32 sums are turned around in shared
+        // memory (pitch 33 floats: no bank conflicts either way), converted
+        // to FP64 row by row into a box and written by a tiled bulk store;
+        // where the output layout does not allow that, each lane stores one
+        // column, 256 contiguous bytes per row and instruction.
+        const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
+        float *trf = reinterpret_cast<float *>(smem) + warp * (32 * 33);
+        // output offset of row (warp's first row) + R; the warp's first row
+        // is slice bs0, row ms0
+        auto out_row = [&](int bs0, int ms0, int R) -> int64_t {
+            int ms = ms0 + R, bs = bs0;
+            while (ms >= p.nm) {
+                ms -= p.nm;
+                ++bs;
+            }
+            return static_cast<int64_t>(bs) * p.batch_stride + static_cast<int64_t>(ms) * p.row_stride;
+        };
+        // tot[32g .. 32g+31] += the TMEM sums of column group g (cross, main)
+        auto read_group = [&](int g) {
+            uint32_t v[32];
+            __syncwarp();
+            tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
+            tmem_ld_wait();
+#pragma unroll
+            for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
+            tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
+            tmem_ld_wait();
+#pragma unroll
+            for (int t = 0; t < 32; ++t) tot[32 * g + t] = __uint_as_float(v[t]) + tot[32 * g + t];
+        };
+        auto store_group = [&](int g) {
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < 32; ++t) trf[lane * 33 + t] = tot[32 * g + t] * unscale;
+            __syncwarp();
+            const int rows = max(0, min(32, rows_valid - 32 * q));
+            const int64_t rq = r0 + 32 * q;
+            const int gc = n0 + L::HC * h + 32 * g;              // first column of the group
+            if (xp.out_rank > 0) {
+                // one 32 x 32 box per warp and group, staged as FP64 rows in
+                // shared memory (two buffers, alternating by group) and
+                // written by the tensor store; rows and columns past the
+                // output are clipped by the copy
+                double *box = reinterpret_cast<double *>(smem + X5_BOX_OFF) +
+                              (static_cast<size_t>(g & 1) * 8 + warp) * (32 * 32);
+                if (lane == 0) bulk_wait_read<1>();     // the buffer's previous store has read it
+                __syncwarp();
+#pragma unroll
+                for (int R = 0; R < 32; ++R) box[R * 32 + lane] = f32_to_f64(trf[R * 33 + lane]);
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0 && rows > 0 && gc < p.ncn) {
+                    const int comp = gc / p.nn;
+                    const int32_t x = gc - comp * p.nn, y = static_cast<int32_t>(rq);
+                    if (xp.out_rank == 3)
+                        tma_store_3d(&out_map, box, x, y, comp);
+                    else
+                        tma_store_2d(&out_map, box, x, y);
+                    bulk_commit();
+                }
+            } else {
+                const int gn = gc + lane;
+                const int bs0 = static_cast<int>(rq / p.nm), ms0 = static_cast<int>(rq % p.nm);
+                if (gn < p.ncn) {
+                    const int comp = gn / p.nn;
+                    double *oc = p.out + comp * p.comp_stride + (gn - comp * p.nn);
+                    for (int R = 0; R < rows; ++R) oc[out_row(bs0, ms0, R)] = f32_to_f64(trf[R * 33 + lane]);
+                }
+            }
+        };
         if (!split) {
             if (ok) {
-                // Every MMA has completed, so the stage buffers are free: each
-                // warp turns its 32 rows x 32 columns blocks around in shared
-                // memory (pitch 33 doubles) and stores them row by row, 256
-                // contiguous bytes per instruction.
                 tc_fence_after();
-                const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
-                double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
-                const int rows = max(0, min(32, rows_valid - 32 * q));
 #pragma unroll
                 for (int g = 0; g < L::HC / 32; ++g) {
-                    uint32_t v[32];
-                    __syncwarp();
-                    tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
-                    tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int t = 0; t < 32; ++t)
-                        tr[lane * 33 + t] = f32_to_f64((__uint_as_float(v[t]) + tot[32 * g + t]) * unscale);
-                    __syncwarp();
-                    const int gn = n0 + L::HC * h + 32 * g + lane;
-                    if (gn < p.ncn) {
-                        const int comp = gn / p.nn;
-                        double *oc = p.out + comp * p.comp_stride + (gn - comp * p.nn);
-                        int64_t rr = r0 + 32 * q;
-                        int bs = static_cast<int>(rr / p.nm), ms = static_cast<int>(rr % p.nm);
-                        for (int R = 0; R < rows; ++R) {
-                            oc[bs * p.batch_stride + static_cast<int64_t>(ms) * p.row_stride] =
-                                tr[R * 33 + lane];
-                            if (++ms == p.nm) {
-                                ms = 0;
-                                ++bs;
-                            }
-                        }
-                    }
+                    read_group(g);
+                    store_group(g);
                 }
                 __syncwarp();
             }
@@ -1067,42 +1109,6 @@ sep_x5_kernel(const X5Params xp) {
             // a split tile: write this part's sums, count the parts, and the
             // last part adds all of them in part order (the result does not
             // depend on which part finishes last), then stores as above
-            const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
-            double *tr = reinterpret_cast<double *>(smem) + warp * (32 * 33);
-            const int rows = max(0, min(32, rows_valid - 32 * q));
-            auto read_group = [&](int g) {
-                uint32_t v[32];
-                __syncwarp();
-                tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
-                tmem_ld_wait();
-#pragma unroll
-                for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
-                tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
-                tmem_ld_wait();
-#pragma unroll
-                for (int t = 0; t < 32; ++t) tot[32 * g + t] = __uint_as_float(v[t]) + tot[32 * g + t];
-            };
-            auto store_group = [&](int g) {
-                __syncwarp();
-#pragma unroll
-                for (int t = 0; t < 32; ++t) tr[lane * 33 + t] = f32_to_f64(tot[32 * g + t] * unscale);
-                __syncwarp();
-                const int gn = n0 + L::HC * h + 32 * g + lane;
-                if (gn < p.ncn) {
-                    const int comp = gn / p.nn;
-                    double *oc = p.out + comp * p.comp_stride + (gn - comp * p.nn);
-                    int64_t rr = r0 + 32 * q;
-                    int bs = static_cast<int>(rr / p.nm), ms = static_cast<int>(rr % p.nm);
-                    for (int R = 0; R < rows; ++R) {
-                        oc[bs * p.batch_stride + static_cast<int64_t>(ms) * p.row_stride] =
-                            tr[R * 33 + lane];
-                        if (++ms == p.nm) {
-                            ms = 0;
-                            ++bs;
-                        }
-                    }
-                }
-            };
             if (ok) {
                 tc_fence_after();
 #pragma unroll
@@ -1142,6 +1148,8 @@ sep_x5_kernel(const X5Params xp) {
         }
     }
 
+    // the tensor stores have read their boxes before shared memory is released
+    if (xp.out_rank > 0 && warp < 8 && lane == 0) bulk_wait_read<0>();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -1400,20 +1408,45 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         xp.ws_cnt = reinterpret_cast<int *>(base + off_cnt);
         if (n_split > 0)
             GSC_CUDA(cudaMemsetAsync(xp.ws_cnt, 0, static_cast<size_t>(n_split) * sizeof(int), st));
+        // The output (ncomp, rows, nn) is dense; tiled bulk stores write it
+        // where its rows are 16-byte aligned and, for several components, no
+        // 32-column group crosses from one component into the next.
+        CUtensorMap om;
+        memset(&om, 0, sizeof(om));
+        xp.out_rank = 0;
+        const bool tma_out = (reinterpret_cast<uintptr_t>(a.out) & 15) == 0 && nn % 2 == 0 &&
+                             (ncomp == 1 || (nn % 32 == 0 && P % 2 == 0)) &&
+                             rows_total < (int64_t(1) << 31);
+        if (tma_out) {
+            EncodeTiledFn fn;
+            GSC_TRY(encode_fn(&fn));
+            const cuuint64_t dims[3] = {static_cast<cuuint64_t>(nn), static_cast<cuuint64_t>(rows_total),
+                                        static_cast<cuuint64_t>(ncomp)};
+            const cuuint64_t strides[2] = {static_cast<cuuint64_t>(nn) * 8,
+                                           static_cast<cuuint64_t>(P) * 8};
+            const cuuint32_t box[3] = {32, 32, 1};
+            const cuuint32_t estr[3] = {1, 1, 1};
+            const int rank = ncomp == 1 ? 2 : 3;
+            const CUresult r = fn(&om, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, rank, a.out, dims, strides, box,
+                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return set_error(GSC_ERR_CUDA, "cuTensorMapEncodeTiled (output) failed");
+            xp.out_rank = rank;
+        }
         tl.begin(K_SEP_TC_F16X5);
         const unsigned g = static_cast<unsigned>(grid);
         if (bnx == 192 && n_split > 0) {
             GSC_TRY((configure_x5<192, true>()));
-            sep_x5_kernel<192, true><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(xp);
+            sep_x5_kernel<192, true><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(om, xp);
         } else if (bnx == 192) {
             GSC_TRY((configure_x5<192, false>()));
-            sep_x5_kernel<192, false><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(xp);
+            sep_x5_kernel<192, false><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(om, xp);
         } else if (n_split > 0) {
             GSC_TRY((configure_x5<256, true>()));
-            sep_x5_kernel<256, true><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(xp);
+            sep_x5_kernel<256, true><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(om, xp);
         } else {
             GSC_TRY((configure_x5<256, false>()));
-            sep_x5_kernel<256, false><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(xp);
+            sep_x5_kernel<256, false><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(om, xp);
         }
     } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);

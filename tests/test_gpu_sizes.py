@@ -112,6 +112,7 @@ GRIDS = [((1, 1), "one point"), ((127, 191), "one row tile, one 192 tile"),
          ((128, 192), "exact tiles"), ((129, 193), "ragged rows and columns"),
          ((1, 256), "one 256 tile"), ((5, 257), "257 columns"),
          ((2, 64, 33), "128 rows over two slices"), ((3, 43, 65), "129 rows over slices"),
+         ((40, 96), "components of 96 columns"), ((3, 50, 64), "components of 64 columns"),
          ((0, 9), "no points")]
 
 
