@@ -781,7 +781,7 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     for (int64_t i = 0; i < count; ++i) {
         const gsc_batch_item &x = items[i];
         const size_t n = static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
-        segs.push_back(HostSeg{x.out, n * sizeof(double)});
+        segs.push_back(HostSeg{is_pinned_host(x.out) ? nullptr : x.out, n * sizeof(double)});
     }
     Prefault pf;
     pf.start_many(segs);

@@ -649,7 +649,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(run_points(*ctx, ro, a, st));
     if (os_p == 1 && (nout == 1 || os_d == P)) {
         Prefault pf;
-        pf.start(out, n_out * sizeof(double));
+        if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
         pf.join();
         GSC_CUDA(cudaMemcpyAsync(out, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
         GSC_CUDA(cudaStreamSynchronize(st));
@@ -864,7 +864,7 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     // output pages are faulted in on host threads while the GPU computes;
     // the result then moves by DMA straight into the caller's array
     Prefault pf;
-    pf.start(out, n_out * sizeof(double));
+    if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
     pf.join();
     GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
     GSC_TRY(check_status(*ctx, st));

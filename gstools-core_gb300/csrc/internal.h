@@ -124,6 +124,9 @@ int get_ctx(int device, DeviceCtx **out);
 int alloc_device(void **p, size_t bytes, const char *what);
 int alloc_pinned(void **p, size_t bytes, const char *what);
 int ensure_dev(DeviceCtx &ctx, DevBuf &buf, size_t bytes);
+// true for page-locked host memory (host_pool.cu): its pages need no
+// faulting in before a copy lands there
+bool is_pinned_host(const void *p);
 int ensure_pinned(DeviceCtx &ctx, size_t bytes);
 // memcpy with up to 8 host threads for large blocks
 void parallel_copy(void *dst, const void *src, size_t bytes);

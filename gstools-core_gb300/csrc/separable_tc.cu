@@ -687,7 +687,7 @@ struct X5Params {
 // copies, so no wait of theirs can block the MMA that would release it.
 constexpr int X5_BK = 32;
 constexpr int X5_STAGES = 3;
-constexpr int X5_BOX_OFF = 65536;   // epilogue: FP64 output boxes (2 x 8 warps x 8 KB)
+constexpr int X5_BOX_OFF = 65536;   // epilogue: FP64 output boxes (2 x 8 warps x 2 x 4 KB)
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
 constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
@@ -1025,11 +1025,10 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         if (ok) ok = wait_chunk(NC - 1);
         // ---- epilogue ------------------------------------------------------
         // Every MMA has completed, so the stage buffers are free.  A warp's
-        // 32 rows x 32 columns of FP32 sums are turned around in shared
-        // memory (pitch 33 floats: no bank conflicts either way), converted
-        // to FP64 row by row into a box and written by a tiled bulk store;
-        // where the output layout does not allow that, each lane stores one
-        // column, 256 contiguous bytes per row and instruction.
+        // 32 rows x 32 columns of FP32 sums are converted to FP64 into
+        // swizzled boxes in shared memory and written by tiled bulk stores;
+        // where the output layout does not allow those, they are turned
+        // around in shared memory and each lane stores one column.
         const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
         float *trf = reinterpret_cast<float *>(smem) + warp * (32 * 33);
         // output offset of row (warp's first row) + R; the warp's first row
@@ -1056,36 +1055,49 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
             for (int t = 0; t < 32; ++t) tot[32 * g + t] = __uint_as_float(v[t]) + tot[32 * g + t];
         };
         auto store_group = [&](int g) {
-            __syncwarp();
-#pragma unroll
-            for (int t = 0; t < 32; ++t) trf[lane * 33 + t] = tot[32 * g + t] * unscale;
-            __syncwarp();
             const int rows = max(0, min(32, rows_valid - 32 * q));
             const int64_t rq = r0 + 32 * q;
             const int gc = n0 + L::HC * h + 32 * g;              // first column of the group
             if (xp.out_rank > 0) {
-                // one 32 x 32 box per warp and group, staged as FP64 rows in
-                // shared memory (two buffers, alternating by group) and
-                // written by the tensor store; rows and columns past the
-                // output are clipped by the copy
-                double *box = reinterpret_cast<double *>(smem + X5_BOX_OFF) +
-                              (static_cast<size_t>(g & 1) * 8 + warp) * (32 * 32);
-                if (lane == 0) bulk_wait_read<1>();     // the buffer's previous store has read it
+                // Two boxes of 16 columns x 32 rows per warp and group, FP64,
+                // in the 128-byte swizzled layout of the tensor map: this
+                // thread's row is 128 bytes, its 16-byte pair c of columns
+                // sits at chunk c ^ (row & 7), so a warp's 16-byte stores
+                // meet no bank conflict.  Two buffers alternate by group;
+                // rows and columns past the output are clipped by the copy.
+                unsigned char *bx = smem + X5_BOX_OFF + (static_cast<size_t>(g & 1) * 8 + warp) * 8192;
+                if (lane == 0) bulk_wait_read<1>();     // the buffer's previous stores have read it
                 __syncwarp();
 #pragma unroll
-                for (int R = 0; R < 32; ++R) box[R * 32 + lane] = f32_to_f64(trf[R * 33 + lane]);
+                for (int hb = 0; hb < 2; ++hb)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        const int t = 32 * g + 16 * hb + 2 * c;
+                        *reinterpret_cast<double2 *>(bx + hb * 4096 + lane * 128 + ((c ^ (lane & 7)) << 4)) =
+                            make_double2(f32_to_f64(tot[t] * unscale), f32_to_f64(tot[t + 1] * unscale));
+                    }
                 fence_proxy_async_smem();
                 __syncwarp();
                 if (lane == 0 && rows > 0 && gc < p.ncn) {
                     const int comp = gc / p.nn;
                     const int32_t x = gc - comp * p.nn, y = static_cast<int32_t>(rq);
-                    if (xp.out_rank == 3)
-                        tma_store_3d(&out_map, box, x, y, comp);
-                    else
-                        tma_store_2d(&out_map, box, x, y);
+#pragma unroll
+                    for (int hb = 0; hb < 2; ++hb) {
+                        if (x + 16 * hb >= p.nn) break;
+                        if (xp.out_rank == 3)
+                            tma_store_3d(&out_map, bx + hb * 4096, x + 16 * hb, y, comp);
+                        else
+                            tma_store_2d(&out_map, bx + hb * 4096, x + 16 * hb, y);
+                    }
                     bulk_commit();
                 }
             } else {
+                // transposed through shared memory (pitch 33 floats), one
+                // column per lane: 256 contiguous bytes per row and store
+                __syncwarp();
+#pragma unroll
+                for (int t = 0; t < 32; ++t) trf[lane * 33 + t] = tot[32 * g + t] * unscale;
+                __syncwarp();
                 const int gn = gc + lane;
                 const int bs0 = static_cast<int>(rq / p.nm), ms0 = static_cast<int>(rq % p.nm);
                 if (gn < p.ncn) {
@@ -1424,11 +1436,11 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
                                         static_cast<cuuint64_t>(ncomp)};
             const cuuint64_t strides[2] = {static_cast<cuuint64_t>(nn) * 8,
                                            static_cast<cuuint64_t>(P) * 8};
-            const cuuint32_t box[3] = {32, 32, 1};
+            const cuuint32_t box[3] = {16, 32, 1};            // 128-byte rows
             const cuuint32_t estr[3] = {1, 1, 1};
             const int rank = ncomp == 1 ? 2 : 3;
             const CUresult r = fn(&om, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, rank, a.out, dims, strides, box,
-                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                   CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return set_error(GSC_ERR_CUDA, "cuTensorMapEncodeTiled (output) failed");
             xp.out_rank = rank;

@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import ctypes
 import operator
+import weakref
 
 import numpy as np
 
@@ -39,7 +40,7 @@ __all__ = ["summate", "summate_incompr", "summate_fourier", "summate_device",
            "summate_structured_device", "summate_incompr_structured_device",
            "summate_fourier_structured_device", "Batch", "summate_batch", "last_batch_config",
            "sample_modes", "sample_modes_batch_device",
-           "device_status", "release_buffers",
+           "device_status", "release_buffers", "host_pool_stats", "host_pool_trim",
            "device_count", "last_timings", "GscError", "__version__"]
 
 __version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
@@ -81,6 +82,40 @@ def _strides(a: np.ndarray):
     return tuple(s // a.itemsize for s in a.strides)
 
 
+_POOL_MIN_BYTES = 1 << 20
+
+
+def _result(shape, order="C") -> np.ndarray:
+    """A new float64 result array.  From 1 MiB up its memory comes from the
+    library's pool of pinned host blocks, which takes the block back when the
+    array and every view of it are gone: repeated calls reuse resident pages
+    instead of faulting in fresh ones (the result is still a new array each
+    call, as the reference returns)."""
+    n = 1
+    for s in shape if isinstance(shape, tuple) else (shape,):
+        n *= int(s)
+    nbytes = 8 * n
+    if nbytes >= _POOL_MIN_BYTES:
+        ptr = ctypes.c_void_p()
+        if _native.lib.gsc_host_alloc(nbytes, ctypes.byref(ptr)) == 0:
+            buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+            weakref.finalize(buf, _native.lib.gsc_host_free, ptr.value).atexit = False
+            return np.ndarray(shape, dtype=np.float64, buffer=buf, order=order)
+    return np.empty(shape, dtype=np.float64, order=order)
+
+
+def host_pool_stats() -> dict:
+    """Bytes of pinned result memory handed out and cached by the pool."""
+    live, cached = ctypes.c_int64(), ctypes.c_int64()
+    _native.check(_native.lib.gsc_host_pool_stats(ctypes.byref(live), ctypes.byref(cached)))
+    return {"live_bytes": live.value, "cached_bytes": cached.value}
+
+
+def host_pool_trim() -> None:
+    """Releases the pool's cached (free) pinned blocks."""
+    _native.check(_native.lib.gsc_host_pool_trim())
+
+
 def _opts(form, tolerance, timing, device=-1, stream=None):
     flags = _native.GSC_FLAG_TIMING if timing else 0
     return _native.make_opts(form=form, device=device, flags=flags, stream=stream,
@@ -113,7 +148,7 @@ def summate(cov_samples, z1, z2, pos, num_threads=None, *, form="auto", toleranc
     cov, z1, z2, pos = _prepare(cov_samples, z1, z2, pos, num_threads)
     dim, n = cov.shape
     p = pos.shape[1]
-    out = np.empty(p, dtype=np.float64)
+    out = _result(p)
     cs, zs1, zs2, ps = _strides(cov), _strides(z1), _strides(z2), _strides(pos)
     o = _opts(form, tolerance, timing, device)
     _native.check(_native.lib.gsc_summate_f64(
@@ -135,7 +170,7 @@ def summate_incompr(cov_samples, z1, z2, pos, num_threads=None, *, form="auto", 
     if dim not in (2, 3):
         raise ValueError("Only two- and three-dimensional problems are supported.")
     p = pos.shape[1]
-    out = np.empty((dim, p), dtype=np.float64, order="F")
+    out = _result((dim, p), order="F")
     cs, zs1, zs2, ps = _strides(cov), _strides(z1), _strides(z2), _strides(pos)
     os_ = _strides(out)
     o = _opts(form, tolerance, timing, device)
@@ -160,7 +195,7 @@ def summate_fourier(spectrum_factor, modes, z1, z2, pos, num_threads=None, *, fo
     # the reference zips sf with the mode columns, which asserts equal length
     _assert_eq(sf.shape[0], n)
     p = pos.shape[1]
-    out = np.empty(p, dtype=np.float64)
+    out = _result(p)
     ms, zs1, zs2, ps = _strides(modes), _strides(z1), _strides(z2), _strides(pos)
     o = _opts(form, tolerance, timing, device)
     _native.check(_native.lib.gsc_summate_fourier_f64(
@@ -258,7 +293,7 @@ def _structured_host(fn, cov_samples, z1, z2, axes, num_threads, form, tolerance
     npts = 1
     for a in ax[:dim]:
         npts *= a.shape[0]
-    out = np.empty((dim, npts) if incompr else npts, dtype=np.float64)
+    out = _result((dim, npts) if incompr else npts)
     args = []
     for a in ax:
         if a is None:
@@ -491,7 +526,7 @@ def summate_batch(items, *, form="auto", tolerance=None, device=-1, timing=False
         if kind == "fourier":
             sf = np.ascontiguousarray(_array(it["spectrum_factor"], "spectrum_factor", 1))
             _assert_eq(sf.shape[0], n)
-        out = np.empty((dim, p) if kind == "incompr" else p, dtype=np.float64)
+        out = _result((dim, p) if kind == "incompr" else p)
         keep += [cov, z1, z2, pos, sf, out]
         outs.append(out)
         arr[i] = _native.GscBatchItem(dim, _native.BATCH_KINDS[kind], n, p, cov.ctypes.data,

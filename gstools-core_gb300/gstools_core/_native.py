@@ -165,6 +165,10 @@ SIGNATURES = {
     "gsc_selftest_batch_queue": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _I32,
                                                 ctypes.POINTER(GscBatchConfig), _I32, _I32]),
     "gsc_release_buffers": (ctypes.c_int, [_I32]),
+    "gsc_host_alloc": (ctypes.c_int, [_I64, ctypes.POINTER(ctypes.c_void_p)]),
+    "gsc_host_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "gsc_host_pool_trim": (ctypes.c_int, []),
+    "gsc_host_pool_stats": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
 }
 
 

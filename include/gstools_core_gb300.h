@@ -132,6 +132,21 @@ int gsc_device_status(int32_t device);
  * call). */
 int gsc_release_buffers(int32_t device);
 
+/* Pinned host blocks for result arrays.  gsc_host_alloc returns a block of
+ * page-locked host memory of at least `bytes` (rounded up to 2 MiB), taken
+ * from the pool's free blocks of that rounded size when there is one;
+ * gsc_host_free hands it back (the pool keeps up to GSC_HOST_POOL_MB MiB of
+ * free blocks, default 8192, and releases the rest); gsc_host_pool_trim
+ * releases every free block; gsc_host_pool_stats reports the bytes handed
+ * out and the bytes cached.  Results written into such blocks by the
+ * host-pointer entry points move by DMA with no page faults.  No reference
+ * counterpart (the reference returns freshly allocated arrays,
+ * src/lib.rs:47,64). */
+int gsc_host_alloc(int64_t bytes, void **ptr);
+int gsc_host_free(void *ptr);
+int gsc_host_pool_trim(void);
+int gsc_host_pool_stats(int64_t *live_bytes, int64_t *cached_bytes);
+
 /* ---- scalar randomization method: src/field.rs:37-65 ------------------ */
 /* u[p] = sum_j z1[j] cos(k_j . x_p) + z2[j] sin(k_j . x_p)
  * cov (dim, n_modes), z1/z2 (n_modes), pos (dim, n_points), out (n_points).
