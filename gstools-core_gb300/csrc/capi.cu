@@ -754,7 +754,8 @@ static int check_structured(int64_t dim, int64_t N, const int64_t *n, bool incom
 // All pointers are device pointers; out is (ncomp, P) row-major.
 static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov, const double *z1,
                           const double *z2, int64_t dim, int64_t N, const double *const *axis,
-                          const int64_t *n, bool incompr, double *out, cudaStream_t st) {
+                          const int64_t *n, bool incompr, double *out, cudaStream_t st,
+                          const std::function<int(int64_t, int64_t)> *on_rows = nullptr) {
     int64_t P = 1;
     for (int d = 0; d < dim; ++d) P *= n[d];
     if (P == 0) return GSC_OK;
@@ -775,6 +776,7 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
         a.chunk_kblocks = 0;
         a.out = out;
         a.status = ctx.status;
+        a.on_rows = on_rows;
         return form == GSC_FORM_SEP_F64 ? sep_f64_run(ctx, a, st) : sep_tc_run(ctx, a, st);
     }
     // plain FP64 forms on the expanded grid
@@ -859,14 +861,44 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     // output buffer 128-byte aligned after the inputs
     double *dout = reinterpret_cast<double *>(
         (reinterpret_cast<uintptr_t>(d + n_in) + 127) & ~static_cast<uintptr_t>(127));
-    GSC_TRY(run_structured(*ctx, ro, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr, dout,
-                           st));
-    // output pages are faulted in on host threads while the GPU computes;
-    // the result then moves by DMA straight into the caller's array
-    Prefault pf;
-    if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
-    pf.join();
-    GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    // A pinned result (resident pages) is copied in row ranges as the
+    // launches that complete them are queued, on a second stream, so the
+    // copy of one wave's rows overlaps the computing of the next.
+    const bool pinned = is_pinned_host(out);
+    const int64_t nn_last = n[dim - 1];                 // output elements per (slice, row)
+    int64_t rows_copied = 0;
+    bool copying = false;
+    std::function<int(int64_t, int64_t)> on_rows = [&](int64_t lo, int64_t hi) -> int {
+        if (!ctx->copy_stream)
+            GSC_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        if (!ctx->chunk_ev)
+            GSC_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev, cudaEventDisableTiming));
+        GSC_CUDA(cudaEventRecord(ctx->chunk_ev, st));
+        GSC_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_ev, 0));
+        copying = true;
+        for (int64_t c = 0; c < nout; ++c)
+            GSC_CUDA(cudaMemcpyAsync(out + c * P + lo * nn_last, dout + c * P + lo * nn_last,
+                                     static_cast<size_t>((hi - lo) * nn_last) * sizeof(double),
+                                     cudaMemcpyDeviceToHost, ctx->copy_stream));
+        rows_copied = hi;
+        return GSC_OK;
+    };
+    int rc = run_structured(*ctx, ro, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr, dout,
+                            st, pinned ? &on_rows : nullptr);
+    if (copying) {
+        // queued copies land in the caller's array: they finish before return
+        const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+        if (rc == GSC_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize (result copies)");
+    }
+    GSC_TRY(rc);
+    if (!copying || rows_copied * nn_last != P) {
+        // output pages are faulted in on host threads while the GPU computes;
+        // the result then moves by DMA straight into the caller's array
+        Prefault pf;
+        if (!pinned) pf.start(out, n_out * sizeof(double));
+        pf.join();
+        GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
     GSC_TRY(check_status(*ctx, st));
     return GSC_OK;
 }

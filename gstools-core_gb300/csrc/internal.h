@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -83,6 +84,8 @@ struct DeviceCtx {
     cudaEvent_t sampling_ev = nullptr;
     int *status = nullptr;           // sticky kernel status word (device)
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};   // pipelined device-to-host staging
+    cudaStream_t copy_stream = nullptr;  // result copies overlapping later launches
+    cudaEvent_t chunk_ev = nullptr;      // "rows so far are done" on the compute stream
     gsc_batch *batch = nullptr;      // plan of the last host-pointer batch call
     std::vector<int64_t> batch_sig;  // its shape signature (reused when equal)
 };
@@ -202,6 +205,11 @@ struct SepArgs {
     int chunk_kblocks;        // k-blocks per FP32 accumulation chunk, 0 = default
     double *out;              // (ncomp, prod n) row-major, device
     int *status;              // device status word (0 = ok)
+    // sep_f16x5 only: when set, the GEMM runs as one launch per wave of
+    // whole row tiles and this is called after each launch is queued with
+    // the (slice, row) range [lo, hi) whose output that launch completes,
+    // so that the caller can queue its copy while the next launch computes
+    const std::function<int(int64_t lo, int64_t hi)> *on_rows = nullptr;
 };
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);
 int sep_f64_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st);   // separable_f64.cu

@@ -663,6 +663,7 @@ struct X5Params {
     // tile runs as ksplit CTAs over consecutive parts of its k-blocks, whose
     // FP32 partials meet in `ws` ([slot][part][column][row]); the last part
     // to finish (counted in ws_cnt[slot]) adds them in part order and stores.
+    int tile0;               // first tile of this launch (launches of wave-sized row ranges)
     int full_tiles, ksplit;
     float *ws;
     int *ws_cnt;
@@ -759,7 +760,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     // a launch without split tiles compiles the split path out
     const int u = static_cast<int>(blockIdx.x) - xp.full_tiles;
     const bool split = SPLIT && u >= 0;
-    const int tile = split ? xp.full_tiles + u / xp.ksplit : static_cast<int>(blockIdx.x);
+    const int tile = xp.tile0 + (split ? xp.full_tiles + u / xp.ksplit : static_cast<int>(blockIdx.x));
     const int part = split ? u % xp.ksplit : 0;
     const int kbeg = split ? static_cast<int>(static_cast<int64_t>(part) * p.kb_total / xp.ksplit) : 0;
     const int KB = split ? static_cast<int>(static_cast<int64_t>(part + 1) * p.kb_total / xp.ksplit) - kbeg
@@ -1126,7 +1127,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
 #pragma unroll
                 for (int g = 0; g < L::HC / 32; ++g) read_group(g);
             }
-            const int slot = tile - xp.full_tiles, ks = xp.ksplit;
+            const int slot = tile - xp.tile0 - xp.full_tiles, ks = xp.ksplit;
             float *wsl = xp.ws + static_cast<int64_t>(slot) * ks * BNX * BM;
             // this thread's column c of part k sits at col0[(k * BNX + c) * BM]
             float *col0 = wsl + static_cast<int64_t>(L::HC * h) * BM + r;
@@ -1280,11 +1281,17 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const int64_t rows_total = static_cast<int64_t>(nb) * nm;
     const int m_tiles = x5 ? static_cast<int>((rows_total + BM - 1) / BM) : (nm + BM - 1) / BM;
 
-    // x5 tail split: the tiles of an incomplete last wave run as ksplit CTAs
-    // each over a share of the k-blocks, when that shortens the schedule
-    const int64_t tiles = static_cast<int64_t>(m_tiles) * n_tiles;
-    int64_t full_tiles = tiles, n_split = 0;
-    int ksplit = 1;
+    // x5 launches: all row tiles at once, or (with a row hook) one launch per
+    // wave of whole row tiles.  Tail split: the tiles of an incomplete last
+    // wave run as ksplit CTAs each over a share of the k-blocks, when that
+    // shortens the schedule.
+    struct Launch {
+        int64_t m0, m1, full_tiles, n_split;
+        int ksplit;
+    };
+    std::vector<Launch> launches;
+    int64_t n_split = 0;          // most split tiles of any launch
+    int ksplit = 1;               // and their most parts
     if (x5) {
         int sms = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device) != cudaSuccess ||
@@ -1292,19 +1299,34 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             cudaGetLastError();
             sms = 152;
         }
-        const int64_t waves = tiles / sms, rem = tiles % sms;
-        double best = static_cast<double>(waves + (rem > 0 ? 1 : 0));
-        for (int k = 2; k <= kMaxSplit && rem > 0 && KB / k >= 8; ++k) {
-            // a part costs 1/k of a tile plus ~5 % for its partial traffic
-            const double span = waves + std::ceil(static_cast<double>(rem * k) / sms) / k * 1.05;
-            if (span < best - 1e-9) {
-                best = span;
-                ksplit = k;
+        const int64_t per = (a.on_rows && static_cast<int64_t>(m_tiles) * n_tiles > sms)
+                                ? std::max<int64_t>(1, sms / n_tiles)
+                                : m_tiles;
+        for (int64_t m0 = 0; m0 < m_tiles; m0 += per) {
+            Launch l;
+            l.m0 = m0;
+            l.m1 = std::min<int64_t>(m_tiles, m0 + per);
+            const int64_t tiles = (l.m1 - l.m0) * n_tiles;
+            l.full_tiles = tiles;
+            l.n_split = 0;
+            l.ksplit = 1;
+            const int64_t waves = tiles / sms, rem = tiles % sms;
+            double best = static_cast<double>(waves + (rem > 0 ? 1 : 0));
+            for (int k = 2; k <= kMaxSplit && rem > 0 && KB / k >= 8; ++k) {
+                // a part costs 1/k of a tile plus ~5 % for its partial traffic
+                const double span = waves + std::ceil(static_cast<double>(rem * k) / sms) / k * 1.05;
+                if (span < best - 1e-9) {
+                    best = span;
+                    l.ksplit = k;
+                }
             }
-        }
-        if (ksplit > 1) {
-            full_tiles = tiles - rem;
-            n_split = rem;
+            if (l.ksplit > 1) {
+                l.full_tiles = tiles - rem;
+                l.n_split = rem;
+                n_split = std::max(n_split, rem);
+                ksplit = std::max(ksplit, l.ksplit);
+            }
+            launches.push_back(l);
         }
     }
 
@@ -1403,7 +1425,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.batch_stride = static_cast<int64_t>(nm) * nn;
     p.row_stride = nn;
     p.status = status;
-    const int64_t grid = x5 ? full_tiles + n_split * ksplit
+    const int64_t grid = x5 ? static_cast<int64_t>(m_tiles) * n_tiles + n_split * ksplit
                             : static_cast<int64_t>(nb) * m_tiles * n_tiles;
     if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
     TimedLaunch tl(st);
@@ -1414,12 +1436,8 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         xp.g1 = reinterpret_cast<const unsigned char *>(t.ghi);
         xp.g2 = reinterpret_cast<const unsigned char *>(t.glo);
         xp.bt = reinterpret_cast<const unsigned char *>(t.btab);
-        xp.full_tiles = static_cast<int>(full_tiles);
-        xp.ksplit = ksplit;
         xp.ws = reinterpret_cast<float *>(base + off_ws);
         xp.ws_cnt = reinterpret_cast<int *>(base + off_cnt);
-        if (n_split > 0)
-            GSC_CUDA(cudaMemsetAsync(xp.ws_cnt, 0, static_cast<size_t>(n_split) * sizeof(int), st));
         // The output (ncomp, rows, nn) is dense; tiled bulk stores write it
         // where its rows are 16-byte aligned and, for several components, no
         // 32-column group crosses from one component into the next.
@@ -1446,19 +1464,29 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             xp.out_rank = rank;
         }
         tl.begin(K_SEP_TC_F16X5);
-        const unsigned g = static_cast<unsigned>(grid);
-        if (bnx == 192 && n_split > 0) {
-            GSC_TRY((configure_x5<192, true>()));
-            sep_x5_kernel<192, true><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(om, xp);
-        } else if (bnx == 192) {
-            GSC_TRY((configure_x5<192, false>()));
-            sep_x5_kernel<192, false><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(om, xp);
-        } else if (n_split > 0) {
-            GSC_TRY((configure_x5<256, true>()));
-            sep_x5_kernel<256, true><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(om, xp);
-        } else {
-            GSC_TRY((configure_x5<256, false>()));
-            sep_x5_kernel<256, false><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(om, xp);
+        for (const Launch &l : launches) {
+            xp.tile0 = static_cast<int>(l.m0 * n_tiles);
+            xp.full_tiles = static_cast<int>(l.full_tiles);
+            xp.ksplit = l.ksplit;
+            if (l.n_split > 0)
+                GSC_CUDA(cudaMemsetAsync(xp.ws_cnt, 0, static_cast<size_t>(l.n_split) * sizeof(int), st));
+            const unsigned g = static_cast<unsigned>(l.full_tiles + l.n_split * l.ksplit);
+            if (bnx == 192 && l.n_split > 0) {
+                GSC_TRY((configure_x5<192, true>()));
+                sep_x5_kernel<192, true><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(om, xp);
+            } else if (bnx == 192) {
+                GSC_TRY((configure_x5<192, false>()));
+                sep_x5_kernel<192, false><<<g, X5_THREADS, X5Layout<192>::SMEM, st>>>(om, xp);
+            } else if (l.n_split > 0) {
+                GSC_TRY((configure_x5<256, true>()));
+                sep_x5_kernel<256, true><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(om, xp);
+            } else {
+                GSC_TRY((configure_x5<256, false>()));
+                sep_x5_kernel<256, false><<<g, X5_THREADS, X5Layout<256>::SMEM, st>>>(om, xp);
+            }
+            GSC_CUDA(cudaGetLastError());
+            if (a.on_rows)
+                GSC_TRY((*a.on_rows)(l.m0 * BM, std::min<int64_t>(l.m1 * BM, rows_total)));
         }
     } else {
         tl.begin(bf16 ? K_SEP_TC_BF16 : K_SEP_TC_F16);
