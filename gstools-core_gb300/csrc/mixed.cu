@@ -32,6 +32,7 @@
 
 #include <algorithm>
 
+#include "dfturns.cuh"
 #include "internal.h"
 
 namespace gsc {
@@ -47,15 +48,6 @@ constexpr int kMxTile = 32;          // modes per FP32 accumulation tile
 constexpr int kMxRec = 20;
 constexpr int kMxRot = 12;           // offset of the rotated pairs
 constexpr int kMxRec64 = 4;          // doubles per mode (FP64-phase variant): kappa0..2, -
-constexpr double kInv2Pi = 0.15915494309189535;   // fl(1 / (2 pi))
-constexpr float kTwoPiF = 6.2831854820251465f;     // fl32(2 pi)
-constexpr float kRoundF = 12582912.0f;             // 1.5 * 2^23: x + kRoundF rounds x
-
-// sin(2 pi f) = f * S(f^2), cos(2 pi f) = C(f^2) on |f| <= 1/8 (fitted here)
-constexpr float kS0 = 6.2831854820251465f, kS1 = -41.34170150756836f, kS2 = 81.60517883300781f,
-                kS3 = -76.6958236694336f, kS4 = 41.41468811035156f;
-constexpr float kC0 = 1.0f, kC1 = -19.739208221435547f, kC2 = 64.93931579589844f,
-                kC3 = -85.44285583496094f, kC4 = 59.220428466796875f;
 
 __device__ __forceinline__ void mixed_mode_entry(const double *__restrict__ cov, double z1j,
                                                  double z2j, int64_t dim, int64_t n_modes,
@@ -139,16 +131,8 @@ __global__ void batch_mixed_table_kernel(const BatchItem *__restrict__ items,
 // rotation by q quarter turns is taken from the mode's rotated weight pairs
 // `ab` (indexed by q mod 4) instead of permuting and negating sin and cos.
 __device__ __forceinline__ float mixed_term(float th, float tl, const float2 *ab) {
-    const float qf = fmaf(th, 4.0f, kRoundF);
-    const float q = qf - kRoundF;
-    const int qi = __float_as_int(qf);                       // low bits: q mod 4
-    const float f = fmaf(q, -0.25f, th);                     // exact, |f| <= 1/8
-    const float f2 = f * f;
-    float s = fmaf(fmaf(fmaf(fmaf(kS4, f2, kS3), f2, kS2), f2, kS1), f2, kS0) * f;
-    float c = fmaf(fmaf(fmaf(fmaf(kC4, f2, kC3), f2, kC2), f2, kC1), f2, kC0);
-    const float tw = tl * kTwoPiF;                           // first-order low-part correction
-    const float s1 = fmaf(tw, c, s);
-    const float c1 = fmaf(-tw, s, c);
+    float s1, c1;
+    const int qi = sincos_turns_reduced(th, tl, s1, c1);    // low bits: q mod 4
     const float2 w = ab[qi & 3];
     return fmaf(w.x, c1, w.y * s1);
 }

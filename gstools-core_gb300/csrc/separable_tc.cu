@@ -43,6 +43,7 @@
 #include <cmath>
 #include <mutex>
 
+#include "dfturns.cuh"
 #include "internal.h"
 #include "sm100.cuh"
 
@@ -166,6 +167,11 @@ struct TabArgs {
     int tiled;                   // x5 form: B table and G stored as contiguous stage blocks
     int kbt;                     // x5 form: k-blocks (16 modes each)
     int bn;                      // x5 form: G rows per stage block (tile width)
+    // x5 form: FP32 inputs of the tables (sep_x5_split_kernel): per mode
+    // kRecX5 floats, per axis point an (hi, lo) pair, axes b | m | n
+    float *mrec;
+    float2 *axs;
+    int ax_off_m, ax_off_n;      // first m / n point in axs (b starts at 0)
 };
 
 // s_a[j] = (z1_j - i z2_j) e^{i k_x,j X_a} (3-D) or z1_j - i z2_j (2-D), times
@@ -564,8 +570,117 @@ __device__ void wnorm_block(const double *__restrict__ z1, const double *__restr
     }
 }
 
+// ---- FP32 factor tables of the x5 form ------------------------------------
+// Per mode j (kRecX5 floats): kappa_d = k_d / 2 pi as hi, lo (d = 0..2), z1
+// and z2 as hi, lo, the projector weights of the incompressible field
+// (src/field.rs:138-152; 1 for the scalar field) as hi, lo.  Per axis point:
+// x as hi, lo.  With these the tables need no FP64 arithmetic (cis_tab and
+// compensated FP32 products), at the accuracy of the FP64 recipe.
+constexpr int kRecX5 = 16;   // kh0-2 kl0-2 z1h z2h z1l z2l wh0-2 wl0-2
+
+__global__ void __launch_bounds__(256) sep_x5_split_kernel(TabArgs t, int64_t n_ax) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < t.n_modes) {
+        const int j = static_cast<int>(i);
+        float *r = t.mrec + static_cast<int64_t>(j) * kRecX5;
+        double k[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (d < t.dim) k[d] = t.cov[d * t.n_modes + j];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double kap = k[d] * kInv2Pi;
+            const float hi = __double2float_rn(kap);
+            r[d] = hi;
+            r[3 + d] = __double2float_rn(kap - static_cast<double>(hi));
+        }
+        const double z1 = t.z1[j], z2 = t.z2[j];
+        r[6] = __double2float_rn(z1);
+        r[7] = __double2float_rn(z2);
+        r[8] = __double2float_rn(z1 - static_cast<double>(r[6]));
+        r[9] = __double2float_rn(z2 - static_cast<double>(r[7]));
+        double w[3] = {1.0, 1.0, 1.0};
+        if (t.incompr) {
+            double kk = 0.0;
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if (d < t.dim) kk = __dadd_rn(kk, __dmul_rn(k[d], k[d]));
+            const double k_2 = __ddiv_rn(k[0], kk);
+            w[0] = __dadd_rn(1.0, -__dmul_rn(k[0], k_2));
+            w[1] = -__dmul_rn(k[1], k_2);
+            w[2] = -__dmul_rn(k[2], k_2);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float h = __double2float_rn(w[c]);
+            r[10 + c] = h;
+            r[13 + c] = __double2float_rn(w[c] - static_cast<double>(h));
+        }
+        return;
+    }
+    const int64_t a = i - t.n_modes;
+    if (a >= n_ax) return;
+    double x;
+    if (a < t.ax_off_m) x = t.ax_b[a];
+    else if (a < t.ax_off_n) x = t.ax_m[a - t.ax_off_m];
+    else x = t.ax_n[a - t.ax_off_n];
+    const float hi = __double2float_rn(x);
+    t.axs[a] = make_float2(hi, __double2float_rn(x - static_cast<double>(hi)));
+}
+
+// e^{i k x} for the mode component (kh, kl) (turns) and the axis point
+// (xh, xl): FP32 pairs while |kappa x| < 2^22 turns, else the FP64
+// reduction on k and x themselves.
+__device__ __forceinline__ float2 cis_tab(float kh, float kl, float2 x, const double *k,
+                                          const double *xd) {
+    if (fabsf(kh * x.x) < 4194304.0f) return cis_turns_acc(kh, kl, x.x, x.y);
+    return cis_f32(*k * *xd);
+}
+
+// a * b + c * d for FP32 pairs a, c (hi, lo) and FP32 b, d, to about half
+// an FP32 ulp: exact products of the high parts, TwoSum, small terms added
+__device__ __forceinline__ float dot2_pair(float ah, float al, float b, float ch, float cl, float d) {
+    const float p1 = ah * b, e1 = fmaf(ah, b, -p1);
+    const float p2 = ch * d, e2 = fmaf(ch, d, -p2);
+    const float s = p1 + p2;
+    const float bb = s - p1;
+    const float es = (p1 - (s - bb)) + (p2 - bb);
+    return s + (es + (e1 + e2) + fmaf(al, b, cl * d));
+}
+
+// s_a[j] = (z1_j - i z2_j) e^{i k_x,j X_a} (3-D) or z1_j - i z2_j (2-D), FP32
+__device__ __forceinline__ void svec_x5_entry(const TabArgs &t, int64_t i) {
+    const int b = static_cast<int>(i / t.n_modes), j = static_cast<int>(i % t.n_modes);
+    const float *r = t.mrec + static_cast<int64_t>(j) * kRecX5;
+    float2 w = make_float2(__double2float_rn(t.z1[j]), __double2float_rn(-t.z2[j]));
+    if (t.dim == 3) {
+        const float2 e = cis_tab(r[0], r[3], t.axs[b], t.cov + j, t.ax_b + b);
+        // (z1 - i z2) e with z1, z2 as FP32 pairs, rounded about once
+        w = make_float2(dot2_pair(r[6], r[8], e.x, r[7], r[9], e.y),
+                        dot2_pair(r[6], r[8], e.y, -r[7], -r[9], e.x));
+    }
+    t.svec[i] = w;
+}
+
+// B table of the x5 form: per k-block of 16 modes [nm rows][16 modes] float2,
+// the row's 16-byte chunk c (modes 2c, 2c+1) at position c ^ (m & 7)
+__device__ __forceinline__ void btab_x5_entry(const TabArgs &t, int64_t i) {
+    const int e = static_cast<int>(i & 15);
+    const int64_t row = i >> 4;                      // kb * nm + m
+    const int m = static_cast<int>(row % t.nm_ld);
+    const int kb = static_cast<int>(row / t.nm_ld);
+    const int j = kb * 16 + ((((e >> 1) ^ (m & 7)) << 1) | (e & 1));
+    float2 v = make_float2(0.f, 0.f);
+    if (m < t.nm && j < t.n_modes) {
+        const float *r = t.mrec + static_cast<int64_t>(j) * kRecX5;
+        v = cis_tab(r[t.km_dim], r[3 + t.km_dim], t.axs[t.ax_off_m + m],
+                    t.cov + t.km_dim * t.n_modes + j, t.ax_m + m);
+    }
+    t.btab[i] = v;
+}
+
 // G table of the x5 form.  Element (component c, rows 8g .. 8g+7 of the
-// column axis, mode j): the projector weight is formed once for the 8 rows.
+// column axis, mode j): the mode's record is read once for the 8 rows.
 // G1 on the 11-bit integer grid (units of 2^15 / 2^10 = 32), G2 the f16 rest;
 // stored as contiguous stage blocks, one per (tile of t.bn rows, k-block of
 // 16 modes), already in the 64-byte-swizzled K-major layout the MMA reads:
@@ -596,29 +711,27 @@ __device__ __forceinline__ void gtab_x5_entry(const TabArgs &t, int64_t i) {
         nrows = min(kGtabRows, t.ncn_pad - row0);
     }
     const bool live = c < t.ncomp && j < t.n_modes;
-    double pw = 1.0;
-    if (live && t.incompr) {
-        // projector weight, as the reference forms it (src/field.rs:138-152)
-        double kk = 0.0;
-        for (int d = 0; d < t.dim; ++d) {
-            const double kd = t.cov[d * t.n_modes + j];
-            kk = __dadd_rn(kk, __dmul_rn(kd, kd));
+    float pwh = 1.0f, pwl = 0.f, kh = 0.f, kl = 0.f;
+    if (live) {
+        const float *rec = t.mrec + static_cast<int64_t>(j) * kRecX5;
+        if (t.incompr) {                       // projector weight (src/field.rs:138-152)
+            pwh = rec[10 + c];
+            pwl = rec[13 + c];
         }
-        const double k0 = t.cov[j];
-        const double k_2 = __ddiv_rn(k0, kk);
-        pw = (c == 0) ? __dadd_rn(1.0, -__dmul_rn(k0, k_2))
-                      : -__dmul_rn(t.cov[c * t.n_modes + j], k_2);
+        kh = rec[t.kn_dim];
+        kl = rec[3 + t.kn_dim];
     }
-    const double kn = live ? t.cov[t.kn_dim * t.n_modes + j] : 0.0;
     const float gs = static_cast<float>(1 << (kLeadBitsG - 1)), gu = kUnit / gs;
     const int kb = j / 16, jl = j % 16;
     for (int u = 0; u < nrows; ++u) {
         const int row = row0 + u;
         float re = 0.f, im = 0.f;
         if (live) {
-            const float2 e = cis_f32(kn * t.ax_n[row - c * t.nn]);
-            re = static_cast<float>(pw * e.x);
-            im = static_cast<float>(-(pw * e.y));
+            const int n = row - c * t.nn;
+            const float2 e = cis_tab(kh, kl, t.axs[t.ax_off_n + n], t.cov + t.kn_dim * t.n_modes + j,
+                                     t.ax_n + n);
+            re = fmaf(pwh, e.x, pwl * e.x);
+            im = -fmaf(pwh, e.y, pwl * e.y);
         }
         const float g1r = rintf(re * gs) * gu, g1i = rintf(im * gs) * gu;
         const __half2 h1 = __floats2half2_rn(g1r, g1i);
@@ -643,12 +756,12 @@ sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) 
     int64_t i = static_cast<int64_t>(blockIdx.x - 1) * 256 + threadIdx.x;
     const int64_t b_svec = (n_svec + 255) / 256 * 256, b_btab = (n_btab + 255) / 256 * 256;
     if (i < b_svec) {
-        if (i < n_svec) svec_entry(t, i, 1.0);
+        if (i < n_svec) svec_x5_entry(t, i);
         return;
     }
     i -= b_svec;
     if (i < b_btab) {
-        if (i < n_btab) btab_entry(t, i);
+        if (i < n_btab) btab_x5_entry(t, i);
         return;
     }
     i -= b_btab;
@@ -1341,7 +1454,12 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const size_t off_ws = align_up(off_glo + g_bytes, 1024);
     const size_t ws_bytes = static_cast<size_t>(n_split) * ksplit * bnx * BM * sizeof(float);
     const size_t off_cnt = align_up(off_ws + ws_bytes, 1024);
-    const size_t total = off_cnt + static_cast<size_t>(n_split) * sizeof(int) + 256;
+    // x5: FP32 mode records and axis splits for the tables
+    const int ax_off_m = dim == 3 ? nb : 0, ax_off_n = ax_off_m + nm;
+    const int64_t n_ax = static_cast<int64_t>(ax_off_n) + nn;
+    const size_t off_mrec = align_up(off_cnt + static_cast<size_t>(n_split) * sizeof(int), 1024);
+    const size_t off_axs = align_up(off_mrec + (x5 ? sizeof(float) * kRecX5 * static_cast<size_t>(N) : 0), 1024);
+    const size_t total = off_axs + (x5 ? sizeof(float2) * static_cast<size_t>(n_ax) : 0) + 256;
     GSC_TRY(ensure_dev(ctx, ctx.scratch, total));
     GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
     unsigned char *base = static_cast<unsigned char *>(ctx.scratch.ptr);
@@ -1375,6 +1493,10 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.tiled = x5 ? 1 : 0;
     t.kbt = KB;
     t.bn = bnx;
+    t.mrec = reinterpret_cast<float *>(base + off_mrec);
+    t.axs = reinterpret_cast<float2 *>(base + off_axs);
+    t.ax_off_m = ax_off_m;
+    t.ax_off_n = ax_off_n;
 
     {
         TimedLaunch tl(st);
@@ -1385,6 +1507,8 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             const int64_t ng = gtab_x5_groups(ncomp, nn, ncn_pad) * (k_pad / 2);
             const int64_t blocks = 1 + (n1 + 255) / 256 + (n2 + 255) / 256 + (ng + 255) / 256;
             if (blocks > 0x7fffffff) return set_error(GSC_ERR_INVALID, "tables too large");
+            const int64_t ns = N + n_ax;
+            sep_x5_split_kernel<<<static_cast<unsigned>((ns + 255) / 256), 256, 0, st>>>(t, n_ax);
             sep_x5_tables_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(t, n1, n2, ng);
         } else {
             if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
