@@ -679,14 +679,14 @@ __device__ __forceinline__ void btab_x5_entry(const TabArgs &t, int64_t i) {
     t.btab[i] = v;
 }
 
-// G table of the x5 form.  Element (component c, rows 8g .. 8g+7 of the
-// column axis, mode j): the mode's record is read once for the 8 rows.
+// G table of the x5 form.  Element (component c, rows kGtabRows g .. of the
+// column axis, mode j): the mode's record is read once for those rows.
 // G1 on the 11-bit integer grid (units of 2^15 / 2^10 = 32), G2 the f16 rest;
 // stored as contiguous stage blocks, one per (tile of t.bn rows, k-block of
 // 16 modes), already in the 64-byte-swizzled K-major layout the MMA reads:
 // row r at r * 64 bytes, 16-byte chunk c at c ^ ((r >> 1) & 3).
-constexpr int kGtabRows = 8;
-// groups of kGtabRows rows: ncomp * ceil(nn / 8) real ones, then the zero
+constexpr int kGtabRows = 2;
+// groups of kGtabRows rows: ncomp * ceil(nn / kGtabRows) real ones, then the zero
 // padding rows [ncomp * nn, ncn_pad)
 __host__ __device__ __forceinline__ int64_t gtab_x5_groups(int ncomp, int nn, int ncn_pad) {
     const int64_t real = static_cast<int64_t>(ncomp) * ((nn + kGtabRows - 1) / kGtabRows);
@@ -746,7 +746,8 @@ __device__ __forceinline__ void gtab_x5_entry(const TabArgs &t, int64_t i) {
 }
 
 // All tables of the x5 form in one launch: block 0 the normaliser, then
-// blocks of s-vector, B-table and G-table elements.
+// blocks of G-table (several rows per thread: scheduled first), s-vector and
+// B-table elements.
 __global__ void __launch_bounds__(256)
 sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) {
     if (blockIdx.x == 0) {
@@ -754,18 +755,18 @@ sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) 
         return;
     }
     int64_t i = static_cast<int64_t>(blockIdx.x - 1) * 256 + threadIdx.x;
-    const int64_t b_svec = (n_svec + 255) / 256 * 256, b_btab = (n_btab + 255) / 256 * 256;
+    const int64_t b_gtab = (n_gtab + 255) / 256 * 256, b_svec = (n_svec + 255) / 256 * 256;
+    if (i < b_gtab) {
+        if (i < n_gtab) gtab_x5_entry(t, i);
+        return;
+    }
+    i -= b_gtab;
     if (i < b_svec) {
         if (i < n_svec) svec_x5_entry(t, i);
         return;
     }
     i -= b_svec;
-    if (i < b_btab) {
-        if (i < n_btab) btab_x5_entry(t, i);
-        return;
-    }
-    i -= b_btab;
-    if (i < n_gtab) gtab_x5_entry(t, i);
+    if (i < n_btab) btab_x5_entry(t, i);
 }
 
 struct X5Params {
