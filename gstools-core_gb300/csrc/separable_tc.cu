@@ -773,12 +773,13 @@ struct X5Params {
     TcParams base;
     const float *wnorm;      // {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W}
     const unsigned char *g1, *g2, *bt;   // stage blocks (see the table kernels)
-    // Tail split: tiles [0, full_tiles) run whole, one per CTA; each later
-    // tile runs as ksplit CTAs over consecutive parts of its k-blocks, whose
+    // Tail split: tiles [0, full_tiles) run whole, one per CTA; each of the
+    // n_split later tiles runs as ksplit CTAs (the launch's first n_split *
+    // ksplit blocks) over consecutive parts of its k-blocks, whose
     // FP32 partials meet in `ws` ([slot][part][column][row]); the last part
     // to finish (counted in ws_cnt[slot]) adds them in part order and stores.
     int tile0;               // first tile of this launch (launches of wave-sized row ranges)
-    int full_tiles, ksplit;
+    int full_tiles, ksplit, n_split;
     float *ws;
     int *ws_cnt;
     // 2 or 3: the output is written by tiled bulk stores through the kernel's
@@ -872,9 +873,12 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     // Rows are the nb * nm (x-slice, y) pairs taken in order, so a 128-row
     // tile may span two or more slices and no slice pads a partial tile.
     // a launch without split tiles compiles the split path out
-    const int u = static_cast<int>(blockIdx.x) - xp.full_tiles;
-    const bool split = SPLIT && u >= 0;
-    const int tile = xp.tile0 + (split ? xp.full_tiles + u / xp.ksplit : static_cast<int>(blockIdx.x));
+    // the parts of split tiles come first, so that they finish early and the
+    // SMs of the first wave do not all reach their epilogues at once
+    const int u = static_cast<int>(blockIdx.x);
+    const int n_parts = SPLIT ? xp.n_split * xp.ksplit : 0;
+    const bool split = SPLIT && u < n_parts;
+    const int tile = xp.tile0 + (split ? xp.full_tiles + u / xp.ksplit : u - n_parts);
     const int part = split ? u % xp.ksplit : 0;
     const int kbeg = split ? static_cast<int>(static_cast<int64_t>(part) * p.kb_total / xp.ksplit) : 0;
     const int KB = split ? static_cast<int>(static_cast<int64_t>(part + 1) * p.kb_total / xp.ksplit) - kbeg
@@ -1593,6 +1597,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             xp.tile0 = static_cast<int>(l.m0 * n_tiles);
             xp.full_tiles = static_cast<int>(l.full_tiles);
             xp.ksplit = l.ksplit;
+            xp.n_split = static_cast<int>(l.n_split);
             if (l.n_split > 0)
                 GSC_CUDA(cudaMemsetAsync(xp.ws_cnt, 0, static_cast<size_t>(l.n_split) * sizeof(int), st));
             const unsigned g = static_cast<unsigned>(l.full_tiles + l.n_split * l.ksplit);
