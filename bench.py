@@ -407,36 +407,8 @@ def run_ours(args, world, rank, local):
                     "reference": "oracle (field.rs restatement), FP64"}
         err = check(out_d)
 
-    # ---- the other forms on the same workload (one timed step each) -------
-    others = {}
-    for oform in ([] if args.no_plain else other_forms(w, form)):
-        ostep, oout = make_device_step(gsc, torch, w, oform, dev, stream)
-        ostep()
-        torch.cuda.synchronize()
-        ot, ok_, _ = timed_steps(torch, gsc, ostep, stream, 2, flush)
-        gsc.device_status()
-        oms = max_over_ranks(world, float(np.mean(ot)))
-        others[oform] = {"value": work * world / (oms * 1e-3) / 1e9, "unit": UNIT,
-                         "ms_per_step": oms,
-                         "kernels_ms": {k: float(np.mean(v)) for k, v in ok_.items()},
-                         "error_vs_oracle": check(oout) if check else None}
-        del oout
-
-    # ---- the plain FP64 kernel on the same workload (the comparison arm) ---
-    plain = None
-    if form != "plain" and not args.no_plain:
-        pstep, _ = make_device_step(gsc, torch, w, "plain", dev, stream)
-        pstep()
-        torch.cuda.synchronize()
-        pt, pk, _ = timed_steps(torch, gsc, pstep, stream, 1, flush)
-        pms = max_over_ranks(world, float(np.mean(pt)))
-        plain = {"value": work * world / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
-                 "steps": 1, "path": "plain FP64 kernel on the flattened meshgrid"
-                 if w["pos"] is None else "plain FP64 kernel",
-                 "kernels_ms": {k: float(np.mean(v)) for k, v in pk.items()}}
-        plain["speedup_of_chosen_form"] = value / plain["value"]
-
-    # ---- e2e through the public host API -----------------------------------
+    # ---- e2e through the public host API (before the long comparison arms,
+    # so that it runs in the same state of the GPU as the timed steps) ------
     e2e = None
     if not args.no_e2e:
         nout = w["dim"] if w["incompr"] else 1
@@ -483,6 +455,35 @@ def run_ours(args, world, rank, local):
                   "h2d_bytes_per_step": int((w["cov"].size + 2 * N + flat.size) * 8),
                   "d2h_bytes_per_step": int((w["dim"] if w["incompr"] else 1) * P * 8)}
         del flat
+
+    # ---- the other forms on the same workload (one timed step each) -------
+    others = {}
+    for oform in ([] if args.no_plain else other_forms(w, form)):
+        ostep, oout = make_device_step(gsc, torch, w, oform, dev, stream)
+        ostep()
+        torch.cuda.synchronize()
+        ot, ok_, _ = timed_steps(torch, gsc, ostep, stream, 2, flush)
+        gsc.device_status()
+        oms = max_over_ranks(world, float(np.mean(ot)))
+        others[oform] = {"value": work * world / (oms * 1e-3) / 1e9, "unit": UNIT,
+                         "ms_per_step": oms,
+                         "kernels_ms": {k: float(np.mean(v)) for k, v in ok_.items()},
+                         "error_vs_oracle": check(oout) if check else None}
+        del oout
+
+    # ---- the plain FP64 kernel on the same workload (the comparison arm) ---
+    plain = None
+    if form != "plain" and not args.no_plain:
+        pstep, _ = make_device_step(gsc, torch, w, "plain", dev, stream)
+        pstep()
+        torch.cuda.synchronize()
+        pt, pk, _ = timed_steps(torch, gsc, pstep, stream, 1, flush)
+        pms = max_over_ranks(world, float(np.mean(pt)))
+        plain = {"value": work * world / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
+                 "steps": 1, "path": "plain FP64 kernel on the flattened meshgrid"
+                 if w["pos"] is None else "plain FP64 kernel",
+                 "kernels_ms": {k: float(np.mean(v)) for k, v in pk.items()}}
+        plain["speedup_of_chosen_form"] = value / plain["value"]
 
     # ---- CPU baseline (rank 0, N=1 only) -----------------------------------
     cpu = None
@@ -641,6 +642,25 @@ def run_ours_batch(args, world, rank, local):
                "points_checked": "512 per realization of 0, 1, 100, 255, 256, 301, 511",
                "reference": "oracle (field.rs restatement), FP64"}
 
+    # e2e through the host-array API (before the plain FP64 arm, so that it runs
+    # in the same state of the GPU as the timed steps)
+    e2e = None
+    if not args.no_e2e:
+        host = [{"kind": "scalar", "cov": it["cov"], "z1": it["z1"], "z2": it["z2"],
+                 "pos": it["pos"]} for it in items]
+        gsc.summate_batch(host, form=form)          # plan + tuning + staging buffers
+        ts = []
+        for _ in range(max(1, min(args.steps, 3))):
+            barrier(world)
+            t0 = time.perf_counter()
+            gsc.summate_batch(host, form=form)
+            ts.append(time.perf_counter() - t0)
+        t_e2e = max_over_ranks(world, float(np.mean(ts)))
+        e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes),
+               "ms_per_step": t_e2e * 1e3, "api": "gstools_core.summate_batch",
+               "timing": "host wall clock around the synchronous call"}
+
     # the plain FP64 form of the same ensemble (one graph step)
     plain = None
     if not args.no_plain and form != "plain":
@@ -659,24 +679,6 @@ def run_ours_batch(args, world, rank, local):
                  "steps": 1, "path": "persistent FP64 batch kernel", "config": pplan.config}
         plain["speedup_of_chosen_form"] = value / plain["value"]
         pplan.close()
-
-    # e2e through the host-array API
-    e2e = None
-    if not args.no_e2e:
-        host = [{"kind": "scalar", "cov": it["cov"], "z1": it["z1"], "z2": it["z2"],
-                 "pos": it["pos"]} for it in items]
-        gsc.summate_batch(host, form=form)          # plan + tuning + staging buffers
-        ts = []
-        for _ in range(max(1, min(args.steps, 3))):
-            barrier(world)
-            t0 = time.perf_counter()
-            gsc.summate_batch(host, form=form)
-            ts.append(time.perf_counter() - t0)
-        t_e2e = max_over_ranks(world, float(np.mean(ts)))
-        e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
-               "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes),
-               "ms_per_step": t_e2e * 1e3, "api": "gstools_core.summate_batch",
-               "timing": "host wall clock around the synchronous call"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
