@@ -4,8 +4,9 @@
 // (src/lib.rs:47,64: into_pyarray_bound).  A fresh array of fresh pages
 // costs a page fault per page on first touch, which for a 134 MB field takes
 // several times longer than the GPU computing it.  The Python layer
-// therefore allocates result arrays of 1 MiB and more from this pool: blocks
-// of pinned (page-locked, always resident) host memory, rounded up to 2 MiB,
+// therefore allocates result arrays of 64 KiB and more from this pool: blocks
+// of pinned (page-locked, always resident) host memory, rounded up to 64 KiB
+// (2 MiB above 2 MiB),
 // handed back to the pool when the last view of the array dies and reused by
 // the next result of the same rounded size.  The device-to-host copy then
 // runs at the link's speed with no fault on either side.
@@ -26,7 +27,13 @@
 namespace gsc {
 namespace {
 
-constexpr size_t kGrain = size_t(2) << 20;
+constexpr size_t kGrain = size_t(2) << 20;        // blocks above 2 MiB: 2 MiB multiples
+constexpr size_t kSmallGrain = size_t(64) << 10;  // up to 2 MiB: 64 KiB multiples
+
+size_t round_block(size_t bytes) {
+    const size_t g = bytes <= kGrain ? kSmallGrain : kGrain;
+    return (bytes + g - 1) / g * g;
+}
 
 struct HostPool {
     std::mutex mu;
@@ -73,7 +80,7 @@ int gsc_host_alloc(int64_t bytes, void **ptr) {
     *ptr = nullptr;
     if (bytes <= 0) return set_error(GSC_ERR_INVALID, "bytes must be positive");
     if (bytes > (int64_t(1) << 42)) return set_error(GSC_ERR_INVALID, "bytes too large");
-    const size_t rounded = (static_cast<size_t>(bytes) + kGrain - 1) / kGrain * kGrain;
+    const size_t rounded = round_block(static_cast<size_t>(bytes));
     HostPool &hp = pool();
     {
         std::lock_guard<std::mutex> lk(hp.mu);

@@ -27,7 +27,6 @@ from __future__ import annotations
 
 import ctypes
 import operator
-import weakref
 
 import numpy as np
 
@@ -82,11 +81,11 @@ def _strides(a: np.ndarray):
     return tuple(s // a.itemsize for s in a.strides)
 
 
-_POOL_MIN_BYTES = 1 << 20
+_POOL_MIN_BYTES = 1 << 16
 
 
 def _result(shape, order="C") -> np.ndarray:
-    """A new float64 result array.  From 1 MiB up its memory comes from the
+    """A new float64 result array.  From 64 KiB up its memory comes from the
     library's pool of pinned host blocks, which takes the block back when the
     array and every view of it are gone: repeated calls reuse resident pages
     instead of faulting in fresh ones (the result is still a new array each
@@ -98,10 +97,37 @@ def _result(shape, order="C") -> np.ndarray:
     if nbytes >= _POOL_MIN_BYTES:
         ptr = ctypes.c_void_p()
         if _native.lib.gsc_host_alloc(nbytes, ctypes.byref(ptr)) == 0:
-            buf = (ctypes.c_char * nbytes).from_address(ptr.value)
-            weakref.finalize(buf, _native.lib.gsc_host_free, ptr.value).atexit = False
-            return np.ndarray(shape, dtype=np.float64, buffer=buf, order=order)
+            return np.asarray(_PoolBlock(ptr.value, shape, order))
     return np.empty(shape, dtype=np.float64, order=order)
+
+
+class _PoolBlock:
+    """Owner of a pinned pool block, exposed to numpy as a float64 array
+    (the array's base): the block returns to the pool when the last array
+    or view referring to it is gone."""
+    __slots__ = ("ptr", "__array_interface__")
+    _free = _native.lib.gsc_host_free
+
+    def __init__(self, ptr, shape, order):
+        shape = tuple(shape) if isinstance(shape, tuple) else (int(shape),)
+        strides = None
+        if order == "F" and len(shape) > 1:
+            strides, step = [], 8
+            for s in shape:
+                strides.append(step)
+                step *= int(s)
+            strides = tuple(strides)
+        self.ptr = ptr
+        self.__array_interface__ = {"data": (ptr, False), "shape": shape, "typestr": "<f8",
+                                    "strides": strides, "version": 3}
+
+    def __del__(self):
+        if self.ptr:
+            try:
+                _PoolBlock._free(self.ptr)
+            except Exception:      # interpreter teardown: the OS reclaims the block
+                pass
+            self.ptr = None
 
 
 def host_pool_stats() -> dict:

@@ -133,7 +133,8 @@ int gsc_device_status(int32_t device);
 int gsc_release_buffers(int32_t device);
 
 /* Pinned host blocks for result arrays.  gsc_host_alloc returns a block of
- * page-locked host memory of at least `bytes` (rounded up to 2 MiB), taken
+ * page-locked host memory of at least `bytes` (rounded up to a multiple of
+ * 64 KiB, or of 2 MiB above 2 MiB), taken
  * from the pool's free blocks of that rounded size when there is one;
  * gsc_host_free hands it back (the pool keeps up to GSC_HOST_POOL_MB MiB of
  * free blocks, default 8192, and releases the rest); gsc_host_pool_trim

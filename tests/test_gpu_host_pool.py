@@ -1,7 +1,7 @@
 """Result arrays from the pinned host pool (GPU tests).
 
 Host-array calls return new arrays, as the reference does (src/lib.rs:47,
-64); from 1 MiB up their memory is a pinned block of the library's pool,
+64); from 64 KiB up their memory is a pinned block of the library's pool,
 handed back when the array and all its views are gone.  Checked here: the
 results are right (against the oracle), a dropped result's block is reused
 by the next call of that size, a surviving view keeps its block (a later
@@ -71,7 +71,7 @@ def test_incompr_and_structured_results(gsc):
 
 
 def test_small_results_are_plain_arrays(gsc):
-    cov, z1, z2, pos = _case(5, p=1000)
+    cov, z1, z2, pos = _case(5, p=1000)          # 8 KB: below the pool's 64 KiB
     gc.collect()
     before = gsc.host_pool_stats()["live_bytes"]
     a = gsc.summate(cov, z1, z2, pos, form="plain")
