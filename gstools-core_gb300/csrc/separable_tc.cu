@@ -121,6 +121,20 @@ __device__ __forceinline__ double f32_to_f64(float f) {
     return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
+// f32_to_f64(f * 2^k) for |k| small enough that no finite product leaves
+// the normal FP64 range: the power of two is added to the exponent
+// (ebias = (896 + k) << 20), so the scaling costs nothing and stays exact.
+// FP32 zeros and subnormals give signed zeros, Inf and NaN stay Inf and NaN.
+__device__ __forceinline__ double f32_to_f64_pow2(float f, uint32_t ebias) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t a = u & 0x7FFFFFFFu, sign = u & 0x80000000u;
+    uint32_t hi = ((a >> 3) + ebias) | sign;
+    hi = a >= 0x7F800000u ? (sign | 0x7FF00000u | ((a & 0x7FFFFFu) >> 3) | (a > 0x7F800000u ? 0x80000u : 0u))
+                          : hi;
+    const bool tiny = a < 0x00800000u;
+    return __hiloint2double(static_cast<int>(tiny ? sign : hi), static_cast<int>(tiny ? 0u : u << 29));
+}
+
 template <bool BF16>
 struct Split;
 template <>
@@ -1149,6 +1163,12 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         // where the output layout does not allow those, they are turned
         // around in shared memory and each lane stores one column.
         const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
+        // unscale is a power of two (W and 2^30 are): as a normal FP32
+        // number its exponent goes into the conversion (else the product is
+        // formed first)
+        const int uexp = static_cast<int>((__float_as_uint(unscale) >> 23) & 0xFF);
+        const bool pow2 = uexp > 0 && uexp < 255 && (__float_as_uint(unscale) & 0x7FFFFFu) == 0;
+        const uint32_t ebias = static_cast<uint32_t>(uexp - 127 + 896) << 20;
         float *trf = reinterpret_cast<float *>(smem) + warp * (32 * 33);
         // output offset of row (warp's first row) + R; the warp's first row
         // is slice bs0, row ms0
@@ -1193,7 +1213,8 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                     for (int c = 0; c < 8; ++c) {
                         const int t = 32 * g + 16 * hb + 2 * c;
                         *reinterpret_cast<double2 *>(bx + hb * 4096 + lane * 128 + ((c ^ (lane & 7)) << 4)) =
-                            make_double2(f32_to_f64(tot[t] * unscale), f32_to_f64(tot[t + 1] * unscale));
+                            pow2 ? make_double2(f32_to_f64_pow2(tot[t], ebias), f32_to_f64_pow2(tot[t + 1], ebias))
+                                 : make_double2(f32_to_f64(tot[t] * unscale), f32_to_f64(tot[t + 1] * unscale));
                     }
                 fence_proxy_async_smem();
                 __syncwarp();
