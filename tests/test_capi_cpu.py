@@ -134,3 +134,19 @@ def test_no_device_fails_loudly(gsc):
         gsc.summate(cov, z1, z2, pos)
     with pytest.raises(gsc.GscError, match="no usable CUDA device"):
         gsc.summate_incompr(cov, z1, z2, pos)
+
+
+def test_result_pool_without_device(gsc):
+    """Without a device the pinned pool cannot allocate: results fall back to
+    ordinary numpy arrays, and the pool's bookkeeping calls still answer."""
+    import ctypes
+    from gstools_core import _native
+    if gsc.device_count() > 0:
+        pytest.skip("a CUDA device is present")
+    a = gsc._result((3, 100_000), order="F")
+    assert a.flags.owndata and a.flags.f_contiguous and a.shape == (3, 100_000)
+    ptr = ctypes.c_void_p()
+    assert _native.lib.gsc_host_alloc(1 << 20, ctypes.byref(ptr)) == _native.GSC_ERR_NO_DEVICE
+    assert _native.lib.gsc_host_free(None) == 0
+    assert gsc.host_pool_stats() == {"live_bytes": 0, "cached_bytes": 0}
+    gsc.host_pool_trim()
