@@ -33,6 +33,11 @@
 //   warp  8    TMA: loads the G tiles (hi, lo) of each k-block
 //   warp  9    MMA issuer (one thread) and TMEM owner
 // Two pipeline stages of 96 KB (F hi/lo 2 x 16 KB, G hi/lo 2 x 32 KB).
+//
+// The form chosen at the 1e-6 bar, "f16x5" (sep_x5_kernel below), keeps the
+// same factorisation but sums its leading product exactly on an integer
+// grid; its precision scheme, pipeline, tail split and epilogue are
+// described with it, its FP32 factor tables with sep_x5_split_kernel.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -520,19 +525,21 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 // random modes, as GSTools draws them; a field value beyond ~12 standard
 // deviations would start rounding the main sum.)  The four cross products
 // F2G1 + F1G2 + F2G2 + F3G1 (about 2^-7 of the field) go to a second TMEM
-// accumulator that the epilogue drains every KC = 4 k-blocks into FP32
+// accumulator that the workers drain every KC = 16 k-blocks into FP32
 // totals held in registers, so their rounding never builds up at full
 // magnitude.  Representation: F to about 2^-29, G to 2^-22 relative; the
 // product F3G2 (below 2^-28) is dropped.
 //
-// Warp roles (16 warps, 512 threads launched at 128 registers each, then
-// re-split with setmaxnreg: epilogue 160, producers 152, TMA/MMA 40):
-//   warps 0-7   epilogue: warp w reads TMEM lanes 32*(w%4).., columns
-//               128*(w/4) .. +128 (cross totals live in 128 registers)
-//   warps 8-11  producers: F1, F2, F3 tiles of each k-block
-//   warp 12     TMA: G1, G2 tiles
-//   warp 13     MMA issuer and TMEM owner; warps 14-15 idle
-// Stages: F1/F2/F3 3 x 16 KB + G1/G2 2 x 32 KB = 112 KB, two stages.
+// Warp roles (12 warps, 384 threads launched at 168 registers each, then
+// re-split with setmaxnreg, X5Layout):
+//   warps 0-7   workers: warp w builds the F1, F2, F3 slices of TMEM lanes
+//               (rows) 32*(w%4).. for half the modes of each k-block, drains
+//               columns HC*(w/4) .. +HC of the cross accumulator into
+//               register totals, and writes the output in the epilogue
+//   warp 8      bulk copies: G1, G2 and the tile's B rows per k-block
+//   warp 9      MMA issuer and TMEM owner; warps 10-11 idle
+// Stages: F1/F2/F3 3 x 8 KB + G1/G2 2 x BNX * 64 B + B rows 16 KB (72 KB
+// for BNX = 256), three stages.
 // ---------------------------------------------------------------------------
 constexpr int X5_THREADS = 384;                 // 8 worker warps + 4 control warps
 constexpr int X5_LAUNCH_REGS = 168;             // 65536 / 384, rounded down to 8
