@@ -1,0 +1,39 @@
+"""bench.py's reference arm and JSON contract, on the CPU.
+
+`bench.py --impl reference` times the reference's CPU algorithm (the oracle
+restatement) on the host cores and prints one JSON line with the same
+metric, unit and workload as the GPU arm, plus `impl`, `cpu_baseline` and an
+`e2e` entry with no transfers.  Checked here for the default workload (C2)
+and C1 with a short CPU sample.
+"""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def _reference_line(*extra):
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+           "--warmup", "1", "--cpu-seconds", "0.3", *extra]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    return json.loads(lines[0])
+
+
+@pytest.mark.parametrize("workload", [None, "c1"])
+def test_reference_arm_contract(workload):
+    d = _reference_line(*([] if workload is None else ["--workload", workload]))
+    assert d["impl"] == "reference"
+    assert d["config"]["workload"] == (workload or "c2")
+    assert d["unit"] == "Gpoint*modes/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 1
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
