@@ -7,9 +7,10 @@
 // (GB300 runs FP64 at 1/64 of the FP32 rate).  sin(2 pi f), cos(2 pi f) on
 // |f| <= 1/8 come from polynomials fitted for this project (FP32
 // coefficients, max error 8.5e-8 / 5.7e-8 over the interval), corrected to
-// first order for the low part of the phase.  Used by the mixed summators
-// (mixed.cu) and the factor tables of the separable tensor-core form
-// (separable_tc.cu).
+// first order for the low part of the phase (the mixed summators,
+// mixed.cu).  The factor tables of the separable tensor-core form
+// (separable_tc.cu) take the same phase reduction and sincosf for the last
+// step (cis_turns_acc).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -42,31 +43,13 @@ __device__ __forceinline__ int sincos_turns_reduced(float th, float tl, float &s
     return __float_as_int(qf);
 }
 
-// (cos, sin) of 2 pi (kh + kl)(xh + xl): the product split exactly into its
-// rounded value and error, whole turns dropped, small terms added in FP32.
-// Valid while |kh * xh| stays below 2^22 turns (the caller checks).
-__device__ __forceinline__ float2 cis_turns(float kh, float kl, float xh, float xl) {
-    const float pr = kh * xh;
-    const float e = fmaf(kh, xh, -pr);                       // exact
-    const float a = pr - rintf(pr);                          // exact
-    const float b = fmaf(kh, xl, fmaf(kl, xh, e));
-    const float th = a + b;
-    const float tl = b - (th - a);
-    float s, c;
-    const int q = sincos_turns_reduced(th, tl, s, c);
-    switch (q & 3) {
-        case 0: return make_float2(c, s);
-        case 1: return make_float2(-s, c);
-        case 2: return make_float2(-c, -s);
-        default: return make_float2(s, -c);
-    }
-}
-
 // (cos, sin) of 2 pi (kh + kl)(xh + xl) to about the accuracy of CUDA's
-// sincosf: the reduced phase in turns (as in cis_turns) less its quarter
-// turns, turned into radians as an FP32 pair, sincosf of the high part,
-// first-order correction for the low part, rotation by the quarter turns.
-// For the factor tables, where accuracy counts more than speed.
+// sincosf: the product split exactly into its rounded value and error,
+// whole turns dropped, small terms added in FP32; the reduced phase less
+// its quarter turns turned into radians as an FP32 pair, sincosf of the
+// high part, first-order correction for the low part, rotation by the
+// quarter turns.  Valid while |kh * xh| stays below 2^22 turns (the caller
+// checks).  For factor tables, where accuracy counts more than speed.
 __device__ __forceinline__ float2 cis_turns_acc(float kh, float kl, float xh, float xl) {
     const float pr = kh * xh;
     const float e = fmaf(kh, xh, -pr);                       // exact

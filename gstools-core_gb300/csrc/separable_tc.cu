@@ -183,7 +183,6 @@ struct TabArgs {
     float2 *btab;                // [n_modes][nm]
     uint32_t *ghi, *glo;         // [ncn_pad][k_pad/2] packed (re, -im) pairs
     float *wnorm;                // x5 form: {W, 1/W}, W = 2^ceil(log2 max|z1 - i z2|)
-    int tiled;                   // x5 form: B table and G stored as contiguous stage blocks
     int kbt;                     // x5 form: k-blocks (16 modes each)
     int bn;                      // x5 form: G rows per stage block (tile width)
     // x5 form: FP32 inputs of the tables (sep_x5_split_kernel): per mode
@@ -214,25 +213,11 @@ __global__ void sep_svec_kernel(TabArgs t) {
     svec_entry(t, i, t.wnorm ? static_cast<double>(t.wnorm[1]) : 1.0);
 }
 
-// B table [n_modes][nm_ld], columns nm .. nm_ld-1 zero.  For the x5 form
-// (tiled) the values are stored per k-block of 16 modes as [nm rows][16
-// modes] float2, 128 bytes per row with the row's 16-byte chunk c (modes 2c,
-// 2c+1) at position c ^ (m & 7): any run of consecutive rows is one
-// contiguous block that a bulk copy moves into a stage unchanged, and
-// eight consecutive rows read the same logical chunk from eight different
-// bank groups.
+// B table [n_modes][nm_ld], columns nm .. nm_ld-1 zero (the f16x3 / bf16x3
+// forms; the x5 form's tiled table is btab_x5_entry).
 __device__ __forceinline__ void btab_entry(const TabArgs &t, int64_t i) {
-    int j, m;
-    if (t.tiled) {   // i walks the stored layout, so the stores are contiguous
-        const int e = static_cast<int>(i & 15);
-        const int64_t row = i >> 4;                      // kb * nm + m
-        m = static_cast<int>(row % t.nm_ld);
-        const int kb = static_cast<int>(row / t.nm_ld);
-        j = kb * 16 + ((((e >> 1) ^ (m & 7)) << 1) | (e & 1));
-    } else {
-        j = static_cast<int>(i / t.nm_ld);
-        m = static_cast<int>(i % t.nm_ld);
-    }
+    const int j = static_cast<int>(i / t.nm_ld);
+    const int m = static_cast<int>(i % t.nm_ld);
     const float2 v = (m < t.nm && j < t.n_modes)
                          ? cis_f32(t.cov[t.km_dim * t.n_modes + j] * t.ax_m[m])
                          : make_float2(0.f, 0.f);
@@ -240,10 +225,8 @@ __device__ __forceinline__ void btab_entry(const TabArgs &t, int64_t i) {
 }
 
 __global__ void sep_btab_kernel(TabArgs t) {
-    // the tiled layout also zero-fills the modes past n_modes of the last k-block
-    const int64_t nj = t.tiled ? static_cast<int64_t>(t.kbt) * 16 : t.n_modes;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= nj * t.nm_ld) return;
+    if (i >= static_cast<int64_t>(t.n_modes) * t.nm_ld) return;
     btab_entry(t, i);
 }
 
@@ -684,7 +667,12 @@ __device__ __forceinline__ void svec_x5_entry(const TabArgs &t, int64_t i) {
 }
 
 // B table of the x5 form: per k-block of 16 modes [nm rows][16 modes] float2,
-// the row's 16-byte chunk c (modes 2c, 2c+1) at position c ^ (m & 7)
+// 128 bytes per row with the row's 16-byte chunk c (modes 2c, 2c+1) at
+// position c ^ (m & 7): any run of consecutive rows is one contiguous block
+// that a bulk copy moves into a stage unchanged, and eight consecutive rows
+// read the same logical chunk from eight different bank groups.  i walks
+// the stored layout (contiguous stores); modes past n_modes of the last
+// k-block are zero.
 __device__ __forceinline__ void btab_x5_entry(const TabArgs &t, int64_t i) {
     const int e = static_cast<int>(i & 15);
     const int64_t row = i >> 4;                      // kb * nm + m
@@ -1523,7 +1511,6 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.ghi = reinterpret_cast<uint32_t *>(base + off_ghi);
     t.glo = reinterpret_cast<uint32_t *>(base + off_glo);
     t.wnorm = x5 ? reinterpret_cast<float *>(base + off_wn) : nullptr;
-    t.tiled = x5 ? 1 : 0;
     t.kbt = KB;
     t.bn = bnx;
     t.mrec = reinterpret_cast<float *>(base + off_mrec);
