@@ -43,7 +43,7 @@ const char *kernel_name(int32_t id) {
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
         "mixed_f64phase", "sep_f64_dmma", "fourier_scale", "batch_tables", "batch_plain",
-        "batch_mixed", "sample_modes",
+        "batch_mixed", "sample_modes", "sep_split",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }

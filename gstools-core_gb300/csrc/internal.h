@@ -55,6 +55,7 @@ enum KernelId : int32_t {
     K_BATCH_PLAIN = 18,    // persistent FP64 batch kernel (device work queue)
     K_BATCH_MIXED = 19,    // persistent mixed-precision batch kernel
     K_SAMPLE_MODES = 20,   // on-device spectral sampling (Philox4x32-10)
+    K_SEP_SPLIT = 21,      // FP32 inputs of the x5 factor tables
     K_COUNT
 };
 const char *kernel_name(int32_t id);

@@ -1520,7 +1520,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
 
     {
         TimedLaunch tl(st);
-        tl.begin(K_SEP_TABLES);
+        // one timing record per launch
         const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(bt_modes) * nm_ld;
         const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
         if (x5) {
@@ -1528,17 +1528,30 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
             const int64_t blocks = 1 + (n1 + 255) / 256 + (n2 + 255) / 256 + (ng + 255) / 256;
             if (blocks > 0x7fffffff) return set_error(GSC_ERR_INVALID, "tables too large");
             const int64_t ns = N + n_ax;
+            tl.begin(K_SEP_SPLIT);
             sep_x5_split_kernel<<<static_cast<unsigned>((ns + 255) / 256), 256, 0, st>>>(t, n_ax);
+            tl.end();
+            tl.begin(K_SEP_TABLES);
             sep_x5_tables_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(t, n1, n2, ng);
+            tl.end();
         } else {
-            if (n1 > 0) sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
-            if (n2 > 0) sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
+            if (n1 > 0) {
+                tl.begin(K_SEP_TABLES);
+                sep_svec_kernel<<<static_cast<unsigned>((n1 + 255) / 256), 256, 0, st>>>(t);
+                tl.end();
+            }
+            if (n2 > 0) {
+                tl.begin(K_SEP_TABLES);
+                sep_btab_kernel<<<static_cast<unsigned>((n2 + 255) / 256), 256, 0, st>>>(t);
+                tl.end();
+            }
+            tl.begin(K_SEP_TABLES);
             if (bf16)
                 sep_gtab_kernel<true><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
             else
                 sep_gtab_kernel<false><<<static_cast<unsigned>((n3 + 255) / 256), 256, 0, st>>>(t);
+            tl.end();
         }
-        tl.end();
         GSC_CUDA(cudaGetLastError());
     }
 
