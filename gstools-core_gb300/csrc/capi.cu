@@ -43,7 +43,7 @@ const char *kernel_name(int32_t id) {
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
         "mixed_f64phase", "sep_f64_dmma", "fourier_scale", "batch_tables", "batch_plain",
-        "batch_mixed", "sample_modes", "sep_split",
+        "batch_mixed", "sample_modes", "sep_split", "copy_h2d", "copy_d2h",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -627,11 +627,14 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
 
     double *h = static_cast<double *>(ctx->pinned);
     double *d = static_cast<double *>(ctx->io.ptr);
+    TimedLaunch tc(st);
+    tc.begin(K_COPY_H2D);
     GSC_TRY(upload2(st, d, h, 0, cov, cs_d, cs_n, dim, N));
     GSC_TRY(upload2(st, d, h, n_cov, z1, 0, z1s, 1, N));
     GSC_TRY(upload2(st, d, h, n_cov + N, z2, 0, z2s, 1, N));
     if (sf) GSC_TRY(upload2(st, d, h, n_cov + 2 * N, sf, 0, sfs, 1, N));
     GSC_TRY(upload2(st, d, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P));
+    tc.end();
     if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
                                   d + n_cov + N, st));
     PlainArgs a;
@@ -651,12 +654,16 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
         Prefault pf;
         if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
         pf.join();
+        tc.begin(K_COPY_D2H);
         GSC_CUDA(cudaMemcpyAsync(out, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+        tc.end();
         GSC_CUDA(cudaStreamSynchronize(st));
         return GSC_OK;
     }
     double *ho = h + n_in;
+    tc.begin(K_COPY_D2H);
     GSC_CUDA(cudaMemcpyAsync(ho, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    tc.end();
     GSC_CUDA(cudaStreamSynchronize(st));
     for (int64_t i = 0; i < nout; ++i) {
         if (os_p == 1 && (nout == 1 || os_d == P)) {
@@ -845,6 +852,8 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out) * sizeof(double) + 1024));
     double *h = static_cast<double *>(ctx->pinned);
     double *d = static_cast<double *>(ctx->io.ptr);
+    TimedLaunch tc(st);
+    tc.begin(K_COPY_H2D);
     GSC_TRY(upload2(st, d, h, 0, cov, cs_d, cs_n, dim, N));
     GSC_TRY(upload2(st, d, h, n_cov, z1, 0, z1s, 1, N));
     GSC_TRY(upload2(st, d, h, n_cov + N, z2, 0, z2s, 1, N));
@@ -856,6 +865,7 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         dax[k] = d + off;
         off += static_cast<size_t>(n[k]);
     }
+    tc.end();
     if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
                                   d + n_cov + N, st));
     // output buffer 128-byte aligned after the inputs
@@ -897,7 +907,9 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         Prefault pf;
         if (!pinned) pf.start(out, n_out * sizeof(double));
         pf.join();
+        tc.begin(K_COPY_D2H);
         GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+        tc.end();
     }
     GSC_TRY(check_status(*ctx, st));
     return GSC_OK;

@@ -56,6 +56,8 @@ enum KernelId : int32_t {
     K_BATCH_MIXED = 19,    // persistent mixed-precision batch kernel
     K_SAMPLE_MODES = 20,   // on-device spectral sampling (Philox4x32-10)
     K_SEP_SPLIT = 21,      // FP32 inputs of the x5 factor tables
+    K_COPY_H2D = 22,       // host-to-device copies of a host-pointer call (not a kernel)
+    K_COPY_D2H = 23,       // device-to-host copies of a host-pointer call (not a kernel)
     K_COUNT
 };
 const char *kernel_name(int32_t id);

@@ -127,3 +127,19 @@ def test_wave_launches_with_overlapped_copies(gsc, incompr, shape):
     rms = float(np.sqrt(np.mean(ref ** 2)))
     assert float(np.sqrt(np.mean(err ** 2))) / rms <= 2.5e-7
     assert rel_err(got, ref) <= 1.5e-6
+
+
+def test_host_calls_time_their_copies(gsc):
+    """With timing on, a host-array call reports its host-device copies
+    (copy_h2d, copy_d2h) beside its kernels."""
+    cov, z1, z2, pos = _case(9)
+    for call in (lambda: gsc.summate(cov, z1, z2, pos, form="mixed", timing=True),
+                 lambda: gsc.summate_structured(cov, z1, z2, (np.arange(8.0),) * 3, form="sep_f64",
+                                                timing=True),
+                 lambda: gsc.summate_batch([{"cov": cov, "z1": z1, "z2": z2, "pos": pos}] * 2,
+                                           form="plain", timing=True)):
+        call()
+        call()                                   # a batch plan is reused on the second call
+        t = dict(gsc.last_timings())
+        assert "copy_h2d" in t and "copy_d2h" in t and t["copy_h2d"] >= 0 and t["copy_d2h"] >= 0
+        assert any(not k.startswith("copy_") for k in t)
