@@ -937,6 +937,7 @@ MIXED_FP32_OPS = {1: 35, 2: 43, 3: 51}
 # capture each (summaries in profiles/); None where no capture exists
 PROFILED_TRAFFIC = {
     ("sep_tc_f16x5", "c2"): (12.49e6 + 88.12e6, "profiles/sep_tc_f16x5_c2.md"),
+    ("sep_tc_f16x5", "c4"): (167.4e6, "profiles/sep_tc_f16x5_c4.md"),
     ("mixed_scalar", "c1"): (1.69e6, "profiles/mixed_scalar_c1.md"),
     ("plain_f64_scalar", "c1"): (5.8e6, "profiles/plain_f64_scalar_c1.md"),
 }
