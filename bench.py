@@ -38,6 +38,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -130,11 +131,15 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # the raw samples go to GSC_CLOCKS_CSV when set (kept), else to a temporary file
+        self.keep = bool(os.environ.get("GSC_CLOCKS_CSV"))
+        self.path = os.environ.get("GSC_CLOCKS_CSV") or os.path.join(
+            tempfile.gettempdir(), f"gsc_clocks_{os.getpid()}_{device_index}.csv")
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            if os.path.dirname(self.path):
+                os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}",
@@ -157,7 +162,14 @@ class ClockSampler:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
-        for line in open(self.path):
+        with open(self.path) as fh:
+            lines = fh.readlines()
+        if not self.keep:
+            try:
+                os.remove(self.path)
+            except OSError:
+                pass
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue

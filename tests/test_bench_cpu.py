@@ -37,3 +37,21 @@ def test_reference_arm_contract(workload):
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_clock_summary(tmp_path, monkeypatch):
+    """The clock record: median SM clock, max clock, throttle reasons seen."""
+    sys.path.insert(0, ROOT)
+    import bench
+    csv = tmp_path / "clocks.csv"
+    csv.write_text("0, 1965, 2070, 810.5, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+                   "0, 2040, 2070, 1210.0, 0x4, Not Active, Not Active, Not Active, Active\n"
+                   "0, 2010, 2070, [N/A], 0x0, Not Active, Not Active, Not Active, Not Active\n"
+                   "garbage\n")
+    monkeypatch.delenv("GSC_CLOCKS_CSV", raising=False)
+    s = bench.ClockSampler(0)
+    s.path, s.proc = str(csv), object()
+    d = s.summary()
+    assert d["sm_mhz"] == 2010.0 and d["sm_max_mhz"] == 2070.0 and d["samples"] == 3
+    assert d["reasons"] == ["sw_power_cap"] and d["power_w_max"] == 1210.0
+    assert not csv.exists()                      # temporary samples are removed
