@@ -499,19 +499,22 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 //   F (rows, |F| <= 1 after dividing s by W)  = F1 + F2 + F3
 //   G (columns, |G| <= 1)                     = G1 + G2
 // in units of 2^15:  F1 = 2^15 * rint(F * 2^(bF-1)) / 2^(bF-1)  (bF-bit integer grid),
-//                    G1 = 2^15 * rint(G * 2^10) / 2^10           (11-bit integer grid),
+//                    G1 = 2^15 * rint(G * 2^11) / 2^11           (12-bit integer grid),
 // F2 = f16(F*2^15 - F1), F3 = f16(F*2^15 - F1 - F2), G2 = f16(G*2^15 - G1).
-// Every product F1*G1 is an integer multiple of 2^(30-(bF-1)-10) ("counts");
+// Every product F1*G1 is an integer multiple of 2^(30-(bF-1)-11) ("counts");
 // bF (3..9) is picked on the device so that six standard deviations of the
 // field stay below 2^23 counts, so the "main" TMEM accumulator adds them
 // EXACTLY whatever the hardware rounding.  (Exactness holds for fields of
 // random modes, as GSTools draws them; a field value beyond ~12 standard
 // deviations would start rounding the main sum.)  The four cross products
-// F2G1 + F1G2 + F2G2 + F3G1 (about 2^-7 of the field) go to a second TMEM
+// F2G1 + F1G2 + F2G2 + F3G1 (about 2^-bF of the field) go to a second TMEM
 // accumulator that the workers drain every KC = 16 k-blocks into FP32
 // totals held in registers, so their rounding never builds up at full
-// magnitude.  Representation: F to about 2^-29, G to 2^-22 relative; the
-// product F3G2 (below 2^-28) is dropped.
+// magnitude.  Representation: F to about 2^-(bF+22), G to 2^-24 relative
+// (integers up to 2^11 are exact in f16, so 12 bits is the widest exact G
+// grid; the exact main sum's budget fixes bF + bG, and G's single rest
+// slice makes G the coarser factor); the product F3G2 (below 2^-28) is
+// dropped.
 //
 // Warp roles (12 warps, 384 threads launched at 168 registers each, then
 // re-split with setmaxnreg, X5Layout):
@@ -527,14 +530,14 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 constexpr int X5_THREADS = 384;                 // 8 worker warps + 4 control warps
 constexpr int X5_LAUNCH_REGS = 168;             // 65536 / 384, rounded down to 8
 constexpr float kUnit = 32768.0f;            // 2^15
-constexpr int kLeadBitsG = 11;               // G1 grid: 2^15 * rint(G * 2^10) / 2^10
+constexpr int kLeadBitsG = 12;               // G1 grid: 2^15 * rint(G * 2^11) / 2^11
 
 // Normaliser and leading-grid width of the x5 form, one block of 256 threads:
 //   W = 2^e >= max |z1 - i z2|  (so |s / W| <= 1 and |F| <= 1),
 //   the leading F grid 2^(bF-1) with bF (3..9) chosen so that the expected
 //   extreme of the exact main sum, about 6 * sqrt(sum |w|^2 / 2) / W *
 //   2^(bF+bG-2) counts (6 standard deviations of the field), stays below
-//   2^23 counts with bG = 11: one bit of headroom under FP32's 2^24.
+//   2^23 counts with bG = 12: one bit of headroom under FP32's 2^24.
 // The s vector is stored unnormalised; the slicing constants absorb 1/W (a
 // power of two, so the slices are those of s / W bit for bit):
 //   wnorm = {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W}
@@ -690,7 +693,7 @@ __device__ __forceinline__ void btab_x5_entry(const TabArgs &t, int64_t i) {
 
 // G table of the x5 form.  Element (component c, rows kGtabRows g .. of the
 // column axis, mode j): the mode's record is read once for those rows.
-// G1 on the 11-bit integer grid (units of 2^15 / 2^10 = 32), G2 the f16 rest;
+// G1 on the 12-bit integer grid (units of 2^15 / 2^11 = 16), G2 the f16 rest;
 // stored as contiguous stage blocks, one per (tile of t.bn rows, k-block of
 // 16 modes), already in the 64-byte-swizzled K-major layout the MMA reads:
 // row r at r * 64 bytes, 16-byte chunk c at c ^ ((r >> 1) & 3).
