@@ -6,7 +6,7 @@
 // of absolute accuracy for |k.x| up to ~1e6 with FP32 instructions only
 // (GB300 runs FP64 at 1/64 of the FP32 rate).  sin(2 pi f), cos(2 pi f) on
 // |f| <= 1/8 come from polynomials fitted for this project (FP32
-// coefficients, max error 8.5e-8 / 5.7e-8 over the interval), corrected to
+// coefficients, max error 8.6e-8 / 5.8e-8 over the interval), corrected to
 // first order for the low part of the phase (the mixed summators,
 // mixed.cu).  The factor tables of the separable tensor-core form
 // (separable_tc.cu) take the same phase reduction and sincosf for the last

@@ -16,7 +16,7 @@
 //    (FP64 would spend 9 FP64 instructions per point*mode here);
 //  * sincos(2 pi theta): quadrant by rounding 4 theta, then sin/cos of
 //    2 pi f, |f| <= 1/8, by polynomials fitted for this kernel (FP32
-//    coefficients, max error 8.5e-8 / 5.7e-8 over the interval), corrected
+//    coefficients, max error 8.6e-8 / 5.8e-8 over the interval), corrected
 //    to first order for the low part of the phase;
 //  * z1 cos + z2 sin accumulated in FP32 over tiles of 32 modes with Kahan
 //    compensation (plain FP32 sums alone reached 1.0e-6 of the field RMS on a
