@@ -2,9 +2,11 @@
 //
 // A phase k.x is carried as theta = kappa.x turns, kappa = k / 2 pi, with
 // kappa and x each split into FP32 hi + lo parts (48 significant bits).
-// Whole turns drop out exactly, so the reduced phase keeps about 2^-40 turns
-// of absolute accuracy for |k.x| up to ~1e6 with FP32 instructions only
-// (GB300 runs FP64 at 1/64 of the FP32 rate).  sin(2 pi f), cos(2 pi f) on
+// Whole turns drop out exactly, so the reduced phase of one product keeps
+// about |theta| * 2^-46 turns of absolute accuracy (2^-29 turns at |k.x| =
+// 1e6) with FP32 instructions only (GB300 runs FP64 at 1/64 of the FP32
+// rate); summing the fractions of several products in FP32 adds up to 2^-24
+// turns where one product is under a turn (mixed.cu).  sin(2 pi f), cos(2 pi f) on
 // |f| <= 1/8 come from polynomials fitted for this project (FP32
 // coefficients, max error 8.6e-8 / 5.8e-8 over the interval), corrected to
 // first order for the low part of the phase (the mixed summators,

@@ -11,9 +11,12 @@
 //    significant bits each); per dimension p = kh*xh is split exactly into
 //    p (rounded) and fma(kh, xh, -p), the integer turns rint(p) are dropped
 //    exactly, and the small terms kh*xl + kl*xh are added in FP32.  The
-//    reduced phase keeps about 2^-40 turns of absolute accuracy for |k.x|
-//    up to 1e6, far beyond what FP32 can represent as a plain product
-//    (FP64 would spend 9 FP64 instructions per point*mode here);
+//    reduced phase is accurate to |theta| * 2^-46 turns (2^-29 turns at
+//    |k.x| = 1e6, where a plain FP32 product keeps no fraction at all) while
+//    every dimension's product is at least one turn; where one is smaller,
+//    the FP32 sum of the dimensions' fractions rounds at the total's ulp,
+//    up to 2^-24 turns (3.7e-7 rad).  FP64 would spend 9 FP64 instructions
+//    per point*mode here;
 //  * sincos(2 pi theta): quadrant by rounding 4 theta, then sin/cos of
 //    2 pi f, |f| <= 1/8, by polynomials fitted for this kernel (FP32
 //    coefficients, max error 8.6e-8 / 5.8e-8 over the interval), corrected
@@ -220,7 +223,7 @@ __device__ __forceinline__ void mixed_block(const double *__restrict__ pos, int6
                         const float kh = mr[d], kl = mr[3 + d];
                         const float pr = kh * xh[r][d];
                         const float e = fmaf(kh, xh[r][d], -pr);      // exact
-                        a += pr - rintf(pr);                            // exact
+                        a += pr - rintf(pr);   // fraction exact; the sum rounds below 1 turn
                         b = fmaf(kh, xl[r][d], fmaf(kl, xh[r][d], e + b));
                     }
                     const float a2 = a - rintf(a);
