@@ -505,8 +505,9 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 // bF (3..9) is picked on the device so that six standard deviations of the
 // field stay below 2^23 counts, so the "main" TMEM accumulator adds them
 // EXACTLY whatever the hardware rounding.  (Exactness holds for fields of
-// random modes, as GSTools draws them; a field value beyond ~12 standard
-// deviations would start rounding the main sum.)  The four cross products
+// random modes, as GSTools draws them, while the budget asks for bF >= 3:
+// up to about 1.8e6 modes of standard-normal z1, z2.  A field value beyond
+// ~12 standard deviations would start rounding the main sum.)  The four cross products
 // F2G1 + F1G2 + F2G2 + F3G1 (about 2^-bF of the field) go to a second TMEM
 // accumulator that the workers drain every KC = 16 k-blocks into FP32
 // totals held in registers, so their rounding never builds up at full
