@@ -411,7 +411,8 @@ def run_ours(args, world, rank, local):
     err, check = None, None
     if not args.no_check:
         rng = np.random.default_rng(7)
-        idx = np.sort(rng.choice(P, size=min(P, 2048), replace=False))
+        # every point up to 2^17 (C1 in full), else a seeded 2^16-point subset; all modes
+        idx = np.sort(rng.choice(P, size=P if P <= 1 << 17 else 1 << 16, replace=False))
         pos_s = sample_points(w, idx)
         fn = oracle.summator_incompr if w["incompr"] else oracle.summator
         ref = fn(w["cov"], w["z1"], w["z2"], pos_s, num_threads=host_cores())
