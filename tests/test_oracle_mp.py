@@ -105,3 +105,20 @@ def test_heavy_tail_phases_are_large():
     cov, _, _, pos = _inputs(31, 3, 48, 16, True)
     ph = np.abs(cov.T @ pos)
     assert ph.max() > 1e4
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_summator_fourier_against_high_precision(dim):
+    """sum_j f_j (z1_j cos + z2_j sin) (src/field.rs:219-249), one more
+    rounding per term for the spectrum factor."""
+    cov, z1, z2, pos = _inputs(200 + dim, dim, 40, 12, False)
+    sf = np.random.default_rng(dim).uniform(0.1, 2.0, cov.shape[1])
+    got = oracle.summator_fourier(sf, cov, z1, z2, pos, num_threads=1)
+    for i in range(pos.shape[1]):
+        terms, mags = _terms(cov, z1, z2, pos[:, i])
+        acc, partial_sizes = mpmath.mpf(0), 0.0
+        for j, t in enumerate(terms):
+            acc += mpmath.mpf(sf[j]) * t
+            partial_sizes += abs(float(acc))
+        bound = U * (4.0 * float(np.dot(sf, mags)) + partial_sizes)
+        assert abs(got[i] - float(acc)) <= bound, (i, got[i], float(acc), bound)
