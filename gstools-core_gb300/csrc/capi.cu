@@ -1136,6 +1136,20 @@ int gsc_selftest_fail_alloc(int32_t countdown) {
     return GSC_OK;
 }
 
+int gsc_selftest_detect_grid(const double *pos, int64_t ps_d, int64_t ps_p, int64_t dim,
+                             int64_t n_points, int64_t *n_axes) {
+    if (!n_axes) return set_error(GSC_ERR_INVALID, "n_axes is NULL");
+    n_axes[0] = n_axes[1] = n_axes[2] = 0;
+    if (dim < 0 || n_points < 0) return set_error(GSC_ERR_INVALID, "negative dimension or count");
+    if (n_points > 0 && !pos) return set_error(GSC_ERR_INVALID, "pos is NULL");
+    std::vector<double> ax[3];
+    int64_t n[3] = {0, 0, 0};
+    if (n_points > 0 && detect_grid(pos, ps_d, ps_p, dim, n_points, ax, n)) {
+        for (int d = 0; d < 3; ++d) n_axes[d] = d < dim ? n[d] : 0;
+    }
+    return GSC_OK;
+}
+
 int gsc_summate_structured_f64(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
                                int64_t z1s, const double *z2, int64_t z2s, int64_t dim,
                                int64_t n_modes, const double *a0, int64_t n0, int64_t s0,

@@ -162,6 +162,8 @@ SIGNATURES = {
                                             _I64, _P, _P, _P, _OPTS]),
     "gsc_selftest_wait_timeout": (ctypes.c_int, [_I32, _I64]),
     "gsc_selftest_fail_alloc": (ctypes.c_int, [_I32]),
+    "gsc_selftest_detect_grid": (ctypes.c_int, [_P, _I64, _I64, _I64, _I64,
+                                                ctypes.POINTER(ctypes.c_int64)]),
     "gsc_selftest_batch_queue": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _I32,
                                                 ctypes.POINTER(GscBatchConfig), _I32, _I32]),
     "gsc_release_buffers": (ctypes.c_int, [_I32]),

@@ -395,6 +395,18 @@ int gsc_selftest_wait_timeout(int32_t device, int64_t limit_us);
  * counterpart. */
 int gsc_selftest_fail_alloc(int32_t countdown);
 
+/* Structured-mesh recognition of the point entry points, on host arrays
+ * alone (no device is touched): for pos (dim, n_points) with element
+ * strides, sets n_axes[0..2] to the axis lengths when the points are
+ * meshgrid(*axes, indexing="ij") flattened in C order, as GSTools passes a
+ * structured mesh, every point compared with the rebuilt axes (n_axes[d] = 0
+ * for d >= dim).  All three are 0 when the points are no such mesh or would
+ * not be routed (dim not 2 or 3, fewer than 4096 points, an axis of one
+ * point).  Returns GSC_OK, or GSC_ERR_INVALID for NULL pointers and negative
+ * sizes.  No reference counterpart. */
+int gsc_selftest_detect_grid(const double *pos, int64_t pos_stride_d, int64_t pos_stride_p,
+                             int64_t dim, int64_t n_points, int64_t *n_axes);
+
 /* Work-queue check of the batch planner, on the host only (no device is
  * touched; the items' pointers are ignored): builds the cost-sorted work
  * queue that gsc_batch_create would build for `items` with configuration
