@@ -145,6 +145,38 @@ int get_ctx(int device, DeviceCtx **out) {
     return GSC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// per-device kernel set-up
+// ---------------------------------------------------------------------------
+struct OnceRegistry {
+    std::mutex mu;
+    std::vector<std::pair<const void *, int>> done;   // (key, device) pairs set up
+
+    int run(const void *key, int device, const std::function<int()> &setup) {
+        std::lock_guard<std::mutex> lk(mu);
+        for (const auto &d : done)
+            if (d.first == key && d.second == device) return GSC_OK;
+        const int rc = setup();
+        if (rc == GSC_OK) done.emplace_back(key, device);
+        return rc;
+    }
+};
+static OnceRegistry g_once;
+
+int once_per_device(const void *key, int device, const std::function<int()> &setup) {
+    return g_once.run(key, device, setup);
+}
+
+int smem_attr(const void *fn, size_t smem) {
+    int device = 0;
+    GSC_CUDA(cudaGetDevice(&device));
+    return g_once.run(fn, device, [fn, smem]() -> int {
+        GSC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+        return GSC_OK;
+    });
+}
+
 // Allocation-failure injection (gsc_selftest_fail_alloc): -1 = off, k >= 0 =
 // the k-th next allocation of a library buffer fails as out of memory.
 static std::atomic<int> g_fail_alloc{-1};

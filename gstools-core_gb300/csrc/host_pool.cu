@@ -12,7 +12,9 @@
 // runs at the link's speed with no fault on either side.
 //
 // The pool keeps at most `limit` bytes of free blocks (GSC_HOST_POOL_MB,
-// default 8192 MiB); a block freed beyond that is released.  Thread safe.
+// default 2048 MiB, so that a shared host keeps its page-locked memory
+// bounded; gsc_host_pool_trim releases every free block); a block freed
+// beyond that is released.  Thread safe.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -42,7 +44,7 @@ struct HostPool {
     size_t cached = 0;                                    // bytes in free_blocks
     size_t limit = 0;
     HostPool() {
-        size_t mb = 8192;
+        size_t mb = 2048;
         if (const char *e = getenv("GSC_HOST_POOL_MB")) {
             char *end = nullptr;
             const unsigned long long v = strtoull(e, &end, 10);

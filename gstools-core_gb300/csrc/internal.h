@@ -124,6 +124,17 @@ int check_device_ptr(const void *p, const char *name);
 
 // Returns the context of `device` (-1 = current), initialising it once.
 int get_ctx(int device, DeviceCtx **out);
+
+// One-time set-up of a kernel on one device.  Launch attributes such as
+// cudaFuncAttributeMaxDynamicSharedMemorySize belong to the device that was
+// current when they were set, so a process-wide "done" flag would leave every
+// later device unconfigured.  `setup` runs with that device current, under a
+// lock shared by all threads, until it succeeds once for the pair (key,
+// device); later calls return GSC_OK without running it.
+int once_per_device(const void *key, int device, const std::function<int()> &setup);
+// cudaFuncSetAttribute(fn, MaxDynamicSharedMemorySize, smem) on the current
+// device, once per (fn, device).
+int smem_attr(const void *fn, size_t smem);
 // Makes `buf` hold at least `bytes`; waits for in-flight users before growing.
 // cudaMalloc / cudaHostAlloc with the allocation-failure injection of
 // gsc_selftest_fail_alloc; GSC_ERR_NOMEM on failure, *p = nullptr.

@@ -32,6 +32,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -391,12 +392,7 @@ int launch_main(dim3 grid, size_t smem, cudaStream_t st, const double *pos, int6
                 const double2 *wtab, const double *rec, int64_t nc, int64_t mps, int accumulate,
                 double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
     auto fn = plain_kernel<D, R, INC, LIBM>;
-    static bool configured = false;   // per instantiation
-    if (!configured) {
-        GSC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
-        configured = true;
-    }
+    GSC_TRY(smem_attr(reinterpret_cast<const void *>(fn), smem));   // once per device
     fn<<<grid, kThreads, smem, st>>>(pos, P, wtab, rec, nc, mps, accumulate, dst, sd, sp,
                                      split_stride);
     GSC_CUDA(cudaGetLastError());
@@ -424,12 +420,15 @@ int dispatch_dim(int64_t dim, dim3 grid, size_t smem, cudaStream_t st, const dou
 }
 
 int sm_count(int device) {
-    static int cached[64] = {0};
-    if (device >= 0 && device < 64 && cached[device]) return cached[device];
+    static std::atomic<int> cached[64];   // zero-initialised (static storage)
+    if (device >= 0 && device < 64) {
+        const int c = cached[device].load(std::memory_order_relaxed);
+        if (c) return c;
+    }
     int n = 0;
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0)
         n = 152;
-    if (device >= 0 && device < 64) cached[device] = n;
+    if (device >= 0 && device < 64) cached[device].store(n, std::memory_order_relaxed);
     return n;
 }
 
@@ -636,19 +635,7 @@ BatchPlainFn batch_plain_fn(int R, int tile) {
     return nullptr;
 }
 int configure_batch_plain(BatchPlainFn fn, int tile) {
-    static std::mutex mu;
-    static BatchPlainFn done[8] = {nullptr};
-    std::lock_guard<std::mutex> lk(mu);
-    for (auto f : done)
-        if (f == fn) return GSC_OK;
-    GSC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(batch_plain_smem(tile))));
-    for (auto &f : done)
-        if (!f) {
-            f = fn;
-            break;
-        }
-    return GSC_OK;
+    return smem_attr(reinterpret_cast<const void *>(fn), batch_plain_smem(tile));   // per device
 }
 }  // namespace
 
@@ -704,9 +691,19 @@ int batch_plain_launch(int R, int tile, int blocks, const BatchItem *items,
 // them) race on the array.
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char
-    gsc_noalloc_scratch[gsc::kNoAllocModes * 256 * 16 + gsc::kNoAllocModes * 12 * 8];
+    gsc_noalloc_scratch[gsc::kNoAllocModes *
+                        (gsc::kPlainTableBytesPerMode + gsc::kPlainRecBytesPerMode)];
 
 namespace gsc {
+
+// the array is sliced below as kNoAllocModes tables of kM double2 followed by
+// kNoAllocModes records of kRec doubles: its size must follow those constants
+static_assert(kPlainTableBytesPerMode == kM * sizeof(double2) &&
+                  kPlainRecBytesPerMode == kRec * sizeof(double),
+              "the fixed table array is sized from the plain kernel's per-mode layout");
+static_assert(sizeof(gsc_noalloc_scratch) ==
+                  kNoAllocModes * (kM * sizeof(double2) + kRec * sizeof(double)),
+              "fixed table array size");
 
 static std::mutex g_noalloc_mu;
 static void *g_noalloc_addr[64] = {nullptr};

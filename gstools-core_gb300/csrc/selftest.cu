@@ -8,8 +8,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "internal.h"
 #include "sm100.cuh"
@@ -62,4 +65,52 @@ extern "C" int gsc_selftest_wait_timeout(int32_t device, int64_t limit_us) {
         GSC_CUDA(cudaStreamSynchronize(st));
     }
     return gsc_device_status(ctx->device);
+}
+
+// Per-device set-up registry under concurrent first calls (host only): the
+// stand-in keys are addresses inside a static array, the stand-in device
+// ordinals start far above any real one, so no real kernel's entry is hit.
+extern "C" int gsc_selftest_once_per_device(int32_t n_devices, int32_t n_keys, int32_t n_threads,
+                                            int64_t *setups) {
+    if (n_devices < 1 || n_devices > 64 || n_keys < 1 || n_keys > 64 || n_threads < 1 ||
+        n_threads > 64 || !setups)
+        return set_error(GSC_ERR_INVALID, "n_devices, n_keys, n_threads must lie in [1, 64]");
+    static char stand_in[64];
+    static std::atomic<int> round{0};
+    // each call gets fresh device ordinals, so the registry's entries from an
+    // earlier call do not count
+    const int dev0 = (1 << 20) + round.fetch_add(1) * 64;
+    const int pairs = n_devices * n_keys;
+    std::vector<std::atomic<int>> tries(pairs), ok(pairs);
+    for (int i = 0; i < pairs; ++i) tries[i] = ok[i] = 0;
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t)
+        th.emplace_back([&, t] {
+            for (int v = 0; v < pairs; ++v) {
+                const int i = (v * 7 + t * 13) % pairs;   // a different order per thread
+                const int k = i % n_keys, d = i / n_keys;
+                once_per_device(&stand_in[k], dev0 + d, [&, i]() -> int {
+                    if (tries[i].fetch_add(1) == 0)
+                        return set_error(GSC_ERR_CUDA, "stand-in set-up fails once");
+                    ok[i].fetch_add(1);
+                    return GSC_OK;
+                });
+            }
+            // a second sweep: every pair is set up by now (its first sweep
+            // retried a failure), so nothing runs again
+            for (int i = 0; i < pairs; ++i)
+                once_per_device(&stand_in[i % n_keys], dev0 + i / n_keys, [&, i]() -> int {
+                    ok[i].fetch_add(1);
+                    return GSC_OK;
+                });
+        });
+    for (auto &x : th) x.join();
+    int64_t total = 0;
+    bool good = true;
+    for (int i = 0; i < pairs; ++i) {
+        total += ok[i];
+        if (ok[i] != 1 || tries[i] > 2) good = false;
+    }
+    *setups = total;
+    return good ? GSC_OK : set_error(GSC_ERR_KERNEL, "a pair was set up other than exactly once");
 }

@@ -1353,44 +1353,31 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 template <bool BF16>
 int configure_tc() {
-    static bool done = false;
-    if (!done) {
-        GSC_CUDA(cudaFuncSetAttribute(sep_tc_kernel<BF16>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(kSmemBytes)));
-        done = true;
-    }
-    return GSC_OK;
+    return smem_attr(reinterpret_cast<const void *>(sep_tc_kernel<BF16>), kSmemBytes);
 }
 
 }  // namespace
 
 namespace {
-// One-time set-up of an x5 instantiation.  The warps re-balance their
-// registers with setmaxnreg; the increases can only be served from what the
-// block was launched with, so a build that launches with fewer registers
-// must not run.
+// Set-up of an x5 instantiation on the current device (once per device).
+// The warps re-balance their registers with setmaxnreg; the increases can
+// only be served from what the block was launched with, so a build that
+// launches with fewer registers must not run.
 template <int BNX, bool SPLIT>
 int configure_x5() {
-    static std::once_flag once;
-    static int rc = GSC_OK;
-    std::call_once(once, [] {
+    int device = 0;
+    GSC_CUDA(cudaGetDevice(&device));
+    const void *fn = reinterpret_cast<const void *>(sep_x5_kernel<BNX, SPLIT>);
+    return once_per_device(fn, device, [fn]() -> int {
         cudaFuncAttributes fa{};
-        cudaError_t e = cudaFuncGetAttributes(&fa, sep_x5_kernel<BNX, SPLIT>);
-        if (e != cudaSuccess) {
-            rc = cuda_fail(e, "cudaFuncGetAttributes (x5)");
-            return;
-        }
+        GSC_CUDA(cudaFuncGetAttributes(&fa, fn));
         if (fa.numRegs * X5_THREADS <
-            4 * 32 * (2 * X5Layout<BNX>::WORK_REGS + X5Layout<BNX>::CTRL_REGS)) {
-            rc = set_error(GSC_ERR_KERNEL, "x5 kernel built with too few registers per thread");
-            return;
-        }
-        e = cudaFuncSetAttribute(sep_x5_kernel<BNX, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(X5Layout<BNX>::SMEM));
-        if (e != cudaSuccess) rc = cuda_fail(e, "cudaFuncSetAttribute (x5)");
+            4 * 32 * (2 * X5Layout<BNX>::WORK_REGS + X5Layout<BNX>::CTRL_REGS))
+            return set_error(GSC_ERR_KERNEL, "x5 kernel built with too few registers per thread");
+        GSC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(X5Layout<BNX>::SMEM)));
+        return GSC_OK;
     });
-    return rc;
 }
 }  // namespace
 

@@ -164,6 +164,7 @@ SIGNATURES = {
     "gsc_selftest_fail_alloc": (ctypes.c_int, [_I32]),
     "gsc_selftest_detect_grid": (ctypes.c_int, [_P, _I64, _I64, _I64, _I64,
                                                 ctypes.POINTER(ctypes.c_int64)]),
+    "gsc_selftest_once_per_device": (ctypes.c_int, [_I32, _I32, _I32, ctypes.POINTER(_I64)]),
     "gsc_selftest_batch_queue": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _I32,
                                                 ctypes.POINTER(GscBatchConfig), _I32, _I32]),
     "gsc_release_buffers": (ctypes.c_int, [_I32]),

@@ -137,7 +137,7 @@ int gsc_release_buffers(int32_t device);
  * 64 KiB, or of 2 MiB above 2 MiB), taken
  * from the pool's free blocks of that rounded size when there is one;
  * gsc_host_free hands it back (the pool keeps up to GSC_HOST_POOL_MB MiB of
- * free blocks, default 8192, and releases the rest); gsc_host_pool_trim
+ * free blocks, default 2048, and releases the rest); gsc_host_pool_trim
  * releases every free block; gsc_host_pool_stats reports the bytes handed
  * out and the bytes cached.  Results written into such blocks by the
  * host-pointer entry points move by DMA with no page faults.  No reference
@@ -406,6 +406,20 @@ int gsc_selftest_fail_alloc(int32_t countdown);
  * sizes.  No reference counterpart. */
 int gsc_selftest_detect_grid(const double *pos, int64_t pos_stride_d, int64_t pos_stride_p,
                              int64_t dim, int64_t n_points, int64_t *n_axes);
+
+/* Per-device kernel set-up, on the host only (no device is touched): the
+ * registry that every launch path uses to set a kernel's launch attributes
+ * once per (kernel, device) -- cudaFuncSetAttribute applies to the device
+ * current at the time, so a process-wide flag would leave later devices
+ * unconfigured -- is driven by `n_threads` threads (1 .. 64) at once over
+ * `n_keys` stand-in kernels (1 .. 64) and `n_devices` stand-in device
+ * ordinals (1 .. 64), each thread visiting every pair in its own order.
+ * Every pair's set-up fails on its first attempt and succeeds on the second.
+ * Sets *setups to the number of successful set-ups and returns GSC_OK when
+ * each pair succeeded exactly once and was tried no more than twice, else
+ * GSC_ERR_KERNEL.  No reference counterpart. */
+int gsc_selftest_once_per_device(int32_t n_devices, int32_t n_keys, int32_t n_threads,
+                                 int64_t *setups);
 
 /* Work-queue check of the batch planner, on the host only (no device is
  * touched; the items' pointers are ignored): builds the cost-sorted work

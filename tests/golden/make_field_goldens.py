@@ -8,7 +8,7 @@ Reads the test module of the reference crate's ``src/field.rs`` (fixtures
 line number of every literal, to ``field_rs_goldens.json`` beside this
 script.  The JSON is committed; the tests never read the reference tree.
 
-Usage:  python tests/golden/make_field_goldens.py [path/to/reference]
+Usage:  python tests/golden/make_field_goldens.py path/to/reference
 """
 from __future__ import annotations
 
@@ -18,8 +18,6 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
-
 
 def _literals(text: str, start: int):
     """Yield (kind, line, value) for every arr1/arr2 literal after ``start``."""
@@ -79,4 +77,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF)
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_field_goldens.py path/to/reference  (the GSTools-Core source tree)")
+    main(sys.argv[1])
