@@ -114,6 +114,8 @@ struct gsc_batch {
     double *d_rec = nullptr;                 // FP64 form: mode records
     float *d_frec = nullptr;                 // mixed forms: records
     double *d_rec64 = nullptr;
+    unsigned long long *d_fxrange = nullptr; // mixed form: range words of every item
+    int *range_flag = nullptr;               // mixed form: the device's sticky range word
     double *d_part = nullptr;
     size_t part_cap = 0;
     int32_t *d_red_items = nullptr;
@@ -141,7 +143,8 @@ struct gsc_batch {
         for (void *p : {static_cast<void *>(d_items), static_cast<void *>(d_prefix),
                         static_cast<void *>(d_units), static_cast<void *>(d_counter), d_tab,
                         static_cast<void *>(d_rec), static_cast<void *>(d_frec),
-                        static_cast<void *>(d_rec64), static_cast<void *>(d_part),
+                        static_cast<void *>(d_rec64), static_cast<void *>(d_fxrange),
+                        static_cast<void *>(d_part),
                         static_cast<void *>(d_red_items), static_cast<void *>(d_red_prefix)})
             if (p) cudaFree(p);
         if (prev >= 0 && prev != device) cudaSetDevice(prev);
@@ -157,10 +160,12 @@ int dmalloc(void **p, size_t bytes) {
 }
 
 bool is_plain(const gsc_batch &b) { return b.form == GSC_FORM_PLAIN_F64; }
+bool is_fx(const gsc_batch &b) { return b.form == GSC_FORM_MIXED; }
 
 int occupancy(const gsc_batch &b, const Cfg &c) {
+    if (is_fx(b)) return batch_fx_occupancy(c.R);
     return is_plain(b) ? batch_plain_occupancy(c.R, c.tile, b.device)
-                       : batch_mixed_occupancy(c.R, b.form == GSC_FORM_MIXED_F64PHASE, b.device);
+                       : batch_mixed_occupancy(c.R, true, b.device);
 }
 
 // Item table, mode prefix and total work of a plan from the caller's item
@@ -400,6 +405,10 @@ int upload_units(gsc_batch &b, const std::vector<BatchUnit> &units) {
 }
 
 int enqueue_tables(gsc_batch &b, cudaStream_t st) {
+    if (is_fx(b))
+        return batch_fx_tables(b.d_items, b.d_prefix, static_cast<int64_t>(b.items.size()),
+                               b.total_modes, reinterpret_cast<uint32_t *>(b.d_frec), b.d_fxrange,
+                               b.range_flag, st);
     if (is_plain(b))
         return batch_plain_tables(b.d_items, b.d_prefix, static_cast<int64_t>(b.items.size()),
                                   b.total_modes, b.d_tab, b.d_rec, st);
@@ -410,6 +419,9 @@ int enqueue_tables(gsc_batch &b, cudaStream_t st) {
 int enqueue_sum(gsc_batch &b, const Cfg &c, int blocks, int64_t n_units, cudaStream_t st) {
     GSC_CUDA(cudaMemsetAsync(b.d_counter, 0, sizeof(int), st));
     if (n_units == 0) return GSC_OK;
+    if (is_fx(b))
+        return batch_fx_launch(c.R, blocks, b.d_items, b.d_units, n_units, b.d_counter,
+                               reinterpret_cast<const uint32_t *>(b.d_frec), b.d_fxrange, st);
     if (is_plain(b))
         return batch_plain_launch(c.R, c.tile, blocks, b.d_items, b.d_units, n_units, b.d_counter,
                                   b.d_tab, b.d_rec, st);
@@ -566,6 +578,12 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
     if (is_plain(*b)) {
         GSC_TRY(dmalloc(&b->d_tab, M * kPlainTableBytesPerMode));
         GSC_TRY(dmalloc(reinterpret_cast<void **>(&b->d_rec), M * kPlainRecBytesPerMode));
+    } else if (is_fx(*b)) {
+        GSC_TRY(dmalloc(reinterpret_cast<void **>(&b->d_frec), M * kFxRecBytesPerMode));
+        GSC_TRY(dmalloc(reinterpret_cast<void **>(&b->d_fxrange), nit * 4 * sizeof(unsigned long long)));
+        DeviceCtx *ctx = nullptr;
+        GSC_TRY(get_ctx(b->device, &ctx));
+        b->range_flag = ctx->status + 4;        // the sticky range word gsc_device_status reads
     } else {
         GSC_TRY(dmalloc(reinterpret_cast<void **>(&b->d_frec), M * kMixedRecBytesPerMode));
         GSC_TRY(dmalloc(reinterpret_cast<void **>(&b->d_rec64), M * kMixedRec64BytesPerMode));
@@ -581,7 +599,8 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
         c.R = config->points_per_thread;
         c.tile = is_plain(*b) ? config->tile_modes : 32;
         c.upb = config->units_per_block;
-        const bool ok = is_plain(*b) ? batch_plain_config_ok(c.R, c.tile) : batch_mixed_config_ok(c.R);
+        const bool ok = is_plain(*b) ? batch_plain_config_ok(c.R, c.tile)
+                         : is_fx(*b) ? batch_fx_config_ok(c.R) : batch_mixed_config_ok(c.R);
         if (!ok)
             return set_error(GSC_ERR_INVALID,
                              "unsupported batch configuration (points per thread 2, 4, 8; tile "
@@ -822,6 +841,7 @@ int gsc_selftest_batch_queue(const gsc_batch_item *items, int64_t count, int32_t
     c.tile = is_plain(b) ? config->tile_modes : 32;
     c.upb = config->units_per_block;
     const bool ok = c.upb > 0 && (is_plain(b) ? batch_plain_config_ok(c.R, c.tile)
+                                  : is_fx(b)  ? batch_fx_config_ok(c.R)
                                               : batch_mixed_config_ok(c.R));
     if (!ok) return set_error(GSC_ERR_INVALID, "unsupported batch configuration");
     std::vector<BatchUnit> units;

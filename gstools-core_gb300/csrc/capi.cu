@@ -321,12 +321,21 @@ static bool is_mixed(int form) {
     return form == GSC_FORM_MIXED || form == GSC_FORM_MIXED_F64PHASE;
 }
 
-// plain or mixed forms on explicit points (device pointers in `a`)
-static int run_points(DeviceCtx &ctx, const Resolved &ro, PlainArgs &a, cudaStream_t st) {
+static int point_form(const Resolved &ro, const PlainArgs &a) {
     int f = ro.form;
     if (f == GSC_FORM_AUTO) f = ro.tolerance >= kBoundMixed ? GSC_FORM_MIXED : GSC_FORM_PLAIN_F64;
     const bool mixed_ok = a.dim >= 1 && a.dim <= 3 && !(a.incompr && a.dim == 1);
-    if (is_mixed(f) && mixed_ok) return mixed_run(ctx, a, f == GSC_FORM_MIXED_F64PHASE, st);
+    return (is_mixed(f) && !mixed_ok) ? GSC_FORM_PLAIN_F64 : f;
+}
+
+// plain or mixed forms on explicit points (device pointers in `a`);
+// range_flag: device word the mixed form sets when a wave number is past its
+// integer phase range (see mixed_fx.cu)
+static int run_points(DeviceCtx &ctx, const Resolved &ro, PlainArgs &a, cudaStream_t st,
+                      int *range_flag) {
+    const int f = point_form(ro, a);
+    if (f == GSC_FORM_MIXED) return mixed_fx_run(ctx, a, range_flag, st);
+    if (f == GSC_FORM_MIXED_F64PHASE) return mixed_run(ctx, a, true, st);
     a.variant = f == GSC_FORM_PLAIN_F64_LIBM ? 1 : 0;
     return plain_run(ctx, a, st);
 }
@@ -343,16 +352,42 @@ static int structured_form(const Resolved &r, int64_t dim) {
     return f;
 }
 
-// Reads and clears the sticky status word after the stream has finished.
+// Words of the per-device status buffer (256 bytes of device memory):
+//   [0] sticky pipeline status: a bounded wait gave up (sm100.cuh codes)
+//   [1] the last sep_f16x5 call's bound flag (written by every such call):
+//       1 when its inputs break the exact leading sum's bound
+//   [2] sticky: an explicit sep_f16x5 call on device pointers was flagged
+//       and left its output invalid
+//   [3] the last host-pointer mixed call's range flag (cleared by the call)
+//   [4] sticky: a mixed call on device pointers (or a batch) met a wave
+//       number past the integer phase range (its output is invalid)
+constexpr int kStatusPipeline = 0, kStatusX5Flag = 1, kStatusX5Sticky = 2, kStatusFxFlag = 3,
+              kStatusFxSticky = 4;
+
+static const char *kFxRangeMsg =
+    "mixed: a wave number times the largest coordinate exceeds 2^30 turns, past the range of "
+    "its integer phase; the output is invalid.  Use form AUTO on host arrays (which recomputes "
+    "such calls on the plain FP64 kernel) or plain";
+static const char *kX5BoundMsg =
+    "sep_f16x5: these inputs break the bound that keeps its leading sum exact (weights far "
+    "from random, e.g. in phase at a grid point); the output is invalid.  Use form AUTO (which "
+    "recomputes such calls on sep_f64) or sep_f64";
+
+// Reads and clears the sticky status words after the stream has finished.
 static int check_status(DeviceCtx &ctx, cudaStream_t st) {
-    int v = 0;
-    GSC_CUDA(cudaMemcpyAsync(&v, ctx.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int v[5] = {0, 0, 0, 0, 0};
+    GSC_CUDA(cudaMemcpyAsync(v, ctx.status, sizeof(v), cudaMemcpyDeviceToHost, st));
     GSC_CUDA(cudaStreamSynchronize(st));
-    if (v != 0) {
-        GSC_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(int), st));
+    if (v[kStatusPipeline] != 0 || v[kStatusX5Sticky] != 0 || v[kStatusFxSticky] != 0) {
+        for (int w : {kStatusPipeline, kStatusX5Sticky, kStatusFxSticky})
+            GSC_CUDA(cudaMemsetAsync(ctx.status + w, 0, sizeof(int), st));
         GSC_CUDA(cudaStreamSynchronize(st));
-        return set_error(GSC_ERR_KERNEL, "a tensor-core pipeline wait gave up (status " +
-                                             std::to_string(v) + "); the output is invalid");
+        if (v[kStatusPipeline] != 0)
+            return set_error(GSC_ERR_KERNEL, "a tensor-core pipeline wait gave up (status " +
+                                                 std::to_string(v[kStatusPipeline]) +
+                                                 "); the output is invalid");
+        if (v[kStatusX5Sticky] != 0) return set_error(GSC_ERR_KERNEL, kX5BoundMsg);
+        return set_error(GSC_ERR_KERNEL, kFxRangeMsg);
     }
     return GSC_OK;
 }
@@ -681,7 +716,23 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     a.out = d + n_in;
     a.out_sd = P;
     a.out_sp = 1;
-    GSC_TRY(run_points(*ctx, ro, a, st));
+    const bool fx = point_form(ro, a) == GSC_FORM_MIXED;
+    if (fx) GSC_CUDA(cudaMemsetAsync(ctx->status + kStatusFxFlag, 0, sizeof(int), st));
+    GSC_TRY(run_points(*ctx, ro, a, st, ctx->status + kStatusFxFlag));
+    if (fx) {
+        // wave numbers past the integer phase range: AUTO recomputes on the
+        // plain FP64 kernel, an explicit mixed form reports it
+        int flag = 0;
+        GSC_CUDA(cudaMemcpyAsync(&flag, ctx->status + kStatusFxFlag, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        if (flag) {
+            if (ro.form != GSC_FORM_AUTO) return set_error(GSC_ERR_KERNEL, kFxRangeMsg);
+            Resolved rp = ro;
+            rp.form = GSC_FORM_PLAIN_F64;
+            GSC_TRY(run_points(*ctx, rp, a, st, nullptr));
+        }
+    }
     if (os_p == 1 && (nout == 1 || os_d == P)) {
         Prefault pf;
         if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
@@ -764,7 +815,7 @@ static int dev_plain(const double *cov, const double *z1, const double *z2, cons
     a.out = out;
     a.out_sd = P;
     a.out_sp = 1;
-    return run_points(*ctx, ro, a, ro.stream);
+    return run_points(*ctx, ro, a, ro.stream, ctx->status + kStatusFxSticky);
 }
 
 // ---------------------------------------------------------------------------
@@ -843,7 +894,7 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
     a.out_sp = 1;
     Resolved rp = ro;
     rp.form = form;
-    return run_points(ctx, rp, a, st);
+    return run_points(ctx, rp, a, st, ctx.status + kStatusFxSticky);
 }
 
 static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,

@@ -46,8 +46,8 @@ enum KernelId : int32_t {
     K_GRID_EXPAND = 9,     // meshgrid of structured axes (plain form on grids)
     K_SEP_TC_F16X5 = 10,   // tcgen05 separable contraction, exact leading term
     K_MIXED_MODES = 11,    // per-mode records of the mixed form
-    K_MIXED_SCALAR = 12,   // mixed form, double-float phase, scalar field
-    K_MIXED_INCOMPR = 13,  // mixed form, double-float phase, vector field
+    K_MIXED_SCALAR = 12,   // mixed form, integer phase, scalar field
+    K_MIXED_INCOMPR = 13,  // mixed form, integer phase, vector field
     K_MIXED_F64PHASE = 14, // mixed form with the phase in FP64
     K_SEP_F64 = 15,        // separable contraction on the FP64 MMA
     K_FOURIER_SCALE = 16,  // spectrum factor folded into z1, z2 (Fourier method)
@@ -199,7 +199,14 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st);
 int split_reduce(const double *part, int64_t S, int64_t nout, int64_t P, double *out, int64_t sd,
                  int64_t sp, cudaStream_t st);
 
-// ---- mixed-precision summators (mixed.cu) -----------------------------------
+// ---- mixed-precision summators (mixed_fx.cu, mixed.cu) ------------------------
+// GSC_FORM_MIXED: integer fixed-point phase, table and polynomial e^{i theta}
+// (mixed_fx.cu).  range_flag (device word, may be null) is set to 1 when a
+// wave number is too large for the integer phase at these positions (the
+// output is then invalid).
+int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream_t st);
+// GSC_FORM_MIXED_F64PHASE: FP64 phase, FP32 sincos polynomials (mixed.cu);
+// f64phase = false forwards to mixed_fx_run.
 int mixed_run(DeviceCtx &ctx, const PlainArgs &a, bool f64phase, cudaStream_t st);
 
 // Allocation-free scalar summator (plain.cu): per-mode tables in a fixed
@@ -269,6 +276,17 @@ constexpr int64_t kPlainTableBytesPerMode = 256 * 16;   // W_j[a], a < 256, doub
 constexpr int64_t kPlainRecBytesPerMode = 12 * 8;
 constexpr int64_t kMixedRecBytesPerMode = 20 * 4;
 constexpr int64_t kMixedRec64BytesPerMode = 4 * 8;
+constexpr int64_t kFxRecBytesPerMode = 44 * 4;      // mixed_fx.cu mode record
+// Batched mixed form (mixed_fx.cu): records of every item's modes, the range
+// words of every item's positions (4 x uint64 per item), the range flag.
+int batch_fx_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,
+                    int64_t total_modes, uint32_t *rec, unsigned long long *maxbits,
+                    int *range_flag, cudaStream_t st);
+bool batch_fx_config_ok(int R);
+int batch_fx_occupancy(int R);
+int batch_fx_launch(int R, int blocks, const BatchItem *items, const BatchUnit *units,
+                    int64_t n_units, int *counter, const uint32_t *rec,
+                    const unsigned long long *maxbits, cudaStream_t st);
 
 // Fourier method (src/field.rs:219-249): z1s[j] = sf[j] * z1[j],
 // z2s[j] = sf[j] * z2[j], device pointers; z1s may alias z1 (in place).

@@ -369,6 +369,8 @@ int mx_sm_count(int device) {
 }  // namespace
 
 int mixed_run(DeviceCtx &ctx, const PlainArgs &a, bool f64phase, cudaStream_t st) {
+    // the double-float phase of GSC_FORM_MIXED became mixed_fx.cu's integer phase
+    if (!f64phase) return mixed_fx_run(ctx, a, nullptr, st);
     const int64_t P = a.n_points, N = a.n_modes, dim = a.dim;
     if (P == 0) return GSC_OK;
     const int64_t nout = a.incompr ? dim : 1;
@@ -423,18 +425,14 @@ int mixed_run(DeviceCtx &ctx, const PlainArgs &a, bool f64phase, cudaStream_t st
                                  nc > 0 ? std::min<int64_t>(S, (nc + mps_c - 1) / mps_c) : 1));
         const dim3 gl = first ? grid : g;
         TimedLaunch tl(st);
-        tl.begin(f64phase ? K_MIXED_F64PHASE : (a.incompr ? K_MIXED_INCOMPR : K_MIXED_SCALAR));
+        tl.begin(K_MIXED_F64PHASE);
         int rc;
         if (a.incompr)
-            rc = f64phase ? dispatch_mixed<true, true>(dim, gl, st, a.pos, P, rec, rec64, nc, mps_c,
-                                                       !first, dst, sd, sp, split_stride)
-                          : dispatch_mixed<true, false>(dim, gl, st, a.pos, P, rec, rec64, nc,
-                                                        mps_c, !first, dst, sd, sp, split_stride);
+            rc = dispatch_mixed<true, true>(dim, gl, st, a.pos, P, rec, rec64, nc, mps_c, !first,
+                                            dst, sd, sp, split_stride);
         else
-            rc = f64phase ? dispatch_mixed<false, true>(dim, gl, st, a.pos, P, rec, rec64, nc,
-                                                        mps_c, !first, dst, sd, sp, split_stride)
-                          : dispatch_mixed<false, false>(dim, gl, st, a.pos, P, rec, rec64, nc,
-                                                         mps_c, !first, dst, sd, sp, split_stride);
+            rc = dispatch_mixed<false, true>(dim, gl, st, a.pos, P, rec, rec64, nc, mps_c, !first,
+                                             dst, sd, sp, split_stride);
         tl.end();
         if (rc != GSC_OK) return rc;
         first = 0;
@@ -462,21 +460,17 @@ int batch_mixed_tables(const BatchItem *items, const int64_t *mode_prefix, int64
 namespace {
 using BatchMixedFn = void (*)(const BatchItem *, const BatchUnit *, int64_t, int *, const float *,
                               const double *);
+// the FP64-phase variant only: GSC_FORM_MIXED batches run mixed_fx.cu's kernel
 BatchMixedFn batch_mixed_fn(int R, bool f64p) {
-    if (f64p) {
-        if (R == 2) return batch_mixed_kernel<2, true>;
-        if (R == 4) return batch_mixed_kernel<4, true>;
-        if (R == 8) return batch_mixed_kernel<8, true>;
-    } else {
-        if (R == 2) return batch_mixed_kernel<2, false>;
-        if (R == 4) return batch_mixed_kernel<4, false>;
-        if (R == 8) return batch_mixed_kernel<8, false>;
-    }
+    if (!f64p) return nullptr;
+    if (R == 2) return batch_mixed_kernel<2, true>;
+    if (R == 4) return batch_mixed_kernel<4, true>;
+    if (R == 8) return batch_mixed_kernel<8, true>;
     return nullptr;
 }
 }  // namespace
 
-bool batch_mixed_config_ok(int R) { return batch_mixed_fn(R, false) != nullptr; }
+bool batch_mixed_config_ok(int R) { return batch_mixed_fn(R, true) != nullptr; }
 
 int batch_mixed_occupancy(int R, bool f64phase, int device) {
     BatchMixedFn fn = batch_mixed_fn(R, f64phase);

@@ -1,0 +1,571 @@
+// mixed_fx.cu -- the mixed-precision summators for unstructured points
+// (form GSC_FORM_MIXED), sm_103a.
+//
+// Same sums as plain.cu (reference src/field.rs:37-65 and :97-182) for points
+// without grid structure, where no tensor-core factorisation exists and every
+// point*mode needs its own phase.  GB300 runs FP64 at 1/64 of the FP32
+// rate, so the phase is formed in 32-bit integer arithmetic, where a product
+// modulo 2^32 drops whole turns for free:
+//
+//  * phase in units of 2^-32 turn.  Per call and dimension d, positions are
+//    taken as 61-bit fixed-point integers X = rint(x * 2^s_d) + 2^60 (s_d
+//    from the largest |x_d|: exact for every FP64 coordinate below 2^53
+//    units), split X = Xh 2^29 + Xl.  Per mode, B = kappa_d 2^(61 - s_d)
+//    (kappa = k / 2 pi turns per unit) is held as BI + BF 2^-32.  Then
+//      theta = sum_d  BI Xh + hi32(BF Xh) + hi32(BI * 8 Xl)   (mod 2^32)
+//    is kappa.x (plus a per-mode constant folded into the table below) to
+//    within 3 units per dimension (1.3e-8 rad for three dimensions, at any
+//    |k.x| below 2^30 turns): three 32-bit integer multiply-adds per
+//    dimension, where a double-float product takes eight FP32 instructions
+//    and an FP64 one 1/64 of the pipe.  BI is stored biased by 2^31, so
+//    both high products are unsigned; the bias's effect is a per-point
+//    constant taken out once per point;
+//  * e^{i theta}: theta + 2^27 selects by its top 4 bits one of 16 entries
+//    of the mode's table T[m] = (z1 - i z2) e^{2 pi i (m/16 - phi)} (phi the
+//    per-mode constant; built in FP64 per mode, stored as FP32), the
+//    remainder r (|r| <= 1/32 turn) goes through sin and cos Taylor
+//    polynomials of degree 5 and 6 (truncation below 2.3e-9):
+//    term = Re(T e^{i r});
+//  * the terms are summed in FP32 over tiles of 32 modes with Kahan
+//    compensation, each tile folded into a double-float (TwoSum) running
+//    total, converted to FP64 at the end.
+// Phases beyond 2^30 turns (|k| * max|x| > 6.7e9) do not fit the integer
+// range; such calls are flagged in the range word (the caller recomputes them
+// on the FP64 kernel or reports it).  Non-finite coordinates give NaN, as the
+// reference does.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "dfturns.cuh"
+#include "internal.h"
+
+namespace gsc {
+namespace {
+
+constexpr int kFxThreads = 128;
+static_assert(kFxThreads == kBatchThreads, "batch units assume the block size");
+constexpr int kFxR = 4;                 // points per thread
+constexpr int kFxTile = 32;             // modes per staged tile = accumulation tile
+// 32-bit words per mode: [0..2] BI' (BI + 2^31), [3] w0, [4..6] BF, [7] w1,
+// [8] w2 (projector weights of the incompressible field, FP32), [12..43] the
+// table T[m] as (re, im) FP32 pairs.  A record is 176 bytes, so the 16 table
+// entries of one mode fill the 32 shared-memory banks once: a warp's gather
+// from them is free of bank conflicts.
+constexpr int kFxTab = 12;
+constexpr int kFxRecWords = kFxTab + 32;
+static_assert(kFxRecWords * 4 == kFxRecBytesPerMode, "record layout");
+// radians per unit of the remainder times 16: 2 pi / 2^36
+constexpr float kFxRad = 6.2831854820251465f / 68719476736.0f;
+// Taylor coefficients of sin r = r + r^3 S3 + r^5 S5, cos r = 1 + r^2 C2 +
+// r^4 C4 + r^6 C6 on |r| <= pi/16
+constexpr float kFxS3 = -1.0f / 6.0f, kFxS5 = 1.0f / 120.0f;
+constexpr float kFxC2 = -0.5f, kFxC4 = 1.0f / 24.0f, kFxC6 = -1.0f / 720.0f;
+
+// Fixed-point scale s_d of dimension d from the largest finite |x_d|
+// (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.
+__device__ __forceinline__ int fx_scale(unsigned long long maxbits) {
+    const double m = __longlong_as_double(static_cast<long long>(maxbits));
+    int e = 0;
+    if (m > 0.0) frexp(m, &e);                  // m in [2^(e-1), 2^e)
+    return 60 - e;
+}
+
+// Largest finite |x_d| of pos (dim, P) into maxbits[d] (as the bit pattern
+// of a non-negative double, which orders like the value); maxbits zeroed
+// before.  One warp-level reduction, then one atomic per warp and dimension.
+__device__ __forceinline__ void fx_range_part(const double *__restrict__ pos, int64_t P, int dim,
+                                              int64_t i0, int64_t stride,
+                                              unsigned long long *maxbits) {
+    unsigned long long m[3] = {0ull, 0ull, 0ull};
+    for (int64_t i = i0; i < P; i += stride)
+        for (int d = 0; d < dim && d < 3; ++d) {
+            const double v = fabs(pos[d * P + i]);
+            if (v <= 1.7976931348623157e308)           // finite
+                m[d] = max(m[d], static_cast<unsigned long long>(__double_as_longlong(v)));
+        }
+    for (int d = 0; d < dim && d < 3; ++d) {
+        unsigned long long v = m[d];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((threadIdx.x & 31) == 0 && v) atomicMax(maxbits + d, v);
+    }
+}
+
+__global__ void fx_range_kernel(const double *__restrict__ pos, int64_t P, int dim,
+                                unsigned long long *maxbits) {
+    fx_range_part(pos, P, dim, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x,
+                  static_cast<int64_t>(gridDim.x) * blockDim.x, maxbits);
+}
+
+// The record of mode j (see kFxRecWords).  range_flag (may be null) is set
+// to 1 when a wave number is too large for the integer phase at these
+// positions.
+__device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double z2, int dim,
+                              int64_t n_modes, int64_t j, int incompr,
+                              const unsigned long long *maxbits, uint32_t *__restrict__ r,
+                              int *range_flag) {
+    double k[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
+    bool finite = isfinite(z1) && isfinite(z2);
+    double phi = 0.0;                               // units of 2^-32 turn
+    for (int d = 0; d < 3; ++d) {
+        int32_t bi = 0;
+        uint32_t bf = 0;
+        if (d < dim) {
+            finite = finite && isfinite(k[d]);
+            const double B = ldexp(k[d] * kInv2Pi, 61 - fx_scale(maxbits[d]));
+            if (fabs(B) < 2147483648.0) {
+                const long long bq = __double2ll_rn(ldexp(B, 32));     // B to 2^-32
+                bi = static_cast<int32_t>(bq >> 32);
+                bf = static_cast<uint32_t>(bq);
+                // B 2^31 mod 2^32: what the offset 2^60 of X adds to theta
+                phi += static_cast<double>(static_cast<uint32_t>(bq >> 1)) + 0.5 * (bq & 1);
+            } else if (isfinite(B) && range_flag) {
+                *range_flag = 1;
+            }
+        }
+        r[d] = static_cast<uint32_t>(bi) + 0x80000000u;
+        r[4 + d] = bf;
+    }
+    double w[3] = {0.0, 0.0, 0.0};
+    if (incompr) {   // projector as the reference forms it (src/field.rs:138-152)
+        double kk = 0.0;
+        for (int d = 0; d < dim; ++d) kk = __dadd_rn(kk, __dmul_rn(k[d], k[d]));
+        const double k_2 = __ddiv_rn(k[0], kk);
+        w[0] = __dadd_rn(1.0, -__dmul_rn(k[0], k_2));
+        w[1] = -__dmul_rn(k[1], k_2);
+        w[2] = -__dmul_rn(k[2], k_2);
+    }
+    r[3] = __float_as_uint(__double2float_rn(w[0]));
+    r[7] = __float_as_uint(__double2float_rn(w[1]));
+    r[8] = __float_as_uint(__double2float_rn(w[2]));
+    r[9] = r[10] = r[11] = 0u;
+    phi = fmod(phi, 4294967296.0);
+    const float nanf_ = __int_as_float(0x7fffffff);
+    for (int m = 0; m < 16; ++m) {
+        // (z1 - i z2) e^{2 pi i (m 2^28 - phi) / 2^32}
+        double s, c;
+        sincos((static_cast<double>(m) * 268435456.0 - phi) * 1.4629180792671596e-09, &s, &c);
+        const float tr = __double2float_rn(z1 * c + z2 * s);
+        const float ti = __double2float_rn(z1 * s - z2 * c);
+        r[kFxTab + 2 * m] = __float_as_uint(finite ? tr : nanf_);
+        r[kFxTab + 2 * m + 1] = __float_as_uint(finite ? ti : nanf_);
+    }
+}
+
+__global__ void fx_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+                               const double *__restrict__ z2, int dim, int64_t n_modes,
+                               int64_t j0, int64_t nc, int incompr,
+                               const unsigned long long *maxbits, uint32_t *__restrict__ rec,
+                               int *range_flag) {
+    const int64_t jl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (jl >= nc) return;
+    const int64_t j = j0 + jl;
+    fx_mode_entry(cov, z1[j], z2[j], dim, n_modes, j, incompr, maxbits, rec + jl * kFxRecWords,
+                  range_flag);
+}
+
+// Kahan step: (sum, cmp) += a, cmp holding minus the lost low-order part
+__device__ __forceinline__ void fx_kahan(float &sum, float &cmp, float a) {
+    const float y = a - cmp;
+    const float t = sum + y;
+    cmp = (t - sum) - y;
+    sum = t;
+}
+
+// Knuth's TwoSum: (hi, lo) += a
+__device__ __forceinline__ void fx_two_sum(float &hi, float &lo, float a) {
+    const float s = hi + a;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (a - bb);
+    hi = s;
+    lo += e;
+}
+
+// One block's work: the kFxThreads*R points from p_first (thread t owns
+// p_first + t + r*kFxThreads), modes [jb, je) of the records `rec`; sums
+// written (accumulate=0) or added at dst + i*sd + p*sp.  maxbits: the
+// positions' range words (scales); srec: shared staging of kFxTile records.
+template <int D, int R, bool INC>
+__device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t P, int64_t p_first,
+                                         const uint32_t *__restrict__ rec, int64_t jb, int64_t je,
+                                         int accumulate, double *__restrict__ dst, int64_t sd,
+                                         int64_t sp, const unsigned long long *maxbits,
+                                         uint32_t *srec) {
+    constexpr int NOUT = INC ? D : 1;
+    const int tid = threadIdx.x;
+    const int64_t p0 = p_first + tid;
+
+    int sc[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) sc[d] = fx_scale(maxbits[d]);
+    uint32_t xh[R][D], x8l[R][D], cp[R];
+    bool bad[R];
+    float hi[R][NOUT], lo[R][NOUT];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int64_t p = p0 + r * kFxThreads;
+        // 2^27 centres the remainder on the table entry; + D offsets the
+        // mean truncation of the two high products per dimension
+        uint32_t c = 0x08000000u + D;
+        bad[r] = false;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double x = p < P ? pos[d * P + p] : 0.0;
+            bad[r] = bad[r] || !isfinite(x);
+            const long long X = isfinite(x) ? __double2ll_rn(ldexp(x, sc[d])) : 0ll;
+            const unsigned long long Xp = static_cast<unsigned long long>(X) + (1ull << 60);
+            const uint32_t h = static_cast<uint32_t>(Xp >> 29);
+            const uint32_t l = static_cast<uint32_t>(Xp) & 0x1FFFFFFFu;
+            xh[r][d] = h;
+            x8l[r][d] = l << 3;
+            // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32) and 4 Xl
+            c -= 4u * l + ((h & 1u) << 31);
+        }
+        cp[r] = c;
+#pragma unroll
+        for (int i = 0; i < NOUT; ++i) hi[r][i] = lo[r][i] = 0.f;
+    }
+
+    for (int64_t t0 = jb; t0 < je; t0 += kFxTile) {
+        const int tm = static_cast<int>(min(static_cast<int64_t>(kFxTile), je - t0));
+        __syncthreads();
+        {
+            const uint4 *src = reinterpret_cast<const uint4 *>(rec + t0 * kFxRecWords);
+            uint4 *dstv = reinterpret_cast<uint4 *>(srec);
+            for (int i = tid; i < tm * (kFxRecWords / 4); i += kFxThreads) dstv[i] = src[i];
+        }
+        __syncthreads();
+        float acc[R][NOUT], cmp[R][NOUT];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
+        for (int m = 0; m < tm; ++m) {
+            const uint32_t *mr = srec + m * kFxRecWords;
+            const uint4 h0 = *reinterpret_cast<const uint4 *>(mr);       // BI'0..2, w0
+            const uint4 h1 = *reinterpret_cast<const uint4 *>(mr + 4);   // BF0..2, w1
+            const uint32_t bi[3] = {h0.x, h0.y, h0.z}, bf[3] = {h1.x, h1.y, h1.z};
+            float w[3] = {0.f, 0.f, 0.f};
+            if (INC) {
+                w[0] = __uint_as_float(h0.w);
+                w[1] = __uint_as_float(h1.w);
+                w[2] = __uint_as_float(mr[8]);
+            }
+            const unsigned char *tab = reinterpret_cast<const unsigned char *>(mr + kFxTab);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                uint32_t t = cp[r];
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    t += __umulhi(bi[d], x8l[r][d]);
+                    t += __umulhi(bf[d], xh[r][d]);
+                    t += bi[d] * xh[r][d];
+                }
+                // t = theta + 2^27: entry m = t >> 28 (theta rounded to 1/16
+                // turn), remainder theta - m 2^28 = low28(t) - 2^27, taken as
+                // the signed value ((low28(t) << 4) ^ 2^31) (16 per unit)
+                const float2 T = *reinterpret_cast<const float2 *>(tab + ((t >> 25) & 0x78u));
+                const float rr = static_cast<float>(static_cast<int>((t << 4) ^ 0x80000000u)) * kFxRad;
+                const float r2 = rr * rr;
+                const float sn = fmaf(rr * r2, fmaf(r2, kFxS5, kFxS3), rr);
+                const float cs = fmaf(r2, fmaf(r2, fmaf(r2, kFxC6, kFxC4), kFxC2), 1.0f);
+                const float term = fmaf(T.x, cs, -T.y * sn);
+                if (INC) {
+#pragma unroll
+                    for (int i = 0; i < NOUT; ++i) fx_kahan(acc[r][i], cmp[r][i], w[i] * term);
+                } else {
+                    fx_kahan(acc[r][0], cmp[r][0], term);
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int i = 0; i < NOUT; ++i) {
+                fx_two_sum(hi[r][i], lo[r][i], acc[r][i]);
+                lo[r][i] -= cmp[r][i];
+            }
+    }
+
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int64_t p = p0 + r * kFxThreads;
+        if (p >= P) continue;
+#pragma unroll
+        for (int i = 0; i < NOUT; ++i) {
+            double v = static_cast<double>(hi[r][i]) + static_cast<double>(lo[r][i]);
+            if (bad[r]) v = __longlong_as_double(0x7ff8000000000000ll);
+            double *o = dst + i * sd + p * sp;
+            *o = accumulate ? *o + v : v;
+        }
+    }
+}
+
+// Four resident blocks per SM leave up to 128 registers per thread, room to
+// interleave the R points' integer and FP32 chains.
+template <int D, bool INC>
+__global__ void __launch_bounds__(kFxThreads, 4)
+mixed_fx_kernel(const double *__restrict__ pos, int64_t P, const uint32_t *__restrict__ rec,
+                const unsigned long long *__restrict__ maxbits, int64_t nc, int64_t mps,
+                int accumulate, double *__restrict__ dst, int64_t sd, int64_t sp,
+                int64_t split_stride) {
+    __shared__ __align__(16) uint32_t srec[kFxTile * kFxRecWords];
+    const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
+    const int64_t je = min(nc, jb + mps);
+    fx_block<D, kFxR, INC>(pos, P, static_cast<int64_t>(blockIdx.x) * (kFxThreads * kFxR), rec, jb,
+                           je, accumulate, dst + static_cast<int64_t>(blockIdx.y) * split_stride,
+                           sd, sp, maxbits, srec);
+}
+
+template <int D, bool INC>
+int launch_fx(dim3 grid, cudaStream_t st, const double *pos, int64_t P, const uint32_t *rec,
+              const unsigned long long *maxbits, int64_t nc, int64_t mps, int accumulate,
+              double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    mixed_fx_kernel<D, INC><<<grid, kFxThreads, 0, st>>>(pos, P, rec, maxbits, nc, mps, accumulate,
+                                                         dst, sd, sp, split_stride);
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+int dispatch_fx(int64_t dim, bool inc, dim3 grid, cudaStream_t st, const double *pos, int64_t P,
+                const uint32_t *rec, const unsigned long long *maxbits, int64_t nc, int64_t mps,
+                int accumulate, double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+    if (dim == 1 && !inc)
+        return launch_fx<1, false>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd, sp,
+                                   split_stride);
+    if (dim == 2)
+        return inc ? launch_fx<2, true>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd,
+                                        sp, split_stride)
+                   : launch_fx<2, false>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
+                                         sd, sp, split_stride);
+    if (dim == 3)
+        return inc ? launch_fx<3, true>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd,
+                                        sp, split_stride)
+                   : launch_fx<3, false>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
+                                         sd, sp, split_stride);
+    return set_error(GSC_ERR_DIM, "the mixed form supports dimensions 1, 2, 3 (incompressible: 2, 3)");
+}
+
+int fx_sm_count(int device) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 152;
+    }
+    return n;
+}
+
+// ---- batched ensembles ------------------------------------------------------------
+// Range words of every item: block b of the grid walks item b's positions.
+__global__ void batch_fx_range_kernel(const BatchItem *__restrict__ items,
+                                      unsigned long long *maxbits) {
+    const BatchItem &it = items[blockIdx.x];
+    fx_range_part(it.pos, it.n_points, it.dim, threadIdx.x, blockDim.x, maxbits + 4 * blockIdx.x);
+}
+
+// Records of every item, one thread per mode (Fourier factor folded into z1,
+// z2 first).
+__global__ void batch_fx_table_kernel(const BatchItem *__restrict__ items,
+                                      const int64_t *__restrict__ prefix, int64_t n_items,
+                                      int64_t total, const unsigned long long *maxbits,
+                                      uint32_t *__restrict__ rec, int *range_flag) {
+    const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int64_t lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const BatchItem &it = items[lo];
+    const int64_t j = g - it.mode_off;
+    double z1j = it.z1[j], z2j = it.z2[j];
+    if (it.sf) {
+        const double f = it.sf[j];
+        z1j = __dmul_rn(f, z1j);
+        z2j = __dmul_rn(f, z2j);
+    }
+    fx_mode_entry(it.cov, z1j, z2j, it.dim, it.n_modes, j, it.incompr, maxbits + 4 * lo,
+                  rec + g * kFxRecWords, range_flag);
+}
+
+// Persistent batch kernel (see batch_plain_kernel in plain.cu).
+template <int R>
+__global__ void __launch_bounds__(kFxThreads)
+batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict__ units,
+                int64_t n_units, int *__restrict__ counter, const uint32_t *__restrict__ rec,
+                const unsigned long long *__restrict__ maxbits) {
+    __shared__ __align__(16) uint32_t srec[kFxTile * kFxRecWords];
+    __shared__ int s_unit;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1);
+        __syncthreads();
+        const int64_t u = s_unit;
+        if (u >= n_units) break;
+        const BatchUnit w = units[u];
+        const BatchItem &it = items[w.item];
+        const int64_t P = it.n_points;
+        const int64_t nout = it.incompr ? it.dim : 1;
+        double *dst = it.splits > 1 ? it.part + static_cast<int64_t>(w.split) * nout * P : it.out;
+        const uint32_t *rc = rec + it.mode_off * kFxRecWords;
+        const unsigned long long *mb = maxbits + 4 * w.item;
+        switch (it.dim * 2 + it.incompr) {
+            case 2:
+                fx_block<1, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                break;
+            case 4:
+                fx_block<2, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                break;
+            case 5:
+                fx_block<2, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                break;
+            case 6:
+                fx_block<3, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                break;
+            case 7:
+                fx_block<3, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                break;
+            default:
+                break;
+        }
+    }
+}
+
+using BatchFxFn = void (*)(const BatchItem *, const BatchUnit *, int64_t, int *, const uint32_t *,
+                           const unsigned long long *);
+BatchFxFn batch_fx_fn(int R) {
+    if (R == 2) return batch_fx_kernel<2>;
+    if (R == 4) return batch_fx_kernel<4>;
+    if (R == 8) return batch_fx_kernel<8>;
+    return nullptr;
+}
+
+}  // namespace
+
+int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream_t st) {
+    const int64_t P = a.n_points, N = a.n_modes, dim = a.dim;
+    if (P == 0) return GSC_OK;
+    const int64_t nout = a.incompr ? dim : 1;
+    if (dim < 1 || dim > 3 || (a.incompr && dim == 1))
+        return set_error(GSC_ERR_DIM, "the mixed form supports dimensions 1, 2, 3 (incompressible: 2, 3)");
+    constexpr int64_t kChunk = 1 << 20;   // modes per record build
+    const int64_t pts_per_block = static_cast<int64_t>(kFxThreads) * kFxR;
+    const int64_t bx = (P + pts_per_block - 1) / pts_per_block;
+    if (bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
+    const int64_t chunk = std::min<int64_t>(N, kChunk);
+    // mode splits: enough blocks for 8 per SM when the points alone are few
+    const int64_t want_blocks = static_cast<int64_t>(fx_sm_count(ctx.device)) * 8;
+    int64_t S = std::max<int64_t>(1, (want_blocks + bx - 1) / bx);
+    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kFxTile)));
+    S = std::min<int64_t>(S, 64);
+    int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
+    mps = (mps + kFxTile - 1) / kFxTile * kFxTile;
+    if (mps > 0) S = std::max<int64_t>(1, (chunk + mps - 1) / mps);
+    if (N == 0) S = 1;
+
+    const size_t rec_bytes = static_cast<size_t>(chunk) * kFxRecBytesPerMode;
+    const size_t part_bytes = S > 1 ? static_cast<size_t>(S) * nout * P * sizeof(double) : 0;
+    const size_t off_mb = (rec_bytes + 255) / 256 * 256;
+    const size_t off_part = off_mb + 256;
+    GSC_TRY(ensure_dev(ctx, ctx.scratch, off_part + part_bytes + 256));
+    GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
+    unsigned char *sbase = static_cast<unsigned char *>(ctx.scratch.ptr);
+    uint32_t *rec = reinterpret_cast<uint32_t *>(sbase);
+    unsigned long long *maxbits = reinterpret_cast<unsigned long long *>(sbase + off_mb);
+    double *part = reinterpret_cast<double *>(sbase + off_part);
+
+    double *dst = S > 1 ? part : a.out;
+    const int64_t sd = S > 1 ? P : a.out_sd;
+    const int64_t sp = S > 1 ? 1 : a.out_sp;
+    const int64_t split_stride = S > 1 ? nout * P : 0;
+    const dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(S));
+
+    {
+        TimedLaunch tl(st);
+        tl.begin(K_MIXED_MODES);
+        GSC_CUDA(cudaMemsetAsync(maxbits, 0, 4 * sizeof(unsigned long long), st));
+        const int64_t rb = std::min<int64_t>((P + 255) / 256, 4 * fx_sm_count(ctx.device));
+        fx_range_kernel<<<static_cast<unsigned>(std::max<int64_t>(rb, 1)), 256, 0, st>>>(
+            a.pos, P, static_cast<int>(dim), maxbits);
+        tl.end();
+        GSC_CUDA(cudaGetLastError());
+    }
+    int64_t j0 = 0;
+    int first = 1;
+    do {
+        const int64_t nc = std::min<int64_t>(N - j0, kChunk);
+        if (nc > 0) {
+            TimedLaunch tl(st);
+            tl.begin(K_MIXED_MODES);
+            fx_mode_kernel<<<static_cast<unsigned>((nc + 127) / 128), 128, 0, st>>>(
+                a.cov, a.z1, a.z2, static_cast<int>(dim), N, j0, nc, a.incompr ? 1 : 0, maxbits,
+                rec, range_flag);
+            tl.end();
+            GSC_CUDA(cudaGetLastError());
+        }
+        const int64_t mps_c = nc > 0 ? std::min<int64_t>(mps, nc) : 0;
+        const dim3 g(grid.x, static_cast<unsigned>(
+                                 nc > 0 ? std::min<int64_t>(S, (nc + mps_c - 1) / mps_c) : 1));
+        TimedLaunch tl(st);
+        tl.begin(a.incompr ? K_MIXED_INCOMPR : K_MIXED_SCALAR);
+        const int rc = dispatch_fx(dim, a.incompr, first ? grid : g, st, a.pos, P, rec, maxbits, nc,
+                                   mps_c, !first, dst, sd, sp, split_stride);
+        tl.end();
+        if (rc != GSC_OK) return rc;
+        first = 0;
+        j0 += nc;
+    } while (j0 < N);
+
+    if (S > 1) GSC_TRY(split_reduce(part, S, nout, P, a.out, a.out_sd, a.out_sp, st));
+    GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+    return GSC_OK;
+}
+
+// ---- batched ensembles ----------------------------------------------------------
+int batch_fx_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,
+                    int64_t total_modes, uint32_t *rec, unsigned long long *maxbits,
+                    int *range_flag, cudaStream_t st) {
+    if (n_items == 0) return GSC_OK;
+    TimedLaunch tl(st);
+    tl.begin(K_BATCH_TABLES);
+    GSC_CUDA(cudaMemsetAsync(maxbits, 0, static_cast<size_t>(n_items) * 4 * sizeof(unsigned long long),
+                             st));
+    batch_fx_range_kernel<<<static_cast<unsigned>(n_items), 1024, 0, st>>>(items, maxbits);
+    if (total_modes > 0)
+        batch_fx_table_kernel<<<static_cast<unsigned>((total_modes + 127) / 128), 128, 0, st>>>(
+            items, mode_prefix, n_items, total_modes, maxbits, rec, range_flag);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+bool batch_fx_config_ok(int R) { return batch_fx_fn(R) != nullptr; }
+
+int batch_fx_occupancy(int R) {
+    BatchFxFn fn = batch_fx_fn(R);
+    if (!fn) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kFxThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int batch_fx_launch(int R, int blocks, const BatchItem *items, const BatchUnit *units,
+                    int64_t n_units, int *counter, const uint32_t *rec,
+                    const unsigned long long *maxbits, cudaStream_t st) {
+    BatchFxFn fn = batch_fx_fn(R);
+    if (!fn) return set_error(GSC_ERR_INVALID, "unsupported batch configuration");
+    TimedLaunch tl(st);
+    tl.begin(K_BATCH_MIXED);
+    fn<<<blocks, kFxThreads, 0, st>>>(items, units, n_units, counter, rec, maxbits);
+    tl.end();
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+}  // namespace gsc

@@ -68,10 +68,14 @@ extern "C" {
                                   tensor-memory accumulator sums exactly,
                                   the rest drained in chunks; max error
                                   below 1e-6 of the field RMS               */
-#define GSC_FORM_MIXED      6  /* any points: phase in double-float (FP32
-                                  pairs), FP32 sincos, FP32 sums per 32 modes
-                                  with a compensated total; below 1e-6 of
-                                  the field RMS for |k.x| up to ~1e6        */
+#define GSC_FORM_MIXED      6  /* any points: phase k.x mod one turn in
+                                  32-bit fixed point (three integer
+                                  multiply-adds per dimension, within 2^-30
+                                  turns), FP32 table and polynomial sincos,
+                                  FP32 sums per 32 modes with a compensated
+                                  total; below 1e-6 of the field RMS.
+                                  |k| * max|x| beyond 2^30 turns is flagged
+                                  (see gsc_device_status)                    */
 #define GSC_FORM_MIXED_F64PHASE 7 /* as GSC_FORM_MIXED with the phase and its
                                   reduction in FP64                          */
 #define GSC_FORM_SEP_F64    8  /* structured grids: separable contraction in
@@ -119,8 +123,11 @@ const char *gsc_kernel_name(int32_t kernel_id);
 
 /* Status of the kernels launched by device-pointer calls on `device`
  * (-1 = current): waits for them, returns GSC_OK or GSC_ERR_KERNEL (a
- * pipeline wait gave up; the output of that call is invalid), and clears
- * the status.  Host-pointer calls check it themselves. */
+ * pipeline wait gave up, or a GSC_FORM_MIXED call or batch met a wave
+ * number whose phase exceeds its integer range; the output of that call is
+ * invalid), and clears the status.  Host-pointer calls check it themselves
+ * (with GSC_FORM_AUTO a mixed call past the range is recomputed on the plain
+ * FP64 kernel). */
 int gsc_device_status(int32_t device);
 
 /* Frees the scratch memory the library keeps on `device` (-1 = current)
