@@ -842,10 +842,14 @@ static int check_structured(int64_t dim, int64_t N, const int64_t *n, bool incom
 }
 
 // All pointers are device pointers; out is (ncomp, P) row-major.
+// host_call: the caller synchronises and reads the x5 bound flag itself
+// (host-pointer entry points); else a device-pointer call, which queues the
+// FP64 fallback behind an AUTO x5 launch.
 static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov, const double *z1,
                           const double *z2, int64_t dim, int64_t N, const double *const *axis,
                           const int64_t *n, bool incompr, double *out, cudaStream_t st,
-                          const std::function<int(int64_t, int64_t)> *on_rows = nullptr) {
+                          const std::function<int(int64_t, int64_t)> *on_rows = nullptr,
+                          bool host_call = false) {
     int64_t P = 1;
     for (int d = 0; d < dim; ++d) P *= n[d];
     if (P == 0) return GSC_OK;
@@ -867,6 +871,22 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
         a.out = out;
         a.status = ctx.status;
         a.on_rows = on_rows;
+        if (form == GSC_FORM_SEP_F16X5) {
+            a.bound_flag = ctx.status + kStatusX5Flag;
+            if (!host_call && ro.form != GSC_FORM_AUTO) a.bound_sticky = ctx.status + kStatusX5Sticky;
+            GSC_TRY(sep_tc_run(ctx, a, st));
+            if (!host_call && ro.form == GSC_FORM_AUTO) {
+                // the FP64 form, queued behind: its launches do nothing unless
+                // the x5 launch flagged these inputs
+                SepArgs f = a;
+                f.form = GSC_FORM_SEP_F64;
+                f.on_rows = nullptr;
+                f.bound_flag = f.bound_sticky = nullptr;
+                f.run_if = ctx.status + kStatusX5Flag;
+                GSC_TRY(sep_f64_run(ctx, f, st));
+            }
+            return GSC_OK;
+        }
         return form == GSC_FORM_SEP_F64 ? sep_f64_run(ctx, a, st) : sep_tc_run(ctx, a, st);
     }
     // plain FP64 forms on the expanded grid
@@ -977,7 +997,7 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         return GSC_OK;
     };
     int rc = run_structured(*ctx, ro, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr, dout,
-                            st, pinned ? &on_rows : nullptr);
+                            st, pinned ? &on_rows : nullptr, true);
     if (copying) {
         // queued copies land in the caller's array: they finish before return
         const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
@@ -995,6 +1015,25 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         tc.end();
     }
     GSC_TRY(check_status(*ctx, st));
+    if (structured_form(ro, dim) == GSC_FORM_SEP_F16X5) {
+        // inputs past the exact leading sum's bound: AUTO recomputes on the
+        // FP64 form, an explicit sep_f16x5 reports it
+        int flag = 0;
+        GSC_CUDA(cudaMemcpyAsync(&flag, ctx->status + kStatusX5Flag, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        if (flag) {
+            if (ro.form != GSC_FORM_AUTO) return set_error(GSC_ERR_KERNEL, kX5BoundMsg);
+            Resolved rf = ro;
+            rf.form = GSC_FORM_SEP_F64;
+            GSC_TRY(run_structured(*ctx, rf, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr,
+                                   dout, st, nullptr, true));
+            tc.begin(K_COPY_D2H);
+            GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+            tc.end();
+            GSC_TRY(check_status(*ctx, st));
+        }
+    }
     return GSC_OK;
 }
 

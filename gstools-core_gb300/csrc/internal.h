@@ -226,6 +226,16 @@ struct SepArgs {
     int chunk_kblocks;        // k-blocks per FP32 accumulation chunk, 0 = default
     double *out;              // (ncomp, prod n) row-major, device
     int *status;              // device status word (0 = ok)
+    // sep_f16x5 only (device words, may be null): the call sets bound_flag
+    // to 1 when the inputs break the exact main sum's bound (checked before
+    // and while the GEMM runs; its output is then invalid), else 0, and sets
+    // bound_sticky to 1 then
+    int *bound_flag = nullptr;
+    int *bound_sticky = nullptr;
+    // sep_f64 only: null, or a device word; every launch of the call does
+    // nothing while it is 0 (a fallback queued behind an x5 launch whose
+    // bound_flag it is)
+    const int *run_if = nullptr;
     // sep_f16x5 only: when set, the GEMM runs as one launch per wave of
     // whole row tiles and this is called after each launch is queued with
     // the (slice, row) range [lo, hi) whose output that launch completes,

@@ -37,9 +37,11 @@ struct F64Tab {
     double2 *svec;     // [nb][n_modes]
     double2 *btab;     // [n_modes][nm]
     double *g;         // [ncn_pad][k_pad]
+    const int *run_if; // null, or a device word: the launch does nothing while it is 0
 };
 
 __global__ void f64_svec_kernel(F64Tab t) {
+    if (t.run_if && *t.run_if == 0) return;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= static_cast<int64_t>(t.nb) * t.n_modes) return;
     const int b = static_cast<int>(i / t.n_modes), j = static_cast<int>(i % t.n_modes);
@@ -55,6 +57,7 @@ __global__ void f64_svec_kernel(F64Tab t) {
 }
 
 __global__ void f64_btab_kernel(F64Tab t) {
+    if (t.run_if && *t.run_if == 0) return;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= static_cast<int64_t>(t.n_modes) * t.nm) return;
     const int j = static_cast<int>(i / t.nm), m = static_cast<int>(i % t.nm);
@@ -64,6 +67,7 @@ __global__ void f64_btab_kernel(F64Tab t) {
 }
 
 __global__ void f64_gtab_kernel(F64Tab t) {
+    if (t.run_if && *t.run_if == 0) return;
     const int half_k = t.k_pad / 2;
     const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= static_cast<int64_t>(t.ncn_pad) * half_k) return;
@@ -105,10 +109,12 @@ struct F64Params {
     int m_tiles, n_tiles;
     double *out;
     int64_t comp_stride, batch_stride, row_stride;
+    const int *run_if;   // as in F64Tab
 };
 
 __global__ void __launch_bounds__(kF64Threads)
 sep_f64_kernel(const F64Params p) {
+    if (p.run_if && *p.run_if == 0) return;
     __shared__ double As[TM * LDS];
     __shared__ double Bs[TN * LDS];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -230,6 +236,7 @@ int sep_f64_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.svec = reinterpret_cast<double2 *>(base + off_svec);
     t.btab = reinterpret_cast<double2 *>(base + off_btab);
     t.g = reinterpret_cast<double *>(base + off_g);
+    t.run_if = a.run_if;
     {
         TimedLaunch tl(st);
         tl.begin(K_SEP_TABLES);
@@ -256,6 +263,7 @@ int sep_f64_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.comp_stride = P;
     p.batch_stride = static_cast<int64_t>(nm) * nn;
     p.row_stride = nn;
+    p.run_if = a.run_if;
     const int64_t grid = static_cast<int64_t>(nb) * m_tiles * n_tiles;
     if (grid > 0x7fffffff) return set_error(GSC_ERR_INVALID, "grid too large");
     TimedLaunch tl(st);

@@ -140,6 +140,23 @@ __device__ __forceinline__ double f32_to_f64_pow2(float f, uint32_t ebias) {
     return __hiloint2double(static_cast<int>(tiny ? sign : hi), static_cast<int>(tiny ? 0u : u << 29));
 }
 
+// v * 2^q as FP64, exactly, with integer operations only: |v| < 2^31 has at
+// most 31 significant bits; q keeps the result a normal FP64 number.  The
+// sentinel v = -2^31 (a NaN sum) gives NaN.
+__device__ __forceinline__ double i32_to_f64_pow2(int v, int q) {
+    const uint32_t sign = static_cast<uint32_t>(v) & 0x80000000u;
+    const uint32_t a = v < 0 ? 0u - static_cast<uint32_t>(v) : static_cast<uint32_t>(v);
+    const int lz = __clz(a);                     // a in [2^k, 2^(k+1)), k = 31 - lz
+    // a << (lz + 21) as a 64-bit value puts the leading 1 at bit 52; its
+    // words by 32-bit funnel shifts
+    const uint32_t sh = static_cast<uint32_t>(lz) + 21u;              // 21 .. 52
+    const uint32_t mhi = sh >= 32u ? a << (sh - 32u) : __funnelshift_l(a, 0u, sh);
+    const uint32_t mlo = sh >= 32u ? 0u : a << sh;
+    const uint32_t hi = sign | (static_cast<uint32_t>(1023 + 31 - lz + q) << 20) | (mhi & 0xFFFFFu);
+    const double d = __hiloint2double(static_cast<int>(a == 0u ? sign : hi), static_cast<int>(a == 0u ? 0u : mlo));
+    return v == static_cast<int>(0x80000000u) ? __longlong_as_double(0x7ff8000000000000ll) : d;
+}
+
 template <bool BF16>
 struct Split;
 template <>
@@ -183,6 +200,10 @@ struct TabArgs {
     float2 *btab;                // [n_modes][nm]
     uint32_t *ghi, *glo;         // [ncn_pad][k_pad/2] packed (re, -im) pairs
     float *wnorm;                // x5 form: {W, 1/W}, W = 2^ceil(log2 max|z1 - i z2|)
+    int *bound_flag;             // x5 form: 1 when the exact main sum cannot be guaranteed
+    int *bound_sticky;           // x5 form: set to 1 (never cleared here) in that case
+    float *l1kb;                 // x5 form: per k-block bound of the leading products (counts)
+    int kc;                      // x5 form: k-blocks per cross-accumulator chunk
     int kbt;                     // x5 form: k-blocks (16 modes each)
     int bn;                      // x5 form: G rows per stage block (tile width)
     // x5 form: FP32 inputs of the tables (sep_x5_split_kernel): per mode
@@ -502,16 +523,22 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
 //                    G1 = 2^15 * rint(G * 2^11) / 2^11           (12-bit integer grid),
 // F2 = f16(F*2^15 - F1), F3 = f16(F*2^15 - F1 - F2), G2 = f16(G*2^15 - G1).
 // Every product F1*G1 is an integer multiple of 2^(30-(bF-1)-11) ("counts");
-// bF (3..9) is picked on the device so that six standard deviations of the
-// field stay below 2^23 counts, so the "main" TMEM accumulator adds them
-// EXACTLY whatever the hardware rounding.  (Exactness holds for fields of
-// random modes, as GSTools draws them, while the budget asks for bF >= 3:
-// up to about 1.8e6 modes of standard-normal z1, z2.  A field value beyond
-// ~12 standard deviations would start rounding the main sum.)  The four cross products
+// bF (3..9) is picked on the device (wnorm_block) so that six standard
+// deviations of a random field stay below 2^23 counts; every partial sum of
+// the "main" TMEM accumulator is then an FP32 integer and the accumulator
+// adds them EXACTLY whatever the hardware rounding.  For any inputs this is
+// checked as the sum runs: at every chunk boundary the main sum plus the
+// most the next chunk's modes can add (the sum of |F1 G1| over them) must
+// stay within 2^24 counts; inputs that break it (weights far from random,
+// e.g. all in phase at a grid point) are flagged, and the caller recomputes
+// them on the FP64 form or reports it.  The four cross products
 // F2G1 + F1G2 + F2G2 + F3G1 (about 2^-bF of the field) go to a second TMEM
-// accumulator that the workers drain every KC = 16 k-blocks into FP32
-// totals held in registers, so their rounding never builds up at full
-// magnitude.  Representation: F to about 2^-(bF+22), G to 2^-24 relative
+// accumulator that the workers drain every KC = 16 k-blocks (8 for the
+// incompressible field) into FP32 totals held in registers, so their
+// rounding never builds up at full magnitude.  The output is formed without
+// any FP32 rounding at the field's magnitude: the exact main sum and the
+// cross total are turned into one 32-bit integer of 1/64 counts (exact for
+// the main sum) and that into FP64 with integer operations.  Representation: F to about 2^-(bF+22), G to 2^-24 relative
 // (integers up to 2^11 are exact in f16, so 12 bits is the widest exact G
 // grid; the exact main sum's budget fixes bF + bG, and G's single rest
 // slice makes G the coarser factor); the product F3G2 (below 2^-28) is
@@ -533,31 +560,63 @@ constexpr int X5_LAUNCH_REGS = 168;             // 65536 / 384, rounded down to 
 constexpr float kUnit = 32768.0f;            // 2^15
 constexpr int kLeadBitsG = 12;               // G1 grid: 2^15 * rint(G * 2^11) / 2^11
 
+// Sum over n modes of the largest leading product of each, in counts (see
+// wnorm_block): leading grid 2^(bF-1), s1 = sum |w_j| / W over those modes.
+__host__ __device__ __forceinline__ double x5_lead_bound(int bf, double s1, int64_t n) {
+    return 2049.0 * (ldexp(1.0, bf - 1) * (1.0 + 0x1p-21) * s1 + 0.7072 * static_cast<double>(n));
+}
+
 // Normaliser and leading-grid width of the x5 form, one block of 256 threads:
-//   W = 2^e >= max |z1 - i z2|  (so |s / W| <= 1 and |F| <= 1),
-//   the leading F grid 2^(bF-1) with bF (3..9) chosen so that the expected
-//   extreme of the exact main sum, about 6 * sqrt(sum |w|^2 / 2) / W *
-//   2^(bF+bG-2) counts (6 standard deviations of the field), stays below
-//   2^23 counts with bG = 12: one bit of headroom under FP32's 2^24.
-// The s vector is stored unnormalised; the slicing constants absorb 1/W (a
-// power of two, so the slices are those of s / W bit for bit):
-//   wnorm = {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W}
+//   W = 2^e > max |z1 - i z2|  (so |s / W| <= 1 and |F| <= 1),
+//   the leading F grid 2^(bF-1) with bF (3..9) the largest for which six
+//   standard deviations of the field, 6 sqrt(sum |w|^2 / 2) / W 2^(bF+10)
+//   counts, stay below 2^23 counts (one bit under FP32's exact 2^24), and
+//   no window of kc k-blocks can move a partial sum by more than 2^23 counts.
+// Exactness for any inputs rests on a bound, checked while the sum runs:
+// per mode j the leading product is at most
+//     L(j) = 2049 (|w_j| / W (1 + 2^-21) 2^(bF-1) + 0.7072)  counts
+// (|F| <= |w_j| up to FP32 rounding, |G| <= 1, each integer-grid rounding at
+// most half a step per component), so a partial sum within a chunk of
+// k-blocks moves at most by the chunk's sum of L(j).  l1kb[kb] holds that
+// sum per k-block (rounded up); the kernel checks |main| + the next chunk's
+// sum <= 2^24 at every chunk boundary and flags the call otherwise.  When
+// even bF = 3 leaves a window above 2^23, bound_flag is set here and the
+// GEMM skips its work; otherwise it is cleared (the GEMM may set it).
+//   The s vector is stored unnormalised; the slicing constants absorb 1/W (a
+//   power of two, so the slices are those of s / W bit for bit):
+//   wnorm = {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W, flag, 2^(bF-14), q},
+//   an output value being (its 1/64-count integer) * 2^q, q = log2(W) - 16 - bF
 __device__ void wnorm_block(const double *__restrict__ z1, const double *__restrict__ z2, int n,
-                            float *__restrict__ wnorm) {
+                            int kbt, int kc, float *__restrict__ wnorm, float *__restrict__ l1kb,
+                            int *__restrict__ bound_flag, int *__restrict__ bound_sticky) {
     __shared__ double red_max[256], red_sum[256];
+    __shared__ float red_kb[256];
+    __shared__ double s_W;
+    __shared__ int s_bf;
+    // one pass: largest |w|^2, sum of |w|^2, and per k-block the sum of |w|
+    // rounded up (FP32, an upper bound), kept in l1kb until bF is known
     double m = 0.0, sum = 0.0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
-        const double a = z1[j] * z1[j] + z2[j] * z2[j];
-        m = fmax(m, a);
-        sum += a;
+    float mk = 0.f;
+    for (int kb = threadIdx.x; kb < kbt; kb += blockDim.x) {
+        float a1 = 0.f;
+        for (int j = kb * 16; j < kb * 16 + 16 && j < n; ++j) {
+            const double a = z1[j] * z1[j] + z2[j] * z2[j];
+            m = fmax(m, a);
+            sum += a;
+            a1 = __fadd_ru(a1, __fsqrt_ru(__double2float_ru(a)));
+        }
+        l1kb[kb] = a1;
+        mk = fmaxf(mk, a1);
     }
     red_max[threadIdx.x] = m;
     red_sum[threadIdx.x] = sum;
+    red_kb[threadIdx.x] = mk;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o) {
             red_max[threadIdx.x] = fmax(red_max[threadIdx.x], red_max[threadIdx.x + o]);
             red_sum[threadIdx.x] += red_sum[threadIdx.x + o];
+            red_kb[threadIdx.x] = fmaxf(red_kb[threadIdx.x], red_kb[threadIdx.x + o]);
         }
         __syncthreads();
     }
@@ -566,15 +625,36 @@ __device__ void wnorm_block(const double *__restrict__ z1, const double *__restr
         const double mx = sqrt(red_max[0]);
         if (mx > 0.0 && isfinite(mx)) frexp(mx, &e);           // mx in [2^(e-1), 2^e)
         const double W = ldexp(1.0, e);
+        s_W = W;
         const double typ = 6.0 * sqrt(fmax(red_sum[0], 1e-300) * 0.5) / W;
         // 2^(bF - 1 + kLeadBitsG - 1) * typ <= 2^23
         int bf = static_cast<int>(floor(23.0 + 2.0 - kLeadBitsG - log2(fmax(typ, 1.0))));
         bf = bf < 3 ? 3 : (bf > 9 ? 9 : bf);
+        // no window of kc k-blocks may move a partial sum by more than 2^23 counts
+        const double mkw = static_cast<double>(red_kb[0]) / W;
+        auto window = [&](int b) { return kc * x5_lead_bound(b, mkw, 16); };
+        while (bf > 3 && window(bf) > 8388608.0) --bf;
+        const int over = (window(bf) > 8388608.0 || !isfinite(mkw)) ? 1 : 0;
+        s_bf = bf;
         wnorm[0] = static_cast<float>(W);
         wnorm[1] = static_cast<float>(1.0 / W);
         wnorm[2] = static_cast<float>(ldexp(1.0, bf - 1) / W);      // lead scale of s
         wnorm[3] = kUnit / ldexpf(1.0f, bf - 1);                     // lead unit
         wnorm[4] = static_cast<float>(kUnit / W);                    // slice unit of s
+        wnorm[5] = static_cast<float>(over);
+        wnorm[6] = ldexpf(1.0f, bf - 14);                            // sum -> 1/64 counts
+        wnorm[7] = static_cast<float>(e - 16 - bf);                  // 1/64 counts -> field: 2^q
+        if (bound_flag) *bound_flag = over;
+        if (bound_sticky && over) *bound_sticky = 1;
+    }
+    __syncthreads();
+    const int bf = s_bf;
+    const double W = s_W;
+    for (int kb = threadIdx.x; kb < kbt; kb += blockDim.x) {
+        const int cnt = min(16, n - kb * 16);
+        // rounded up: the bound must not shrink in FP32
+        l1kb[kb] = __double2float_ru(x5_lead_bound(bf, static_cast<double>(l1kb[kb]) / W, cnt) *
+                                     (1.0 + 1e-6));
     }
 }
 
@@ -764,7 +844,7 @@ __device__ __forceinline__ void gtab_x5_entry(const TabArgs &t, int64_t i) {
 __global__ void __launch_bounds__(256)
 sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) {
     if (blockIdx.x == 0) {
-        wnorm_block(t.z1, t.z2, t.n_modes, t.wnorm);
+        wnorm_block(t.z1, t.z2, t.n_modes, t.kbt, t.kc, t.wnorm, t.l1kb, t.bound_flag, t.bound_sticky);
         return;
     }
     int64_t i = static_cast<int64_t>(blockIdx.x - 1) * 256 + threadIdx.x;
@@ -784,7 +864,10 @@ sep_x5_tables_kernel(TabArgs t, int64_t n_svec, int64_t n_btab, int64_t n_gtab) 
 
 struct X5Params {
     TcParams base;
-    const float *wnorm;      // {W, 1/W, 2^(bF-1) / W, 2^15 / 2^(bF-1), 2^15 / W}
+    const float *wnorm;      // see wnorm_block
+    const float *l1kb;       // per k-block bound of the leading products, counts
+    int *bound_flag;         // set to 1 when a partial sum could leave FP32's exact range
+    int *bound_sticky;       // null, or set to 1 as well
     const unsigned char *g1, *g2, *bt;   // stage blocks (see the table kernels)
     // Tail split: tiles [0, full_tiles) run whole, one per CTA; each of the
     // n_split later tiles runs as ksplit CTAs (the launch's first n_split *
@@ -793,7 +876,8 @@ struct X5Params {
     // to finish (counted in ws_cnt[slot]) adds them in part order and stores.
     int tile0;               // first tile of this launch (launches of wave-sized row ranges)
     int full_tiles, ksplit, n_split;
-    float *ws;
+    float *ws;               // cross totals of the parts
+    float *ws_main;          // exact main sums of the parts (same layout)
     int *ws_cnt;
     // 2 or 3: the output is written by tiled bulk stores through the kernel's
     // tensor map of that rank ((nn, rows) or (nn, rows, components));
@@ -820,6 +904,10 @@ constexpr int X5_BOX_OFF = 65536;   // epilogue: FP64 output boxes (2 x 8 warps 
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
 constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
+// incompressible fields: the cross accumulator's truncation is the larger part
+// of their error (the transverse components are small), so it is drained
+// twice as often (about 3 % of the GEMM's time on 192^3 x 2048 modes)
+constexpr int X5_CHUNK_INC = 8;
 constexpr int kMaxSplit = 4;                         // most parts a tail tile is split into
 
 // Stage layout for tiles of BNX output columns (256, or 192 where that pads
@@ -868,6 +956,10 @@ __global__ void __launch_bounds__(X5_THREADS, 1)
 sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     using L = X5Layout<BNX>;
     const TcParams &p = xp.base;
+    // inputs whose main sum could leave FP32's exact range are not computed
+    // (the flag is the same for every CTA, so whole CTAs leave before any
+    // barrier or TMEM allocation)
+    if (xp.wnorm[5] != 0.f) return;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
@@ -878,7 +970,8 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     uint64_t *cross_full = bars + 9;            // MMA commit -> workers (per chunk)
     uint64_t *cross_empty = bars + 10;          // workers -> MMA (256 arrivals)
     uint64_t *drain = bars + 11;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 12);
+    uint64_t *main_read = bars + 12;            // workers -> MMA: main sum read (256 arrivals)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 13);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *last_part = reinterpret_cast<volatile int *>(tmem_slot + 2);
 
@@ -918,6 +1011,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         mbar_init(cross_full, 1);
         mbar_init(cross_empty, 256);
         mbar_init(drain, 1);
+        mbar_init(main_read, 256);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -1001,6 +1095,14 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 const uint32_t sa = smem_u32(smem + s * L::STAGE);
                 const uint32_t f1 = sa, f2 = sa + X5_F_BYTES, f3 = sa + 2 * X5_F_BYTES;
                 const uint32_t g1 = sa + L::OFF_G1, g2 = sa + L::OFF_G2;
+                // a new chunk's main MMAs wait until the workers have read
+                // the main sum at the boundary, its cross MMAs until they have
+                // drained the last chunk
+                if (first && c > 0) {
+                    ok = mbar_wait(main_read, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
+                    if (!ok) break;
+                    tc_fence_after();
+                }
 #pragma unroll
                 for (int kk = 0; kk < X5_BK / 16; ++kk) {
                     const uint32_t o = kk * 32;
@@ -1051,8 +1153,40 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
 #pragma unroll
         for (int i = 0; i < L::HC; ++i) tot[i] = 0.f;
         int pend = 0;                                           // next cross chunk to drain
+        // main-sum limit for the chunk after chunk c, in accumulator units:
+        // 2^24 counts less the most that chunk's leading products can add
+        const float cnt_unit = xp.wnorm[3] * 16.0f;             // 2^(20-bF)
+        auto main_limit = [&](int c) -> float {
+            float l1 = 0.f;
+            const int i1 = min(KB, (c + 2) * KC);
+#pragma unroll 1
+            for (int i = (c + 1) * KC; i < i1; ++i) l1 = __fadd_ru(l1, __ldg(xp.l1kb + kb_of(i)));
+            return (16777216.0f - l1) * cnt_unit;
+        };
         auto drain_chunk = [&]() {
             tc_fence_after();
+            // the main sums at the boundary first: the next chunk's main MMAs
+            // resume once every worker has read them
+            float mmax = 0.f;
+#pragma unroll 1
+            for (int g = 0; g < L::HC / 16; ++g) {
+                uint32_t v[16];
+                __syncwarp();
+                tmem_ld16(t_main + lane_off + L::HC * h + 16 * g, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) mmax = fmaxf(mmax, fabsf(__uint_as_float(v[i])));
+            }
+            tc_fence_before();
+            mbar_arrive(main_read);
+            // the main sum at this chunk boundary plus the next chunk's bound
+            // must stay within 2^24 counts.  Rows past the grid are skipped
+            // (their zero s factors meet stale B data, possibly NaN); a NaN
+            // sum (NaN inputs) passes and leaves as NaN
+            if (row_ok && mmax > main_limit(pend)) {
+                *xp.bound_flag = 1;
+                if (xp.bound_sticky) *xp.bound_sticky = 1;
+            }
 #pragma unroll
             for (int g = 0; g < L::HC / 16; ++g) {
                 uint32_t v[16];
@@ -1161,13 +1295,21 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         // swizzled boxes in shared memory and written by tiled bulk stores;
         // where the output layout does not allow those, they are turned
         // around in shared memory and each lane stores one column.
-        const float unscale = xp.wnorm[0] * (1.0f / (kUnit * kUnit));
-        // unscale is a power of two (W and 2^30 are): as a normal FP32
-        // number its exponent goes into the conversion (else the product is
-        // formed first)
-        const int uexp = static_cast<int>((__float_as_uint(unscale) >> 23) & 0xFF);
-        const bool pow2 = uexp > 0 && uexp < 255 && (__float_as_uint(unscale) & 0x7FFFFFu) == 0;
-        const uint32_t ebias = static_cast<uint32_t>(uexp - 127 + 896) << 20;
+        // Each output leaves as a 32-bit integer of 1/64 counts: the exact main
+        // sum times 64 (below 2^30 by the leading-grid bound) plus the cross
+        // total rounded to 1/64 count, summed as integers; it becomes FP64 by
+        // integer operations (i32_to_f64_pow2) with the scale 2^q folded into
+        // the exponent.  No FP32 rounding at the field's magnitude remains.
+        const float to_t = xp.wnorm[6];
+        const int qexp = static_cast<int>(xp.wnorm[7]);
+        // a NaN or infinite sum (NaN inputs) leaves as the sentinel -2^31,
+        // which no finite sum reaches (|main| < 2^30, the cross total far less)
+        auto fixed = [&](float mainv, float crossv) -> float {
+            const bool finite = fabsf(mainv) <= 3.0e38f && fabsf(crossv) <= 3.0e38f;
+            return __int_as_float(finite ? __float2int_rn(mainv * to_t) + __float2int_rn(crossv * to_t)
+                                         : static_cast<int>(0x80000000u));
+        };
+        auto to_f64 = [&](float bits) -> double { return i32_to_f64_pow2(__float_as_int(bits), qexp); };
         float *trf = reinterpret_cast<float *>(smem) + warp * (32 * 33);
         // output offset of row (warp's first row) + R; the warp's first row
         // is slice bs0, row ms0
@@ -1179,18 +1321,24 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
             }
             return static_cast<int64_t>(bs) * p.batch_stride + static_cast<int64_t>(ms) * p.row_stride;
         };
-        // tot[32g .. 32g+31] += the TMEM sums of column group g (cross, main)
-        auto read_group = [&](int g) {
+        // column group g: tot[32g .. 32g+31] += the cross accumulator's last
+        // chunk, then each main sum with its cross total goes to `use` (in
+        // halves of 16, to keep registers free)
+        auto read_group = [&](int g, auto &&use) {
             uint32_t v[32];
             __syncwarp();
             tmem_ld32(t_cross + lane_off + L::HC * h + 32 * g, v);
             tmem_ld_wait();
 #pragma unroll
             for (int t = 0; t < 32; ++t) tot[32 * g + t] += __uint_as_float(v[t]);
-            tmem_ld32(t_main + lane_off + L::HC * h + 32 * g, v);
-            tmem_ld_wait();
 #pragma unroll
-            for (int t = 0; t < 32; ++t) tot[32 * g + t] = __uint_as_float(v[t]) + tot[32 * g + t];
+            for (int hf = 0; hf < 2; ++hf) {
+                uint32_t mv[16];
+                tmem_ld16(t_main + lane_off + L::HC * h + 32 * g + 16 * hf, mv);
+                tmem_ld_wait();
+#pragma unroll
+                for (int t = 0; t < 16; ++t) use(32 * g + 16 * hf + t, __uint_as_float(mv[t]));
+            }
         };
         auto store_group = [&](int g) {
             const int rows = max(0, min(32, rows_valid - 32 * q));
@@ -1212,8 +1360,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                     for (int c = 0; c < 8; ++c) {
                         const int t = 32 * g + 16 * hb + 2 * c;
                         *reinterpret_cast<double2 *>(bx + hb * 4096 + lane * 128 + ((c ^ (lane & 7)) << 4)) =
-                            pow2 ? make_double2(f32_to_f64_pow2(tot[t], ebias), f32_to_f64_pow2(tot[t + 1], ebias))
-                                 : make_double2(f32_to_f64(tot[t] * unscale), f32_to_f64(tot[t + 1] * unscale));
+                            make_double2(to_f64(tot[t]), to_f64(tot[t + 1]));
                     }
                 fence_proxy_async_smem();
                 __syncwarp();
@@ -1235,14 +1382,14 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 // column per lane: 256 contiguous bytes per row and store
                 __syncwarp();
 #pragma unroll
-                for (int t = 0; t < 32; ++t) trf[lane * 33 + t] = tot[32 * g + t] * unscale;
+                for (int t = 0; t < 32; ++t) trf[lane * 33 + t] = tot[32 * g + t];
                 __syncwarp();
                 const int gn = gc + lane;
                 const int bs0 = static_cast<int>(rq / p.nm), ms0 = static_cast<int>(rq % p.nm);
                 if (gn < p.ncn) {
                     const int comp = gn / p.nn;
                     double *oc = p.out + comp * p.comp_stride + (gn - comp * p.nn);
-                    for (int R = 0; R < rows; ++R) oc[out_row(bs0, ms0, R)] = f32_to_f64(trf[R * 33 + lane]);
+                    for (int R = 0; R < rows; ++R) oc[out_row(bs0, ms0, R)] = to_f64(trf[R * 33 + lane]);
                 }
             }
         };
@@ -1251,25 +1398,28 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 tc_fence_after();
 #pragma unroll
                 for (int g = 0; g < L::HC / 32; ++g) {
-                    read_group(g);
+                    read_group(g, [&](int c, float mainv) { tot[c] = fixed(mainv, tot[c]); });
                     store_group(g);
                 }
                 __syncwarp();
             }
         } else if (SPLIT) {
-            // a split tile: write this part's sums, count the parts, and the
-            // last part adds all of them in part order (the result does not
-            // depend on which part finishes last), then stores as above
+            // a split tile: write this part's main sums and cross totals,
+            // count the parts, and the last part adds all of them in part
+            // order (the result does not depend on which part finishes
+            // last; the main sums add exactly), then stores as above
+            const int slot = tile - xp.tile0 - xp.full_tiles, ks = xp.ksplit;
+            const int64_t slot_off = static_cast<int64_t>(slot) * ks * BNX * BM;
+            // this thread's column c of part k sits at col0[(k * BNX + c) * BM]
+            const int64_t c_off = static_cast<int64_t>(L::HC * h) * BM + r;
+            float *col0 = xp.ws + slot_off + c_off;
+            float *colm = xp.ws_main + slot_off + c_off;
             if (ok) {
                 tc_fence_after();
+                float *wm = colm + static_cast<int64_t>(part) * BNX * BM;
 #pragma unroll
-                for (int g = 0; g < L::HC / 32; ++g) read_group(g);
-            }
-            const int slot = tile - xp.tile0 - xp.full_tiles, ks = xp.ksplit;
-            float *wsl = xp.ws + static_cast<int64_t>(slot) * ks * BNX * BM;
-            // this thread's column c of part k sits at col0[(k * BNX + c) * BM]
-            float *col0 = wsl + static_cast<int64_t>(L::HC * h) * BM + r;
-            if (ok) {
+                for (int g = 0; g < L::HC / 32; ++g)
+                    read_group(g, [&](int c, float mainv) { wm[c * BM] = mainv; });
                 float *wp = col0 + static_cast<int64_t>(part) * BNX * BM;
 #pragma unroll
                 for (int c = 0; c < L::HC; ++c) wp[c * BM] = tot[c];
@@ -1283,14 +1433,26 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 __threadfence();
                 if (threadIdx.x == 0) xp.ws_cnt[slot] = 0;          // ready for the next launch
                 // every part (this one included) is read back from the
-                // workspace, so the sums need no second register array
+                // workspace, so the sums need no second register array; the
+                // parts' main sums add exactly while the running total stays
+                // within 2^24 counts
+                const float lim = 16777216.0f * cnt_unit;
+                bool over = false;
 #pragma unroll
                 for (int c = 0; c < L::HC; ++c) {
-                    float a = __ldcg(col0 + c * BM);
+                    float a = __ldcg(col0 + c * BM), mm = __ldcg(colm + c * BM);
 #pragma unroll
                     for (int k = 1; k < kMaxSplit; ++k)
-                        if (k < ks) a += __ldcg(col0 + (k * BNX + c) * BM);
-                    tot[c] = a;
+                        if (k < ks) {
+                            a += __ldcg(col0 + (k * BNX + c) * BM);
+                            mm += __ldcg(colm + (k * BNX + c) * BM);
+                            over = over || fabsf(mm) > lim;
+                        }
+                    tot[c] = fixed(mm, a);
+                }
+                if (over && row_ok) {
+                    *xp.bound_flag = 1;
+                    if (xp.bound_sticky) *xp.bound_sticky = 1;
                 }
 #pragma unroll
                 for (int g = 0; g < L::HC / 32; ++g) store_group(g);
@@ -1384,6 +1546,7 @@ int configure_x5() {
 int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const bool x5 = a.form == GSC_FORM_SEP_F16X5;
     const bool bf16 = a.form == GSC_FORM_SEP_BF16X3;
+    if (x5 && !a.bound_flag) return set_error(GSC_ERR_INVALID, "sep_f16x5 needs a bound flag word");
     const int dim = static_cast<int>(a.dim);
     const int N = static_cast<int>(a.n_modes);
     const int ncomp = a.incompr ? dim : 1;
@@ -1464,12 +1627,15 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
     const size_t off_glo = align_up(off_ghi + g_bytes, 1024);
     const size_t off_ws = align_up(off_glo + g_bytes, 1024);
-    const size_t ws_bytes = static_cast<size_t>(n_split) * ksplit * bnx * BM * sizeof(float);
+    // cross totals and exact main sums of the split parts
+    const size_t ws_half = static_cast<size_t>(n_split) * ksplit * bnx * BM * sizeof(float);
+    const size_t ws_bytes = 2 * ws_half;
     const size_t off_cnt = align_up(off_ws + ws_bytes, 1024);
     // x5: FP32 mode records and axis splits for the tables
     const int ax_off_m = dim == 3 ? nb : 0, ax_off_n = ax_off_m + nm;
     const int64_t n_ax = static_cast<int64_t>(ax_off_n) + nn;
-    const size_t off_mrec = align_up(off_cnt + static_cast<size_t>(n_split) * sizeof(int), 1024);
+    const size_t off_l1 = align_up(off_cnt + static_cast<size_t>(n_split) * sizeof(int), 256);
+    const size_t off_mrec = align_up(off_l1 + (x5 ? sizeof(float) * static_cast<size_t>(KB) : 0), 1024);
     const size_t off_axs = align_up(off_mrec + (x5 ? sizeof(float) * kRecX5 * static_cast<size_t>(N) : 0), 1024);
     const size_t total = off_axs + (x5 ? sizeof(float2) * static_cast<size_t>(n_ax) : 0) + 256;
     GSC_TRY(ensure_dev(ctx, ctx.scratch, total));
@@ -1502,6 +1668,10 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.ghi = reinterpret_cast<uint32_t *>(base + off_ghi);
     t.glo = reinterpret_cast<uint32_t *>(base + off_glo);
     t.wnorm = x5 ? reinterpret_cast<float *>(base + off_wn) : nullptr;
+    t.bound_flag = x5 ? a.bound_flag : nullptr;
+    t.bound_sticky = x5 ? a.bound_sticky : nullptr;
+    t.l1kb = x5 ? reinterpret_cast<float *>(base + off_l1) : nullptr;
+    t.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : (a.incompr ? X5_CHUNK_INC : X5_CHUNK);
     t.kbt = KB;
     t.bn = bnx;
     t.mrec = reinterpret_cast<float *>(base + off_mrec);
@@ -1564,7 +1734,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     p.nn = nn;
     p.ncn = ncn;
     p.kb_total = KB;
-    p.kc = a.chunk_kblocks > 0 ? a.chunk_kblocks : (x5 ? X5_CHUNK : 4);
+    p.kc = x5 ? t.kc : (a.chunk_kblocks > 0 ? a.chunk_kblocks : 4);
     p.m_tiles = m_tiles;
     p.rows_total = rows_total;
     p.n_tiles = n_tiles;
@@ -1581,10 +1751,14 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
         X5Params xp;
         xp.base = p;
         xp.wnorm = t.wnorm;
+        xp.l1kb = t.l1kb;
+        xp.bound_flag = a.bound_flag;
+        xp.bound_sticky = a.bound_sticky;
         xp.g1 = reinterpret_cast<const unsigned char *>(t.ghi);
         xp.g2 = reinterpret_cast<const unsigned char *>(t.glo);
         xp.bt = reinterpret_cast<const unsigned char *>(t.btab);
         xp.ws = reinterpret_cast<float *>(base + off_ws);
+        xp.ws_main = reinterpret_cast<float *>(base + off_ws + ws_half);
         xp.ws_cnt = reinterpret_cast<int *>(base + off_cnt);
         // The output (ncomp, rows, nn) is dense; tiled bulk stores write it
         // where its rows are 16-byte aligned and, for several components, no

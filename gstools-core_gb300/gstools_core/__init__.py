@@ -628,5 +628,9 @@ def release_buffers(device=-1) -> None:
 
 def device_status(device=-1) -> None:
     """Raises GscError if a kernel of an earlier device-array call on ``device``
-    reported a failed pipeline wait (the output of that call is invalid)."""
+    reported a failed pipeline wait, a mixed-form call met a wave number past
+    its integer phase range, or an explicit ``form="sep_f16x5"`` call met
+    inputs past the bound of its exact leading sum (the output of that call is
+    invalid; form "auto" recomputes such calls on an FP64 form).  The report
+    is cleared once raised."""
     _native.check(_native.lib.gsc_device_status(device))

@@ -65,9 +65,14 @@ extern "C" {
                                   (about 5e-5)                                */
 #define GSC_FORM_SEP_F16X5  5  /* structured grids, 5 products: the leading
                                   product on an integer grid that the FP32
-                                  tensor-memory accumulator sums exactly,
-                                  the rest drained in chunks; max error
-                                  below 1e-6 of the field RMS               */
+                                  tensor-memory accumulator sums exactly
+                                  (checked at every chunk boundary), the
+                                  rest drained in chunks, FP64 output
+                                  without FP32 rounding at the field's
+                                  magnitude; max error below 1e-6 of the
+                                  field RMS.  Inputs that break the bound
+                                  (weights far from random) are flagged:
+                                  see gsc_device_status                      */
 #define GSC_FORM_MIXED      6  /* any points: phase k.x mod one turn in
                                   32-bit fixed point (three integer
                                   multiply-adds per dimension, within 2^-30
@@ -123,11 +128,14 @@ const char *gsc_kernel_name(int32_t kernel_id);
 
 /* Status of the kernels launched by device-pointer calls on `device`
  * (-1 = current): waits for them, returns GSC_OK or GSC_ERR_KERNEL (a
- * pipeline wait gave up, or a GSC_FORM_MIXED call or batch met a wave
- * number whose phase exceeds its integer range; the output of that call is
- * invalid), and clears the status.  Host-pointer calls check it themselves
- * (with GSC_FORM_AUTO a mixed call past the range is recomputed on the plain
- * FP64 kernel). */
+ * pipeline wait gave up; a GSC_FORM_MIXED call or batch met a wave number
+ * whose phase exceeds its integer range; or an explicit GSC_FORM_SEP_F16X5
+ * call met inputs past the bound that keeps its leading sum exact; the
+ * output of that call is invalid), and clears the status.  Host-pointer
+ * calls check it themselves.  With GSC_FORM_AUTO such calls are recomputed
+ * on an FP64 form: host-pointer calls after the check, device-pointer x5
+ * calls by a GSC_FORM_SEP_F64 computation queued behind the x5 launch that
+ * does nothing unless the device flagged the inputs. */
 int gsc_device_status(int32_t device);
 
 /* Frees the scratch memory the library keeps on `device` (-1 = current)
