@@ -9,27 +9,34 @@ benchmark data):
   c1  plain 2-D unstructured: 100,000 points in [0,100]^2, 1000 modes,
       Gaussian spectrum (k ~ N(0, 2/l^2), l = 10)
   c2  structured 3-D scalar: 256^3 grid, spacing 1, 2000 modes, exponential
-      spectrum (multivariate Student-t nu=1, / l, l = 20)        [default]
+      spectrum (multivariate Student-t nu=1, / l, l = 20)
   c3  unstructured 3-D: 16,777,216 points in [0,1000]^3, 4096 modes,
       exponential spectrum l = 5
   c4  incompressible 3-D: 192^3 grid, 2048 modes, Gaussian spectrum l = 8
+  c5  batched ensemble: 512 realizations (seed r each; 2-D for r < 256, else
+      3-D; points log-uniform 1e3..1e6 in [0,500]^d; modes log-uniform
+      256..8192; Gaussian spectrum for even r, exponential for odd r,
+      l uniform in [2, 50]) in one persistent launch replayed as a CUDA graph
   field  the reference's criterion field benchmarks (benches/main.rs:51-133):
       summate 2-D and 3-D, summate_incompr 2-D and 3-D, summate_fourier 2-D
       on 10,000 points x 1000 modes, inputs read from the reference's
       benches/input text format (--input-dir; synthesized stand-ins when
       absent); one step = the five calls
-  c5  batched ensemble: 512 realizations (seed r each; 2-D for r < 256, else
-      3-D; points log-uniform 1e3..1e6 in [0,500]^d; modes log-uniform
-      256..8192; Gaussian spectrum for even r, exponential for odd r,
-      l uniform in [2, 50]) in one persistent launch replayed as a CUDA graph
+  all  [default] c1 .. c5 in turn; the JSON line is c5's (the largest
+      workload, 1.7e11 point*modes per step) with every workload's full
+      record under "configs" and a short "summary"
 
 One step = one full summation of the workload.  `value` is timed with CUDA
 events on the launch stream, inputs resident in HBM, L2 flushed (a 256 MiB
 write) before every timed step; `e2e` is the same metric through the public
-host API (numpy in, numpy out, host<->device copies inside the timed call).
+host API at the benchmark spec's tolerance 1e-6 (numpy in, numpy out, host<->device
+copies inside the timed call).  Every workload's output is compared, value
+by value, with an FP64 form on the GPU that is itself checked against the
+oracle in the same run (error_vs_fp64_full), and a seeded subset with the
+oracle directly (error_vs_oracle).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2] [--form auto]
+                    [--workload all] [--form auto]
 """
 from __future__ import annotations
 
@@ -371,16 +378,29 @@ def warm_up(torch, step, w, min_s=0.5, timing=False, flush=None):
     return n
 
 
-def run_ours(args, world, rank, local):
+def full_error(torch, got, ref):
+    """max |got - ref| and RMS(got - ref) over every value, relative to the
+    RMS of ref (device tensors, any shape)."""
+    g = got.reshape(-1)
+    r = ref.reshape(-1)
+    rms = float(torch.sqrt(torch.mean(r * r)))
+    d = (g - r).abs()
+    return {"max_abs_over_rms": float(d.max()) / rms if rms > 0 else float(d.max()),
+            "rms_over_rms": float(torch.sqrt(torch.mean(d * d))) / rms if rms > 0 else 0.0,
+            "values_checked": int(g.numel())}
+
+
+def run_ours(args, world, rank, local, wname, cpu_seconds, form_arg="auto"):
     import torch
     import gstools_core as gsc
     import oracle
 
     torch.cuda.set_device(local)
-    w = workload(args.workload)
+    w = workload(wname)
     P, N = n_points(w), w["cov"].shape[1]
+    nout = w["dim"] if w["incompr"] else 1
     work = float(P) * N
-    form = default_form(w) if args.form == "auto" else args.form
+    form = default_form(w) if form_arg == "auto" else form_arg
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -405,9 +425,9 @@ def run_ours(args, world, rank, local):
     dom = max(kern, key=lambda k: sum(kern[k]))
     launches_per_step = len(kern[dom]) / args.steps
     dom_ms = float(np.mean(kern[dom]))
-    roof = roofline(args, w, dom, dom_ms, launches_per_step)
+    roof = roofline(args, w, dom, dom_ms, launches_per_step, wname=wname)
 
-    # ---- parity spot check of this very output against the oracle ----------
+    # ---- parity of this very output against the oracle on a seeded subset --
     err, check = None, None
     if not args.no_check:
         rng = np.random.default_rng(7)
@@ -427,59 +447,84 @@ def run_ours(args, world, rank, local):
                     "reference": "oracle (field.rs restatement), FP64"}
         err = check(out_d)
 
-    # ---- e2e through the public host API (before the long comparison arms,
-    # so that it runs in the same state of the GPU as the timed steps) ------
-    e2e = None
+    # ---- e2e through the public host API at the benchmark spec's tolerance (before
+    # the long comparison arms, so that it runs in the same state of the GPU
+    # as the timed steps).  The call GSTools makes -- summate(cov_samples, z1,
+    # z2, pos) with pos the flattened meshgrid on structured grids -- plus
+    # tolerance=1e-6; on a grid the library recognises the mesh on the host
+    # and only the modes and the axes cross the bus.
+    e2e, e2e_structured, dropin = None, None, None
     if not args.no_e2e:
-        nout = w["dim"] if w["incompr"] else 1
-        if w["axes"] is not None and form.startswith("sep"):
-            host_call = gsc.summate_incompr_structured if w["incompr"] else gsc.summate_structured
-            host_args = (w["cov"], w["z1"], w["z2"], w["axes"])
+        call = gsc.summate_incompr if w["incompr"] else gsc.summate
+        if w["axes"] is not None:
+            pos_h = flat_grid(w["axes"])
             h2d = (w["cov"].size + 2 * N + sum(len(a) for a in w["axes"])) * 8
         else:
-            pos_h = w["pos"] if w["pos"] is not None else flat_grid(w["axes"])
-            host_call = gsc.summate_incompr if w["incompr"] else gsc.summate
-            host_args = (w["cov"], w["z1"], w["z2"], pos_h)
+            pos_h = w["pos"]
             h2d = (w["cov"].size + 2 * N + pos_h.size) * 8
-        host_call(*host_args, form=form)      # warm the staging buffers
-        ts, kms = [], []
-        for _ in range(max(1, min(args.steps, 3))):
-            barrier(world)
-            t0 = time.perf_counter()
-            host_call(*host_args, form=form, timing=True)
-            ts.append(time.perf_counter() - t0)
-            kms.append(split_timings(gsc.last_timings()))
-        t_e2e = max_over_ranks(world, float(np.mean(ts)))
-        e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nout * P * 8),
-               "ms_per_step": t_e2e * 1e3, "api": "gstools_core." + host_call.__name__,
-               "kernel_ms_per_step": float(np.mean([k for k, _ in kms])),
-               "copy_ms_per_step": float(np.mean([c for _, c in kms])),
-               "timing": "host wall clock around the synchronous call (kernel_ms_per_step, "
-                         "copy_ms_per_step: the call's own kernels and host-device copies, "
-                         "CUDA events on its stream)"}
 
-    # ---- the unmodified GSTools call on a structured mesh: the point API with
-    # the flattened meshgrid and default arguments (routed to the separable
-    # FP64 form, the drop-in accuracy bar)
-    dropin = None
-    if not args.no_e2e and w["axes"] is not None:
-        flat = flat_grid(w["axes"])
-        call = gsc.summate_incompr if w["incompr"] else gsc.summate
-        call(w["cov"], w["z1"], w["z2"], flat)
-        ts = []
-        for _ in range(2):
-            t0 = time.perf_counter()
-            call(w["cov"], w["z1"], w["z2"], flat, timing=True)
-            ts.append(time.perf_counter() - t0)
-        t_d = max_over_ranks(world, float(np.mean(ts)))
-        dropin = {"value": work * world / t_d / 1e9, "unit": UNIT, "ms_per_step": t_d * 1e3,
-                  "api": "gstools_core." + call.__name__ + "(cov_samples, z1, z2, pos) with the "
-                         "flattened meshgrid and default form / tolerance",
-                  "kernels": sorted({k for k, _ in gsc.last_timings() if not k.startswith("copy_")}),
-                  "h2d_bytes_per_step": int((w["cov"].size + 2 * N + flat.size) * 8),
-                  "d2h_bytes_per_step": int((w["dim"] if w["incompr"] else 1) * P * 8)}
-        del flat
+        def host_e2e(fn, fargs, kwargs, reps, h2d_bytes, api):
+            fn(*fargs, **kwargs)                  # staging buffers, result pool
+            ts, kms, names = [], [], set()
+            for _ in range(reps):
+                barrier(world)
+                t0 = time.perf_counter()
+                fn(*fargs, timing=True, **kwargs)
+                ts.append(time.perf_counter() - t0)
+                tl = gsc.last_timings()
+                kms.append(split_timings(tl))
+                names |= {k for k, _ in tl if not k.startswith("copy_")}
+            t = max_over_ranks(world, float(np.mean(ts)))
+            return {"value": work * world / t / 1e9, "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d_bytes), "d2h_bytes_per_step": int(nout * P * 8),
+                    "ms_per_step": t * 1e3, "api": api, "kernels": sorted(names),
+                    "kernel_ms_per_step": float(np.mean([k for k, _ in kms])),
+                    "copy_ms_per_step": float(np.mean([c for _, c in kms])),
+                    "timing": "host wall clock around the synchronous call (kernel_ms_per_step, "
+                              "copy_ms_per_step: the call's own kernels and host-device "
+                              "copies, CUDA events on its stream)"}
+        reps = max(1, min(args.steps, 3))
+        e2e = host_e2e(call, (w["cov"], w["z1"], w["z2"], pos_h), {"tolerance": 1e-6}, reps, h2d,
+                       f"gstools_core.{call.__name__}(cov_samples, z1, z2, pos, tolerance=1e-6)"
+                       + (" with pos the flattened meshgrid" if w["axes"] is not None else ""))
+        if w["axes"] is not None:
+            scall = gsc.summate_incompr_structured if w["incompr"] else gsc.summate_structured
+            e2e_structured = host_e2e(
+                scall, (w["cov"], w["z1"], w["z2"], w["axes"]), {"form": form}, reps, h2d,
+                f"gstools_core.{scall.__name__} (the axes; no reference counterpart)")
+            # default arguments: tolerance 1e-12, routed to the FP64 DMMA form
+            dropin = host_e2e(call, (w["cov"], w["z1"], w["z2"], pos_h), {}, 2, h2d,
+                              f"gstools_core.{call.__name__}(cov_samples, z1, z2, pos) with the "
+                              "flattened meshgrid and default form / tolerance (1e-12)")
+        del pos_h
+
+    # ---- every value against an FP64 form on the GPU, itself checked
+    # against the oracle here: the FP64 DMMA contraction on grids, the plain
+    # FP64 kernel on points (its timed step is the plain arm) --------------------
+    full, plain = None, None
+    ref_form = "sep_f64" if w["axes"] is not None else "plain"
+    if not args.no_check or not args.no_plain:
+        rstep, rout = make_device_step(gsc, torch, w, ref_form, dev, stream)
+        rstep()
+        torch.cuda.synchronize()
+        rt, rk, _ = timed_steps(torch, gsc, rstep, stream, 1, flush)
+        gsc.device_status()
+        rms_ = max_over_ranks(world, float(np.mean(rt)))
+        if not args.no_check:
+            full = full_error(torch, out_d, rout)
+            pin = check(rout)
+            full["reference"] = (f"{ref_form} on the GPU ("
+                                 + ("FP64 DMMA contraction" if ref_form == "sep_f64"
+                                    else "plain FP64 kernel")
+                                 + f"), itself {pin['max_abs_over_rms']:.2e} of RMS from the "
+                                   f"oracle on {pin['points_checked']} points in this run")
+            full["reference_vs_oracle"] = pin["max_abs_over_rms"]
+        if ref_form == "plain" and form != "plain":
+            plain = {"value": work * world / (rms_ * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": rms_,
+                     "steps": 1, "path": "plain FP64 kernel",
+                     "kernels_ms": {k: float(np.mean(v)) for k, v in rk.items()}}
+            plain["speedup_of_chosen_form"] = value / plain["value"]
+        del rout
 
     # ---- the other forms on the same workload (one timed step each) -------
     others = {}
@@ -496,24 +541,23 @@ def run_ours(args, world, rank, local):
                          "error_vs_oracle": check(oout) if check else None}
         del oout
 
-    # ---- the plain FP64 kernel on the same workload (the comparison arm) ---
-    plain = None
-    if form != "plain" and not args.no_plain:
-        pstep, _ = make_device_step(gsc, torch, w, "plain", dev, stream)
+    # ---- the plain FP64 kernel on the flattened meshgrid of a grid ----------
+    if plain is None and form != "plain" and not args.no_plain:
+        pstep, pout = make_device_step(gsc, torch, w, "plain", dev, stream)
         pstep()
         torch.cuda.synchronize()
         pt, pk, _ = timed_steps(torch, gsc, pstep, stream, 1, flush)
         pms = max_over_ranks(world, float(np.mean(pt)))
         plain = {"value": work * world / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
-                 "steps": 1, "path": "plain FP64 kernel on the flattened meshgrid"
-                 if w["pos"] is None else "plain FP64 kernel",
+                 "steps": 1, "path": "plain FP64 kernel on the flattened meshgrid",
                  "kernels_ms": {k: float(np.mean(v)) for k, v in pk.items()}}
         plain["speedup_of_chosen_form"] = value / plain["value"]
+        del pout
 
     # ---- CPU baseline (rank 0, N=1 only) -----------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, cores, m, t = time_cpu(w, 1, args.cpu_seconds)
+        v, cores, m, t = time_cpu(w, 1, cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{m} seeded points of the workload x all {N} modes, "
                          f"{t:.1f} s on {cores} threads (oracle/field_oracle.c, "
@@ -523,26 +567,33 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f16 split operands, f32 accumulation, f64 output" if form.startswith("sep")
-                  else "f32 pairs (phase), f32 (sincos, tile sums), f64 output"
+        "dtype": ("f16 split operands, f32 accumulation (leading product exact), f64 output"
+                  if form == "sep_f16x5" else
+                  "f16/bf16 split operands, f32 accumulation, f64 output" if form.startswith("sep_")
+                  else "u32 fixed-point phase, f32 (sincos, tile sums), f64 output"
+                  if form == "mixed" else
+                  "f64 phase, f32 (sincos, tile sums), f64 output"
                   if form.startswith("mixed") else "f64"),
         "data": "synthetic (seeded numpy default_rng)",
-        "config": {"workload": args.workload, "desc": w["desc"], "points": P, "modes": N,
-                   "form": form,
+        "config": {"workload": wname, "desc": w["desc"], "points": P, "modes": N,
+                   "point_modes": work, "form": form,
                    "l2": "flushed by a 256 MiB write before every timed step",
                    "warmup_steps_run": warm,
                    "clocks_window": "nvidia-smi every 50 ms over warm-up and timed steps",
                    "wall_s": t_wall},
+        "error_vs_fp64_full": full,
         "error_vs_oracle": err,
         "plain_fp64": plain,
         "other_forms": others,
         "kernels_ms_per_step": {k: float(np.sum(v) / args.steps) for k, v in kern.items()},
         "gpu_launches": int(launches),
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "dropin_e2e": dropin,
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "e2e_structured_api": e2e_structured, "dropin_e2e_default_tolerance": dropin,
         "clocks": clk.summary(),
     }
-    if rank == 0:
-        print(json.dumps(line))
+    del out_d, flush
+    torch.cuda.empty_cache()
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -584,7 +635,7 @@ def ensemble_cpu_rate(items, target_s, steps=1):
     return work / t / 1e9, cores, desc, t
 
 
-def run_ours_batch(args, world, rank, local):
+def run_ours_batch(args, world, rank, local, cpu_seconds, form_arg="auto"):
     import torch
     import gstools_core as gsc
     import oracle
@@ -596,7 +647,7 @@ def run_ours_batch(args, world, rank, local):
     for it in items:
         k = (it["pos"].shape[0], False)
         dims[k] = dims.get(k, 0.0) + it["pos"].shape[1] * it["cov"].shape[1] / work
-    form = "mixed" if args.form == "auto" else args.form
+    form = "mixed" if form_arg == "auto" else form_arg
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -634,6 +685,7 @@ def run_ours_batch(args, world, rank, local):
         torch.cuda.synchronize()
         barrier(world)
         t_wall = time.perf_counter() - t_wall
+    gsc.device_status()
     ms_step = max_over_ranks(world, float(np.mean(per_step)))
     value = work * world / (ms_step * 1e-3) / 1e9
 
@@ -646,10 +698,11 @@ def run_ours_batch(args, world, rank, local):
     for name, ms in kt:
         kern[name] = kern.get(name, 0.0) + ms
     dom = max(kern, key=kern.get)
-    roof = roofline(args, None, dom, kern[dom], 1, units=work, op_mix=dims)
+    roof = roofline(args, None, dom, kern[dom], 1, units=work, op_mix=dims, wname="c5")
 
-    # parity on a spread of realizations
+    # parity on a spread of realizations against the oracle
     err = None
+    pin_idx = {}
     if not args.no_check:
         rng = np.random.default_rng(7)
         worst, worst_rms = 0.0, 0.0
@@ -659,6 +712,7 @@ def run_ours_batch(args, world, rank, local):
             idx = np.sort(rng.choice(P, size=min(P, 512), replace=False))
             ref = oracle.summator(it["cov"], it["z1"], it["z2"],
                                   np.ascontiguousarray(it["pos"][:, idx]), num_threads=host_cores())
+            pin_idx[r] = (idx, ref)
             got = dev_items[r]["out"].cpu().numpy()[idx]
             rms = float(np.sqrt(np.mean(ref ** 2)))
             worst = max(worst, float(np.max(np.abs(got - ref)) / rms))
@@ -667,9 +721,11 @@ def run_ours_batch(args, world, rank, local):
                "points_checked": "512 per realization of 0, 1, 100, 255, 256, 301, 511",
                "reference": "oracle (field.rs restatement), FP64"}
 
-    # e2e through the host-array API (before the plain FP64 arm, so that it runs
-    # in the same state of the GPU as the timed steps)
-    e2e = None
+    # e2e through the host-array API (before the plain FP64 arm, so that it
+    # runs in the same state of the GPU as the timed steps): the ensemble
+    # call, and the drop-in -- one summate() per realization at tolerance 1e-6,
+    # as GSTools calls the reference for every field of an ensemble
+    e2e, dropin = None, None
     if not args.no_e2e:
         host = [{"kind": "scalar", "cov": it["cov"], "z1": it["z1"], "z2": it["z2"],
                  "pos": it["pos"]} for it in items]
@@ -684,17 +740,36 @@ def run_ours_batch(args, world, rank, local):
         t_e2e = max_over_ranks(world, float(np.mean(ts)))
         e2e = {"value": work * world / t_e2e / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes),
-               "ms_per_step": t_e2e * 1e3, "api": "gstools_core.summate_batch",
+               "ms_per_step": t_e2e * 1e3, "ms_each": [t * 1e3 for t in ts],
+               "api": "gstools_core.summate_batch (the ensemble in one call; C ABI "
+                      "gsc_summate_batch_f64, no reference counterpart)",
                "kernel_ms_per_step": float(np.mean([k for k, _ in kms])),
                "copy_ms_per_step": float(np.mean([c for _, c in kms])),
                "timing": "host wall clock around the synchronous call (kernel_ms_per_step, "
                          "copy_ms_per_step: the call's own kernels and host-device copies, "
                          "CUDA events on its stream)"}
+        for it in items[:8]:
+            gsc.summate(it["cov"], it["z1"], it["z2"], it["pos"], tolerance=1e-6)
+        ts = []
+        for _ in range(2):
+            barrier(world)
+            t0 = time.perf_counter()
+            for it in items:
+                gsc.summate(it["cov"], it["z1"], it["z2"], it["pos"], tolerance=1e-6)
+            ts.append(time.perf_counter() - t0)
+        t_d = max_over_ranks(world, float(np.mean(ts)))
+        dropin = {"value": work * world / t_d / 1e9, "unit": UNIT, "ms_per_step": t_d * 1e3,
+                  "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes),
+                  "api": "gstools_core.summate(cov_samples, z1, z2, pos, tolerance=1e-6), one "
+                         "call per realization (512 calls per step)",
+                  "timing": "host wall clock around the 512 synchronous calls"}
 
-    # the plain FP64 form of the same ensemble (one graph step)
-    plain = None
-    if not args.no_plain and form != "plain":
-        pplan = gsc.Batch(dev_items, form="plain", timing=True)
+    # the plain FP64 form of the same ensemble (one graph step), whose
+    # outputs are the full-field reference of every realization
+    plain, full = None, None
+    if (not args.no_plain or not args.no_check) and form != "plain":
+        ref_items = [dict(d, out=torch.empty_like(d["out"])) for d in dev_items]
+        pplan = gsc.Batch(ref_items, form="plain", timing=True)
         pplan.run_graph(stream.cuda_stream)
         torch.cuda.synchronize()
         flush.fill_(1)
@@ -708,18 +783,37 @@ def run_ours_batch(args, world, rank, local):
         plain = {"value": work * world / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
                  "steps": 1, "path": "persistent FP64 batch kernel", "config": pplan.config}
         plain["speedup_of_chosen_form"] = value / plain["value"]
+        if not args.no_check:
+            worst, worst_rms, n_vals, pin = 0.0, 0.0, 0, 0.0
+            for d, rd in zip(dev_items, ref_items):
+                e = full_error(torch, d["out"], rd["out"])
+                worst = max(worst, e["max_abs_over_rms"])
+                worst_rms = max(worst_rms, e["rms_over_rms"])
+                n_vals += e["values_checked"]
+            for r, (idx, ref) in pin_idx.items():
+                got = ref_items[r]["out"].cpu().numpy()[idx]
+                pin = max(pin, float(np.max(np.abs(got - ref)) / np.sqrt(np.mean(ref ** 2))))
+            full = {"max_abs_over_rms": worst, "rms_over_rms": worst_rms,
+                    "values_checked": n_vals,
+                    "per": "worst realization (each relative to its own field RMS)",
+                    "reference": f"persistent plain FP64 batch kernel on the GPU, itself "
+                                 f"{pin:.2e} of RMS from the oracle on the checked points "
+                                 f"in this run",
+                    "reference_vs_oracle": pin}
         pplan.close()
+        del ref_items
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, cores, desc, _ = ensemble_cpu_rate(items, args.cpu_seconds)
+        v, cores, desc, _ = ensemble_cpu_rate(items, cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f32 pairs (phase), f32 (sincos, tile sums), f64 output"
+        "dtype": ("u32 fixed-point phase, f32 (sincos, tile sums), f64 output"
+                  if form == "mixed" else "f64 phase, f32 (sincos, tile sums), f64 output"
                   if form.startswith("mixed") else "f64"),
         "data": "synthetic (seeded numpy default_rng, one seed per realization)",
         "config": {"workload": "c5", "desc": "batched ensemble, 512 realizations, "
@@ -731,14 +825,18 @@ def run_ours_batch(args, world, rank, local):
                    "warmup_steps_run": warm,
                    "clocks_window": "nvidia-smi every 50 ms over warm-up and timed steps",
                    "wall_s": t_wall},
+        "error_vs_fp64_full": full,
         "error_vs_oracle": err,
         "plain_fp64": plain,
         "kernels_ms_per_step": kern,
         "gpu_launches": int(len(kt) * args.steps),
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "dropin_e2e": dropin,
+        "clocks": clk.summary(),
     }
-    if rank == 0:
-        print(json.dumps(line))
+    plan.close()
+    del dev_items, flush
+    torch.cuda.empty_cache()
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -789,14 +887,14 @@ def field_oracle(kind, arrs, cores):
     return oracle.summator(*arrs, num_threads=cores)
 
 
-def run_ours_field(args, world, rank, local):
+def run_ours_field(args, world, rank, local, form_arg="auto"):
     import torch
     import gstools_core as gsc
 
     torch.cuda.set_device(local)
     calls, source = field_calls(args)
     work = field_work(calls)
-    form = "plain" if args.form == "auto" else args.form
+    form = "plain" if form_arg == "auto" else form_arg
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -853,7 +951,7 @@ def run_ours_field(args, world, rank, local):
         mix[key] = mix.get(key, 0.0) + u
         units += u
     mix = {k: v / units for k, v in mix.items()}
-    roof = roofline(args, None, dom, tot[dom], 1, units=units, op_mix=mix)
+    roof = roofline(args, None, dom, tot[dom], 1, units=units, op_mix=mix, wname="field")
 
     cores = host_cores()
     per_call, err = {}, {}
@@ -925,8 +1023,7 @@ def run_ours_field(args, world, rank, local):
         "gpu_launches": int(launches),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
     }
-    if rank == 0:
-        print(json.dumps(line))
+    return line
 
 
 def measured_peaks():
@@ -940,10 +1037,13 @@ def measured_peaks():
 # FP64 pipe instructions per point*mode of the plain kernel's table path
 # (phase 2d-1, reduction + polynomials + table combine 12, accumulate 1 or d)
 PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17, (3, True): 20}
-# FP32 FMA-pipe instructions per point*mode of the mixed kernel (double-float
-# phase 8 per dimension + 5, sincos and combine 18, Kahan 4); integer and
-# select instructions run on the ALU pipe and are not counted
-MIXED_FP32_OPS = {1: 35, 2: 43, 3: 51}
+# FMA-pipe instructions per point*mode of the mixed kernel (mixed_fx.cu),
+# counted from the source: the integer phase, 3 IMAD per dimension (IMAD
+# issues on the FMA pipe), then 10 FP32 for the remainder's polynomial and the
+# term, and 4 for the Kahan sum per output component (plus one product by
+# the projector weight per component of the incompressible field); the
+# table index, shifts, conversion and table load run on other pipes
+MIXED_FMA_OPS = {(1, False): 17, (2, False): 20, (3, False): 23, (2, True): 26, (3, True): 34}
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
@@ -951,12 +1051,11 @@ MIXED_FP32_OPS = {1: 35, 2: 43, 3: 51}
 PROFILED_TRAFFIC = {
     ("sep_tc_f16x5", "c2"): (12.49e6 + 88.12e6, "profiles/sep_tc_f16x5_c2.md"),
     ("sep_tc_f16x5", "c4"): (167.4e6, "profiles/sep_tc_f16x5_c4.md"),
-    ("mixed_scalar", "c1"): (1.69e6, "profiles/mixed_scalar_c1.md"),
     ("plain_f64_scalar", "c1"): (5.8e6, "profiles/plain_f64_scalar_c1.md"),
 }
 
 
-def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None):
+def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None, wname=None):
     """Roofline entry for the dominant kernel.
 
     Tensor-core forms (bound "tensor"): FLOPs per launch = products x 2 x
@@ -964,7 +1063,7 @@ def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None):
     the number of split products the kernel issues: 5 for sep_f16x5, 3 for
     sep_f16x3 / sep_bf16x3), against the measured dense 16-bit peak.
     FP64 and FP32 forms (bounds "fp64" / "fp32"): the pipe instructions the
-    kernel issues per point*mode (PLAIN_FP64_OPS / MIXED_FP32_OPS), each
+    kernel issues per point*mode (PLAIN_FP64_OPS / MIXED_FMA_OPS), each
     counted as one fused multiply-add (2 FLOPs, the unit of the peak), against
     cuBLAS DGEMM / SGEMM (TF32 off) measured on this GPU."""
     import torch
@@ -972,7 +1071,7 @@ def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None):
         P, N = n_points(w), w["cov"].shape[1]
         units = P * N
     per_launch_units = units / max(launches_per_step, 1)
-    traffic, tsrc = PROFILED_TRAFFIC.get((dom, getattr(args, "workload", None)), (None, None))
+    traffic, tsrc = PROFILED_TRAFFIC.get((dom, wname), (None, None))
     entry = _roofline_entry(args, w, dom, dom_ms, per_launch_units, op_mix, torch)
     entry["traffic"] = traffic
     if tsrc:
@@ -1001,16 +1100,22 @@ def _roofline_entry(args, w, dom, dom_ms, per_launch_units, op_mix, torch):
     if op_mix is None:
         op_mix = {(w["dim"], bool(w["incompr"])): 1.0}
     if mixed:
-        ops = sum(f * MIXED_FP32_OPS[k[0]] * (k[0] if k[1] else 1) for k, f in op_mix.items())
+        ops = sum(f * MIXED_FMA_OPS[k] for k, f in op_mix.items())
     else:
         ops = sum(f * PLAIN_FP64_OPS[k] for k, f in op_mix.items())
     achieved = 2.0 * ops * per_launch_units / (dom_ms * 1e-3) / 1e12
     peak, how = (fp32_peak(torch) if mixed else fp64_peak(torch))
+    # the algorithmic work per point*mode: 2d+3 FLOPs and one sincos (scalar),
+    # 4d+2 FLOPs and one sincos (incompressible)
+    alg = sum(f * ((4 * k[0] + 2) if k[1] else (2 * k[0] + 3)) for k, f in op_mix.items())
+    rate = per_launch_units / (dom_ms * 1e-3)
     return {"bound": "fp32" if mixed else "fp64", "kernel": dom, "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "traffic": None, "peak_source": how,
             "pipe_ops_per_point_mode": ops,
-            "note": f"{ops:.1f} {'FP32' if mixed else 'FP64'} pipe instructions per point*mode "
+            "algorithmic": {"flops_per_point_mode": alg, "tflops": alg * rate / 1e12,
+                            "sincos_per_s": rate},
+            "note": f"{ops:.1f} {'FMA' if mixed else 'FP64'} pipe instructions per point*mode "
                     f"(from the kernel source), each counted as one FMA = 2 FLOPs"}
 
 
@@ -1054,11 +1159,13 @@ def fp32_peak(torch):
 
 
 # ---------------------------------------------------------------------------
-def run_reference(args, world, rank):
-    """The reference's CPU algorithm (oracle restatement) on the host cores."""
-    if rank != 0:
-        return
-    if args.workload == "field":
+def reference_line(args, world, wname, cpu_seconds):
+    """The reference's CPU algorithm (oracle restatement) on the host cores,
+    one JSON record for workload `wname`."""
+    common = {"impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": world,
+              "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f64"}
+    if wname == "field":
         calls, source = field_calls(args)
         work = field_work(calls)
         cores = host_cores()
@@ -1070,52 +1177,87 @@ def run_reference(args, world, rank):
             ts.append(time.perf_counter() - t0)
         t = float(np.mean(ts))
         v = work / t / 1e9
-        print(json.dumps({
-            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": source,
-            "config": {"workload": "field", "desc": "benches/main.rs field benchmarks",
-                       "form": "reference CPU (rayon-equivalent restatement)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "the full five calls per step"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }))
-        return
-    if args.workload == "c5":
+        return dict(common, value=v, ms_per_step=t * 1e3, data=source,
+                    config={"workload": "field", "desc": "benches/main.rs field benchmarks",
+                            "form": "reference CPU (rayon-equivalent restatement)"},
+                    cpu_baseline={"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": "the full five calls per step"},
+                    e2e={"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+    if wname == "c5":
         items = ensemble()
-        v, cores, desc, t = ensemble_cpu_rate(items, args.cpu_seconds, max(1, args.steps))
-        line = {
-            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded numpy default_rng, one seed per realization)",
-            "config": {"workload": "c5", "desc": "batched ensemble, 512 realizations",
-                       "form": "reference CPU (rayon-equivalent restatement)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": desc},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }
-        print(json.dumps(line))
-        return
-    w = workload(args.workload)
+        v, cores, desc, t = ensemble_cpu_rate(items, cpu_seconds, max(1, args.steps))
+        return dict(common, value=v, ms_per_step=t * 1e3,
+                    data="synthetic (seeded numpy default_rng, one seed per realization)",
+                    config={"workload": "c5", "desc": "batched ensemble, 512 realizations",
+                            "form": "reference CPU (rayon-equivalent restatement)"},
+                    cpu_baseline={"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": desc},
+                    e2e={"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+    w = workload(wname)
     N = w["cov"].shape[1]
-    v, cores, m, t = time_cpu(w, max(1, args.steps), args.cpu_seconds)
-    line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded numpy default_rng)",
-        "config": {"workload": args.workload, "desc": w["desc"], "points": n_points(w),
-                   "modes": N, "form": "reference CPU (rayon-equivalent restatement)"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{m} seeded points x all {N} modes per step"},
-        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the Rust crate cannot be compiled here (no cargo/rustc); the arm times "
-                "oracle/field_oracle.c, a bit-exact restatement of src/field.rs, on all host "
-                "threads",
-    }
+    v, cores, m, t = time_cpu(w, max(1, args.steps), cpu_seconds)
+    return dict(common, value=v, ms_per_step=t * 1e3, data="synthetic (seeded numpy default_rng)",
+                config={"workload": wname, "desc": w["desc"], "points": n_points(w), "modes": N,
+                        "form": "reference CPU (rayon-equivalent restatement)"},
+                cpu_baseline={"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                              "sample": f"{m} seeded points x all {N} modes per step"},
+                e2e={"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                note="the Rust crate cannot be compiled here (no cargo/rustc); the arm times "
+                     "oracle/field_oracle.c, a bit-exact restatement of src/field.rs, on all "
+                     "host threads")
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    if args.workload != "all":
+        print(json.dumps(reference_line(args, world, args.workload, args.cpu_seconds)))
+        return
+    line = reference_line(args, world, HEADLINE, args.cpu_seconds)
+    configs = {n: reference_line(args, world, n, args.cpu_seconds_other)
+               for n in ALL_WORKLOADS if n != HEADLINE}
+    configs[HEADLINE] = dict(line)
+    line["configs"] = configs
+    line["config"] = dict(line["config"],
+                          workload=f"{HEADLINE} (headline; every workload under configs)")
     print(json.dumps(line))
+
+
+ALL_WORKLOADS = ("c1", "c2", "c3", "c4", "c5")
+HEADLINE = "c5"          # the largest workload: 1.7e11 point*modes per step
+
+
+def run_workload(args, world, rank, local, wname, cpu_seconds, form_arg):
+    if wname == "c5":
+        return run_ours_batch(args, world, rank, local, cpu_seconds, form_arg)
+    if wname == "field":
+        return run_ours_field(args, world, rank, local, form_arg)
+    return run_ours(args, world, rank, local, wname, cpu_seconds, form_arg)
+
+
+def run_all(args, world, rank, local):
+    """Every workload in turn; the headline's JSON record carries them all."""
+    lines = {}
+    for n in ALL_WORKLOADS:
+        lines[n] = run_workload(args, world, rank, local, n,
+                                args.cpu_seconds if n == HEADLINE else args.cpu_seconds_other,
+                                "auto")
+    head = dict(lines[HEADLINE])
+    head["configs"] = lines
+    head["config"] = dict(head["config"],
+                          workload=f"{HEADLINE} (headline; every workload under configs)")
+    fr = [l["error_vs_fp64_full"]["max_abs_over_rms"] for l in lines.values()
+          if l.get("error_vs_fp64_full")]
+    head["summary"] = {
+        n: {"value": l["value"], "form": l["config"]["form"], "ms_per_step": l["ms_per_step"],
+            "e2e": (l.get("e2e") or {}).get("value"),
+            "max_err_full": (l.get("error_vs_fp64_full") or {}).get("max_abs_over_rms"),
+            "speedup_vs_plain_fp64": (l.get("plain_fp64") or {}).get("speedup_of_chosen_form"),
+            "roofline_frac": (l.get("roofline") or {}).get("frac"),
+            "cpu": (l.get("cpu_baseline") or {}).get("value")}
+        for n, l in lines.items()}
+    head["summary"]["max_err_full_all"] = max(fr) if fr else None
+    return head
 
 
 def main():
@@ -1124,11 +1266,15 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "field"])
+    ap.add_argument("--workload", default="all",
+                    choices=["all", "c1", "c2", "c3", "c4", "c5", "field"])
     ap.add_argument("--input-dir", default=None,
                     help="benches/input directory of the reference (workload field)")
-    ap.add_argument("--form", default="auto")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--form", default="auto", help="form of a single workload (not 'all')")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU baseline sample of the headline (or the single) workload")
+    ap.add_argument("--cpu-seconds-other", type=float, default=3.0,
+                    help="CPU baseline sample of the other workloads of 'all'")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")
@@ -1139,12 +1285,14 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
-    elif args.workload == "c5":
-        run_ours_batch(args, world, rank, local)
-    elif args.workload == "field":
-        run_ours_field(args, world, rank, local)
     else:
-        run_ours(args, world, rank, local)
+        if args.workload == "all":
+            line = run_all(args, world, rank, local)
+        else:
+            line = run_workload(args, world, rank, local, args.workload, args.cpu_seconds,
+                                args.form)
+        if rank == 0:
+            print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -3,8 +3,9 @@
 `bench.py --impl reference` times the reference's CPU algorithm (the oracle
 restatement) on the host cores and prints one JSON line with the same
 metric, unit and workload as the GPU arm, plus `impl`, `cpu_baseline` and an
-`e2e` entry with no transfers.  Checked here for the default workload (C2)
-and C1 with a short CPU sample.
+`e2e` entry with no transfers.  Checked here for the default run (every
+workload, C5 the headline with the others under `configs`) and for C1 alone,
+with short CPU samples.
 """
 import json
 import os
@@ -18,7 +19,7 @@ from conftest import ROOT
 
 def _reference_line(*extra):
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-           "--warmup", "1", "--cpu-seconds", "0.3", *extra]
+           "--warmup", "1", "--cpu-seconds", "0.3", "--cpu-seconds-other", "0.2", *extra]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -30,7 +31,14 @@ def _reference_line(*extra):
 def test_reference_arm_contract(workload):
     d = _reference_line(*([] if workload is None else ["--workload", workload]))
     assert d["impl"] == "reference"
-    assert d["config"]["workload"] == (workload or "c2")
+    if workload is None:
+        assert d["config"]["workload"].startswith("c5")
+        assert sorted(d["configs"]) == ["c1", "c2", "c3", "c4", "c5"]
+        for name, c in d["configs"].items():
+            assert c["impl"] == "reference" and c["value"] > 0, name
+            assert c["config"]["workload"] == name
+    else:
+        assert d["config"]["workload"] == workload
     assert d["unit"] == "Gpoint*modes/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 1
     cb = d["cpu_baseline"]
