@@ -723,41 +723,19 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     double *d = static_cast<double *>(ctx->io.ptr);
     double *dout = d + n_in;
     std::vector<gsc_batch_item> dev(static_cast<size_t>(count));
-    // Large arrays move by DMA straight from the caller's memory; runs of
-    // small ones are packed into the pinned buffer and moved together.
-    constexpr size_t kDirect = size_t(1) << 20;
-    size_t off = 0, oo = 0, run = 0;
-    int rc = GSC_OK;
-    auto flush = [&]() {
-        if (off > run && rc == GSC_OK) {
-            const cudaError_t e = cudaMemcpyAsync(d + run, h + run, (off - run) * sizeof(double),
-                                                  cudaMemcpyHostToDevice, st);
-            if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync (batch inputs)");
-        }
-        run = off;
-    };
+    // Every input is packed back to back into the pinned staging and moved
+    // in 64 MiB chunks (h2d_packed): one pageable copy per array would pay
+    // the driver's fixed cost hundreds of times.
+    std::vector<HostSrc> in_segs;
+    in_segs.reserve(static_cast<size_t>(count) * 5);
+    size_t off = 0, oo = 0;
     auto put = [&](const double *src, int64_t n) -> const double * {
         if (n <= 0) return nullptr;
-        const size_t bytes = static_cast<size_t>(n) * sizeof(double);
         const double *r = d + off;
-        if (bytes >= kDirect) {
-            flush();
-            if (rc == GSC_OK) {
-                const cudaError_t e = cudaMemcpyAsync(d + off, src, bytes, cudaMemcpyHostToDevice, st);
-                if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpyAsync (batch inputs)");
-            }
-            off += static_cast<size_t>(n);
-            run = off;
-        } else {
-            parallel_copy(h + off, src, bytes);
-            off += static_cast<size_t>(n);
-        }
+        in_segs.push_back(HostSrc{src, off * sizeof(double), static_cast<size_t>(n) * sizeof(double)});
+        off += static_cast<size_t>(n);
         return r;
     };
-    // the copies are timed here only when the plan is reused (a new plan's
-    // creation starts the call's timing afresh)
-    TimedLaunch tc(st);
-    tc.begin(K_COPY_H2D);
     for (int64_t i = 0; i < count; ++i) {
         const gsc_batch_item &x = items[i];
         gsc_batch_item &y = dev[static_cast<size_t>(i)];
@@ -770,7 +748,11 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         y.out = x.n_points > 0 ? dout + oo : nullptr;
         oo += static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
     }
-    flush();
+    // the copies are timed here only when the plan is reused (a new plan's
+    // creation starts the call's timing afresh)
+    TimedLaunch tc(st);
+    tc.begin(K_COPY_H2D);
+    const int rc = h2d_packed(st, d, h, in_segs);
     tc.end();
     GSC_TRY(rc);
     // the plan of the previous call is reused when the shapes match

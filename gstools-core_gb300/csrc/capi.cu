@@ -415,6 +415,50 @@ void parallel_copy(void *dst, const void *src, size_t n) {
     for (auto &x : th) x.join();
 }
 
+int h2d_packed(cudaStream_t st, void *d, void *h, const std::vector<HostSrc> &segs) {
+    constexpr size_t kChunk = size_t(64) << 20;
+    size_t total = 0;
+    for (const auto &sg : segs) total = std::max(total, sg.off + sg.bytes);
+    if (total == 0) return GSC_OK;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t T = std::max<size_t>(1, std::min<size_t>(16, hw ? hw : 1));
+    // bytes [a, b) of the packed image, from the segments they belong to
+    // (segments in increasing offset order)
+    auto copy_range = [&](size_t a, size_t b) {
+        size_t k = static_cast<size_t>(
+            std::upper_bound(segs.begin(), segs.end(), a,
+                             [](size_t v, const HostSrc &x) { return v < x.off; }) - segs.begin());
+        k = k > 0 ? k - 1 : 0;
+        for (; k < segs.size() && segs[k].off < b; ++k) {
+            const size_t lo = std::max(a, segs[k].off), hi = std::min(b, segs[k].off + segs[k].bytes);
+            if (lo < hi)
+                memcpy(static_cast<char *>(h) + lo,
+                       static_cast<const char *>(segs[k].src) + (lo - segs[k].off), hi - lo);
+        }
+    };
+    for (size_t c0 = 0; c0 < total; c0 += kChunk) {
+        const size_t c1 = std::min(total, c0 + kChunk);
+        const size_t n = c1 - c0;
+        const size_t t_used = std::max<size_t>(1, std::min<size_t>(T, n / (size_t(1) << 20)));
+        if (t_used == 1) {
+            copy_range(c0, c1);
+        } else {
+            std::vector<std::thread> th;
+            const size_t per = (n + t_used - 1) / t_used;
+            for (size_t t = 1; t < t_used; ++t) {
+                const size_t a = c0 + t * per, b = std::min(c1, a + per);
+                if (a < b) th.emplace_back(copy_range, a, b);
+            }
+            copy_range(c0, std::min(c1, c0 + per));
+            for (auto &x : th) x.join();
+        }
+        // this chunk's DMA runs while the host copies the next one
+        GSC_CUDA(cudaMemcpyAsync(static_cast<char *>(d) + c0, static_cast<char *>(h) + c0, n,
+                                 cudaMemcpyHostToDevice, st));
+    }
+    return GSC_OK;
+}
+
 int d2h_scatter(DeviceCtx &ctx, cudaStream_t st, const void *src, size_t n,
                 const std::vector<HostSeg> &segs) {
     constexpr size_t kChunk = size_t(32) << 20;
@@ -562,12 +606,14 @@ static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int
 // ---------------------------------------------------------------------------
 constexpr int64_t kGridMinPoints = 4096;   // smaller grids are not worth routing
 
-// Runs f(begin, end) over [0, n) on up to 8 host threads (one for small n).
+// Runs f(begin, end) over [0, n) on up to max_threads host threads (one for
+// small n).
 template <class F>
-static void parallel_ranges(int64_t n, int64_t min_per_thread, F f) {
+static void parallel_ranges(int64_t n, int64_t min_per_thread, F f, int64_t max_threads = 8) {
     const unsigned hw = std::thread::hardware_concurrency();
     const int64_t T = std::max<int64_t>(
-        1, std::min<int64_t>(std::min<int64_t>(8, hw ? hw : 1), n / std::max<int64_t>(1, min_per_thread)));
+        1, std::min<int64_t>(std::min<int64_t>(max_threads, hw ? hw : 1),
+                             n / std::max<int64_t>(1, min_per_thread)));
     if (T <= 1) {
         f(int64_t(0), n);
         return;
@@ -611,17 +657,31 @@ static bool detect_grid(const double *pos, int64_t sd, int64_t sp, int64_t dim, 
         ax[2].resize(static_cast<size_t>(n[2]));
         for (int64_t c = 0; c < n[2]; ++c) ax[2][c] = at(2, c);
     }
+    // every point against the axes, slice by slice on all host cores (the
+    // check reads the whole array once; no divisions in the loops, which
+    // vectorise for contiguous rows)
     std::atomic<bool> ok(true);
-    parallel_ranges(P, int64_t(1) << 20, [&](int64_t b, int64_t e) {
-        for (int64_t i = b; i < e && ok.load(std::memory_order_relaxed); ++i) {
-            bool good = at(0, i) == ax[0][i / L0];
-            if (dim == 3)
-                good = good && at(1, i) == ax[1][(i / L1) % n[1]] && at(2, i) == ax[2][i % n[2]];
-            else
-                good = good && at(1, i) == ax[1][i % n[1]];
+    const double *a0 = ax[0].data(), *a1 = ax[1].data(), *a2 = dim == 3 ? ax[2].data() : nullptr;
+    const int64_t n1 = n[1], n2 = n[2];
+    parallel_ranges(n[0], std::max<int64_t>(1, (int64_t(1) << 18) / L0), [&](int64_t s0, int64_t s1) {
+        for (int64_t a = s0; a < s1 && ok.load(std::memory_order_relaxed); ++a) {
+            const int64_t base = a * L0;
+            const double x0 = a0[a];
+            bool good = true;
+            for (int64_t i = 0; i < L0; ++i) good &= at(0, base + i) == x0;
+            if (dim == 3) {
+                for (int64_t b = 0; b < n1; ++b) {
+                    const double x1 = a1[b];
+                    const int64_t off = base + b * L1;
+                    for (int64_t c = 0; c < n2; ++c)
+                        good &= (at(1, off + c) == x1) & (at(2, off + c) == a2[c]);
+                }
+            } else {
+                for (int64_t b = 0; b < n1; ++b) good &= at(1, base + b) == a1[b];
+            }
             if (!good) ok.store(false, std::memory_order_relaxed);
         }
-    });
+    }, 64);
     return ok.load();
 }
 

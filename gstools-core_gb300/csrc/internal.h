@@ -147,6 +147,18 @@ bool is_pinned_host(const void *p);
 int ensure_pinned(DeviceCtx &ctx, size_t bytes);
 // memcpy with up to 8 host threads for large blocks
 void parallel_copy(void *dst, const void *src, size_t bytes);
+// Host arrays packed back to back into pinned staging `h` and moved to the
+// device range `d` (same byte offsets; segments in increasing offset order):
+// chunks of 64 MiB are copied by all host cores, and each chunk's DMA runs
+// while the next is copied.  One DMA per chunk instead of one pageable copy
+// per array (each pageable copy pays a fixed cost in the driver, which
+// dominates for many arrays of a few MB).
+struct HostSrc {
+    const void *src;
+    size_t off;     // byte offset in h and d
+    size_t bytes;
+};
+int h2d_packed(cudaStream_t st, void *d, void *h, const std::vector<HostSrc> &segs);
 // Device -> pageable host through the pinned buffer in 32 MiB chunks, the DMA
 // of one chunk overlapping the host copy of the previous one; returns after
 // the data is in `dst` (synchronises `st`).
