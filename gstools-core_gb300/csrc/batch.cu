@@ -80,16 +80,6 @@ __global__ void batch_reduce_kernel(const BatchItem *__restrict__ items,
     it.out[e] = s;
 }
 
-struct TuneKey {
-    int device, form;
-    int64_t n_items, log2_work, log2_units;
-    bool operator<(const TuneKey &o) const {
-        return std::tie(device, form, n_items, log2_work, log2_units) <
-               std::tie(o.device, o.form, o.n_items, o.log2_work, o.log2_units);
-    }
-};
-std::mutex g_tune_mu;
-std::map<TuneKey, Cfg> g_tune_cache;
 
 }  // namespace
 }  // namespace gsc
@@ -608,19 +598,23 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
     } else {
         int64_t pts = 0;
         for (auto &it : b->items) pts += it.n_points;
-        TuneKey key{device, form, count,
-                    static_cast<int64_t>(std::floor(std::log2(std::max(1.0, b->total_work)))),
-                    static_cast<int64_t>(std::floor(std::log2(std::max<double>(1.0, pts))))};
-        bool hit = false;
-        {
-            std::lock_guard<std::mutex> lk(g_tune_mu);
-            auto f = g_tune_cache.find(key);
-            if (f != g_tune_cache.end()) {
-                c = f->second;
-                hit = true;
-            }
-        }
-        if (!hit) {
+        // the autotuner's cache (tuner.cu): device, form, item count and the
+        // buckets of the total work and point count
+        const std::string key = device_name(device) + "|batch|f" + std::to_string(form) + "|c" +
+                                std::to_string(count) + "|w" +
+                                std::to_string(tune_bucket(b->total_work)) + "|p" +
+                                std::to_string(tune_bucket(static_cast<double>(pts)));
+        int v[4] = {0, 0, 0, 0};
+        const int mode = tune_mode();
+        if (mode != 0 && tune_get(key, v)) {
+            c.R = v[0];
+            c.tile = v[1];
+            c.upb = v[2];
+            const bool ok = c.upb > 0 && (is_plain(*b) ? batch_plain_config_ok(c.R, c.tile)
+                                          : is_fx(*b) ? batch_fx_config_ok(c.R)
+                                                      : batch_mixed_config_ok(c.R));
+            if (!ok) c = Cfg{};                  // an entry from an older build
+        } else if (mode == 2) {
             // the tuner reads the inputs: let pending work on them finish
             GSC_CUDA(cudaDeviceSynchronize());
             timing_reset(false);
@@ -628,9 +622,10 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
             GSC_CUDA(cudaStreamSynchronize(b->cap_stream));
             c = b->cfg;
             b->tuned = 1;
-            std::lock_guard<std::mutex> lk(g_tune_mu);
-            g_tune_cache[key] = c;
+            const int nv[4] = {c.R, c.tile, c.upb, 0};
+            tune_put(key, nv);
         }
+        if (!is_plain(*b)) c.tile = 32;          // the mixed forms stage 32 modes
     }
     GSC_TRY(apply_config(*b, c));
     GSC_CUDA(cudaStreamSynchronize(b->cap_stream));

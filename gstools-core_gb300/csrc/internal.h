@@ -20,6 +20,9 @@ namespace gsc {
 int set_error(int code, const std::string &msg);   // records msg, returns code
 int cuda_fail(cudaError_t e, const char *what);     // GSC_ERR_CUDA / NOMEM
 
+// GSC_OK, or the library's status for a failed CUDA call
+inline int cuda_ok(cudaError_t e) { return e == cudaSuccess ? GSC_OK : cuda_fail(e, "CUDA call"); }
+
 #define GSC_CUDA(call)                                         \
     do {                                                       \
         cudaError_t e_ = (call);                               \
@@ -180,6 +183,15 @@ struct Prefault {
     void join();
     ~Prefault() { join(); }
 };
+
+// ---- autotuner cache (tuner.cu) ----------------------------------------------
+// Tuned launch configurations keyed by text (device name, kernel family,
+// shape buckets), in memory and, with a cache file, persisted.
+bool tune_get(const std::string &key, int v[4]);
+void tune_put(const std::string &key, const int v[4]);
+int tune_mode();                  // 0 fixed defaults, 1 cached entries only, 2 tune on a miss
+std::string device_name(int device);
+int tune_bucket(double v);        // e with v in [2^(e-1), 2^e) (0 below 1)
 
 // ---- timing ---------------------------------------------------------------
 struct TimedLaunch {

@@ -46,7 +46,8 @@ namespace {
 
 constexpr int kFxThreads = 128;
 static_assert(kFxThreads == kBatchThreads, "batch units assume the block size");
-constexpr int kFxR = 4;                 // points per thread
+constexpr int kFxR = 4;                 // points per thread when untuned
+constexpr int kFxW = 8;                 // target blocks per SM when untuned
 constexpr int kFxTile = 32;             // modes per staged tile = accumulation tile
 // 32-bit words per mode: [0..2] BI' (BI + 2^31), [3] w0, [4..6] BF, [7] w1,
 // [8] w2 (projector weights of the incompressible field, FP32), [12..43] the
@@ -62,6 +63,14 @@ constexpr float kFxRad = 6.2831854820251465f / 68719476736.0f;
 // r^4 C4 + r^6 C6 on |r| <= pi/16
 constexpr float kFxS3 = -1.0f / 6.0f, kFxS5 = 1.0f / 120.0f;
 constexpr float kFxC2 = -0.5f, kFxC4 = 1.0f / 24.0f, kFxC6 = -1.0f / 720.0f;
+
+// cos(2 pi m / 16), m = 0..15, to FP64 rounding (from cos(pi/8) =
+// sqrt(2 + sqrt 2) / 2 and cos(pi/4) = sqrt(2) / 2)
+__constant__ double kSixteenthCos[16] = {
+    1.0, 0.9238795325112867, 0.7071067811865476, 0.38268343236508984,
+    0.0, -0.38268343236508984, -0.7071067811865476, -0.9238795325112867,
+    -1.0, -0.9238795325112867, -0.7071067811865476, -0.38268343236508984,
+    0.0, 0.38268343236508984, 0.7071067811865476, 0.9238795325112867};
 
 // Fixed-point scale s_d of dimension d from the largest finite |x_d|
 // (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.
@@ -143,13 +152,18 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
     r[8] = __float_as_uint(__double2float_rn(w[2]));
     r[9] = r[10] = r[11] = 0u;
     phi = fmod(phi, 4294967296.0);
+    // T[m] = (z1 - i z2) e^{-2 pi i phi / 2^32} e^{2 pi i m / 16}: one FP64
+    // sincos for the mode's rotation, the sixteenth turns from a table (FP64
+    // products, a few FP64 ulps)
+    double s0, c0;
+    sincos(phi * -1.4629180792671596e-09, &s0, &c0);
+    const double ar = z1 * c0 + z2 * s0, ai = z1 * s0 - z2 * c0;   // (z1 - i z2) e^{i a}
     const float nanf_ = __int_as_float(0x7fffffff);
+#pragma unroll
     for (int m = 0; m < 16; ++m) {
-        // (z1 - i z2) e^{2 pi i (m 2^28 - phi) / 2^32}
-        double s, c;
-        sincos((static_cast<double>(m) * 268435456.0 - phi) * 1.4629180792671596e-09, &s, &c);
-        const float tr = __double2float_rn(z1 * c + z2 * s);
-        const float ti = __double2float_rn(z1 * s - z2 * c);
+        const double cm = kSixteenthCos[m], sm = kSixteenthCos[(m + 12) & 15];   // sin = cos(. - 1/4)
+        const float tr = __double2float_rn(ar * cm - ai * sm);
+        const float ti = __double2float_rn(ar * sm + ai * cm);
         r[kFxTab + 2 * m] = __float_as_uint(finite ? tr : nanf_);
         r[kFxTab + 2 * m + 1] = __float_as_uint(finite ? ti : nanf_);
     }
@@ -304,10 +318,11 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
     }
 }
 
-// Four resident blocks per SM leave up to 128 registers per thread, room to
-// interleave the R points' integer and FP32 chains.
-template <int D, bool INC>
-__global__ void __launch_bounds__(kFxThreads, 4)
+// R points per thread (2, 4 or 8; the autotuner picks).  The launch bound
+// leaves room for several resident blocks, so that the R points' integer and
+// FP32 chains interleave with other warps'.
+template <int D, bool INC, int R>
+__global__ void __launch_bounds__(kFxThreads, R >= 8 ? 3 : 4)
 mixed_fx_kernel(const double *__restrict__ pos, int64_t P, const uint32_t *__restrict__ rec,
                 const unsigned long long *__restrict__ maxbits, int64_t nc, int64_t mps,
                 int accumulate, double *__restrict__ dst, int64_t sd, int64_t sp,
@@ -315,38 +330,69 @@ mixed_fx_kernel(const double *__restrict__ pos, int64_t P, const uint32_t *__res
     __shared__ __align__(16) uint32_t srec[kFxTile * kFxRecWords];
     const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
     const int64_t je = min(nc, jb + mps);
-    fx_block<D, kFxR, INC>(pos, P, static_cast<int64_t>(blockIdx.x) * (kFxThreads * kFxR), rec, jb,
-                           je, accumulate, dst + static_cast<int64_t>(blockIdx.y) * split_stride,
-                           sd, sp, maxbits, srec);
+    fx_block<D, R, INC>(pos, P, static_cast<int64_t>(blockIdx.x) * (kFxThreads * R), rec, jb, je,
+                        accumulate, dst + static_cast<int64_t>(blockIdx.y) * split_stride, sd, sp,
+                        maxbits, srec);
 }
 
 template <int D, bool INC>
-int launch_fx(dim3 grid, cudaStream_t st, const double *pos, int64_t P, const uint32_t *rec,
+int launch_fx(int R, dim3 grid, cudaStream_t st, const double *pos, int64_t P, const uint32_t *rec,
               const unsigned long long *maxbits, int64_t nc, int64_t mps, int accumulate,
               double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
-    mixed_fx_kernel<D, INC><<<grid, kFxThreads, 0, st>>>(pos, P, rec, maxbits, nc, mps, accumulate,
-                                                         dst, sd, sp, split_stride);
+    if (R == 2)
+        mixed_fx_kernel<D, INC, 2><<<grid, kFxThreads, 0, st>>>(pos, P, rec, maxbits, nc, mps,
+                                                                accumulate, dst, sd, sp, split_stride);
+    else if (R == 8)
+        mixed_fx_kernel<D, INC, 8><<<grid, kFxThreads, 0, st>>>(pos, P, rec, maxbits, nc, mps,
+                                                                accumulate, dst, sd, sp, split_stride);
+    else
+        mixed_fx_kernel<D, INC, 4><<<grid, kFxThreads, 0, st>>>(pos, P, rec, maxbits, nc, mps,
+                                                                accumulate, dst, sd, sp, split_stride);
     GSC_CUDA(cudaGetLastError());
     return GSC_OK;
 }
 
-int dispatch_fx(int64_t dim, bool inc, dim3 grid, cudaStream_t st, const double *pos, int64_t P,
-                const uint32_t *rec, const unsigned long long *maxbits, int64_t nc, int64_t mps,
-                int accumulate, double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+int dispatch_fx(int R, int64_t dim, bool inc, dim3 grid, cudaStream_t st, const double *pos,
+                int64_t P, const uint32_t *rec, const unsigned long long *maxbits, int64_t nc,
+                int64_t mps, int accumulate, double *dst, int64_t sd, int64_t sp,
+                int64_t split_stride) {
     if (dim == 1 && !inc)
-        return launch_fx<1, false>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd, sp,
-                                   split_stride);
+        return launch_fx<1, false>(R, grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd,
+                                   sp, split_stride);
     if (dim == 2)
-        return inc ? launch_fx<2, true>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd,
-                                        sp, split_stride)
-                   : launch_fx<2, false>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
+        return inc ? launch_fx<2, true>(R, grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
+                                        sd, sp, split_stride)
+                   : launch_fx<2, false>(R, grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
                                          sd, sp, split_stride);
     if (dim == 3)
-        return inc ? launch_fx<3, true>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst, sd,
-                                        sp, split_stride)
-                   : launch_fx<3, false>(grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
+        return inc ? launch_fx<3, true>(R, grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
+                                        sd, sp, split_stride)
+                   : launch_fx<3, false>(R, grid, st, pos, P, rec, maxbits, nc, mps, accumulate, dst,
                                          sd, sp, split_stride);
     return set_error(GSC_ERR_DIM, "the mixed form supports dimensions 1, 2, 3 (incompressible: 2, 3)");
+}
+
+// Launch shape of one configuration: R points per thread, mode splits so that
+// about W blocks per SM exist when the points alone are few.
+struct FxShape {
+    int R, W;
+    int64_t bx, S, mps;
+};
+FxShape fx_shape(int R, int W, int64_t P, int64_t chunk, int sms) {
+    FxShape f{R, W, 0, 1, 0};
+    const int64_t pts_per_block = static_cast<int64_t>(kFxThreads) * R;
+    f.bx = (P + pts_per_block - 1) / pts_per_block;
+    const int64_t want_blocks = static_cast<int64_t>(sms) * W;
+    int64_t S = std::max<int64_t>(1, (want_blocks + f.bx - 1) / f.bx);
+    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kFxTile)));
+    S = std::min<int64_t>(S, 64);
+    int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
+    mps = (mps + kFxTile - 1) / kFxTile * kFxTile;
+    if (mps > 0) S = std::max<int64_t>(1, (chunk + mps - 1) / mps);
+    if (chunk == 0) S = 1;
+    f.S = S;
+    f.mps = mps;
+    return f;
 }
 
 int fx_sm_count(int device) {
@@ -452,22 +498,33 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
     if (dim < 1 || dim > 3 || (a.incompr && dim == 1))
         return set_error(GSC_ERR_DIM, "the mixed form supports dimensions 1, 2, 3 (incompressible: 2, 3)");
     constexpr int64_t kChunk = 1 << 20;   // modes per record build
-    const int64_t pts_per_block = static_cast<int64_t>(kFxThreads) * kFxR;
-    const int64_t bx = (P + pts_per_block - 1) / pts_per_block;
-    if (bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
     const int64_t chunk = std::min<int64_t>(N, kChunk);
-    // mode splits: enough blocks for 8 per SM when the points alone are few
-    const int64_t want_blocks = static_cast<int64_t>(fx_sm_count(ctx.device)) * 8;
-    int64_t S = std::max<int64_t>(1, (want_blocks + bx - 1) / bx);
-    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kFxTile)));
-    S = std::min<int64_t>(S, 64);
-    int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
-    mps = (mps + kFxTile - 1) / kFxTile * kFxTile;
-    if (mps > 0) S = std::max<int64_t>(1, (chunk + mps - 1) / mps);
-    if (N == 0) S = 1;
+    const int sms = fx_sm_count(ctx.device);
+
+    // configuration: the tuned one for this shape bucket, else the default;
+    // a miss is tuned on this call's data when the call is large (a single
+    // record build, at least 2^31 point*modes)
+    const std::string key = device_name(ctx.device) + "|mixed|d" + std::to_string(dim) +
+                            (a.incompr ? "i" : "s") + "|p" + std::to_string(tune_bucket(double(P))) +
+                            "|n" + std::to_string(tune_bucket(double(N)));
+    int tv[4] = {kFxR, kFxW, 0, 0};
+    const int mode = tune_mode();
+    bool tune = false;
+    if (mode == 0 || !tune_get(key, tv)) {
+        tv[0] = kFxR;
+        tv[1] = kFxW;
+        tune = mode == 2 && N <= kChunk && static_cast<double>(P) * N >= 2147483648.0;
+    }
+    static const int kCandR[3] = {2, 4, 8}, kCandW[3] = {4, 8, 16};
+    FxShape shp = fx_shape(tv[0], tv[1], P, chunk, sms);
+    if (shp.bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
+    int64_t S_max = shp.S;
+    if (tune)
+        for (int r : kCandR)
+            for (int w : kCandW) S_max = std::max(S_max, fx_shape(r, w, P, chunk, sms).S);
 
     const size_t rec_bytes = static_cast<size_t>(chunk) * kFxRecBytesPerMode;
-    const size_t part_bytes = S > 1 ? static_cast<size_t>(S) * nout * P * sizeof(double) : 0;
+    const size_t part_bytes = S_max > 1 ? static_cast<size_t>(S_max) * nout * P * sizeof(double) : 0;
     const size_t off_mb = (rec_bytes + 255) / 256 * 256;
     const size_t off_part = off_mb + 256;
     GSC_TRY(ensure_dev(ctx, ctx.scratch, off_part + part_bytes + 256));
@@ -477,49 +534,97 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
     unsigned long long *maxbits = reinterpret_cast<unsigned long long *>(sbase + off_mb);
     double *part = reinterpret_cast<double *>(sbase + off_part);
 
-    double *dst = S > 1 ? part : a.out;
-    const int64_t sd = S > 1 ? P : a.out_sd;
-    const int64_t sp = S > 1 ? 1 : a.out_sp;
-    const int64_t split_stride = S > 1 ? nout * P : 0;
-    const dim3 grid(static_cast<unsigned>(bx), static_cast<unsigned>(S));
-
     {
         TimedLaunch tl(st);
         tl.begin(K_MIXED_MODES);
         GSC_CUDA(cudaMemsetAsync(maxbits, 0, 4 * sizeof(unsigned long long), st));
-        const int64_t rb = std::min<int64_t>((P + 255) / 256, 4 * fx_sm_count(ctx.device));
+        const int64_t rb = std::min<int64_t>((P + 255) / 256, 4 * static_cast<int64_t>(sms));
         fx_range_kernel<<<static_cast<unsigned>(std::max<int64_t>(rb, 1)), 256, 0, st>>>(
             a.pos, P, static_cast<int>(dim), maxbits);
         tl.end();
         GSC_CUDA(cudaGetLastError());
     }
+    auto build = [&](int64_t j0, int64_t nc) -> int {
+        if (nc <= 0) return GSC_OK;
+        TimedLaunch tl(st);
+        tl.begin(K_MIXED_MODES);
+        fx_mode_kernel<<<static_cast<unsigned>((nc + 127) / 128), 128, 0, st>>>(
+            a.cov, a.z1, a.z2, static_cast<int>(dim), N, j0, nc, a.incompr ? 1 : 0, maxbits, rec,
+            range_flag);
+        tl.end();
+        GSC_CUDA(cudaGetLastError());
+        return GSC_OK;
+    };
+    // the sums of modes [j0, j0 + nc) with records built, into the output
+    // (first chunk) or added to it
+    auto sums = [&](const FxShape &f, int64_t nc, bool first, bool timed) -> int {
+        const bool split = f.S > 1;
+        double *dst = split ? part : a.out;
+        const int64_t sd = split ? P : a.out_sd, sp = split ? 1 : a.out_sp;
+        const int64_t split_stride = split ? nout * P : 0;
+        const int64_t mps_c = nc > 0 ? std::min<int64_t>(f.mps, nc) : 0;
+        const dim3 g(static_cast<unsigned>(f.bx),
+                     static_cast<unsigned>(nc > 0 ? std::min<int64_t>(f.S, (nc + mps_c - 1) / mps_c) : 1));
+        TimedLaunch tl(st);
+        if (timed) tl.begin(a.incompr ? K_MIXED_INCOMPR : K_MIXED_SCALAR);
+        // splits write partials that split_reduce sums into the output; with
+        // several record chunks they accumulate across chunks
+        const int rc = dispatch_fx(f.R, dim, a.incompr, g, st, a.pos, P, rec, maxbits, nc, mps_c,
+                                   first ? 0 : 1, dst, sd, sp, split_stride);
+        if (timed) tl.end();
+        return rc;
+    };
+
+    if (tune) {
+        // every candidate on this call's data, timed by events; the winner
+        // then computes the result
+        GSC_TRY(build(0, chunk));
+        cudaEvent_t e0, e1;
+        GSC_CUDA(cudaEventCreate(&e0));
+        GSC_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int br = kFxR, bw = kFxW;
+        int rc = GSC_OK;
+        for (int r : kCandR)
+            for (int w : kCandW) {
+                const FxShape f = fx_shape(r, w, P, chunk, sms);
+                if (rc == GSC_OK) rc = cuda_ok(cudaEventRecord(e0, st));
+                if (rc == GSC_OK) rc = sums(f, chunk, true, false);
+                if (rc == GSC_OK && f.S > 1)
+                    rc = split_reduce(part, f.S, nout, P, a.out, a.out_sd, a.out_sp, st);
+                if (rc == GSC_OK) rc = cuda_ok(cudaEventRecord(e1, st));
+                if (rc == GSC_OK) rc = cuda_ok(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                if (rc == GSC_OK) rc = cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
+                if (rc == GSC_OK && ms < best) {
+                    best = ms;
+                    br = r;
+                    bw = w;
+                }
+            }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        GSC_TRY(rc);
+        const int v[4] = {br, bw, 0, 0};
+        tune_put(key, v);
+        shp = fx_shape(br, bw, P, chunk, sms);
+        GSC_TRY(sums(shp, chunk, true, true));
+        if (shp.S > 1) GSC_TRY(split_reduce(part, shp.S, nout, P, a.out, a.out_sd, a.out_sp, st));
+        GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
+        return GSC_OK;
+    }
+
     int64_t j0 = 0;
-    int first = 1;
+    bool first = true;
     do {
         const int64_t nc = std::min<int64_t>(N - j0, kChunk);
-        if (nc > 0) {
-            TimedLaunch tl(st);
-            tl.begin(K_MIXED_MODES);
-            fx_mode_kernel<<<static_cast<unsigned>((nc + 127) / 128), 128, 0, st>>>(
-                a.cov, a.z1, a.z2, static_cast<int>(dim), N, j0, nc, a.incompr ? 1 : 0, maxbits,
-                rec, range_flag);
-            tl.end();
-            GSC_CUDA(cudaGetLastError());
-        }
-        const int64_t mps_c = nc > 0 ? std::min<int64_t>(mps, nc) : 0;
-        const dim3 g(grid.x, static_cast<unsigned>(
-                                 nc > 0 ? std::min<int64_t>(S, (nc + mps_c - 1) / mps_c) : 1));
-        TimedLaunch tl(st);
-        tl.begin(a.incompr ? K_MIXED_INCOMPR : K_MIXED_SCALAR);
-        const int rc = dispatch_fx(dim, a.incompr, first ? grid : g, st, a.pos, P, rec, maxbits, nc,
-                                   mps_c, !first, dst, sd, sp, split_stride);
-        tl.end();
-        if (rc != GSC_OK) return rc;
-        first = 0;
+        GSC_TRY(build(j0, nc));
+        GSC_TRY(sums(shp, nc, first, true));
+        first = false;
         j0 += nc;
     } while (j0 < N);
 
-    if (S > 1) GSC_TRY(split_reduce(part, S, nout, P, a.out, a.out_sd, a.out_sp, st));
+    if (shp.S > 1) GSC_TRY(split_reduce(part, shp.S, nout, P, a.out, a.out_sd, a.out_sp, st));
     GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
     return GSC_OK;
 }

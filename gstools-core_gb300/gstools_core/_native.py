@@ -167,6 +167,12 @@ SIGNATURES = {
     "gsc_selftest_once_per_device": (ctypes.c_int, [_I32, _I32, _I32, ctypes.POINTER(_I64)]),
     "gsc_selftest_batch_queue": (ctypes.c_int, [ctypes.POINTER(GscBatchItem), _I64, _I32,
                                                 ctypes.POINTER(GscBatchConfig), _I32, _I32]),
+    "gsc_tune_cache_open": (ctypes.c_int, [ctypes.c_char_p]),
+    "gsc_tune_cache_size": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
+    "gsc_tune_cache_get": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32)]),
+    "gsc_tune_cache_put": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32)]),
+    "gsc_tune_cache_clear": (ctypes.c_int, []),
+    "gsc_tune_set_mode": (ctypes.c_int, [_I32]),
     "gsc_release_buffers": (ctypes.c_int, [_I32]),
     "gsc_host_alloc": (ctypes.c_int, [_I64, ctypes.POINTER(ctypes.c_void_p)]),
     "gsc_host_free": (ctypes.c_int, [ctypes.c_void_p]),

@@ -393,6 +393,27 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
  * `device` (-1 = current). */
 int gsc_last_batch_config(int32_t device, gsc_batch_config *config);
 
+/* ---- autotuner cache ------------------------------------------------------ */
+/* Launch choices that depend on a call's shape (points per thread and mode
+ * splits of the mixed kernel, the batch planner's configuration) are timed on
+ * the call's own data the first time a shape bucket is seen on a device and
+ * kept, keyed by the device's name, the kernel family and the buckets.  With
+ * a cache file the entries persist across processes: gsc_tune_cache_open
+ * reads `path` if it exists and writes every new entry to it (NULL: memory
+ * only); a file whose header, entries or checksum do not match is refused
+ * (GSC_ERR_INVALID) and then neither read nor overwritten.  The environment
+ * variable GSC_TUNE_CACHE names a file to open on first use.
+ * gsc_tune_set_mode: 0 fixed default configurations, 1 cached entries only,
+ * 2 (default, or GSC_TUNE) tune on a miss.  get/put/clear/size inspect the
+ * cache (put writes an entry as the tuner does).  No reference counterpart:
+ * the reference has no tunable launch parameters. */
+int gsc_tune_cache_open(const char *path);
+int gsc_tune_cache_size(int64_t *entries);
+int gsc_tune_cache_get(const char *key, int32_t *values);
+int gsc_tune_cache_put(const char *key, const int32_t *values);
+int gsc_tune_cache_clear(void);
+int gsc_tune_set_mode(int32_t mode);
+
 /* ---- self-test of the failure path -------------------------------------- */
 /* Runs one CTA that waits, with the bounded wait of the tensor-core
  * pipelines, on a barrier nothing completes; the wait gives up after
