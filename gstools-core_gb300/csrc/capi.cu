@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -43,7 +44,7 @@ const char *kernel_name(int32_t id) {
         "split_reduce", "generic_f64", "sep_tables", "sep_tc_f16x3", "sep_tc_bf16x3",
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
         "mixed_f64phase", "sep_f64_dmma", "fourier_scale", "batch_tables", "batch_plain",
-        "batch_mixed", "sample_modes", "sep_split", "copy_h2d", "copy_d2h",
+        "batch_mixed", "sample_modes", "sep_split", "copy_h2d", "copy_d2h", "interleave",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -92,12 +93,13 @@ void TimedLaunch::begin(int32_t kid) {
         return;
     }
     cudaEventRecord(r.a, st);
+    rec = t_recs.size();
     t_recs.push_back(r);
 }
 
 void TimedLaunch::end() {
-    if (!on) return;
-    cudaEventRecord(t_recs.back().b, st);
+    if (!on || rec >= t_recs.size()) return;
+    cudaEventRecord(t_recs[rec].b, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -628,11 +630,12 @@ static void parallel_ranges(int64_t n, int64_t min_per_thread, F f, int64_t max_
     for (auto &x : th) x.join();
 }
 
-// If pos (dim, P) holds meshgrid(axes, indexing="ij") flattened in C order --
-// how GSTools lays out the points of a structured mesh before it calls
-// summate -- returns true with the axes (every point checked, bit for bit).
-static bool detect_grid(const double *pos, int64_t sd, int64_t sp, int64_t dim, int64_t P,
-                        std::vector<double> ax[3], int64_t n[3]) {
+// If pos (dim, P) may hold meshgrid(axes, indexing="ij") flattened in C
+// order -- how GSTools lays out the points of a structured mesh before it
+// calls summate -- returns true with the candidate axes, read from the run
+// lengths of the first coordinates (a few reads per axis value).
+static bool grid_candidate(const double *pos, int64_t sd, int64_t sp, int64_t dim, int64_t P,
+                           std::vector<double> ax[3], int64_t n[3]) {
     if ((dim != 2 && dim != 3) || P < kGridMinPoints) return false;
     auto at = [=](int64_t d, int64_t i) { return pos[d * sd + i * sp]; };
     // axis 0 is constant over runs of L0 = n1 (* n2) points, axis 1 (3-D) over L1 = n2
@@ -657,12 +660,19 @@ static bool detect_grid(const double *pos, int64_t sd, int64_t sp, int64_t dim, 
         ax[2].resize(static_cast<size_t>(n[2]));
         for (int64_t c = 0; c < n[2]; ++c) ax[2][c] = at(2, c);
     }
-    // every point against the axes, slice by slice on all host cores (the
-    // check reads the whole array once; no divisions in the loops, which
-    // vectorise for contiguous rows)
+    return true;
+}
+
+// Every point of pos against the candidate axes, bit for bit, slice by
+// slice on all host cores (the check reads the whole array once; no
+// divisions in the loops, which vectorise for contiguous rows).
+static bool grid_verify(const double *pos, int64_t sd, int64_t sp, int64_t dim,
+                        const std::vector<double> ax[3], const int64_t n[3],
+                        int64_t max_threads = 64) {
+    auto at = [=](int64_t d, int64_t i) { return pos[d * sd + i * sp]; };
     std::atomic<bool> ok(true);
     const double *a0 = ax[0].data(), *a1 = ax[1].data(), *a2 = dim == 3 ? ax[2].data() : nullptr;
-    const int64_t n1 = n[1], n2 = n[2];
+    const int64_t n1 = n[1], n2 = dim == 3 ? n[2] : 1, L0 = n1 * n2, L1 = n2;
     parallel_ranges(n[0], std::max<int64_t>(1, (int64_t(1) << 18) / L0), [&](int64_t s0, int64_t s1) {
         for (int64_t a = s0; a < s1 && ok.load(std::memory_order_relaxed); ++a) {
             const int64_t base = a * L0;
@@ -681,15 +691,29 @@ static bool detect_grid(const double *pos, int64_t sd, int64_t sp, int64_t dim, 
             }
             if (!good) ok.store(false, std::memory_order_relaxed);
         }
-    }, 64);
+    }, max_threads);
     return ok.load();
+}
+
+static bool detect_grid(const double *pos, int64_t sd, int64_t sp, int64_t dim, int64_t P,
+                        std::vector<double> ax[3], int64_t n[3]) {
+    return grid_candidate(pos, sd, sp, dim, P, ax, n) && grid_verify(pos, sd, sp, dim, ax, n);
+}
+
+// [lo, hi) byte range spanned by a (rows, cols) view with element strides
+static void view_span(const double *p, int64_t s0, int64_t s1, int64_t rows, int64_t cols,
+                      uintptr_t &lo, uintptr_t &hi) {
+    int64_t a = 0, b = 0;
+    for (int64_t s : {s0 * (rows - 1), s1 * (cols - 1)}) (s < 0 ? a : b) += s;
+    lo = reinterpret_cast<uintptr_t>(p + a);
+    hi = reinterpret_cast<uintptr_t>(p + b + 1);
 }
 
 static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
                            int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
                            const double *const *ax, const int64_t *n, const int64_t *sx,
                            double *out, bool incompr, const gsc_opts *opts,
-                           const double *sf, int64_t sfs);
+                           const double *sf, int64_t sfs, bool interleave = false);
 
 // ---------------------------------------------------------------------------
 // host-pointer path shared by the scalar and incompressible summators
@@ -718,23 +742,51 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
 
     // AUTO on a flattened structured mesh: the separable forms on its axes
     // (FP64 DMMA at the default tolerance, within the same 1e-12 bar)
+    // The candidate axes come from the first coordinates' run lengths; the
+    // check of every point (one read of the whole array on the host cores)
+    // runs on a host thread while the GPU computes on the candidate axes.  A
+    // check that fails discards that result: the point kernels recompute it.
     if (ro.form == GSC_FORM_AUTO) {
         std::vector<double> axv[3];
         int64_t n[3] = {1, 1, 1};
-        if (detect_grid(pos, ps_d, ps_p, dim, P, axv, n)) {
+        if (grid_candidate(pos, ps_d, ps_p, dim, P, axv, n)) {
             const double *axp[3] = {axv[0].data(), axv[1].data(), dim == 3 ? axv[2].data() : nullptr};
             const int64_t sx[3] = {1, 1, 1};
-            if (os_p == 1 && (nout == 1 || os_d == P))
-                return host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx, out,
-                                       incompr, opts, sf, sfs);
-            std::vector<double> tmp(static_cast<size_t>(nout * P));
-            GSC_TRY(host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx,
-                                    tmp.data(), incompr, opts, sf, sfs));
-            parallel_ranges(P, int64_t(1) << 18, [&](int64_t b, int64_t e) {
-                for (int64_t i = 0; i < nout; ++i)
-                    for (int64_t p = b; p < e; ++p) out[i * os_d + p * os_p] = tmp[i * P + p];
-            });
-            return GSC_OK;
+            const bool c_out = os_p == 1 && (nout == 1 || os_d == P);
+            const bool f_out = !c_out && os_d == 1 && os_p == nout;   // summate_incompr's layout
+            std::unique_ptr<double[]> tmp;
+            if (!c_out && !f_out) tmp.reset(new double[static_cast<size_t>(nout * P)]);
+            double *dst = tmp ? tmp.get() : out;
+            // the result may be written while the points are read only if
+            // the two do not share memory
+            uintptr_t plo, phi, olo, ohi;
+            view_span(pos, ps_d, ps_p, dim, P, plo, phi);
+            view_span(dst, tmp ? P : os_d, tmp ? 1 : os_p, nout, P, olo, ohi);
+            const bool overlap_ok = ohi <= plo || phi <= olo;
+            bool is_grid = false;
+            int rc = GSC_OK;
+            if (overlap_ok) {
+                // one core stays free for this thread, which issues the GPU work
+                const unsigned hw = std::thread::hardware_concurrency();
+                const int64_t workers = std::max<int64_t>(1, static_cast<int64_t>(hw ? hw : 2) - 1);
+                std::thread check([&] { is_grid = grid_verify(pos, ps_d, ps_p, dim, axv, n, workers); });
+                rc = host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx, dst,
+                                     incompr, opts, sf, sfs, f_out);
+                check.join();
+            } else if ((is_grid = grid_verify(pos, ps_d, ps_p, dim, axv, n))) {
+                rc = host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx, dst,
+                                     incompr, opts, sf, sfs, f_out);
+            }
+            if (is_grid) {
+                GSC_TRY(rc);
+                if (tmp)
+                    parallel_ranges(P, int64_t(1) << 18, [&](int64_t b, int64_t e) {
+                        for (int64_t i = 0; i < nout; ++i)
+                            for (int64_t p = b; p < e; ++p) out[i * os_d + p * os_p] = tmp[i * P + p];
+                    });
+                return GSC_OK;
+            }
+            timing_reset(ro.flags & GSC_FLAG_TIMING);   // not a grid: the point kernels below
         }
     }
 
@@ -773,9 +825,14 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     a.n_modes = N;
     a.n_points = P;
     a.incompr = incompr;
+    // a C-ordered or Fortran-ordered result leaves the device in its own
+    // layout (the kernels write with the output's strides), so it moves in
+    // one contiguous copy
+    const bool c_order = os_p == 1 && (nout == 1 || os_d == P);
+    const bool f_order = !c_order && os_d == 1 && os_p == nout;
     a.out = d + n_in;
-    a.out_sd = P;
-    a.out_sp = 1;
+    a.out_sd = f_order ? 1 : P;
+    a.out_sp = f_order ? nout : 1;
     const bool fx = point_form(ro, a) == GSC_FORM_MIXED;
     if (fx) GSC_CUDA(cudaMemsetAsync(ctx->status + kStatusFxFlag, 0, sizeof(int), st));
     GSC_TRY(run_points(*ctx, ro, a, st, ctx->status + kStatusFxFlag));
@@ -793,7 +850,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
             GSC_TRY(run_points(*ctx, rp, a, st, nullptr));
         }
     }
-    if (os_p == 1 && (nout == 1 || os_d == P)) {
+    if (c_order || f_order) {
         Prefault pf;
         if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
         pf.join();
@@ -808,13 +865,10 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_CUDA(cudaMemcpyAsync(ho, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
     tc.end();
     GSC_CUDA(cudaStreamSynchronize(st));
-    for (int64_t i = 0; i < nout; ++i) {
-        if (os_p == 1 && (nout == 1 || os_d == P)) {
-            parallel_copy(out + i * os_d, ho + i * P, sizeof(double) * static_cast<size_t>(P));
-        } else {
-            for (int64_t p = 0; p < P; ++p) out[i * os_d + p * os_p] = ho[i * P + p];
-        }
-    }
+    parallel_ranges(P, int64_t(1) << 18, [&](int64_t b, int64_t e) {
+        for (int64_t i = 0; i < nout; ++i)
+            for (int64_t p = b; p < e; ++p) out[i * os_d + p * os_p] = ho[i * P + p];
+    });
     return GSC_OK;
 }
 
@@ -981,7 +1035,9 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
                            int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
                            const double *const *ax, const int64_t *n, const int64_t *sx,
                            double *out, bool incompr, const gsc_opts *opts,
-                           const double *sf, int64_t sfs) {
+                           const double *sf, int64_t sfs, bool interleave) {
+    // interleave: out is a Fortran-ordered (nout, P) array, i.e. (P, nout)
+    // row-major; the result is rearranged on the device before its copy
     Resolved ro;
     GSC_TRY(resolve_opts(opts, &ro));
     GSC_TRY(check_structured(dim, N, n, incompr));
@@ -1012,7 +1068,8 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     // inputs, and the two 32 MiB stages of the output copy
     GSC_TRY(ensure_pinned(*ctx, std::max(n_in * sizeof(double),
                                          std::min(n_out * sizeof(double), size_t(64) << 20))));
-    GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out) * sizeof(double) + 1024));
+    if (nout == 1) interleave = false;
+    GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out * (interleave ? 2 : 1)) * sizeof(double) + 1024));
     double *h = static_cast<double *>(ctx->pinned);
     double *d = static_cast<double *>(ctx->io.ptr);
     TimedLaunch tc(st);
@@ -1034,6 +1091,13 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     // output buffer 128-byte aligned after the inputs
     double *dout = reinterpret_cast<double *>(
         (reinterpret_cast<uintptr_t>(d + n_in) + 127) & ~static_cast<uintptr_t>(127));
+    double *dil = interleave ? dout + n_out : nullptr;       // (P, nout) layout
+    // the rows [lo, hi) of the result, in the caller's layout, ready on st
+    // for a copy: the device result itself or its interleaved rows
+    auto result_rows = [&](int64_t lo, int64_t hi) -> int {
+        if (interleave) GSC_TRY(interleave_rows(dout, nout, P, lo * n[dim - 1], hi * n[dim - 1], dil, st));
+        return GSC_OK;
+    };
     // A pinned result (resident pages) is copied in row ranges as the
     // launches that complete them are queued, on a second stream, so the
     // copy of one wave's rows overlaps the computing of the next.
@@ -1046,13 +1110,20 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
             GSC_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
         if (!ctx->chunk_ev)
             GSC_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev, cudaEventDisableTiming));
+        GSC_TRY(result_rows(lo, hi));
         GSC_CUDA(cudaEventRecord(ctx->chunk_ev, st));
         GSC_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_ev, 0));
         copying = true;
-        for (int64_t c = 0; c < nout; ++c)
-            GSC_CUDA(cudaMemcpyAsync(out + c * P + lo * nn_last, dout + c * P + lo * nn_last,
-                                     static_cast<size_t>((hi - lo) * nn_last) * sizeof(double),
+        if (interleave) {
+            const int64_t e0 = lo * nn_last * nout, ne = (hi - lo) * nn_last * nout;
+            GSC_CUDA(cudaMemcpyAsync(out + e0, dil + e0, static_cast<size_t>(ne) * sizeof(double),
                                      cudaMemcpyDeviceToHost, ctx->copy_stream));
+        } else {
+            for (int64_t c = 0; c < nout; ++c)
+                GSC_CUDA(cudaMemcpyAsync(out + c * P + lo * nn_last, dout + c * P + lo * nn_last,
+                                         static_cast<size_t>((hi - lo) * nn_last) * sizeof(double),
+                                         cudaMemcpyDeviceToHost, ctx->copy_stream));
+        }
         rows_copied = hi;
         return GSC_OK;
     };
@@ -1069,9 +1140,11 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         // the result then moves by DMA straight into the caller's array
         Prefault pf;
         if (!pinned) pf.start(out, n_out * sizeof(double));
+        GSC_TRY(result_rows(0, P / nn_last));
         pf.join();
         tc.begin(K_COPY_D2H);
-        GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaMemcpyAsync(out, interleave ? dil : dout, n_out * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st));
         tc.end();
     }
     GSC_TRY(check_status(*ctx, st));
@@ -1088,8 +1161,10 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
             rf.form = GSC_FORM_SEP_F64;
             GSC_TRY(run_structured(*ctx, rf, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr,
                                    dout, st, nullptr, true));
+            GSC_TRY(result_rows(0, P / nn_last));
             tc.begin(K_COPY_D2H);
-            GSC_CUDA(cudaMemcpyAsync(out, dout, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+            GSC_CUDA(cudaMemcpyAsync(out, interleave ? dil : dout, n_out * sizeof(double),
+                                     cudaMemcpyDeviceToHost, st));
             tc.end();
             GSC_TRY(check_status(*ctx, st));
         }

@@ -61,6 +61,7 @@ enum KernelId : int32_t {
     K_SEP_SPLIT = 21,      // FP32 inputs of the x5 factor tables
     K_COPY_H2D = 22,       // host-to-device copies of a host-pointer call (not a kernel)
     K_COPY_D2H = 23,       // device-to-host copies of a host-pointer call (not a kernel)
+    K_INTERLEAVE = 24,     // (nout, P) rows to the (P, nout) layout of a Fortran-ordered result
     K_COUNT
 };
 const char *kernel_name(int32_t id);
@@ -199,6 +200,7 @@ struct TimedLaunch {
     bool on = false;
     cudaStream_t st = nullptr;
     int32_t id = 0;
+    size_t rec = 0;            // its record (timed launches may nest)
     void begin(int32_t kid);   // records a start event when timing is on
     void end();                // records the stop event
 };
@@ -330,5 +332,10 @@ int fourier_scale(const double *sf, const double *z1, const double *z2, int64_t 
 // meshgrid(axis..., indexing="ij") flattened: pos[d * P + p], device
 int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double *pos,
                 cudaStream_t st);
+
+// dst[p * nout + c] = src[c * P + p] for points p in [p0, p1): the rows of a
+// (nout, P) result in the layout of a Fortran-ordered (nout, P) array
+int interleave_rows(const double *src, int64_t nout, int64_t P, int64_t p0, int64_t p1,
+                    double *dst, cudaStream_t st);
 
 }  // namespace gsc

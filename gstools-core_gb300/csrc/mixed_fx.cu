@@ -73,12 +73,53 @@ __constant__ double kSixteenthCos[16] = {
     0.0, 0.38268343236508984, 0.7071067811865476, 0.9238795325112867};
 
 // Fixed-point scale s_d of dimension d from the largest finite |x_d|
-// (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.
+// (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.  The
+// exponent e with m in [2^(e-1), 2^e) comes from the bits alone (GB300's
+// FP64 pipe runs at 1/64 of the integer rate).
 __device__ __forceinline__ int fx_scale(unsigned long long maxbits) {
-    const double m = __longlong_as_double(static_cast<long long>(maxbits));
+    const int eb = static_cast<int>(maxbits >> 52);
     int e = 0;
-    if (m > 0.0) frexp(m, &e);                  // m in [2^(e-1), 2^e)
+    if (eb != 0) e = eb - 1022;                                  // normal
+    else if (maxbits != 0) e = (64 - __clzll(static_cast<long long>(maxbits))) - 1074;   // subnormal
     return 60 - e;
+}
+
+// X' = rint(x 2^s) + 2^60 (round half to even) of a finite x with
+// |x| 2^s < 2^60, by integer operations on the bits b of x: x 2^s =
+// mant 2^sh exactly, so X is mant shifted left, or shifted right and rounded
+// on the bits shifted out.  Equal to __double2ll_rn(ldexp(x, s)) + 2^60.
+__device__ __forceinline__ unsigned long long fx_fixed(unsigned long long b, int s) {
+    const int eb = static_cast<int>((b >> 52) & 0x7ff);
+    const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
+    const int sh = (eb ? eb : 1) - 1075 + s;
+    unsigned long long q = 0;
+    if (sh >= 0) {
+        q = mant << sh;                  // sh < 8 below the scale's bound
+    } else if (sh > -64) {
+        const int k = -sh;
+        q = mant >> k;
+        const unsigned long long rem = mant & ((1ull << k) - 1ull), half = 1ull << (k - 1);
+        q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
+    }                                    // else |x 2^s| < 2^-11: 0
+    return ((b >> 63) ? 0ull - q : q) + (1ull << 60);
+}
+
+// The exact FP64 value of an FP32 number, by integer operations
+__device__ __forceinline__ double fx_widen(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned long long bits = static_cast<unsigned long long>(u >> 31) << 63;
+    if (e == 0xffu) {
+        bits |= 0x7ff0000000000000ull | (static_cast<unsigned long long>(m) << 29);
+    } else if (e != 0u) {
+        bits |= (static_cast<unsigned long long>(e + 896u) << 52) |
+                (static_cast<unsigned long long>(m) << 29);
+    } else if (m != 0u) {                // subnormal m 2^-149, leading bit at 31 - clz(m)
+        const int lz = __clz(static_cast<int>(m));
+        bits |= (static_cast<unsigned long long>(905 - lz) << 52) |
+                (static_cast<unsigned long long>((m << (lz - 8)) & 0x7fffffu) << 29);
+    }
+    return __longlong_as_double(static_cast<long long>(bits));
 }
 
 // Largest finite |x_d| of pos (dim, P) into maxbits[d] (as the bit pattern
@@ -90,9 +131,11 @@ __device__ __forceinline__ void fx_range_part(const double *__restrict__ pos, in
     unsigned long long m[3] = {0ull, 0ull, 0ull};
     for (int64_t i = i0; i < P; i += stride)
         for (int d = 0; d < dim && d < 3; ++d) {
-            const double v = fabs(pos[d * P + i]);
-            if (v <= 1.7976931348623157e308)           // finite
-                m[d] = max(m[d], static_cast<unsigned long long>(__double_as_longlong(v)));
+            // |x| as bits (sign cleared), kept when finite
+            const unsigned long long v =
+                static_cast<unsigned long long>(__double_as_longlong(pos[d * P + i])) &
+                0x7fffffffffffffffull;
+            if (v < 0x7ff0000000000000ull) m[d] = max(m[d], v);
         }
     for (int d = 0; d < dim && d < 3; ++d) {
         unsigned long long v = m[d];
@@ -227,10 +270,11 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
         bad[r] = false;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            const double x = p < P ? pos[d * P + p] : 0.0;
-            bad[r] = bad[r] || !isfinite(x);
-            const long long X = isfinite(x) ? __double2ll_rn(ldexp(x, sc[d])) : 0ll;
-            const unsigned long long Xp = static_cast<unsigned long long>(X) + (1ull << 60);
+            const unsigned long long xb =
+                p < P ? static_cast<unsigned long long>(__double_as_longlong(pos[d * P + p])) : 0ull;
+            const bool fin = ((xb >> 52) & 0x7ffull) != 0x7ffull;
+            bad[r] = bad[r] || !fin;
+            const unsigned long long Xp = fx_fixed(fin ? xb : 0ull, sc[d]);
             const uint32_t h = static_cast<uint32_t>(Xp >> 29);
             const uint32_t l = static_cast<uint32_t>(Xp) & 0x1FFFFFFFu;
             xh[r][d] = h;
@@ -310,7 +354,7 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
         if (p >= P) continue;
 #pragma unroll
         for (int i = 0; i < NOUT; ++i) {
-            double v = static_cast<double>(hi[r][i]) + static_cast<double>(lo[r][i]);
+            double v = fx_widen(hi[r][i]) + fx_widen(lo[r][i]);
             if (bad[r]) v = __longlong_as_double(0x7ff8000000000000ll);
             double *o = dst + i * sd + p * sp;
             *o = accumulate ? *o + v : v;
@@ -503,7 +547,8 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
 
     // configuration: the tuned one for this shape bucket, else the default;
     // a miss is tuned on this call's data when the call is large (a single
-    // record build, at least 2^31 point*modes)
+    // record build, at least 2^26 point*modes; tuning costs about nine
+    // calls once per shape bucket)
     const std::string key = device_name(ctx.device) + "|mixed|d" + std::to_string(dim) +
                             (a.incompr ? "i" : "s") + "|p" + std::to_string(tune_bucket(double(P))) +
                             "|n" + std::to_string(tune_bucket(double(N)));
@@ -513,7 +558,7 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
     if (mode == 0 || !tune_get(key, tv)) {
         tv[0] = kFxR;
         tv[1] = kFxW;
-        tune = mode == 2 && N <= kChunk && static_cast<double>(P) * N >= 2147483648.0;
+        tune = mode == 2 && N <= kChunk && static_cast<double>(P) * N >= 67108864.0;
     }
     static const int kCandR[3] = {2, 4, 8}, kCandW[3] = {4, 8, 16};
     FxShape shp = fx_shape(tv[0], tv[1], P, chunk, sms);

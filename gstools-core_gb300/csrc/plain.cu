@@ -450,6 +450,17 @@ __global__ void grid_expand_kernel(const double *__restrict__ a0, const double *
     }
 }
 
+// (nout, P) rows -> (P, nout) for the points [p0, p0 + n): each thread moves
+// one point's nout values (coalesced reads per component; a warp's nout
+// stores cover one contiguous run of 32 * nout values).
+__global__ void interleave_kernel(const double *__restrict__ src, int nout, int64_t P, int64_t p0,
+                                  int64_t n, double *__restrict__ dst) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t p = p0 + i;
+    for (int c = 0; c < nout; ++c) dst[p * nout + c] = src[c * P + p];
+}
+
 // Fourier method: the spectrum factor multiplies z1 cos + z2 sin of its mode
 // (src/field.rs:241-242), so folding it into z1, z2 once per call lets every
 // summator form compute the Fourier field unchanged.
@@ -495,6 +506,19 @@ int grid_expand(const double *const *axis, const int64_t *n, int64_t dim, double
     if (P == 0) return GSC_OK;
     grid_expand_kernel<<<static_cast<unsigned>((P + 255) / 256), 256, 0, st>>>(
         axis[0], axis[1], dim == 3 ? axis[2] : nullptr, n[0], n[1], n2, static_cast<int>(dim), pos);
+    GSC_CUDA(cudaGetLastError());
+    return GSC_OK;
+}
+
+int interleave_rows(const double *src, int64_t nout, int64_t P, int64_t p0, int64_t p1,
+                    double *dst, cudaStream_t st) {
+    const int64_t n = p1 - p0;
+    if (n <= 0) return GSC_OK;
+    TimedLaunch tl(st);
+    tl.begin(K_INTERLEAVE);
+    interleave_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(
+        src, static_cast<int>(nout), P, p0, n, dst);
+    tl.end();
     GSC_CUDA(cudaGetLastError());
     return GSC_OK;
 }

@@ -96,3 +96,45 @@ def test_explicit_form_is_not_routed(gsc):
     pos = _flat(axes)
     gsc.summate(cov, z1, z2, pos, form="plain", timing=True)
     assert "sep_f64_dmma" not in _kernels(gsc)
+
+
+def test_incompr_grid_fortran_output_waves(gsc):
+    """A grid of many row tiles at tolerance 1e-6 (sep_f16x5 in waves): the
+    rows of each wave are rearranged into the Fortran-ordered result on the
+    device and copied while the next wave computes."""
+    cov, z1, z2, axes = _case(7, (160, 256, 40), 200)
+    pos = _flat(axes)
+    out = gsc.summate_incompr(cov, z1, z2, pos, tolerance=1e-6, timing=True)
+    k = _kernels(gsc)
+    assert "sep_tc_f16x5" in k and "interleave" in k
+    # every timed launch has its own record, nested ones included
+    assert all(ms >= 0 for _, ms in gsc.last_timings())
+    assert out.flags.f_contiguous and out.shape == (3, pos.shape[1])
+    idx = np.sort(np.random.default_rng(0).choice(pos.shape[1], 4096, replace=False))
+    ref = oracle.summator_incompr(cov, z1, z2, np.ascontiguousarray(pos[:, idx]), num_threads=NT)
+    assert rel_err(out[:, idx], ref) <= 1e-6
+    # the same field through the structured entry point, C-ordered
+    ref_s = gsc.summate_incompr_structured(cov, z1, z2, axes, tolerance=1e-6)
+    assert np.array_equal(out, ref_s.reshape(3, -1))
+
+
+@pytest.mark.parametrize("grid", [True, False])
+def test_incompr_any_output_strides(gsc, grid):
+    """The C ABI takes any element strides for the result: a padded
+    (n_points, 4) buffer neither C- nor Fortran-ordered, on a grid and off
+    it."""
+    import ctypes
+    from gstools_core import _native
+    cov, z1, z2, axes = _case(8, (12, 20, 30), 150)
+    pos = _flat(axes)
+    if not grid:
+        pos[0, 7] += 1e-9
+    P = pos.shape[1]
+    buf = np.full((P, 4), np.nan)
+    rc = _native.lib.gsc_summate_incompr_f64(
+        cov.ctypes.data, cov.shape[1], 1, z1.ctypes.data, 1, z2.ctypes.data, 1,
+        pos.ctypes.data, P, 1, 3, cov.shape[1], P, buf.ctypes.data, 1, 4, None)
+    assert rc == 0, _native.lib.gsc_last_error()
+    assert np.isnan(buf[:, 3]).all()
+    ref = oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)
+    assert rel_err(buf[:, :3].T, ref) <= 1e-12

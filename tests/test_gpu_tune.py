@@ -1,6 +1,6 @@
 """Tuned launches of the mixed kernel (GPU test).
 
-A mixed-form call of at least 2^31 point*modes whose shape bucket has no
+A mixed-form call of at least 2^26 point*modes whose shape bucket has no
 cache entry times nine candidate launches (2, 4 or 8 points per thread x 4, 8
 or 16 target blocks per SM for the mode splits) on its own data and keeps the
 fastest; later calls of the bucket reuse it.  Checked: the tuned call, the
