@@ -886,9 +886,13 @@ struct X5Params {
 };
 
 // Pipeline of the x5 kernel: k-blocks of 32 K elements (16 modes), three
-// stages of 72 KB: F1 F2 F3 (128 rows x 64 B each), G1 G2 (256 rows x 64 B,
-// 64-byte swizzle) and the B-table tile (16 modes x 128 rows of float2),
-// the last three moved by contiguous bulk copies from pre-tiled tables.
+// stages of 56 KB: F1 F2 F3 (128 rows x 64 B each) and G1 G2 (256 rows x
+// 64 B, 64-byte swizzle), and a separate three-slot ring of B-table tiles
+// (16 modes x 128 rows of float2, 16 KB), G and B moved by contiguous bulk
+// copies from pre-tiled tables.  A B slot is refilled as soon as the workers
+// have sliced it (three k-blocks ahead), not when the MMA releases the
+// stage, so the slicing of a stage overlaps the copy of its G slices instead
+// of following it.
 //
 // Warp roles (12 warps): warps 0-7 are "workers": worker warp w builds, for
 // rows 32*(w%4) .. +31 of the F tile, the modes 8*(w/4) .. +7 of every
@@ -918,9 +922,10 @@ struct X5Layout {
     static constexpr int G_BYTES = BNX * X5_BK * 2;      // 16 KB / 12 KB
     static constexpr int OFF_G1 = 3 * X5_F_BYTES;
     static constexpr int OFF_G2 = OFF_G1 + G_BYTES;
-    static constexpr int OFF_BT = OFF_G2 + G_BYTES;
-    static constexpr int STAGE = OFF_BT + X5_BT_BYTES;   // 72 KB / 64 KB
-    static constexpr size_t SMEM = X5_STAGES * STAGE + 1024 + 256;
+    static constexpr int STAGE = OFF_G2 + G_BYTES;       // 56 KB / 48 KB: F slices and G
+    static constexpr int OFF_B = X5_STAGES * STAGE;      // the ring of B-table tiles
+    static constexpr int DATA = OFF_B + X5_STAGES * X5_BT_BYTES;
+    static constexpr size_t SMEM = DATA + 1024 + 256;
     static constexpr int HC = BNX / 2;                   // columns per worker half
     // setmaxnreg split: workers hold HC FP32 totals; the narrower tile leaves
     // the control warps room (chosen where ptxas reports no spills)
@@ -928,10 +933,11 @@ struct X5Layout {
     static constexpr int CTRL_REGS = BNX == 256 ? 48 : 80;
     static_assert(4 * 32 * (2 * WORK_REGS + CTRL_REGS) <= X5_THREADS * X5_LAUNCH_REGS,
                   "setmaxnreg split exceeds the registers the block is launched with");
-    static_assert(OFF_G2 % 1024 == 0 && OFF_BT % 1024 == 0 && STAGE % 1024 == 0,
+    static_assert(OFF_G2 % 1024 == 0 && OFF_B % 1024 == 0 && STAGE % 1024 == 0 &&
+                      X5_BT_BYTES % 1024 == 0,
                   "stage operands must be 1024-byte aligned");
     static_assert(HC % 32 == 0 && BNX % 16 == 0 && BNX <= 256, "tile width");
-    static_assert(8 * 32 * 33 * 4 <= X5_BOX_OFF && X5_BOX_OFF + 2 * 8 * 32 * 32 * 8 <= X5_STAGES * STAGE,
+    static_assert(8 * 32 * 33 * 4 <= X5_BOX_OFF && X5_BOX_OFF + 2 * 8 * 32 * 32 * 8 <= DATA,
                   "epilogue buffers must fit in the stage memory");
 };
 constexpr int kTmaWarpX5 = 8, kMmaWarpX5 = 9;
@@ -963,15 +969,17 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + X5_STAGES * L::STAGE);
-    uint64_t *full_t = bars;                    // [3] copies -> workers, MMA (1 arrival + bytes)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::DATA);
+    uint64_t *full_t = bars;                    // [3] G copies -> MMA (1 arrival + bytes)
     uint64_t *full_a = bars + 3;                // [3] workers -> MMA (256 arrivals)
-    uint64_t *empty = bars + 6;                 // [3] MMA commit -> copy warp
+    uint64_t *empty = bars + 6;                 // [3] MMA commit -> copy warp, workers
     uint64_t *cross_full = bars + 9;            // MMA commit -> workers (per chunk)
     uint64_t *cross_empty = bars + 10;          // workers -> MMA (256 arrivals)
     uint64_t *drain = bars + 11;
     uint64_t *main_read = bars + 12;            // workers -> MMA: main sum read (256 arrivals)
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 13);
+    uint64_t *b_full = bars + 13;               // [3] B copies -> workers (1 arrival + bytes)
+    uint64_t *b_empty = bars + 16;              // [3] workers -> copy warp (256 arrivals)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 19);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *last_part = reinterpret_cast<volatile int *>(tmem_slot + 2);
 
@@ -1007,6 +1015,8 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
             mbar_init(&full_t[s], 1);
             mbar_init(&full_a[s], 256);
             mbar_init(&empty[s], 1);
+            mbar_init(&b_full[s], 1);
+            mbar_init(&b_empty[s], 256);
         }
         mbar_init(cross_full, 1);
         mbar_init(cross_empty, 256);
@@ -1046,7 +1056,30 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 }
                 if (r < rows_valid) n_runs = -1;   // more runs (short y axis): computed per copy
             }
-            int issued = 0;
+            // B rows of k-block i into ring slot i % X5_STAGES: one copy per run
+            auto copy_b = [&](int i) {
+                const int sb = i % X5_STAGES;
+                unsigned char *bd = smem + L::OFF_B + sb * X5_BT_BYTES;
+                const unsigned char *bk = xp.bt + static_cast<int64_t>(kb_of(i)) * p.nm * 128;
+                mbar_arrive_expect_tx(&b_full[sb], rows_valid * 128);
+                if (n_runs >= 0) {
+#pragma unroll
+                    for (int k = 0; k < kMaxRuns; ++k)
+                        if (k < n_runs)
+                            bulk_copy_g2s(bd + run_r[k] * 128,
+                                          bk + static_cast<int64_t>(run_m[k]) * 128,
+                                          run_len[k] * 128, &b_full[sb]);
+                } else {
+                    for (int r = 0, m = static_cast<int>(r0 % p.nm); r < rows_valid; m = 0) {
+                        const int len = min(rows_valid - r, p.nm - m);
+                        bulk_copy_g2s(bd + r * 128, bk + static_cast<int64_t>(m) * 128, len * 128,
+                                      &b_full[sb]);
+                        r += len;
+                    }
+                }
+            };
+            int issued = 0, issued_b = 0;
+            for (; issued_b < min(KB, X5_STAGES); ++issued_b) copy_b(issued_b);
             for (int i = 0; i < KB; ++i) {
                 const int s = i % X5_STAGES, n = i / X5_STAGES, kb = kb_of(i);
                 if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, abort_flag, p.status,
@@ -1054,31 +1087,24 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                     break;
                 unsigned char *st = smem + s * L::STAGE;
                 const int64_t gblk = (static_cast<int64_t>(nt) * p.kb_total + kb) * L::G_BYTES;
-                mbar_arrive_expect_tx(&full_t[s], 2 * L::G_BYTES + rows_valid * 128);
+                mbar_arrive_expect_tx(&full_t[s], 2 * L::G_BYTES);
                 bulk_copy_g2s(st + L::OFF_G1, xp.g1 + gblk, L::G_BYTES, &full_t[s]);
                 bulk_copy_g2s(st + L::OFF_G2, xp.g2 + gblk, L::G_BYTES, &full_t[s]);
-                // B rows of the tile: one copy per run
-                const unsigned char *bk = xp.bt + static_cast<int64_t>(kb) * p.nm * 128;
-                if (n_runs >= 0) {
-#pragma unroll
-                    for (int k = 0; k < kMaxRuns; ++k)
-                        if (k < n_runs)
-                            bulk_copy_g2s(st + L::OFF_BT + run_r[k] * 128,
-                                          bk + static_cast<int64_t>(run_m[k]) * 128,
-                                          run_len[k] * 128, &full_t[s]);
-                } else {
-                    for (int r = 0, m = static_cast<int>(r0 % p.nm); r < rows_valid; m = 0) {
-                        const int len = min(rows_valid - r, p.nm - m);
-                        bulk_copy_g2s(st + L::OFF_BT + r * 128, bk + static_cast<int64_t>(m) * 128,
-                                      len * 128, &full_t[s]);
-                        r += len;
-                    }
-                }
                 ++issued;
+                // B slot of k-block i, refilled with k-block i + 3 once the
+                // workers have sliced k-block i
+                if (issued_b < KB) {
+                    if (!mbar_wait(&b_empty[s], n & 1, abort_flag, p.status, kErrTimeoutEmpty))
+                        break;
+                    copy_b(issued_b++);
+                }
             }
-            if (*abort_flag)
+            if (*abort_flag) {
                 for (int i = issued > X5_STAGES ? issued - X5_STAGES : 0; i < issued; ++i)
                     mbar_wait_drain(&full_t[i % X5_STAGES], (i / X5_STAGES) & 1, p.status);
+                for (int i = issued_b > X5_STAGES ? issued_b - X5_STAGES : 0; i < issued_b; ++i)
+                    mbar_wait_drain(&b_full[i % X5_STAGES], (i / X5_STAGES) & 1, p.status);
+            }
         } else if (warp == kMmaWarpX5 && lane == 0) {
             // ---- MMA ---------------------------------------------------------
             const uint32_t idesc = idesc_f16(BM, BNX, false);
@@ -1095,21 +1121,12 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 const uint32_t sa = smem_u32(smem + s * L::STAGE);
                 const uint32_t f1 = sa, f2 = sa + X5_F_BYTES, f3 = sa + 2 * X5_F_BYTES;
                 const uint32_t g1 = sa + L::OFF_G1, g2 = sa + L::OFF_G2;
-                // a new chunk's main MMAs wait until the workers have read
-                // the main sum at the boundary, its cross MMAs until they have
-                // drained the last chunk
-                if (first && c > 0) {
-                    ok = mbar_wait(main_read, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
-                    if (!ok) break;
-                    tc_fence_after();
-                }
-#pragma unroll
-                for (int kk = 0; kk < X5_BK / 16; ++kk) {
-                    const uint32_t o = kk * 32;
-                    mma_f16_ss(t_main, desc_k_sw64(f1 + o), desc_k_sw64(g1 + o), idesc,
-                               (i > 0 || kk > 0) ? 1u : 0u);
-                }
-                if (first && c > 0) {
+                // At a chunk boundary the cross MMAs go first, once the
+                // workers have drained the last chunk; the main MMAs follow
+                // once they have also read the main sum, a read that overlaps
+                // those cross MMAs (other TMEM columns).
+                const bool boundary = first && c > 0;
+                if (boundary) {
                     ok = mbar_wait(cross_empty, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
                     if (!ok) break;
                     tc_fence_after();
@@ -1122,6 +1139,17 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                     mma_f16_ss(t_cross, desc_k_sw64(f1 + o), desc_k_sw64(g2 + o), idesc, 1u);
                     mma_f16_ss(t_cross, desc_k_sw64(f2 + o), desc_k_sw64(g2 + o), idesc, 1u);
                     mma_f16_ss(t_cross, desc_k_sw64(f3 + o), desc_k_sw64(g1 + o), idesc, 1u);
+                }
+                if (boundary) {
+                    ok = mbar_wait(main_read, (c - 1) & 1, abort_flag, p.status, kErrTimeoutAcc);
+                    if (!ok) break;
+                    tc_fence_after();
+                }
+#pragma unroll
+                for (int kk = 0; kk < X5_BK / 16; ++kk) {
+                    const uint32_t o = kk * 32;
+                    mma_f16_ss(t_main, desc_k_sw64(f1 + o), desc_k_sw64(g1 + o), idesc,
+                               (i > 0 || kk > 0) ? 1u : 0u);
                 }
                 mma_commit(&empty[s]);
                 if (last) mma_commit(cross_full);
@@ -1165,8 +1193,25 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         };
         auto drain_chunk = [&]() {
             tc_fence_after();
-            // the main sums at the boundary first: the next chunk's main MMAs
-            // resume once every worker has read them
+            // the cross chunk first (two loads in flight per wait): the next
+            // chunk's cross MMAs start once every worker has drained it
+#pragma unroll
+            for (int g = 0; g < L::HC / 32; ++g) {
+                uint32_t v[16], w[16];
+                __syncwarp();
+                tmem_ld16(t_cross + lane_off + L::HC * h + 32 * g, v);
+                tmem_ld16(t_cross + lane_off + L::HC * h + 32 * g + 16, w);
+                tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    tot[32 * g + i] += __uint_as_float(v[i]);
+                    tot[32 * g + 16 + i] += __uint_as_float(w[i]);
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(cross_empty);
+            // then the main sums at the boundary, while those cross MMAs run:
+            // the next chunk's main MMAs start once every worker has read them
             float mmax = 0.f;
 #pragma unroll 1
             for (int g = 0; g < L::HC / 16; ++g) {
@@ -1187,17 +1232,6 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 *xp.bound_flag = 1;
                 if (xp.bound_sticky) *xp.bound_sticky = 1;
             }
-#pragma unroll
-            for (int g = 0; g < L::HC / 16; ++g) {
-                uint32_t v[16];
-                __syncwarp();
-                tmem_ld16(t_cross + lane_off + L::HC * h + 16 * g, v);
-                tmem_ld_wait();
-#pragma unroll
-                for (int i = 0; i < 16; ++i) tot[16 * g + i] += __uint_as_float(v[i]);
-            }
-            tc_fence_before();
-            mbar_arrive(cross_empty);
             ++pend;
         };
         // Decisions that lead to a warp-collective TMEM load are taken by the
@@ -1216,13 +1250,18 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
             const bool got = mbar_wait(cross_full, c & 1, abort_flag, p.status, kErrTimeoutAcc);
             return __all_sync(0xffffffffu, got);
         };
+        // k-block i may be sliced once its B tile has arrived and the MMA has
+        // released the F slices of stage s (k-block i - 3)
+        auto stage_ready = [&](int s, int n) {
+            return warp_passed(&b_full[s], n & 1) && (n == 0 || warp_passed(&empty[s], (n - 1) & 1));
+        };
         // waits for stage s, draining chunks meanwhile; false on timeout/abort
-        auto wait_stage = [&](int s, uint32_t parity) -> bool {
-            if (warp_passed(&full_t[s], parity)) return true;
+        auto wait_stage = [&](int s, int n) -> bool {
+            if (stage_ready(s, n)) return true;
             const uint64_t t0 = globaltimer_ns();
             for (uint32_t it = 1;; ++it) {
                 poll_drain();
-                if (warp_passed(&full_t[s], parity)) return true;
+                if (stage_ready(s, n)) return true;
                 if ((it & 63) == 0) {
                     int stop = *abort_flag ? 1 : (globaltimer_ns() - t0 > kWaitLimitNs ? 2 : 0);
                     stop = __shfl_sync(0xffffffffu, stop, 0);
@@ -1248,12 +1287,12 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
             const int s = i % X5_STAGES, n = i / X5_STAGES;
             float2 sn[8];
             if (i + 1 < KB) load_s(kb_of(i + 1), sn);
-            if (!wait_stage(s, n & 1)) {
+            if (!wait_stage(s, n)) {
                 ok = false;
                 break;
             }
             unsigned char *st = smem + s * L::STAGE;
-            const unsigned char *brow = st + L::OFF_BT + r * 128;
+            const unsigned char *brow = smem + L::OFF_B + s * X5_BT_BYTES + r * 128;
 #pragma unroll
             for (int cc = 0; cc < 2; ++cc) {          // 16-byte chunks 2h, 2h+1: modes 4c .. 4c+3
                 const int c = 2 * h + cc;
@@ -1279,6 +1318,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
             }
             fence_proxy_async_smem();
             mbar_arrive(&full_a[s]);
+            mbar_arrive(&b_empty[s]);
 #pragma unroll
             for (int t = 0; t < 8; ++t) sj[t] = sn[t];
             poll_drain();
