@@ -96,11 +96,13 @@ def workload(name: str):
     raise SystemExit(f"unknown workload {name}")
 
 
-def ensemble(count=512):
+def ensemble(count=512, stride=1):
     """The c5 ensemble: per realization r, rng = default_rng(r), draws in the
-    order P, N, l, pos, cov, z1, z2."""
+    order P, N, l, pos, cov, z1, z2.  stride > 1 keeps realizations 0,
+    stride, 2 stride, ... (the same mix of sizes and dimensions at 1/stride
+    of the work: a small case of the same kernel for profilers)."""
     items = []
-    for r in range(count):
+    for r in range(0, count, stride):
         rng = np.random.default_rng(r)
         d = 2 if r < count // 2 else 3
         P = int(round(10 ** rng.uniform(3, 6)))
@@ -641,7 +643,7 @@ def run_ours_batch(args, world, rank, local, cpu_seconds, form_arg="auto"):
     import oracle
 
     torch.cuda.set_device(local)
-    items = ensemble()
+    items = ensemble(stride=args.ensemble_stride)
     work = float(sum(it["pos"].shape[1] * it["cov"].shape[1] for it in items))
     dims = {}
     for it in items:
@@ -816,7 +818,9 @@ def run_ours_batch(args, world, rank, local, cpu_seconds, form_arg="auto"):
                   if form == "mixed" else "f64 phase, f32 (sincos, tile sums), f64 output"
                   if form.startswith("mixed") else "f64"),
         "data": "synthetic (seeded numpy default_rng, one seed per realization)",
-        "config": {"workload": "c5", "desc": "batched ensemble, 512 realizations, "
+        "config": {"workload": "c5" if args.ensemble_stride == 1 else
+                   f"c5 every {args.ensemble_stride}th realization (profiling case)",
+                   "desc": f"batched ensemble, {len(items)} realizations, "
                    f"{sum(it['pos'].shape[1] for it in items)} points, "
                    f"{sum(it['cov'].shape[1] for it in items)} modes in total",
                    "point_modes": work, "form": form, "plan": cfg, "plan_s": t_plan,
@@ -1275,6 +1279,9 @@ def main():
                     help="CPU baseline sample of the headline (or the single) workload")
     ap.add_argument("--cpu-seconds-other", type=float, default=3.0,
                     help="CPU baseline sample of the other workloads of 'all'")
+    ap.add_argument("--ensemble-stride", type=int, default=1,
+                    help="c5: every k-th realization only (a small case for profilers; "
+                         "not a bench line)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")

@@ -73,53 +73,12 @@ __constant__ double kSixteenthCos[16] = {
     0.0, 0.38268343236508984, 0.7071067811865476, 0.9238795325112867};
 
 // Fixed-point scale s_d of dimension d from the largest finite |x_d|
-// (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.  The
-// exponent e with m in [2^(e-1), 2^e) comes from the bits alone (GB300's
-// FP64 pipe runs at 1/64 of the integer rate).
+// (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.
 __device__ __forceinline__ int fx_scale(unsigned long long maxbits) {
-    const int eb = static_cast<int>(maxbits >> 52);
+    const double m = __longlong_as_double(static_cast<long long>(maxbits));
     int e = 0;
-    if (eb != 0) e = eb - 1022;                                  // normal
-    else if (maxbits != 0) e = (64 - __clzll(static_cast<long long>(maxbits))) - 1074;   // subnormal
+    if (m > 0.0) frexp(m, &e);                  // m in [2^(e-1), 2^e)
     return 60 - e;
-}
-
-// X' = rint(x 2^s) + 2^60 (round half to even) of a finite x with
-// |x| 2^s < 2^60, by integer operations on the bits b of x: x 2^s =
-// mant 2^sh exactly, so X is mant shifted left, or shifted right and rounded
-// on the bits shifted out.  Equal to __double2ll_rn(ldexp(x, s)) + 2^60.
-__device__ __forceinline__ unsigned long long fx_fixed(unsigned long long b, int s) {
-    const int eb = static_cast<int>((b >> 52) & 0x7ff);
-    const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | (eb ? (1ull << 52) : 0ull);
-    const int sh = (eb ? eb : 1) - 1075 + s;
-    unsigned long long q = 0;
-    if (sh >= 0) {
-        q = mant << sh;                  // sh < 8 below the scale's bound
-    } else if (sh > -64) {
-        const int k = -sh;
-        q = mant >> k;
-        const unsigned long long rem = mant & ((1ull << k) - 1ull), half = 1ull << (k - 1);
-        q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
-    }                                    // else |x 2^s| < 2^-11: 0
-    return ((b >> 63) ? 0ull - q : q) + (1ull << 60);
-}
-
-// The exact FP64 value of an FP32 number, by integer operations
-__device__ __forceinline__ double fx_widen(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-    unsigned long long bits = static_cast<unsigned long long>(u >> 31) << 63;
-    if (e == 0xffu) {
-        bits |= 0x7ff0000000000000ull | (static_cast<unsigned long long>(m) << 29);
-    } else if (e != 0u) {
-        bits |= (static_cast<unsigned long long>(e + 896u) << 52) |
-                (static_cast<unsigned long long>(m) << 29);
-    } else if (m != 0u) {                // subnormal m 2^-149, leading bit at 31 - clz(m)
-        const int lz = __clz(static_cast<int>(m));
-        bits |= (static_cast<unsigned long long>(905 - lz) << 52) |
-                (static_cast<unsigned long long>((m << (lz - 8)) & 0x7fffffu) << 29);
-    }
-    return __longlong_as_double(static_cast<long long>(bits));
 }
 
 // Largest finite |x_d| of pos (dim, P) into maxbits[d] (as the bit pattern
@@ -270,11 +229,10 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
         bad[r] = false;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            const unsigned long long xb =
-                p < P ? static_cast<unsigned long long>(__double_as_longlong(pos[d * P + p])) : 0ull;
-            const bool fin = ((xb >> 52) & 0x7ffull) != 0x7ffull;
-            bad[r] = bad[r] || !fin;
-            const unsigned long long Xp = fx_fixed(fin ? xb : 0ull, sc[d]);
+            const double x = p < P ? pos[d * P + p] : 0.0;
+            bad[r] = bad[r] || !isfinite(x);
+            const long long X = isfinite(x) ? __double2ll_rn(ldexp(x, sc[d])) : 0ll;
+            const unsigned long long Xp = static_cast<unsigned long long>(X) + (1ull << 60);
             const uint32_t h = static_cast<uint32_t>(Xp >> 29);
             const uint32_t l = static_cast<uint32_t>(Xp) & 0x1FFFFFFFu;
             xh[r][d] = h;
@@ -354,7 +312,7 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
         if (p >= P) continue;
 #pragma unroll
         for (int i = 0; i < NOUT; ++i) {
-            double v = fx_widen(hi[r][i]) + fx_widen(lo[r][i]);
+            double v = static_cast<double>(hi[r][i]) + static_cast<double>(lo[r][i]);
             if (bad[r]) v = __longlong_as_double(0x7ff8000000000000ll);
             double *o = dst + i * sd + p * sp;
             *o = accumulate ? *o + v : v;

@@ -156,95 +156,3 @@ def test_field_against_the_oracle():
     err = np.abs(got - ref).max() / np.sqrt(np.mean(ref ** 2))
     assert err <= 1e-6, err
 
-
-# ---- the prologue's integer conversions, restated --------------------------
-M64 = (1 << 64) - 1
-
-
-def bits_scale(maxbits):
-    """fx_scale: 60 - e with m in [2^(e-1), 2^e), from the bits of m >= 0."""
-    eb = maxbits >> 52
-    if eb:
-        e = eb - 1022
-    elif maxbits:
-        e = maxbits.bit_length() - 1074
-    else:
-        e = 0
-    return 60 - e
-
-
-def bits_fixed(b, s):
-    """fx_fixed: rint(x 2^s) + 2^60 (mod 2^64) from the bits b of x."""
-    eb = (b >> 52) & 0x7FF
-    mant = (b & ((1 << 52) - 1)) | ((1 << 52) if eb else 0)
-    sh = (eb if eb else 1) - 1075 + s
-    q = 0
-    if sh >= 0:
-        q = (mant << sh) & M64
-    elif sh > -64:
-        k = -sh
-        q = mant >> k
-        rem, half = mant & ((1 << k) - 1), 1 << (k - 1)
-        q += 1 if (rem > half or (rem == half and q & 1)) else 0
-    return (((-q) & M64 if b >> 63 else q) + (1 << 60)) & M64
-
-
-def bits_widen(u):
-    """fx_widen: the FP64 bits of the FP32 number with bits u."""
-    e, m = (u >> 23) & 0xFF, u & 0x7FFFFF
-    bits = (u >> 31) << 63
-    if e == 0xFF:
-        bits |= 0x7FF0000000000000 | (m << 29)
-    elif e:
-        bits |= ((e + 896) << 52) | (m << 29)
-    elif m:
-        lz = 32 - m.bit_length()
-        bits |= ((905 - lz) << 52) | (((m << (lz - 8)) & 0x7FFFFF) << 29)
-    return bits
-
-
-def _u64(x):
-    return int(np.array(x, dtype=np.float64).view(np.uint64))
-
-
-def test_integer_scale_matches_frexp():
-    rng = np.random.default_rng(4)
-    vals = [0.0, 5e-324, 1e-310, 2.2250738585072014e-308, 0.5, 1.0, 1.5, 2.0, 100.0, 1e300,
-            1.7976931348623157e308] + list(np.abs(rng.standard_normal(200)) * 10.0 ** rng.integers(-300, 300, 200))
-    for v in vals:
-        assert bits_scale(_u64(v)) == scale(v), v
-
-
-def test_integer_fixed_point_matches_rint_ldexp():
-    """Every rounding case: exact shifts, halves (ties to even), subnormals,
-    zero of either sign, values far below one unit, both signs."""
-    rng = np.random.default_rng(5)
-    cases = []
-    for maxabs in (1.0, 100.0, 1000.0, 3.0e5, 1e-3, 2.0 ** 59, 2.0 ** 61, 1e-310, 7.0):
-        s = scale(maxabs)
-        xs = list(rng.uniform(-maxabs, maxabs, 300)) + [0.0, -0.0, maxabs, -maxabs,
-                                                        5e-324, -5e-324, maxabs * 2.0 ** -70]
-        # exact halves of a unit and their neighbours
-        for j in range(1, 40):
-            h = np.ldexp(2 * j + 1, -s - 1)             # (j + 1/2) units
-            if abs(h) < maxabs:
-                xs += [h, -h, np.nextafter(h, 0.0), np.nextafter(h, np.inf)]
-        cases += [(x, s) for x in xs]
-    for x, s in cases:
-        want = (int(np.rint(np.ldexp(x, s))) + (1 << 60)) & M64
-        assert bits_fixed(_u64(x), s) == want, (x, s)
-
-
-def test_integer_widening_is_exact():
-    rng = np.random.default_rng(6)
-    us = list(rng.integers(0, 1 << 32, 20000, dtype=np.uint64)) + [
-        0, 0x80000000, 1, 0x80000001, 0x007FFFFF, 0x00400000, 0x7F800000, 0xFF800000,
-        0x7FC00000, 0x3F800000, 0x00800000]
-    for u in us:
-        u = int(u)
-        f = np.array(u, dtype=np.uint32).view(np.float32)
-        got = bits_widen(u)
-        if np.isnan(f):
-            assert (got >> 52) & 0x7FF == 0x7FF and got & ((1 << 52) - 1)
-        else:
-            assert got == _u64(np.float64(f)), hex(u)
