@@ -33,7 +33,7 @@ import numpy as np
 from . import _native
 from ._native import GscError, device_count, last_timings
 
-__all__ = ["summate", "summate_incompr", "summate_fourier", "summate_device",
+__all__ = ["summate", "summate_incompr", "summate_fourier", "randomization_field", "summate_device",
            "summate_incompr_device", "summate_fourier_device",
            "summate_structured", "summate_incompr_structured", "summate_fourier_structured",
            "summate_structured_device", "summate_incompr_structured_device",
@@ -284,6 +284,39 @@ def summate_incompr_device(cov_samples, z1, z2, pos, out, *, form="auto", tolera
     o = _opts(form, tolerance, timing, device, stream)
     _native.check(_native.lib.gsc_summate_incompr_dev(
         *args, dim, n, p, _cuda_view(out, "out", (dim, p)), ctypes.byref(o)))
+    return out
+
+
+def randomization_field(cov_samples, z1, z2, pos, scale, offset=0.0, *, incompr=False,
+                        form="auto", tolerance=None, timing=False, device=-1):
+    """The normalised field a randomization-method generator returns from
+    these modes: ``offset + scale * summate(...)`` for a scalar field, and
+    ``offset * e_1 + scale * summate_incompr(...)`` with ``incompr=True``
+    (extension; no reference counterpart).
+
+    This is the affine step GSTools' generators wrap around the summators.
+    ``RandMeth`` scales the summed modes by ``sqrt(var / mode_no)``, and the
+    mean of the spatial random field is added after. ``IncomprRandMeth``
+    adds a mean velocity along e_1 to a scaled sum. Pass those as ``scale``
+    and ``offset``. The scale multiplies z1 and z2 before the sum, so every
+    computation form, including the separable ones that flattened meshes
+    are routed to, computes the scaled field directly: one rounding per
+    mode, within every form's bar. The offset is added to the result in
+    place. A nugget is left to the caller: it is random, drawn by the
+    caller's generator.
+    """
+    z1 = _array(z1, "z1", 1)
+    z2 = _array(z2, "z2", 1)
+    s = float(scale)
+    fn = summate_incompr if incompr else summate
+    out = fn(cov_samples, z1 * s, z2 * s, pos, form=form, tolerance=tolerance, timing=timing,
+             device=device)
+    off = float(offset)
+    if off != 0.0:
+        if incompr:
+            out[0] += off
+        else:
+            out += off
     return out
 
 
