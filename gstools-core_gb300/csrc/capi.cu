@@ -433,7 +433,7 @@ int h2d_packed(cudaStream_t st, void *d, void *h, const std::vector<HostSrc> &se
         k = k > 0 ? k - 1 : 0;
         for (; k < segs.size() && segs[k].off < b; ++k) {
             const size_t lo = std::max(a, segs[k].off), hi = std::min(b, segs[k].off + segs[k].bytes);
-            if (lo < hi)
+            if (lo < hi && segs[k].src)
                 memcpy(static_cast<char *>(h) + lo,
                        static_cast<const char *>(segs[k].src) + (lo - segs[k].off), hi - lo);
         }
@@ -588,6 +588,19 @@ static int upload2(cudaStream_t st, double *d, double *h, size_t off, const doub
         GSC_CUDA(cudaMemcpyAsync(d + off, h + off, n * sizeof(double), cudaMemcpyHostToDevice, st));
     }
     return GSC_OK;
+}
+
+// Adds a (rows, cols) host view at element offset `off` of the packed input
+// image: contiguous views as segments that h2d_packed copies, others gathered
+// into h now.
+static void stage2(std::vector<HostSrc> &segs, double *h, size_t off, const double *src,
+                   int64_t s0, int64_t s1, int64_t rows, int64_t cols) {
+    const size_t n = static_cast<size_t>(rows * cols);
+    if (n == 0) return;
+    const bool contiguous = s1 == 1 && (rows == 1 || s0 == cols);
+    if (!contiguous) gather2(src, s0, s1, rows, cols, h + off);
+    segs.push_back({contiguous ? static_cast<const void *>(src) : nullptr, off * sizeof(double),
+                    n * sizeof(double)});
 }
 
 static void gather2(const double *src, int64_t s0, int64_t s1, int64_t rows, int64_t cols,
@@ -808,11 +821,16 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     double *d = static_cast<double *>(ctx->io.ptr);
     TimedLaunch tc(st);
     tc.begin(K_COPY_H2D);
-    GSC_TRY(upload2(st, d, h, 0, cov, cs_d, cs_n, dim, N));
-    GSC_TRY(upload2(st, d, h, n_cov, z1, 0, z1s, 1, N));
-    GSC_TRY(upload2(st, d, h, n_cov + N, z2, 0, z2s, 1, N));
-    if (sf) GSC_TRY(upload2(st, d, h, n_cov + 2 * N, sf, 0, sfs, 1, N));
-    GSC_TRY(upload2(st, d, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P));
+    // the inputs as one packed image, moved through the pinned buffer in
+    // chunks (a DMA straight from a large pageable array runs at a fraction
+    // of the link)
+    std::vector<HostSrc> segs;
+    stage2(segs, h, 0, cov, cs_d, cs_n, dim, N);
+    stage2(segs, h, n_cov, z1, 0, z1s, 1, N);
+    stage2(segs, h, n_cov + N, z2, 0, z2s, 1, N);
+    if (sf) stage2(segs, h, n_cov + 2 * N, sf, 0, sfs, 1, N);
+    stage2(segs, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P);
+    GSC_TRY(h2d_packed(st, d, h, segs));
     tc.end();
     if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
                                   d + n_cov + N, st));

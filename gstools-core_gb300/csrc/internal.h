@@ -158,8 +158,8 @@ void parallel_copy(void *dst, const void *src, size_t bytes);
 // per array (each pageable copy pays a fixed cost in the driver, which
 // dominates for many arrays of a few MB).
 struct HostSrc {
-    const void *src;
-    size_t off;     // byte offset in h and d
+    const void *src;  // null: the bytes are already at h + off (gathered there)
+    size_t off;       // byte offset in h and d
     size_t bytes;
 };
 int h2d_packed(cudaStream_t st, void *d, void *h, const std::vector<HostSrc> &segs);

@@ -196,7 +196,8 @@ struct TabArgs {
     int k_pad;                   // K elements per G row (multiple of 64)
     int nm_ld;                   // B-table row length (nm rounded up to 16)
     int ncn_pad;                 // G rows (multiple of BN)
-    float2 *svec;                // [nb][n_modes]
+    float2 *svec;                // [nb][sv_stride]
+    int64_t sv_stride;           // modes per svec row: n_modes, or (x5) kbt * 16 zero-padded
     float2 *btab;                // [n_modes][nm]
     uint32_t *ghi, *glo;         // [ncn_pad][k_pad/2] packed (re, -im) pairs
     float *wnorm;                // x5 form: {W, 1/W}, W = 2^ceil(log2 max|z1 - i z2|)
@@ -287,7 +288,8 @@ __global__ void sep_gtab_kernel(TabArgs t) {
 // GEMM kernel
 // ---------------------------------------------------------------------------
 struct TcParams {
-    const float2 *svec;     // [nb][n_modes]
+    const float2 *svec;     // [nb][sv_stride]
+    int64_t sv_stride;
     const float2 *btab;     // [n_modes][nm_ld]
     int n_modes, nm, nm_ld, nb, nn, ncn;   // ncn = ncomp * nn valid G rows
     int kb_total, kc;               // k-blocks, k-blocks per accumulation chunk
@@ -413,7 +415,7 @@ sep_tc_kernel(const __grid_constant__ CUtensorMap map_ghi,
         const int r = threadIdx.x - 128;
         const int m = m0 + r;
         const bool row_ok = m < p.nm;
-        const float2 *sv = p.svec + static_cast<int64_t>(b) * p.n_modes;
+        const float2 *sv = p.svec + static_cast<int64_t>(b) * p.sv_stride;
         const uint32_t row_off = (r >> 3) * 1024 + (r & 7) * 128;
         float2 cur[32];
         auto load_block = [&](int kb, float2 (&dst)[32]) {
@@ -736,9 +738,15 @@ __device__ __forceinline__ float dot2_pair(float ah, float al, float b, float ch
     return s + (es + (e1 + e2) + fmaf(al, b, cl * d));
 }
 
-// s_a[j] = (z1_j - i z2_j) e^{i k_x,j X_a} (3-D) or z1_j - i z2_j (2-D), FP32
+// s_a[j] = (z1_j - i z2_j) e^{i k_x,j X_a} (3-D) or z1_j - i z2_j (2-D), FP32;
+// rows of sv_stride = 16 * k-blocks entries, zero past n_modes, so that the
+// 16 modes of a k-block are one 128-byte block a bulk copy can move
 __device__ __forceinline__ void svec_x5_entry(const TabArgs &t, int64_t i) {
-    const int b = static_cast<int>(i / t.n_modes), j = static_cast<int>(i % t.n_modes);
+    const int b = static_cast<int>(i / t.sv_stride), j = static_cast<int>(i % t.sv_stride);
+    if (j >= t.n_modes) {
+        t.svec[i] = make_float2(0.f, 0.f);
+        return;
+    }
     const float *r = t.mrec + static_cast<int64_t>(j) * kRecX5;
     float2 w = make_float2(__double2float_rn(t.z1[j]), __double2float_rn(-t.z2[j]));
     if (t.dim == 3) {
@@ -907,6 +915,10 @@ constexpr int X5_STAGES = 3;
 constexpr int X5_BOX_OFF = 65536;   // epilogue: FP64 output boxes (2 x 8 warps x 2 x 4 KB)
 constexpr int X5_F_BYTES = BM * X5_BK * 2;          // 8 KB
 constexpr int X5_BT_BYTES = 16 * BM * 8;            // 16 KB
+// s values staged beside each B tile: 16 modes (128 bytes) for each of the
+// first X5_MAX_SL x-slices a tile's rows fall in
+constexpr int X5_MAX_SL = 4;
+constexpr int X5_BS_BYTES = X5_BT_BYTES + X5_MAX_SL * 128;   // one slot of the B ring
 constexpr int X5_CHUNK = 16;                         // k-blocks per cross drain (256 modes)
 // incompressible fields: the cross accumulator's truncation is the larger part
 // of their error (the transverse components are small), so it is drained
@@ -923,8 +935,8 @@ struct X5Layout {
     static constexpr int OFF_G1 = 3 * X5_F_BYTES;
     static constexpr int OFF_G2 = OFF_G1 + G_BYTES;
     static constexpr int STAGE = OFF_G2 + G_BYTES;       // 56 KB / 48 KB: F slices and G
-    static constexpr int OFF_B = X5_STAGES * STAGE;      // the ring of B-table tiles
-    static constexpr int DATA = OFF_B + X5_STAGES * X5_BT_BYTES;
+    static constexpr int OFF_B = X5_STAGES * STAGE;      // the ring of B-table tiles and s
+    static constexpr int DATA = OFF_B + X5_STAGES * X5_BS_BYTES;
     static constexpr size_t SMEM = DATA + 1024 + 256;
     static constexpr int HC = BNX / 2;                   // columns per worker half
     // setmaxnreg split: workers hold HC FP32 totals; the narrower tile leaves
@@ -933,9 +945,10 @@ struct X5Layout {
     static constexpr int CTRL_REGS = BNX == 256 ? 48 : 80;
     static_assert(4 * 32 * (2 * WORK_REGS + CTRL_REGS) <= X5_THREADS * X5_LAUNCH_REGS,
                   "setmaxnreg split exceeds the registers the block is launched with");
-    static_assert(OFF_G2 % 1024 == 0 && OFF_B % 1024 == 0 && STAGE % 1024 == 0 &&
-                      X5_BT_BYTES % 1024 == 0,
+    static_assert(OFF_G2 % 1024 == 0 && OFF_B % 1024 == 0 && STAGE % 1024 == 0,
                   "stage operands must be 1024-byte aligned");
+    static_assert(X5_BS_BYTES % 128 == 0 && DATA % 16 == 0, "B ring slots: 128-byte aligned");
+    static_assert(DATA + 1024 + 256 <= 232448, "shared memory per block");
     static_assert(HC % 32 == 0 && BNX % 16 == 0 && BNX <= 256, "tile width");
     static_assert(8 * 32 * 33 * 4 <= X5_BOX_OFF && X5_BOX_OFF + 2 * 8 * 32 * 32 * 8 <= DATA,
                   "epilogue buffers must fit in the stage memory");
@@ -971,14 +984,14 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L::DATA);
     uint64_t *full_t = bars;                    // [3] G copies -> MMA (1 arrival + bytes)
-    uint64_t *full_a = bars + 3;                // [3] workers -> MMA (256 arrivals)
+    uint64_t *full_a = bars + 3;                // [3] workers -> MMA (8 arrivals, one per warp)
     uint64_t *empty = bars + 6;                 // [3] MMA commit -> copy warp, workers
     uint64_t *cross_full = bars + 9;            // MMA commit -> workers (per chunk)
-    uint64_t *cross_empty = bars + 10;          // workers -> MMA (256 arrivals)
+    uint64_t *cross_empty = bars + 10;          // workers -> MMA (8 arrivals)
     uint64_t *drain = bars + 11;
-    uint64_t *main_read = bars + 12;            // workers -> MMA: main sum read (256 arrivals)
+    uint64_t *main_read = bars + 12;            // workers -> MMA: main sum read (8 arrivals)
     uint64_t *b_full = bars + 13;               // [3] B copies -> workers (1 arrival + bytes)
-    uint64_t *b_empty = bars + 16;              // [3] workers -> copy warp (256 arrivals)
+    uint64_t *b_empty = bars + 16;              // [3] workers -> copy warp (8 arrivals)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 19);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
     volatile int *last_part = reinterpret_cast<volatile int *>(tmem_slot + 2);
@@ -1013,15 +1026,15 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
     if (threadIdx.x == 0) {
         for (int s = 0; s < X5_STAGES; ++s) {
             mbar_init(&full_t[s], 1);
-            mbar_init(&full_a[s], 256);
+            mbar_init(&full_a[s], 8);           // one arrival per worker warp
             mbar_init(&empty[s], 1);
             mbar_init(&b_full[s], 1);
-            mbar_init(&b_empty[s], 256);
+            mbar_init(&b_empty[s], 8);
         }
         mbar_init(cross_full, 1);
-        mbar_init(cross_empty, 256);
+        mbar_init(cross_empty, 8);
         mbar_init(drain, 1);
-        mbar_init(main_read, 256);
+        mbar_init(main_read, 8);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -1056,12 +1069,21 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 }
                 if (r < rows_valid) n_runs = -1;   // more runs (short y axis): computed per copy
             }
-            // B rows of k-block i into ring slot i % X5_STAGES: one copy per run
+            // B rows of k-block i into ring slot i % X5_STAGES (one copy per
+            // run), and after them the k-block's 16 s values of each of the
+            // tile's first X5_MAX_SL x-slices (128-byte blocks of the padded
+            // s rows)
+            const int bs0 = static_cast<int>(r0 / p.nm);
+            const int n_sl = min(X5_MAX_SL, static_cast<int>((r0 + rows_valid - 1) / p.nm) - bs0 + 1);
             auto copy_b = [&](int i) {
-                const int sb = i % X5_STAGES;
-                unsigned char *bd = smem + L::OFF_B + sb * X5_BT_BYTES;
-                const unsigned char *bk = xp.bt + static_cast<int64_t>(kb_of(i)) * p.nm * 128;
-                mbar_arrive_expect_tx(&b_full[sb], rows_valid * 128);
+                const int sb = i % X5_STAGES, kb = kb_of(i);
+                unsigned char *bd = smem + L::OFF_B + sb * X5_BS_BYTES;
+                const unsigned char *bk = xp.bt + static_cast<int64_t>(kb) * p.nm * 128;
+                mbar_arrive_expect_tx(&b_full[sb], rows_valid * 128 + n_sl * 128);
+                for (int k = 0; k < n_sl; ++k)
+                    bulk_copy_g2s(bd + X5_BT_BYTES + k * 128,
+                                  p.svec + static_cast<int64_t>(bs0 + k) * p.sv_stride + kb * 16, 128,
+                                  &b_full[sb]);
                 if (n_runs >= 0) {
 #pragma unroll
                     for (int k = 0; k < kMaxRuns; ++k)
@@ -1168,7 +1190,7 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
         const bool row_ok = r < rows_valid;
         const int64_t grow = row_ok ? r0 + r : 0;               // (x-slice, y) of the row
         const int bsl = static_cast<int>(grow / p.nm), mrow = static_cast<int>(grow % p.nm);
-        const float2 *sv = p.svec + static_cast<int64_t>(bsl) * p.n_modes;
+        const float2 *sv = p.svec + static_cast<int64_t>(bsl) * p.sv_stride;
         // byte offsets, in this row's 128-byte B line, of the four 16-byte
         // chunks (modes 8h .. 8h+7) the thread reads: chunk c sits at c ^ (m & 7)
         const uint32_t bswz = static_cast<uint32_t>(mrow & 7);
@@ -1209,7 +1231,8 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 }
             }
             tc_fence_before();
-            mbar_arrive(cross_empty);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(cross_empty);
             // then the main sums at the boundary, while those cross MMAs run:
             // the next chunk's main MMAs start once every worker has read them
             float mmax = 0.f;
@@ -1223,7 +1246,8 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 for (int i = 0; i < 16; ++i) mmax = fmaxf(mmax, fabsf(__uint_as_float(v[i])));
             }
             tc_fence_before();
-            mbar_arrive(main_read);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(main_read);
             // the main sum at this chunk boundary plus the next chunk's bound
             // must stay within 2^24 counts.  Rows past the grid are skipped
             // (their zero s factors meet stale B data, possibly NaN); a NaN
@@ -1273,26 +1297,36 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 }
             }
         };
-        float2 sj[8];
-        auto load_s = [&](int kb, float2 (&dst)[8]) {
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int j = kb * 16 + 8 * h + t;
-                dst[t] = (row_ok && j < p.n_modes) ? __ldg(sv + j) : make_float2(0.f, 0.f);
-            }
-        };
+        // this row's x-slice among the tile's staged ones; rows of a later
+        // slice (y axes shorter than 32) read their s values from the table
+        const int sl = bsl - static_cast<int>(r0 / p.nm);
         bool ok = true;
-        load_s(kb_of(0), sj);
         for (int i = 0; i < KB; ++i) {
             const int s = i % X5_STAGES, n = i / X5_STAGES;
-            float2 sn[8];
-            if (i + 1 < KB) load_s(kb_of(i + 1), sn);
             if (!wait_stage(s, n)) {
                 ok = false;
                 break;
             }
             unsigned char *st = smem + s * L::STAGE;
-            const unsigned char *brow = smem + L::OFF_B + s * X5_BT_BYTES + r * 128;
+            const unsigned char *bslot = smem + L::OFF_B + s * X5_BS_BYTES;
+            const unsigned char *brow = bslot + r * 128;
+            float2 sj[8];
+            if (!row_ok) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) sj[t] = make_float2(0.f, 0.f);
+            } else if (sl < X5_MAX_SL) {
+                const float4 *sp = reinterpret_cast<const float4 *>(bslot + X5_BT_BYTES + sl * 128 + 64 * h);
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float4 v = sp[t];
+                    sj[2 * t] = make_float2(v.x, v.y);
+                    sj[2 * t + 1] = make_float2(v.z, v.w);
+                }
+            } else {
+                const int j0 = kb_of(i) * 16 + 8 * h;      // padded rows: zero past n_modes
+#pragma unroll
+                for (int t = 0; t < 8; ++t) sj[t] = __ldg(sv + j0 + t);
+            }
 #pragma unroll
             for (int cc = 0; cc < 2; ++cc) {          // 16-byte chunks 2h, 2h+1: modes 4c .. 4c+3
                 const int c = 2 * h + cc;
@@ -1316,11 +1350,14 @@ sep_x5_kernel(const __grid_constant__ CUtensorMap out_map, const X5Params xp) {
                 *reinterpret_cast<uint4 *>(st + 2 * X5_F_BYTES + phys) =
                     make_uint4(w3[0], w3[1], w3[2], w3[3]);
             }
+            // every thread's slices are visible to the MMA's async proxy,
+            // then one lane per warp arrives for the warp
             fence_proxy_async_smem();
-            mbar_arrive(&full_a[s]);
-            mbar_arrive(&b_empty[s]);
-#pragma unroll
-            for (int t = 0; t < 8; ++t) sj[t] = sn[t];
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&full_a[s]);
+                mbar_arrive(&b_empty[s]);
+            }
             poll_drain();
         }
         // remaining non-final chunks, then the final one (it follows every MMA)
@@ -1661,7 +1698,8 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     // scratch: normaliser, svec, btab, G hi (G1), G lo (G2), split partials
     const size_t off_wn = 0;
     const size_t off_svec = 1024;
-    const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(N), 1024);
+    const int64_t sv_stride = x5 ? static_cast<int64_t>(KB) * 16 : N;
+    const size_t off_btab = align_up(off_svec + sizeof(float2) * nb * static_cast<size_t>(sv_stride), 1024);
     const size_t bt_modes = x5 ? static_cast<size_t>(KB) * 16 : static_cast<size_t>(N);
     const size_t off_ghi = align_up(off_btab + sizeof(float2) * bt_modes * nm_ld, 1024);
     const size_t g_bytes = static_cast<size_t>(ncn_pad) * k_pad * 2;
@@ -1704,6 +1742,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     t.nm_ld = nm_ld;
     t.ncn_pad = ncn_pad;
     t.svec = reinterpret_cast<float2 *>(base + off_svec);
+    t.sv_stride = sv_stride;
     t.btab = reinterpret_cast<float2 *>(base + off_btab);
     t.ghi = reinterpret_cast<uint32_t *>(base + off_ghi);
     t.glo = reinterpret_cast<uint32_t *>(base + off_glo);
@@ -1722,7 +1761,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
     {
         TimedLaunch tl(st);
         // one timing record per launch
-        const int64_t n1 = static_cast<int64_t>(nb) * N, n2 = static_cast<int64_t>(bt_modes) * nm_ld;
+        const int64_t n1 = static_cast<int64_t>(nb) * sv_stride, n2 = static_cast<int64_t>(bt_modes) * nm_ld;
         const int64_t n3 = static_cast<int64_t>(ncn_pad) * (k_pad / 2);
         if (x5) {
             const int64_t ng = gtab_x5_groups(ncomp, nn, ncn_pad) * (k_pad / 2);
@@ -1766,6 +1805,7 @@ int sep_tc_run(DeviceCtx &ctx, const SepArgs &a, cudaStream_t st) {
 
     TcParams p;
     p.svec = t.svec;
+    p.sv_stride = sv_stride;
     p.btab = t.btab;
     p.n_modes = N;
     p.nm = nm;
