@@ -1043,11 +1043,13 @@ def measured_peaks():
 PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17, (3, True): 20}
 # FMA-pipe instructions per point*mode of the mixed kernel (mixed_fx.cu),
 # counted from the source: the integer phase, 3 IMAD per dimension (IMAD
-# issues on the FMA pipe), then 10 FP32 for the remainder's polynomial and the
-# term, and 4 for the Kahan sum per output component (plus one product by
-# the projector weight per component of the incompressible field); the
-# table index, shifts, conversion and table load run on other pipes
-MIXED_FMA_OPS = {(1, False): 17, (2, False): 20, (3, False): 23, (2, True): 26, (3, True): 34}
+# issues on the FMA pipe), then 10 FP32 for the remainder float, its
+# polynomials and the term; two modes' terms are added (one FMA per pair)
+# before a 4-instruction Kahan step, 2.5 per point*mode; the incompressible
+# field weights the pair per component (2 per pair) before its Kahan step,
+# 3 per point*mode and component; the table index, shifts and table load
+# run on other pipes
+MIXED_FMA_OPS = {(1, False): 15.5, (2, False): 18.5, (3, False): 21.5, (2, True): 22, (3, True): 28}
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu

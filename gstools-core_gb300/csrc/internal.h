@@ -312,7 +312,7 @@ constexpr int64_t kPlainTableBytesPerMode = 256 * 16;   // W_j[a], a < 256, doub
 constexpr int64_t kPlainRecBytesPerMode = 12 * 8;
 constexpr int64_t kMixedRecBytesPerMode = 20 * 4;
 constexpr int64_t kMixedRec64BytesPerMode = 4 * 8;
-constexpr int64_t kFxRecBytesPerMode = 44 * 4;      // mixed_fx.cu mode record
+constexpr int64_t kFxRecBytesPerMode = 64 * 4;      // mixed_fx.cu mode record
 // Batched mixed form (mixed_fx.cu): records of every item's modes, the range
 // words of every item's positions (4 x uint64 per item), the range flag.
 int batch_fx_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t n_items,

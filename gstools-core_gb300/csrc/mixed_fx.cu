@@ -20,15 +20,19 @@
 //    and an FP64 one 1/64 of the pipe.  BI is stored biased by 2^31, so
 //    both high products are unsigned; the bias's effect is a per-point
 //    constant taken out once per point;
-//  * e^{i theta}: theta + 2^27 selects by its top 4 bits one of 16 entries
-//    of the mode's table T[m] = (z1 - i z2) e^{2 pi i (m/16 - phi)} (phi the
-//    per-mode constant; built in FP64 per mode, stored as FP32), the
-//    remainder r (|r| <= 1/32 turn) goes through sin and cos Taylor
-//    polynomials of degree 5 and 6 (truncation below 2.3e-9):
-//    term = Re(T e^{i r});
-//  * the terms are summed in FP32 over tiles of 32 modes with Kahan
-//    compensation, each tile folded into a double-float (TwoSum) running
-//    total, converted to FP64 at the end.
+//  * e^{i theta}: theta + 2^27 + 16 selects by its top 4 bits one of 16
+//    entries of the mode's table T[m] = (z1 - i z2) e^{2 pi i (m/16 - phi)}
+//    (phi the per-mode constant; built in FP64 per mode, stored as FP32).
+//    Bits 5..27 of the same word, placed under the exponent of 1.0f, give
+//    1 + u 2^-23 exactly; minus 1.5 that is the remainder r in sixteenths
+//    of a turn (|r| <= 1/2, rounded to 2^-27 turn by the + 16) with no
+//    integer-to-float conversion.  sin and cos of r pi/8 are Taylor
+//    polynomials of degree 5 and 6 in r (truncation below 2.3e-9), and the
+//    term is Re(T e^{i r pi/8});
+//  * the terms of two modes are added, and the pair sums are summed in FP32
+//    over tiles of 32 modes with Kahan compensation; each tile is folded
+//    into a double-float (TwoSum) running total, converted to FP64 at the
+//    end.
 // Phases beyond 2^30 turns (|k| * max|x| > 6.7e9) do not fit the integer
 // range; such calls are flagged in the range word (the caller recomputes them
 // on the FP64 kernel or reports it).  Non-finite coordinates give NaN, as the
@@ -50,19 +54,26 @@ constexpr int kFxR = 4;                 // points per thread when untuned
 constexpr int kFxW = 8;                 // target blocks per SM when untuned
 constexpr int kFxTile = 32;             // modes per staged tile = accumulation tile
 // 32-bit words per mode: [0..2] BI' (BI + 2^31), [3] w0, [4..6] BF, [7] w1,
-// [8] w2 (projector weights of the incompressible field, FP32), [12..43] the
-// table T[m] as (re, im) FP32 pairs.  A record is 176 bytes, so the 16 table
-// entries of one mode fill the 32 shared-memory banks once: a warp's gather
-// from them is free of bank conflicts.
-constexpr int kFxTab = 12;
-constexpr int kFxRecWords = kFxTab + 32;
+// [8] w2 (projector weights of the incompressible field, FP32), [32..63] the
+// table T[m] as (re, im) FP32 pairs; words 9..31 are unused.  A record is
+// 256 bytes and the tile of records in shared memory 256-byte aligned, so
+// a table starts on a 128-byte boundary (its entry's address is one OR) and
+// its 16 entries fill the 32 shared-memory banks once: a warp's gather from
+// them is free of bank conflicts.
+constexpr int kFxTab = 32;
+constexpr int kFxRecWords = 64;
 static_assert(kFxRecWords * 4 == kFxRecBytesPerMode, "record layout");
-// radians per unit of the remainder times 16: 2 pi / 2^36
-constexpr float kFxRad = 6.2831854820251465f / 68719476736.0f;
-// Taylor coefficients of sin r = r + r^3 S3 + r^5 S5, cos r = 1 + r^2 C2 +
-// r^4 C4 + r^6 C6 on |r| <= pi/16
-constexpr float kFxS3 = -1.0f / 6.0f, kFxS5 = 1.0f / 120.0f;
-constexpr float kFxC2 = -0.5f, kFxC4 = 1.0f / 24.0f, kFxC6 = -1.0f / 720.0f;
+// sin(r pi/8) = r (S1 + r^2 (S3 + r^2 S5)), cos(r pi/8) = 1 + r^2 (C2 + r^2
+// (C4 + r^2 C6)) for r in sixteenths of a turn, |r| <= 1/2: the Taylor
+// coefficients of sin and cos scaled by powers of pi/8
+constexpr double kFxPi8 = 0.39269908169872415;                  // pi/8
+constexpr float kFxS1 = static_cast<float>(kFxPi8);
+constexpr float kFxS3 = static_cast<float>(-kFxPi8 * kFxPi8 * kFxPi8 / 6.0);
+constexpr float kFxS5 = static_cast<float>(kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 / 120.0);
+constexpr float kFxC2 = static_cast<float>(-kFxPi8 * kFxPi8 / 2.0);
+constexpr float kFxC4 = static_cast<float>(kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 / 24.0);
+constexpr float kFxC6 =
+    static_cast<float>(-kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 / 720.0);
 
 // cos(2 pi m / 16), m = 0..15, to FP64 rounding (from cos(pi/8) =
 // sqrt(2 + sqrt 2) / 2 and cos(pi/4) = sqrt(2) / 2)
@@ -152,7 +163,7 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
     r[3] = __float_as_uint(__double2float_rn(w[0]));
     r[7] = __float_as_uint(__double2float_rn(w[1]));
     r[8] = __float_as_uint(__double2float_rn(w[2]));
-    r[9] = r[10] = r[11] = 0u;
+    for (int q = 9; q < kFxTab; ++q) r[q] = 0u;
     phi = fmod(phi, 4294967296.0);
     // T[m] = (z1 - i z2) e^{-2 pi i phi / 2^32} e^{2 pi i m / 16}: one FP64
     // sincos for the mode's rotation, the sixteenth turns from a table (FP64
@@ -200,6 +211,37 @@ __device__ __forceinline__ void fx_two_sum(float &hi, float &lo, float a) {
     lo += e;
 }
 
+// FP32 pair at a 32-bit shared-memory address
+__device__ __forceinline__ float2 fx_lds2(uint32_t addr) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+
+// The term Re(T e^{i theta}) of one point*mode: c the point's constant,
+// (xh, x8l) its coordinate words, (bi, bf) the mode's wave-number words, tab
+// the shared-memory address of the mode's 128-byte-aligned table.
+template <int D>
+__device__ __forceinline__ float fx_term(uint32_t c, const uint32_t *xh, const uint32_t *x8l,
+                                         const uint32_t *bi, const uint32_t *bf, uint32_t tab) {
+    uint32_t t = c;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        t += __umulhi(bi[d], x8l[d]);
+        t += __umulhi(bf[d], xh[d]);
+        t += bi[d] * xh[d];
+    }
+    // t = theta + 2^27 + 16: entry m = t >> 28 (theta to the nearest 1/16
+    // turn) at byte 8 m of the table; bits 5..27 are the remainder plus
+    // 1/32 turn in units of 2^-27 turn, as the mantissa of a float in [1, 2)
+    const float2 T = fx_lds2(tab | ((t >> 25) & 0x78u));
+    const float r = __uint_as_float(0x3F800000u | ((t >> 5) & 0x007FFFFFu)) - 1.5f;
+    const float r2 = r * r;
+    const float sn = r * fmaf(r2, fmaf(r2, kFxS5, kFxS3), kFxS1);
+    const float cs = fmaf(r2, fmaf(r2, fmaf(r2, kFxC6, kFxC4), kFxC2), 1.0f);
+    return fmaf(T.x, cs, -T.y * sn);
+}
+
 // One block's work: the kFxThreads*R points from p_first (thread t owns
 // p_first + t + r*kFxThreads), modes [jb, je) of the records `rec`; sums
 // written (accumulate=0) or added at dst + i*sd + p*sp.  maxbits: the
@@ -223,9 +265,10 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int64_t p = p0 + r * kFxThreads;
-        // 2^27 centres the remainder on the table entry; + D offsets the
-        // mean truncation of the two high products per dimension
-        uint32_t c = 0x08000000u + D;
+        // 2^27 centres the remainder on the table entry, + 16 rounds it to
+        // the 2^-27 turn the float takes, + D offsets the mean truncation of
+        // the two high products per dimension
+        uint32_t c = 0x08000000u + 16u + D;
         bad[r] = false;
 #pragma unroll
         for (int d = 0; d < D; ++d) {
@@ -245,13 +288,18 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
         for (int i = 0; i < NOUT; ++i) hi[r][i] = lo[r][i] = 0.f;
     }
 
+    const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(srec));
     for (int64_t t0 = jb; t0 < je; t0 += kFxTile) {
         const int tm = static_cast<int>(min(static_cast<int64_t>(kFxTile), je - t0));
         __syncthreads();
         {
+            // the header (words 0..11) and the table (words 32..63) of each record
             const uint4 *src = reinterpret_cast<const uint4 *>(rec + t0 * kFxRecWords);
             uint4 *dstv = reinterpret_cast<uint4 *>(srec);
-            for (int i = tid; i < tm * (kFxRecWords / 4); i += kFxThreads) dstv[i] = src[i];
+            for (int i = tid; i < tm * (kFxRecWords / 4); i += kFxThreads) {
+                const int q = i & (kFxRecWords / 4 - 1);
+                if (q < 3 || q >= kFxTab / 4) dstv[i] = src[i];
+            }
         }
         __syncthreads();
         float acc[R][NOUT], cmp[R][NOUT];
@@ -259,41 +307,40 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
-        for (int m = 0; m < tm; ++m) {
-            const uint32_t *mr = srec + m * kFxRecWords;
-            const uint4 h0 = *reinterpret_cast<const uint4 *>(mr);       // BI'0..2, w0
-            const uint4 h1 = *reinterpret_cast<const uint4 *>(mr + 4);   // BF0..2, w1
-            const uint32_t bi[3] = {h0.x, h0.y, h0.z}, bf[3] = {h1.x, h1.y, h1.z};
-            float w[3] = {0.f, 0.f, 0.f};
+        // modes in pairs: the two terms are added before the Kahan step
+        for (int m = 0; m < tm; m += 2) {
+            const bool two = m + 1 < tm;
+            const uint32_t *ma = srec + m * kFxRecWords;
+            const uint32_t *mb = two ? ma + kFxRecWords : ma;
+            const uint4 ha0 = *reinterpret_cast<const uint4 *>(ma);       // BI'0..2, w0
+            const uint4 ha1 = *reinterpret_cast<const uint4 *>(ma + 4);   // BF0..2, w1
+            const uint4 hb0 = *reinterpret_cast<const uint4 *>(mb);
+            const uint4 hb1 = *reinterpret_cast<const uint4 *>(mb + 4);
+            const uint32_t bia[3] = {ha0.x, ha0.y, ha0.z}, bfa[3] = {ha1.x, ha1.y, ha1.z};
+            const uint32_t bib[3] = {hb0.x, hb0.y, hb0.z}, bfb[3] = {hb1.x, hb1.y, hb1.z};
+            // the second mode of an odd tile's last pair counts zero times
+            const float sb = two ? 1.0f : 0.0f;
+            float wa[3] = {1.f, 0.f, 0.f}, wb[3] = {sb, 0.f, 0.f};
             if (INC) {
-                w[0] = __uint_as_float(h0.w);
-                w[1] = __uint_as_float(h1.w);
-                w[2] = __uint_as_float(mr[8]);
+                wa[0] = __uint_as_float(ha0.w);
+                wa[1] = __uint_as_float(ha1.w);
+                wa[2] = __uint_as_float(ma[8]);
+                wb[0] = sb * __uint_as_float(hb0.w);
+                wb[1] = sb * __uint_as_float(hb1.w);
+                wb[2] = sb * __uint_as_float(mb[8]);
             }
-            const unsigned char *tab = reinterpret_cast<const unsigned char *>(mr + kFxTab);
+            const uint32_t taba = sbase + static_cast<uint32_t>(m * kFxRecWords + kFxTab) * 4u;
+            const uint32_t tabb = two ? taba + kFxRecWords * 4u : taba;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                uint32_t t = cp[r];
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    t += __umulhi(bi[d], x8l[r][d]);
-                    t += __umulhi(bf[d], xh[r][d]);
-                    t += bi[d] * xh[r][d];
-                }
-                // t = theta + 2^27: entry m = t >> 28 (theta rounded to 1/16
-                // turn), remainder theta - m 2^28 = low28(t) - 2^27, taken as
-                // the signed value ((low28(t) << 4) ^ 2^31) (16 per unit)
-                const float2 T = *reinterpret_cast<const float2 *>(tab + ((t >> 25) & 0x78u));
-                const float rr = static_cast<float>(static_cast<int>((t << 4) ^ 0x80000000u)) * kFxRad;
-                const float r2 = rr * rr;
-                const float sn = fmaf(rr * r2, fmaf(r2, kFxS5, kFxS3), rr);
-                const float cs = fmaf(r2, fmaf(r2, fmaf(r2, kFxC6, kFxC4), kFxC2), 1.0f);
-                const float term = fmaf(T.x, cs, -T.y * sn);
+                const float ta = fx_term<D>(cp[r], xh[r], x8l[r], bia, bfa, taba);
+                const float tb = fx_term<D>(cp[r], xh[r], x8l[r], bib, bfb, tabb);
                 if (INC) {
 #pragma unroll
-                    for (int i = 0; i < NOUT; ++i) fx_kahan(acc[r][i], cmp[r][i], w[i] * term);
+                    for (int i = 0; i < NOUT; ++i)
+                        fx_kahan(acc[r][i], cmp[r][i], fmaf(wa[i], ta, wb[i] * tb));
                 } else {
-                    fx_kahan(acc[r][0], cmp[r][0], term);
+                    fx_kahan(acc[r][0], cmp[r][0], fmaf(sb, tb, ta));
                 }
             }
         }
@@ -329,7 +376,7 @@ mixed_fx_kernel(const double *__restrict__ pos, int64_t P, const uint32_t *__res
                 const unsigned long long *__restrict__ maxbits, int64_t nc, int64_t mps,
                 int accumulate, double *__restrict__ dst, int64_t sd, int64_t sp,
                 int64_t split_stride) {
-    __shared__ __align__(16) uint32_t srec[kFxTile * kFxRecWords];
+    __shared__ __align__(256) uint32_t srec[kFxTile * kFxRecWords];
     const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
     const int64_t je = min(nc, jb + mps);
     fx_block<D, R, INC>(pos, P, static_cast<int64_t>(blockIdx.x) * (kFxThreads * R), rec, jb, je,
@@ -445,7 +492,7 @@ __global__ void __launch_bounds__(kFxThreads)
 batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict__ units,
                 int64_t n_units, int *__restrict__ counter, const uint32_t *__restrict__ rec,
                 const unsigned long long *__restrict__ maxbits) {
-    __shared__ __align__(16) uint32_t srec[kFxTile * kFxRecWords];
+    __shared__ __align__(256) uint32_t srec[kFxTile * kFxRecWords];
     __shared__ int s_unit;
     for (;;) {
         __syncthreads();

@@ -8,13 +8,15 @@ B = kappa 2^(61 - s) as BI + BF 2^-32 with BI biased by 2^31, and
     theta = c_point + sum_d lo32(BI' Xh) + hi32(BF Xh) + hi32(BI' * 8 Xl)
 
 (mod 2^32, units of 2^-32 turn), with the per-point constant c_point taking
-out the bias and a per-mode constant phi folded into the mode's table.
+out the bias (and adding 2^27 + 16, which centres and rounds the remainder)
+and a per-mode constant phi folded into the mode's table.
 Restated here with the same unsigned 32-bit operations and compared with the
 exact rational phase of the FP64 inputs (Python integers): within 4 units
 (2^-30 turns) in 1-3 dimensions, heavy-tailed wave numbers and coordinates of
-either sign.  Then the table and polynomial evaluation of the term, and a
-whole field against the oracle at the form's 1e-6 bar, in FP32 as the kernel
-computes it.
+either sign.  Then the table and polynomial evaluation of the term (the remainder read
+from the phase word's bits as the mantissa of a float in [1, 2)), the pair
+sums of two modes' terms, and a whole field against the oracle at the form's
+1e-6 bar, in FP32 as the kernel computes it.
 """
 from fractions import Fraction
 
@@ -50,9 +52,9 @@ def mode_words(k, s):
 
 
 def fx_theta(k, x, dim):
-    """theta + 2^27 (uint32) of one point*mode and the per-mode phi (exact)."""
+    """theta + 2^27 + 16 (uint32) of one point*mode and the per-mode phi (exact)."""
     s = [scale(abs(x[d])) for d in range(dim)]
-    c = (0x08000000 + dim) & U32
+    c = (0x08000000 + 16 + dim) & U32
     t = 0
     phi = Fraction(0)
     for d in range(dim):
@@ -85,22 +87,64 @@ def test_integer_phase_within_four_units(dim):
         if any(abs(np.ldexp(k[d] * INV2PI, 61 - s[d])) >= 2 ** 31 for d in range(dim)):
             continue
         t, phi = fx_theta(k, x, dim)
-        # t = kappa.x + phi + 2^27 (table centring), modulo one turn
-        want = (exact_turns(k, x, dim) * 2 ** 32 + phi + 2 ** 27) % (2 ** 32)
+        # t = kappa.x + phi + 2^27 + 16 (table centring, remainder rounding),
+        # modulo one turn
+        want = (exact_turns(k, x, dim) * 2 ** 32 + phi + 2 ** 27 + 16) % (2 ** 32)
         err = float((Fraction(t) - want + 2 ** 31) % (2 ** 32) - 2 ** 31)
         worst = max(worst, abs(err))
     assert worst <= 4.0, worst
 
 
+PI8 = np.pi / 8
+S1, S3, S5 = (np.float32(v) for v in (PI8, -PI8 ** 3 / 6, PI8 ** 5 / 120))
+C2, C4, C6 = (np.float32(v) for v in (-PI8 ** 2 / 2, PI8 ** 4 / 24, -PI8 ** 6 / 720))
+
+
+def fma32(a, b, c):
+    """FP32 fused multiply-add: the product of two floats is exact in FP64."""
+    return np.float32(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+def fx_term(t, tab):
+    """The term of one point*mode from its phase word t = theta + 2^27 + 16."""
+    f32 = np.float32
+    m = t >> 28
+    r = f32(np.uint32(0x3F800000 | ((t >> 5) & 0x7FFFFF)).view(np.float32) - f32(1.5))
+    r2 = f32(r * r)
+    sn = f32(r * fma32(r2, fma32(r2, S5, S3), S1))
+    cs = fma32(r2, fma32(r2, fma32(r2, C6, C4), C2), f32(1))
+    return fma32(tab[0][m], cs, -f32(tab[1][m] * sn))
+
+
+def test_remainder_float_and_polynomials():
+    """The remainder float is exact, within 2^-28 turn of the phase's
+    remainder, and the polynomials give e^{i theta} within 3e-9."""
+    rng = np.random.default_rng(5)
+    t = rng.integers(0, 2 ** 32, 20000, dtype=np.uint64).astype(np.uint32)
+    m = t >> 28
+    rem = (t.astype(np.int64) & ((1 << 28) - 1)) - 2 ** 27 - 16     # theta - m 2^28
+    r = (np.uint32(0x3F800000) | ((t >> 5) & 0x7FFFFF)).view(np.float32).astype(np.float64) - 1.5
+    assert np.all(np.abs(r * 2 ** 28 - rem) <= 16)                   # units of 2^-32 turn
+    theta = (m.astype(np.float64) * 2 ** 28 + rem) * (2 * np.pi / 2 ** 32)
+    tab = (np.cos(np.arange(16) * np.pi / 8).astype(np.float32),
+           np.sin(np.arange(16) * np.pi / 8).astype(np.float32))
+    # T = e^{2 pi i m/16}: Re(T e^{ir}) = cos(theta); T = -i e^{...}: sin(theta)
+    got_c = np.array([fx_term(int(v), tab) for v in t])
+    tab_s = (tab[1], -tab[0])
+    got_s = np.array([fx_term(int(v), tab_s) for v in t])
+    assert np.max(np.abs(got_c - np.cos(theta))) < 3e-7          # FP32 table entries
+    assert np.max(np.abs(got_s - np.sin(theta))) < 3e-7
+
+
 def fx_field(cov, z1, z2, pos):
     """The kernel's arithmetic for a scalar field, FP32 where the kernel
-    uses FP32 (table, polynomial, Kahan tile sums, double-float total)."""
+    uses FP32 (table, polynomial, pair sums, Kahan tile sums, double-float
+    total)."""
     dim, n = cov.shape
     P = pos.shape[1]
     s = [scale(np.abs(pos[d]).max()) for d in range(dim)]
     out = np.empty(P)
     f32 = np.float32
-    rad = f32(np.float32(2 * np.pi) / np.float32(2 ** 36))
     tabs, words = [], []
     for j in range(n):
         ws = [mode_words(cov[d, j], s[d]) for d in range(dim)]
@@ -112,35 +156,31 @@ def fx_field(cov, z1, z2, pos):
         words.append(ws)
     for p in range(P):
         pw = [point_words(pos[d, p], s[d]) for d in range(dim)]
-        c = (0x08000000 + dim) & U32
+        c = (0x08000000 + 16 + dim) & U32
         for d in range(dim):
             c = (c - pw[d][2]) & U32
         hi = lo = f32(0)
-        acc = cmp = f32(0)
-        for j in range(n):
-            t = c
-            for d in range(dim):
-                bi, bf, _ = words[j][d]
-                t = (t + ((bi * pw[d][1]) >> 32)) & U32
-                t = (t + ((bf * pw[d][0]) >> 32)) & U32
-                t = (t + bi * pw[d][0]) & U32
-            m = t >> 28
-            u = np.uint32(((t << 4) ^ 0x80000000) & U32).view(np.int32)
-            rr = f32(f32(u) * rad)
-            r2 = f32(rr * rr)
-            sn = f32(rr * r2 * f32(f32(r2 * f32(1 / 120)) + f32(-1 / 6)) + rr)
-            cs = f32(r2 * f32(r2 * f32(r2 * f32(-1 / 720) + f32(1 / 24)) + f32(-0.5)) + f32(1))
-            term = f32(tabs[j][0][m] * cs - tabs[j][1][m] * sn)
-            y = f32(term - cmp)
-            tt = f32(acc + y)
-            cmp = f32(f32(tt - acc) - y)
-            acc = tt
-            if j % 32 == 31 or j == n - 1:
-                sm = f32(hi + acc)
-                bb = f32(sm - hi)
-                e = f32(f32(hi - f32(sm - bb)) + f32(acc - bb))
-                hi, lo = sm, f32(lo + e - cmp)
-                acc = cmp = f32(0)
+        for t0 in range(0, n, 32):
+            acc = cmp = f32(0)
+            terms = []
+            for j in range(t0, min(n, t0 + 32)):
+                t = c
+                for d in range(dim):
+                    bi, bf, _ = words[j][d]
+                    t = (t + ((bi * pw[d][1]) >> 32)) & U32
+                    t = (t + ((bf * pw[d][0]) >> 32)) & U32
+                    t = (t + bi * pw[d][0]) & U32
+                terms.append(fx_term(t, tabs[j]))
+            for q in range(0, len(terms), 2):
+                a = terms[q] if q + 1 == len(terms) else f32(terms[q] + terms[q + 1])
+                y = f32(a - cmp)
+                tt = f32(acc + y)
+                cmp = f32(f32(tt - acc) - y)
+                acc = tt
+            sm = f32(hi + acc)
+            bb = f32(sm - hi)
+            e = f32(f32(hi - f32(sm - bb)) + f32(acc - bb))
+            hi, lo = sm, f32(lo + e - cmp)
         out[p] = float(hi) + float(lo)
     return out
 
