@@ -126,11 +126,12 @@ __global__ void fx_range_kernel(const double *__restrict__ pos, int64_t P, int d
 // positions.
 __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double z2, int dim,
                               int64_t n_modes, int64_t j, int incompr,
-                              const unsigned long long *maxbits, uint32_t *__restrict__ r,
+                              unsigned long long *maxbits, uint32_t *__restrict__ r,
                               int *range_flag) {
     double k[3] = {0.0, 0.0, 0.0};
     for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
     bool finite = isfinite(z1) && isfinite(z2);
+    bool small = true;                              // every |BI| < 2^22
     double phi = 0.0;                               // units of 2^-32 turn
     for (int d = 0; d < 3; ++d) {
         int32_t bi = 0;
@@ -150,6 +151,8 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
         }
         r[d] = static_cast<uint32_t>(bi) + 0x80000000u;
         r[4 + d] = bf;
+        r[9 + d] = __float_as_uint(static_cast<float>(bi));
+        small = small && bi < (1 << 22) && bi > -(1 << 22);
     }
     double w[3] = {0.0, 0.0, 0.0};
     if (incompr) {   // projector as the reference forms it (src/field.rs:138-152)
@@ -163,7 +166,8 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
     r[3] = __float_as_uint(__double2float_rn(w[0]));
     r[7] = __float_as_uint(__double2float_rn(w[1]));
     r[8] = __float_as_uint(__double2float_rn(w[2]));
-    for (int q = 9; q < kFxTab; ++q) r[q] = 0u;
+    if (!small) atomicOr(maxbits + 3, 1ull);
+    for (int q = 12; q < kFxTab; ++q) r[q] = 0u;
     phi = fmod(phi, 4294967296.0);
     // T[m] = (z1 - i z2) e^{-2 pi i phi / 2^32} e^{2 pi i m / 16}: one FP64
     // sincos for the mode's rotation, the sixteenth turns from a table (FP64
@@ -185,7 +189,7 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
 __global__ void fx_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
                                const double *__restrict__ z2, int dim, int64_t n_modes,
                                int64_t j0, int64_t nc, int incompr,
-                               const unsigned long long *maxbits, uint32_t *__restrict__ rec,
+                               unsigned long long *maxbits, uint32_t *__restrict__ rec,
                                int *range_flag) {
     const int64_t jl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (jl >= nc) return;
@@ -221,13 +225,20 @@ __device__ __forceinline__ float2 fx_lds2(uint32_t addr) {
 // The term Re(T e^{i theta}) of one point*mode: c the point's constant,
 // (xh, x8l) its coordinate words, (bi, bf) the mode's wave-number words, tab
 // the shared-memory address of the mode's 128-byte-aligned table.
-template <int D>
+template <int D, bool SMALL>
 __device__ __forceinline__ float fx_term(uint32_t c, const uint32_t *xh, const uint32_t *x8l,
-                                         const uint32_t *bi, const uint32_t *bf, uint32_t tab) {
+                                         const float *xlf, const uint32_t *bi, const uint32_t *bf,
+                                         const float *bif, uint32_t tab) {
     uint32_t t = c;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-        t += __umulhi(bi[d], x8l[d]);
+        if constexpr (SMALL) {
+            // BI Xl 2^-29 (|BI| < 2^22) rounded to an integer by one FP32
+            // fused multiply-add into the mantissa of 1.5 2^23
+            t += __float_as_uint(fmaf(bif[d], xlf[d], 12582912.0f));
+        } else {
+            t += __umulhi(bi[d], x8l[d]);
+        }
         t += __umulhi(bf[d], xh[d]);
         t += bi[d] * xh[d];
     }
@@ -246,8 +257,8 @@ __device__ __forceinline__ float fx_term(uint32_t c, const uint32_t *xh, const u
 // p_first + t + r*kFxThreads), modes [jb, je) of the records `rec`; sums
 // written (accumulate=0) or added at dst + i*sd + p*sp.  maxbits: the
 // positions' range words (scales); srec: shared staging of kFxTile records.
-template <int D, int R, bool INC>
-__device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t P, int64_t p_first,
+template <int D, int R, bool INC, bool SMALL>
+__device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_t P, int64_t p_first,
                                          const uint32_t *__restrict__ rec, int64_t jb, int64_t je,
                                          int accumulate, double *__restrict__ dst, int64_t sd,
                                          int64_t sp, const unsigned long long *maxbits,
@@ -259,7 +270,10 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
     int sc[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) sc[d] = fx_scale(maxbits[d]);
-    uint32_t xh[R][D], x8l[R][D], cp[R];
+    // SMALL: every mode's |BI| < 2^22, and BI Xl 2^-29 is an FP32 product
+    // (xlf = Xl 2^-29); otherwise a high integer product (x8l = 8 Xl)
+    uint32_t xh[R][D], x8l[R][SMALL ? 1 : D], cp[R];
+    float xlf[R][SMALL ? D : 1];
     bool bad[R];
     float hi[R][NOUT], lo[R][NOUT];
 #pragma unroll
@@ -279,9 +293,17 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
             const uint32_t h = static_cast<uint32_t>(Xp >> 29);
             const uint32_t l = static_cast<uint32_t>(Xp) & 0x1FFFFFFFu;
             xh[r][d] = h;
-            x8l[r][d] = l << 3;
-            // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32) and 4 Xl
-            c -= 4u * l + ((h & 1u) << 31);
+            if constexpr (SMALL) {
+                xlf[r][d] = static_cast<float>(l) * 1.862645149230957e-09f;     // Xl 2^-29
+                // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32); the FP32
+                // product of the signed BI leaves 0x4B400000 (the bits of
+                // 1.5 2^23) in theta
+                c -= 0x4B400000u + ((h & 1u) << 31);
+            } else {
+                x8l[r][d] = l << 3;
+                // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32) and 4 Xl
+                c -= 4u * l + ((h & 1u) << 31);
+            }
         }
         cp[r] = c;
 #pragma unroll
@@ -316,25 +338,33 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
             const uint4 ha1 = *reinterpret_cast<const uint4 *>(ma + 4);   // BF0..2, w1
             const uint4 hb0 = *reinterpret_cast<const uint4 *>(mb);
             const uint4 hb1 = *reinterpret_cast<const uint4 *>(mb + 4);
+            const uint4 ha2 = *reinterpret_cast<const uint4 *>(ma + 8);   // w2, BI0..2 as FP32
+            const uint4 hb2 = *reinterpret_cast<const uint4 *>(mb + 8);
             const uint32_t bia[3] = {ha0.x, ha0.y, ha0.z}, bfa[3] = {ha1.x, ha1.y, ha1.z};
             const uint32_t bib[3] = {hb0.x, hb0.y, hb0.z}, bfb[3] = {hb1.x, hb1.y, hb1.z};
+            const float bifa[3] = {__uint_as_float(ha2.y), __uint_as_float(ha2.z),
+                                   __uint_as_float(ha2.w)};
+            const float bifb[3] = {__uint_as_float(hb2.y), __uint_as_float(hb2.z),
+                                   __uint_as_float(hb2.w)};
             // the second mode of an odd tile's last pair counts zero times
             const float sb = two ? 1.0f : 0.0f;
             float wa[3] = {1.f, 0.f, 0.f}, wb[3] = {sb, 0.f, 0.f};
             if (INC) {
                 wa[0] = __uint_as_float(ha0.w);
                 wa[1] = __uint_as_float(ha1.w);
-                wa[2] = __uint_as_float(ma[8]);
+                wa[2] = __uint_as_float(ha2.x);
                 wb[0] = sb * __uint_as_float(hb0.w);
                 wb[1] = sb * __uint_as_float(hb1.w);
-                wb[2] = sb * __uint_as_float(mb[8]);
+                wb[2] = sb * __uint_as_float(hb2.x);
             }
             const uint32_t taba = sbase + static_cast<uint32_t>(m * kFxRecWords + kFxTab) * 4u;
             const uint32_t tabb = two ? taba + kFxRecWords * 4u : taba;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const float ta = fx_term<D>(cp[r], xh[r], x8l[r], bia, bfa, taba);
-                const float tb = fx_term<D>(cp[r], xh[r], x8l[r], bib, bfb, tabb);
+                const float ta =
+                    fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], bia, bfa, bifa, taba);
+                const float tb =
+                    fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], bib, bfb, bifb, tabb);
                 if (INC) {
 #pragma unroll
                     for (int i = 0; i < NOUT; ++i)
@@ -365,6 +395,23 @@ __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t
             *o = accumulate ? *o + v : v;
         }
     }
+}
+
+// The block's work with the product form its modes allow: maxbits[3] is
+// set when some mode of the call (or batch item) has |BI| >= 2^22; the
+// branch is the same for the whole block.
+template <int D, int R, bool INC>
+__device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t P, int64_t p_first,
+                                         const uint32_t *__restrict__ rec, int64_t jb, int64_t je,
+                                         int accumulate, double *__restrict__ dst, int64_t sd,
+                                         int64_t sp, const unsigned long long *maxbits,
+                                         uint32_t *srec) {
+    if (maxbits[3] == 0ull)
+        fx_block_<D, R, INC, true>(pos, P, p_first, rec, jb, je, accumulate, dst, sd, sp, maxbits,
+                                   srec);
+    else
+        fx_block_<D, R, INC, false>(pos, P, p_first, rec, jb, je, accumulate, dst, sd, sp, maxbits,
+                                    srec);
 }
 
 // R points per thread (2, 4 or 8; the autotuner picks).  The launch bound
@@ -465,7 +512,7 @@ __global__ void batch_fx_range_kernel(const BatchItem *__restrict__ items,
 // z2 first).
 __global__ void batch_fx_table_kernel(const BatchItem *__restrict__ items,
                                       const int64_t *__restrict__ prefix, int64_t n_items,
-                                      int64_t total, const unsigned long long *maxbits,
+                                      int64_t total, unsigned long long *maxbits,
                                       uint32_t *__restrict__ rec, int *range_flag) {
     const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (g >= total) return;
@@ -488,7 +535,7 @@ __global__ void batch_fx_table_kernel(const BatchItem *__restrict__ items,
 
 // Persistent batch kernel (see batch_plain_kernel in plain.cu).
 template <int R>
-__global__ void __launch_bounds__(kFxThreads)
+__global__ void __launch_bounds__(kFxThreads, R >= 8 ? 2 : 4)
 batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict__ units,
                 int64_t n_units, int *__restrict__ counter, const uint32_t *__restrict__ rec,
                 const unsigned long long *__restrict__ maxbits) {

@@ -169,3 +169,18 @@ def test_summate_batch_host_api(gsc):
     # the same shapes again reuse the plan; plain FP64 bar on a second ensemble
     outs = gsc.summate_batch(_items(8, SPECS), form="plain")
     _check(_items(8, SPECS), outs, "plain")
+
+
+def test_batch_mixed_both_product_forms(gsc):
+    """Items whose wave numbers times extent keep every |BI| < 2^22 (FP32
+    product of BI Xl 2^-29) beside items beyond it (integer high products),
+    in one persistent launch."""
+    rng = np.random.default_rng(31)
+    items = []
+    for span in (500.0, 3.0e6, 800.0, 2.0e6):
+        n, p = int(rng.integers(200, 700)), int(rng.integers(500, 3000))
+        cov = rng.standard_normal((3, n)) / np.sqrt(rng.chisquare(1, n)) * 0.2
+        items.append({"kind": "scalar", "cov": cov, "z1": rng.standard_normal(n),
+                      "z2": rng.standard_normal(n), "pos": rng.uniform(0.0, span, (3, p))})
+    outs = gsc.summate_batch(items, form="mixed")
+    _check(items, outs, "mixed")

@@ -1,8 +1,8 @@
 """Mixed-precision forms on explicit points against the oracle (GPU tests).
 
-`mixed`: phase in double-float (FP32 pairs), FP32 sincos, FP32 sums per 32
-modes with a compensated total.  `mixed_f64phase`: phase and reduction in
-FP64.  Bar for both: max |err| <= 1e-6 x RMS of the oracle field
+`mixed`: phase as a 32-bit fixed-point integer (units of 2^-32 turn), FP32
+table and polynomial sincos, FP32 pair and tile sums with a compensated
+total.  `mixed_f64phase`: phase and reduction in FP64.  Bar for both: max |err| <= 1e-6 x RMS of the oracle field
 (reference src/field.rs:37-65, :97-182), including the heavy-tailed spectrum
 of the unstructured 3-D benchmark where |k.x| reaches 1e5.
 """
@@ -65,6 +65,32 @@ def test_mixed_heavy_tailed_unstructured(gsc):
         err = rel_err(out, ref)
         e_rms = float(np.sqrt(np.mean((out - ref) ** 2)) / rms(ref))
         print(f"{form} heavy 3-D 4096 modes: max {err:.3e} rms {e_rms:.3e}")
+        assert err <= TOL
+
+
+def _max_bi(cov, pos):
+    """Largest |BI| of the call, the integer part of kappa 2^(61 - s) with
+    2^s the positions' fixed-point scale (max |x| in [2^(e-1), 2^e): s = 60 - e)."""
+    e = np.frexp(np.abs(pos).max(axis=1))[1]
+    return float(np.max(np.abs(cov) / (2.0 * np.pi) * np.ldexp(1.0, e + 1)[:, None]))
+
+
+@pytest.mark.parametrize("incompr", [False, True])
+def test_mixed_both_product_forms(gsc, incompr):
+    """While every |BI| < 2^22 (about 2^21 turns across the domain), the
+    kernel forms BI Xl 2^-29 with an FP32 product; a wider call takes integer
+    high products.  One heavy-tailed call of each, against the oracle."""
+    for span, small in ((1000.0, True), (2.0e6, False)):
+        cov, z1, z2, pos = _case(21, 3, 512, 4096, kscale=0.2, span=span, heavy=True)
+        assert (_max_bi(cov, pos) < 2.0 ** 22) == small
+        if incompr:
+            ref = oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)
+            out = gsc.summate_incompr(cov, z1, z2, pos, form="mixed")
+        else:
+            ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+            out = gsc.summate(cov, z1, z2, pos, form="mixed")
+        err = rel_err(out, ref)
+        print(f"span {span:g} (max |BI| {_max_bi(cov, pos):.3g}): {err:.3e}")
         assert err <= TOL
 
 

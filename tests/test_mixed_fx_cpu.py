@@ -9,7 +9,10 @@ B = kappa 2^(61 - s) as BI + BF 2^-32 with BI biased by 2^31, and
 
 (mod 2^32, units of 2^-32 turn), with the per-point constant c_point taking
 out the bias (and adding 2^27 + 16, which centres and rounds the remainder)
-and a per-mode constant phi folded into the mode's table.
+and a per-mode constant phi folded into the mode's table.  When every mode of
+a call has |BI| < 2^22, the kernel forms BI Xl 2^-29 instead as one FP32
+fused multiply-add of the signed BI and fl(Xl 2^-29) into the mantissa of
+1.5 2^23, rounded to an integer; that form is restated here as well.
 Restated here with the same unsigned 32-bit operations and compared with the
 exact rational phase of the FP64 inputs (Python integers): within 4 units
 (2^-30 turns) in 1-3 dimensions, heavy-tailed wave numbers and coordinates of
@@ -34,12 +37,23 @@ def scale(maxabs):
     return 60 - e
 
 
-def point_words(x, s):
-    """(Xh, 8 Xl, per-point constant part) of one coordinate."""
+def point_words(x, s, small=False):
+    """(Xh, 8 Xl or fl(Xl 2^-29), per-point constant part) of one coordinate."""
     X = int(np.rint(np.ldexp(x, s)))
     Xp = X + (1 << 60)
     h, l = Xp >> 29, Xp & ((1 << 29) - 1)
+    if small:
+        return h, np.float32(np.float32(l) * np.float32(2.0 ** -29)), \
+            (0x4B400000 + ((h & 1) << 31)) & U32
     return h, (l << 3) & U32, (4 * l + ((h & 1) << 31)) & U32
+
+
+def small_product(bi_biased, xlf):
+    """round(BI Xl 2^-29) + 0x4B400000 as the kernel's FP32 fused multiply-add
+    leaves it (exact in FP64 before the one rounding to FP32)."""
+    bi = np.float32(int(bi_biased) - (1 << 31))
+    v = np.float32(np.float64(bi) * np.float64(xlf) + 12582912.0)
+    return int(v.view(np.uint32))
 
 
 def mode_words(k, s):
@@ -51,17 +65,20 @@ def mode_words(k, s):
     return (bi + (1 << 31)) & U32, bf, Fraction((bq >> 1) & U32) + Fraction(bq & 1, 2)
 
 
-def fx_theta(k, x, dim):
+def fx_theta(k, x, dim, small=False):
     """theta + 2^27 + 16 (uint32) of one point*mode and the per-mode phi (exact)."""
     s = [scale(abs(x[d])) for d in range(dim)]
     c = (0x08000000 + 16 + dim) & U32
     t = 0
     phi = Fraction(0)
     for d in range(dim):
-        h, x8l, cd = point_words(x[d], s[d])
+        h, xl, cd = point_words(x[d], s[d], small)
         bi, bf, ph = mode_words(k[d], s[d])
         c = (c - cd) & U32
-        t = (t + ((bi * x8l) >> 32)) & U32
+        if small:
+            t = (t + small_product(bi, xl)) & U32
+        else:
+            t = (t + ((bi * xl) >> 32)) & U32
         t = (t + ((bf * h) >> 32)) & U32
         t = (t + bi * h) & U32
         phi += ph
@@ -75,8 +92,9 @@ def exact_turns(k, x, dim):
                for d in range(dim))
 
 
+@pytest.mark.parametrize("small", [False, True])
 @pytest.mark.parametrize("dim", [1, 2, 3])
-def test_integer_phase_within_four_units(dim):
+def test_integer_phase_within_four_units(dim, small):
     rng = np.random.default_rng(dim)
     worst = 0.0
     for _ in range(3000):
@@ -84,9 +102,10 @@ def test_integer_phase_within_four_units(dim):
         x = rng.uniform(-ext, ext, dim)
         k = rng.standard_normal(dim) / np.sqrt(rng.chisquare(1)) * 10.0 ** rng.uniform(-2, 1)
         s = [scale(abs(x[d])) for d in range(dim)]
-        if any(abs(np.ldexp(k[d] * INV2PI, 61 - s[d])) >= 2 ** 31 for d in range(dim)):
+        lim = 2 ** 22 if small else 2 ** 31
+        if any(abs(np.ldexp(k[d] * INV2PI, 61 - s[d])) >= lim - 1 for d in range(dim)):
             continue
-        t, phi = fx_theta(k, x, dim)
+        t, phi = fx_theta(k, x, dim, small)
         # t = kappa.x + phi + 2^27 + 16 (table centring, remainder rounding),
         # modulo one turn
         want = (exact_turns(k, x, dim) * 2 ** 32 + phi + 2 ** 27 + 16) % (2 ** 32)
@@ -146,6 +165,8 @@ def fx_field(cov, z1, z2, pos):
     out = np.empty(P)
     f32 = np.float32
     tabs, words = [], []
+    small = all(abs(int(mode_words(cov[d, j], s[d])[0]) - (1 << 31)) < (1 << 22)
+                for d in range(dim) for j in range(n))
     for j in range(n):
         ws = [mode_words(cov[d, j], s[d]) for d in range(dim)]
         phi = float(sum(w[2] for w in ws) % (2 ** 32))
@@ -155,7 +176,7 @@ def fx_field(cov, z1, z2, pos):
         tabs.append((tr, ti))
         words.append(ws)
     for p in range(P):
-        pw = [point_words(pos[d, p], s[d]) for d in range(dim)]
+        pw = [point_words(pos[d, p], s[d], small) for d in range(dim)]
         c = (0x08000000 + 16 + dim) & U32
         for d in range(dim):
             c = (c - pw[d][2]) & U32
@@ -167,7 +188,10 @@ def fx_field(cov, z1, z2, pos):
                 t = c
                 for d in range(dim):
                     bi, bf, _ = words[j][d]
-                    t = (t + ((bi * pw[d][1]) >> 32)) & U32
+                    if small:
+                        t = (t + small_product(bi, pw[d][1])) & U32
+                    else:
+                        t = (t + ((bi * pw[d][1]) >> 32)) & U32
                     t = (t + ((bf * pw[d][0]) >> 32)) & U32
                     t = (t + bi * pw[d][0]) & U32
                 terms.append(fx_term(t, tabs[j]))
@@ -185,12 +209,15 @@ def fx_field(cov, z1, z2, pos):
     return out
 
 
-def test_field_against_the_oracle():
+@pytest.mark.parametrize("extent", [1000.0, 2e6])
+def test_field_against_the_oracle(extent):
+    """A heavy-tailed field; at the larger extent some |BI| reach 2^22 and
+    the field takes the integer high products."""
     rng = np.random.default_rng(11)
     n, P = 200, 300
     cov = rng.standard_normal((3, n)) / np.sqrt(rng.chisquare(1, n)) / 5.0   # heavy tails
     z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
-    pos = rng.uniform(0, 1000, (3, P))
+    pos = rng.uniform(0, extent, (3, P))
     ref = oracle.summator(cov, z1, z2, pos)
     got = fx_field(cov, z1, z2, pos)
     err = np.abs(got - ref).max() / np.sqrt(np.mean(ref ** 2))
