@@ -1044,14 +1044,14 @@ PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17,
 # FMA-pipe instructions per point*mode of the mixed kernel (mixed_fx.cu),
 # counted from the source: the integer phase, 3 per dimension (the low and
 # the high integer products of BI Xh and BF Xh, and BI Xl 2^-29 as one FP32
-# FMA, or a third high product on calls with some |BI| >= 2^22; IMAD issues
-# on the FMA pipe), then 10 FP32 for the remainder float, its polynomials
+# FMA, or a third high product on calls with some |BI| >= 2^20; IMAD issues
+# on the FMA pipe), then 9 FP32 for the remainder float, its polynomials
 # and the term; two modes' terms are added (one FMA per pair) before a
 # 4-instruction Kahan step, 2.5 per point*mode; the incompressible field
 # weights the pair per component (2 per pair) before its Kahan step, 3 per
 # point*mode and component; the table index, shifts, the addition of the
 # FP32 product's bits and the table load run on other pipes
-MIXED_FMA_OPS = {(1, False): 15.5, (2, False): 18.5, (3, False): 21.5, (2, True): 22, (3, True): 28}
+MIXED_FMA_OPS = {(1, False): 14.5, (2, False): 17.5, (3, False): 20.5, (2, True): 21, (3, True): 27}
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu

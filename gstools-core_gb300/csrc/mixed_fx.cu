@@ -63,17 +63,20 @@ constexpr int kFxTile = 32;             // modes per staged tile = accumulation 
 constexpr int kFxTab = 32;
 constexpr int kFxRecWords = 64;
 static_assert(kFxRecWords * 4 == kFxRecBytesPerMode, "record layout");
-// sin(r pi/8) = r (S1 + r^2 (S3 + r^2 S5)), cos(r pi/8) = 1 + r^2 (C2 + r^2
-// (C4 + r^2 C6)) for r in sixteenths of a turn, |r| <= 1/2: the Taylor
-// coefficients of sin and cos scaled by powers of pi/8
-constexpr double kFxPi8 = 0.39269908169872415;                  // pi/8
-constexpr float kFxS1 = static_cast<float>(kFxPi8);
-constexpr float kFxS3 = static_cast<float>(-kFxPi8 * kFxPi8 * kFxPi8 / 6.0);
-constexpr float kFxS5 = static_cast<float>(kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 / 120.0);
-constexpr float kFxC2 = static_cast<float>(-kFxPi8 * kFxPi8 / 2.0);
-constexpr float kFxC4 = static_cast<float>(kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 / 24.0);
-constexpr float kFxC6 =
-    static_cast<float>(-kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 * kFxPi8 / 720.0);
+// sin(r pi/8) = r (S1 + r^2 (S3 + r^2 S5)), cos(r pi/8) = C0 + r^2 (C2 + r^2
+// C4) for r in sixteenths of a turn, |r| <= 1/2: minimax (Remez exchange on
+// r^2 in [0, 1/4], absolute error) fits, rounded to FP32; with the rounded
+// coefficients both stay within 6e-9 of sin and cos
+constexpr float kFxS1 = 0.39269909262657166f, kFxS3 = -0.01009317860007286f,
+                kFxS5 = 7.771774107823148e-05f;
+constexpr float kFxC0 = 1.0f, kFxC2 = -0.07710610330104828f, kFxC4 = 0.000988987972959876f;
+// 1.5 2^23: an FP32 sum that stays within 2^22 of it has ulp 1, and the
+// integer it rounds to is its bit pattern minus 0x4B400000
+constexpr float kFxMagic = 12582912.0f;
+constexpr uint32_t kFxMagicBits = 0x4B400000u;
+// the FP32 product form needs |BI| < 2^20 in every dimension (the sum of
+// three products stays within 2^22 of the magic constant)
+constexpr int32_t kFxSmallBI = 1 << 20;
 
 // cos(2 pi m / 16), m = 0..15, to FP64 rounding (from cos(pi/8) =
 // sqrt(2 + sqrt 2) / 2 and cos(pi/4) = sqrt(2) / 2)
@@ -131,7 +134,7 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
     double k[3] = {0.0, 0.0, 0.0};
     for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
     bool finite = isfinite(z1) && isfinite(z2);
-    bool small = true;                              // every |BI| < 2^22
+    bool small = true;                              // every |BI| < 2^20
     double phi = 0.0;                               // units of 2^-32 turn
     for (int d = 0; d < 3; ++d) {
         int32_t bi = 0;
@@ -152,7 +155,7 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
         r[d] = static_cast<uint32_t>(bi) + 0x80000000u;
         r[4 + d] = bf;
         r[9 + d] = __float_as_uint(static_cast<float>(bi));
-        small = small && bi < (1 << 22) && bi > -(1 << 22);
+        small = small && bi < kFxSmallBI && bi > -kFxSmallBI;
     }
     double w[3] = {0.0, 0.0, 0.0};
     if (incompr) {   // projector as the reference forms it (src/field.rs:138-152)
@@ -223,22 +226,25 @@ __device__ __forceinline__ float2 fx_lds2(uint32_t addr) {
 }
 
 // The term Re(T e^{i theta}) of one point*mode: c the point's constant,
-// (xh, x8l) its coordinate words, (bi, bf) the mode's wave-number words, tab
-// the shared-memory address of the mode's 128-byte-aligned table.
+// (xh, x8l / xlf) its coordinate words, (bi, bf / bif) the mode's
+// wave-number words, tab the shared-memory address of the mode's
+// 128-byte-aligned table.
 template <int D, bool SMALL>
 __device__ __forceinline__ float fx_term(uint32_t c, const uint32_t *xh, const uint32_t *x8l,
                                          const float *xlf, const uint32_t *bi, const uint32_t *bf,
                                          const float *bif, uint32_t tab) {
     uint32_t t = c;
+    if constexpr (SMALL) {
+        // sum_d BI Xl 2^-29 (every |BI| < 2^20) rounded to an integer by a
+        // chain of FP32 fused multiply-adds into the mantissa of 1.5 2^23
+        float v = kFxMagic;
+#pragma unroll
+        for (int d = 0; d < D; ++d) v = fmaf(bif[d], xlf[d], v);
+        t += __float_as_uint(v);
+    }
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-        if constexpr (SMALL) {
-            // BI Xl 2^-29 (|BI| < 2^22) rounded to an integer by one FP32
-            // fused multiply-add into the mantissa of 1.5 2^23
-            t += __float_as_uint(fmaf(bif[d], xlf[d], 12582912.0f));
-        } else {
-            t += __umulhi(bi[d], x8l[d]);
-        }
+        if constexpr (!SMALL) t += __umulhi(bi[d], x8l[d]);
         t += __umulhi(bf[d], xh[d]);
         t += bi[d] * xh[d];
     }
@@ -249,8 +255,40 @@ __device__ __forceinline__ float fx_term(uint32_t c, const uint32_t *xh, const u
     const float r = __uint_as_float(0x3F800000u | ((t >> 5) & 0x007FFFFFu)) - 1.5f;
     const float r2 = r * r;
     const float sn = r * fmaf(r2, fmaf(r2, kFxS5, kFxS3), kFxS1);
-    const float cs = fmaf(r2, fmaf(r2, fmaf(r2, kFxC6, kFxC4), kFxC2), 1.0f);
+    const float cs = fmaf(r2, fmaf(r2, kFxC4, kFxC2), kFxC0);
     return fmaf(T.x, cs, -T.y * sn);
+}
+
+// The words of mode m of the staged tile: BI' and BF, BI as FP32, the
+// projector weights (times scale; incompressible field only) and the
+// shared-memory address of the table.
+struct FxModeWords {
+    uint32_t bi[3], bf[3];
+    float bif[3], w[3];
+    uint32_t tab;
+};
+
+template <bool INC>
+__device__ __forceinline__ FxModeWords fx_mode_words(const uint32_t *srec, uint32_t sbase, int m,
+                                                     float scale) {
+    const uint32_t *mr = srec + m * kFxRecWords;
+    const uint4 h0 = *reinterpret_cast<const uint4 *>(mr);         // BI'0..2, w0
+    const uint4 h1 = *reinterpret_cast<const uint4 *>(mr + 4);     // BF0..2, w1
+    const uint4 h2 = *reinterpret_cast<const uint4 *>(mr + 8);     // w2, BI0..2 as FP32
+    FxModeWords o;
+    o.bi[0] = h0.x; o.bi[1] = h0.y; o.bi[2] = h0.z;
+    o.bf[0] = h1.x; o.bf[1] = h1.y; o.bf[2] = h1.z;
+    o.bif[0] = __uint_as_float(h2.y);
+    o.bif[1] = __uint_as_float(h2.z);
+    o.bif[2] = __uint_as_float(h2.w);
+    o.w[0] = o.w[1] = o.w[2] = 0.f;
+    if (INC) {
+        o.w[0] = scale * __uint_as_float(h0.w);
+        o.w[1] = scale * __uint_as_float(h1.w);
+        o.w[2] = scale * __uint_as_float(h2.x);
+    }
+    o.tab = sbase + static_cast<uint32_t>(m * kFxRecWords + kFxTab) * 4u;
+    return o;
 }
 
 // One block's work: the kFxThreads*R points from p_first (thread t owns
@@ -270,7 +308,7 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
     int sc[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) sc[d] = fx_scale(maxbits[d]);
-    // SMALL: every mode's |BI| < 2^22, and BI Xl 2^-29 is an FP32 product
+    // SMALL: every mode's |BI| < 2^20, and BI Xl 2^-29 is an FP32 product
     // (xlf = Xl 2^-29); otherwise a high integer product (x8l = 8 Xl)
     uint32_t xh[R][D], x8l[R][SMALL ? 1 : D], cp[R];
     float xlf[R][SMALL ? D : 1];
@@ -295,16 +333,16 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
             xh[r][d] = h;
             if constexpr (SMALL) {
                 xlf[r][d] = static_cast<float>(l) * 1.862645149230957e-09f;     // Xl 2^-29
-                // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32); the FP32
-                // product of the signed BI leaves 0x4B400000 (the bits of
-                // 1.5 2^23) in theta
-                c -= 0x4B400000u + ((h & 1u) << 31);
+                // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32)
+                c -= (h & 1u) << 31;
             } else {
                 x8l[r][d] = l << 3;
                 // the bias 2^31 of BI' adds 2^31 Xh (mod 2^32) and 4 Xl
                 c -= 4u * l + ((h & 1u) << 31);
             }
         }
+        // the FP32 products of the signed BI leave the bits of 1.5 2^23 in theta
+        if constexpr (SMALL) c -= kFxMagicBits;
         cp[r] = c;
 #pragma unroll
         for (int i = 0; i < NOUT; ++i) hi[r][i] = lo[r][i] = 0.f;
@@ -330,45 +368,23 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
 #pragma unroll
             for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
         // modes in pairs: the two terms are added before the Kahan step
-        for (int m = 0; m < tm; m += 2) {
-            const bool two = m + 1 < tm;
-            const uint32_t *ma = srec + m * kFxRecWords;
-            const uint32_t *mb = two ? ma + kFxRecWords : ma;
-            const uint4 ha0 = *reinterpret_cast<const uint4 *>(ma);       // BI'0..2, w0
-            const uint4 ha1 = *reinterpret_cast<const uint4 *>(ma + 4);   // BF0..2, w1
-            const uint4 hb0 = *reinterpret_cast<const uint4 *>(mb);
-            const uint4 hb1 = *reinterpret_cast<const uint4 *>(mb + 4);
-            const uint4 ha2 = *reinterpret_cast<const uint4 *>(ma + 8);   // w2, BI0..2 as FP32
-            const uint4 hb2 = *reinterpret_cast<const uint4 *>(mb + 8);
-            const uint32_t bia[3] = {ha0.x, ha0.y, ha0.z}, bfa[3] = {ha1.x, ha1.y, ha1.z};
-            const uint32_t bib[3] = {hb0.x, hb0.y, hb0.z}, bfb[3] = {hb1.x, hb1.y, hb1.z};
-            const float bifa[3] = {__uint_as_float(ha2.y), __uint_as_float(ha2.z),
-                                   __uint_as_float(ha2.w)};
-            const float bifb[3] = {__uint_as_float(hb2.y), __uint_as_float(hb2.z),
-                                   __uint_as_float(hb2.w)};
+        int m = 0;
+        for (; m < tm; m += 2) {
             // the second mode of an odd tile's last pair counts zero times
+            const bool two = m + 1 < tm;
             const float sb = two ? 1.0f : 0.0f;
-            float wa[3] = {1.f, 0.f, 0.f}, wb[3] = {sb, 0.f, 0.f};
-            if (INC) {
-                wa[0] = __uint_as_float(ha0.w);
-                wa[1] = __uint_as_float(ha1.w);
-                wa[2] = __uint_as_float(ha2.x);
-                wb[0] = sb * __uint_as_float(hb0.w);
-                wb[1] = sb * __uint_as_float(hb1.w);
-                wb[2] = sb * __uint_as_float(hb2.x);
-            }
-            const uint32_t taba = sbase + static_cast<uint32_t>(m * kFxRecWords + kFxTab) * 4u;
-            const uint32_t tabb = two ? taba + kFxRecWords * 4u : taba;
+            const FxModeWords ma = fx_mode_words<INC>(srec, sbase, m, 1.0f);
+            const FxModeWords mb = fx_mode_words<INC>(srec, sbase, two ? m + 1 : m, sb);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const float ta =
-                    fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], bia, bfa, bifa, taba);
-                const float tb =
-                    fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], bib, bfb, bifb, tabb);
+                const float ta = fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], ma.bi, ma.bf,
+                                                   ma.bif, ma.tab);
+                const float tb = fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], mb.bi, mb.bf,
+                                                   mb.bif, mb.tab);
                 if (INC) {
 #pragma unroll
                     for (int i = 0; i < NOUT; ++i)
-                        fx_kahan(acc[r][i], cmp[r][i], fmaf(wa[i], ta, wb[i] * tb));
+                        fx_kahan(acc[r][i], cmp[r][i], fmaf(ma.w[i], ta, mb.w[i] * tb));
                 } else {
                     fx_kahan(acc[r][0], cmp[r][0], fmaf(sb, tb, ta));
                 }
@@ -398,7 +414,7 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
 }
 
 // The block's work with the product form its modes allow: maxbits[3] is
-// set when some mode of the call (or batch item) has |BI| >= 2^22; the
+// set when some mode of the call (or batch item) has |BI| >= 2^20; the
 // branch is the same for the whole block.
 template <int D, int R, bool INC>
 __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t P, int64_t p_first,

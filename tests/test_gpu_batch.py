@@ -172,7 +172,7 @@ def test_summate_batch_host_api(gsc):
 
 
 def test_batch_mixed_both_product_forms(gsc):
-    """Items whose wave numbers times extent keep every |BI| < 2^22 (FP32
+    """Items whose wave numbers times extent keep every |BI| < 2^20 (FP32
     product of BI Xl 2^-29) beside items beyond it (integer high products),
     in one persistent launch."""
     rng = np.random.default_rng(31)

@@ -10,9 +10,10 @@ B = kappa 2^(61 - s) as BI + BF 2^-32 with BI biased by 2^31, and
 (mod 2^32, units of 2^-32 turn), with the per-point constant c_point taking
 out the bias (and adding 2^27 + 16, which centres and rounds the remainder)
 and a per-mode constant phi folded into the mode's table.  When every mode of
-a call has |BI| < 2^22, the kernel forms BI Xl 2^-29 instead as one FP32
-fused multiply-add of the signed BI and fl(Xl 2^-29) into the mantissa of
-1.5 2^23, rounded to an integer; that form is restated here as well.
+a call has |BI| < 2^20, the kernel forms sum_d BI Xl 2^-29 instead as a
+chain of FP32 fused multiply-adds of the signed BI and fl(Xl 2^-29) into the
+mantissa of 1.5 2^23, rounded to an integer; that form is restated here as
+well.
 Restated here with the same unsigned 32-bit operations and compared with the
 exact rational phase of the FP64 inputs (Python integers): within 4 units
 (2^-30 turns) in 1-3 dimensions, heavy-tailed wave numbers and coordinates of
@@ -43,16 +44,22 @@ def point_words(x, s, small=False):
     Xp = X + (1 << 60)
     h, l = Xp >> 29, Xp & ((1 << 29) - 1)
     if small:
-        return h, np.float32(np.float32(l) * np.float32(2.0 ** -29)), \
-            (0x4B400000 + ((h & 1) << 31)) & U32
+        return h, np.float32(np.float32(l) * np.float32(2.0 ** -29)), ((h & 1) << 31) & U32
     return h, (l << 3) & U32, (4 * l + ((h & 1) << 31)) & U32
 
 
-def small_product(bi_biased, xlf):
-    """round(BI Xl 2^-29) + 0x4B400000 as the kernel's FP32 fused multiply-add
-    leaves it (exact in FP64 before the one rounding to FP32)."""
-    bi = np.float32(int(bi_biased) - (1 << 31))
-    v = np.float32(np.float64(bi) * np.float64(xlf) + 12582912.0)
+MAGIC_BITS = 0x4B400000          # bits of 1.5 2^23
+SMALL_BI = 1 << 20
+
+
+def small_products(bis_biased, xlfs):
+    """round(sum_d BI Xl 2^-29) + 0x4B400000 as the kernel's chain of FP32
+    fused multiply-adds leaves it (each step exact in FP64 before its one
+    rounding to FP32)."""
+    v = np.float32(12582912.0)
+    for bi_biased, xlf in zip(bis_biased, xlfs):
+        bi = np.float32(int(bi_biased) - (1 << 31))
+        v = np.float32(np.float64(bi) * np.float64(xlf) + np.float64(v))
     return int(v.view(np.uint32))
 
 
@@ -71,17 +78,20 @@ def fx_theta(k, x, dim, small=False):
     c = (0x08000000 + 16 + dim) & U32
     t = 0
     phi = Fraction(0)
+    bis, xls = [], []
     for d in range(dim):
         h, xl, cd = point_words(x[d], s[d], small)
         bi, bf, ph = mode_words(k[d], s[d])
         c = (c - cd) & U32
-        if small:
-            t = (t + small_product(bi, xl)) & U32
-        else:
+        bis.append(bi)
+        xls.append(xl)
+        if not small:
             t = (t + ((bi * xl) >> 32)) & U32
         t = (t + ((bf * h) >> 32)) & U32
         t = (t + bi * h) & U32
         phi += ph
+    if small:
+        t = (t + small_products(bis, xls) - MAGIC_BITS) & U32
     return (t + c) & U32, phi
 
 
@@ -102,7 +112,7 @@ def test_integer_phase_within_four_units(dim, small):
         x = rng.uniform(-ext, ext, dim)
         k = rng.standard_normal(dim) / np.sqrt(rng.chisquare(1)) * 10.0 ** rng.uniform(-2, 1)
         s = [scale(abs(x[d])) for d in range(dim)]
-        lim = 2 ** 22 if small else 2 ** 31
+        lim = SMALL_BI if small else 2 ** 31
         if any(abs(np.ldexp(k[d] * INV2PI, 61 - s[d])) >= lim - 1 for d in range(dim)):
             continue
         t, phi = fx_theta(k, x, dim, small)
@@ -115,8 +125,11 @@ def test_integer_phase_within_four_units(dim, small):
 
 
 PI8 = np.pi / 8
-S1, S3, S5 = (np.float32(v) for v in (PI8, -PI8 ** 3 / 6, PI8 ** 5 / 120))
-C2, C4, C6 = (np.float32(v) for v in (-PI8 ** 2 / 2, PI8 ** 4 / 24, -PI8 ** 6 / 720))
+# the kernel's minimax coefficients (FP32) of sin(r pi/8) / r and cos(r pi/8)
+# as polynomials in r^2, |r| <= 1/2
+S1, S3, S5 = (np.float32(v) for v in (0.39269909262657166, -0.01009317860007286,
+                                      7.771774107823148e-05))
+C0, C2, C4 = (np.float32(v) for v in (1.0, -0.07710610330104828, 0.000988987972959876))
 
 
 def fma32(a, b, c):
@@ -131,13 +144,25 @@ def fx_term(t, tab):
     r = f32(np.uint32(0x3F800000 | ((t >> 5) & 0x7FFFFF)).view(np.float32) - f32(1.5))
     r2 = f32(r * r)
     sn = f32(r * fma32(r2, fma32(r2, S5, S3), S1))
-    cs = fma32(r2, fma32(r2, fma32(r2, C6, C4), C2), f32(1))
+    cs = fma32(r2, fma32(r2, C4, C2), C0)
     return fma32(tab[0][m], cs, -f32(tab[1][m] * sn))
+
+
+def test_polynomials_within_their_bound():
+    """The FP32 coefficients, evaluated exactly, stay within 6e-9 of sin and
+    cos over |r| <= 1/2 (sixteenths of a turn)."""
+    r = np.linspace(-0.5, 0.5, 200001)
+    u = r * r
+    sn = r * (np.float64(S1) + u * (np.float64(S3) + u * np.float64(S5)))
+    cs = np.float64(C0) + u * (np.float64(C2) + u * np.float64(C4))
+    assert np.max(np.abs(sn - np.sin(PI8 * r))) < 6e-9
+    assert np.max(np.abs(cs - np.cos(PI8 * r))) < 6e-9
 
 
 def test_remainder_float_and_polynomials():
     """The remainder float is exact, within 2^-28 turn of the phase's
-    remainder, and the polynomials give e^{i theta} within 3e-9."""
+    remainder, and the FP32 evaluation gives e^{i theta} within the FP32
+    table entries' rounding."""
     rng = np.random.default_rng(5)
     t = rng.integers(0, 2 ** 32, 20000, dtype=np.uint64).astype(np.uint32)
     m = t >> 28
@@ -165,7 +190,7 @@ def fx_field(cov, z1, z2, pos):
     out = np.empty(P)
     f32 = np.float32
     tabs, words = [], []
-    small = all(abs(int(mode_words(cov[d, j], s[d])[0]) - (1 << 31)) < (1 << 22)
+    small = all(abs(int(mode_words(cov[d, j], s[d])[0]) - (1 << 31)) < SMALL_BI
                 for d in range(dim) for j in range(n))
     for j in range(n):
         ws = [mode_words(cov[d, j], s[d]) for d in range(dim)]
@@ -186,11 +211,12 @@ def fx_field(cov, z1, z2, pos):
             terms = []
             for j in range(t0, min(n, t0 + 32)):
                 t = c
+                if small:
+                    t = (t + small_products([words[j][d][0] for d in range(dim)],
+                                            [pw[d][1] for d in range(dim)]) - MAGIC_BITS) & U32
                 for d in range(dim):
                     bi, bf, _ = words[j][d]
-                    if small:
-                        t = (t + small_product(bi, pw[d][1])) & U32
-                    else:
+                    if not small:
                         t = (t + ((bi * pw[d][1]) >> 32)) & U32
                     t = (t + ((bf * pw[d][0]) >> 32)) & U32
                     t = (t + bi * pw[d][0]) & U32
@@ -211,7 +237,7 @@ def fx_field(cov, z1, z2, pos):
 
 @pytest.mark.parametrize("extent", [1000.0, 2e6])
 def test_field_against_the_oracle(extent):
-    """A heavy-tailed field; at the larger extent some |BI| reach 2^22 and
+    """A heavy-tailed field; at the larger extent some |BI| reach 2^20 and
     the field takes the integer high products."""
     rng = np.random.default_rng(11)
     n, P = 200, 300
