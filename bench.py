@@ -1046,12 +1046,14 @@ PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17,
 # the high integer products of BI Xh and BF Xh, and BI Xl 2^-29 as one FP32
 # FMA, or a third high product on calls with some |BI| >= 2^20; IMAD issues
 # on the FMA pipe), then 9 FP32 for the remainder float, its polynomials
-# and the term; two modes' terms are added (one FMA per pair) before a
-# 4-instruction Kahan step, 2.5 per point*mode; the incompressible field
-# weights the pair per component (2 per pair) before its Kahan step, 3 per
-# point*mode and component; the table index, shifts, the addition of the
-# FP32 product's bits and the table load run on other pipes
-MIXED_FMA_OPS = {(1, False): 14.5, (2, False): 17.5, (3, False): 20.5, (2, True): 21, (3, True): 27}
+# and the term; four modes' terms are added (3 additions) before a
+# 4-instruction Kahan step, 1.75 per point*mode; the incompressible field
+# weights each pair per component (2 per pair) and adds the pairs before
+# its Kahan step, 2.25 per point*mode and component; the table index,
+# shifts, the addition of the FP32 products' bits and the table load run on
+# other pipes
+MIXED_FMA_OPS = {(1, False): 13.75, (2, False): 16.75, (3, False): 19.75, (2, True): 19.5,
+                 (3, True): 24.75}
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu

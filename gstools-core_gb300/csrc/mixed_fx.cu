@@ -367,10 +367,34 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
-        // modes in pairs: the two terms are added before the Kahan step
-        int m = 0;
-        for (; m < tm; m += 2) {
-            // the second mode of an odd tile's last pair counts zero times
+        // modes in groups of four: two pair sums per point, added, then one
+        // Kahan step; a tile shorter than kFxTile (the last) goes in pairs,
+        // the second mode of an odd tile's last pair counting zero times
+        const int tq = tm == kFxTile ? kFxTile : 0;
+        for (int m = 0; m < tq; m += 4) {
+            float pend[R][NOUT];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const FxModeWords ma = fx_mode_words<INC>(srec, sbase, m + 2 * h, 1.0f);
+                const FxModeWords mb = fx_mode_words<INC>(srec, sbase, m + 2 * h + 1, 1.0f);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const float ta = fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], ma.bi,
+                                                       ma.bf, ma.bif, ma.tab);
+                    const float tb = fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], mb.bi,
+                                                       mb.bf, mb.bif, mb.tab);
+#pragma unroll
+                    for (int i = 0; i < NOUT; ++i) {
+                        const float ps = INC ? fmaf(ma.w[i], ta, mb.w[i] * tb) : ta + tb;
+                        if (h == 0)
+                            pend[r][i] = ps;
+                        else
+                            fx_kahan(acc[r][i], cmp[r][i], pend[r][i] + ps);
+                    }
+                }
+            }
+        }
+        for (int m = tq; m < tm; m += 2) {
             const bool two = m + 1 < tm;
             const float sb = two ? 1.0f : 0.0f;
             const FxModeWords ma = fx_mode_words<INC>(srec, sbase, m, 1.0f);
@@ -381,13 +405,10 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
                                                    ma.bif, ma.tab);
                 const float tb = fx_term<D, SMALL>(cp[r], xh[r], x8l[r], xlf[r], mb.bi, mb.bf,
                                                    mb.bif, mb.tab);
-                if (INC) {
 #pragma unroll
-                    for (int i = 0; i < NOUT; ++i)
-                        fx_kahan(acc[r][i], cmp[r][i], fmaf(ma.w[i], ta, mb.w[i] * tb));
-                } else {
-                    fx_kahan(acc[r][0], cmp[r][0], fmaf(sb, tb, ta));
-                }
+                for (int i = 0; i < NOUT; ++i)
+                    fx_kahan(acc[r][i], cmp[r][i],
+                             INC ? fmaf(ma.w[i], ta, mb.w[i] * tb) : fmaf(sb, tb, ta));
             }
         }
 #pragma unroll
