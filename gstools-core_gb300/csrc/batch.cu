@@ -692,6 +692,8 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     if (count < 0 || (count > 0 && !items)) return set_error(GSC_ERR_INVALID, "bad item list");
     // host-side validation (the plan re-checks shapes and forms)
     size_t n_in = 0, n_out = 0;
+    double total_work = 0.0;
+    std::vector<double> work(static_cast<size_t>(count));
     for (int64_t i = 0; i < count; ++i) {
         const gsc_batch_item &x = items[i];
         if (x.n_modes < 0 || x.n_points < 0 || x.dim < 1 || x.dim > 3)
@@ -701,9 +703,34 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         if ((x.n_modes > 0 && (!x.cov || !x.z1 || !x.z2 || (f && !x.spectrum_factor))) ||
             (x.n_points > 0 && (!x.pos || !x.out)))
             return set_error(GSC_ERR_INVALID, "item " + std::to_string(i) + ": NULL array");
+        const int64_t nout = x.kind == GSC_BATCH_INCOMPR ? x.dim : 1;
         n_in += static_cast<size_t>(x.dim * x.n_modes + 2 * x.n_modes + (f ? x.n_modes : 0) +
                                     x.dim * x.n_points);
-        n_out += static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
+        n_out += static_cast<size_t>(nout * x.n_points);
+        work[static_cast<size_t>(i)] = static_cast<double>(x.n_points) * x.n_modes * nout;
+        total_work += work[static_cast<size_t>(i)];
+    }
+    // Large ensembles run as a few groups of consecutive items, each its own
+    // plan: the inputs of one group are packed and copied
+    // (copy stream) while the previous group computes, and the results of a
+    // group are copied back while the next one computes.  Groups alternate
+    // between two compute streams, so that a group's persistent kernel takes
+    // the SMs that the previous group's last units leave idle.
+    // The first group is small (1/16 of the work), since its copy is the one
+    // that nothing hides; the other three take 5/16 each, whose inputs copy
+    // (about 5 times faster than they compute) within the previous group.
+    const int G = (total_work >= 4.0e9 && count >= 8) ? 4 : 1;
+    static const double kGroupEnd[4] = {1.0 / 16, 6.0 / 16, 11.0 / 16, 1.0};
+    std::vector<int64_t> gstart(static_cast<size_t>(G) + 1, count);
+    gstart[0] = 0;
+    {
+        double acc = 0.0;
+        int g = 1;
+        for (int64_t i = 0; i < count && g < G; ++i) {
+            acc += work[static_cast<size_t>(i)];
+            while (g < G && acc >= total_work * kGroupEnd[g - 1]) gstart[static_cast<size_t>(g++)] = i + 1;
+        }
+        for (; g < G; ++g) gstart[static_cast<size_t>(g)] = count;
     }
     timing_reset(ro.flags & GSC_FLAG_TIMING);
     DeviceCtx *ctx = nullptr;
@@ -712,6 +739,11 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     DeviceGuard g;
     GSC_TRY(g.set(ctx->device));
     cudaStream_t st = ctx->stream;
+    if (!ctx->copy_stream)
+        GSC_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    cudaStream_t cs = ctx->copy_stream;
+    if (G > 1 && !ctx->stream2)
+        GSC_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
     GSC_TRY(ensure_pinned(*ctx, std::max(n_in, n_out) * sizeof(double) + 64));
     GSC_TRY(ensure_dev(*ctx, ctx->io, (n_in + n_out) * sizeof(double) + 256));
     double *h = static_cast<double *>(ctx->pinned);
@@ -721,83 +753,144 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     // Every input is packed back to back into the pinned staging and moved
     // in 64 MiB chunks (h2d_packed): one pageable copy per array would pay
     // the driver's fixed cost hundreds of times.
-    std::vector<HostSrc> in_segs;
-    in_segs.reserve(static_cast<size_t>(count) * 5);
+    std::vector<std::vector<HostSrc>> in_segs(static_cast<size_t>(G));
     size_t off = 0, oo = 0;
-    auto put = [&](const double *src, int64_t n) -> const double * {
-        if (n <= 0) return nullptr;
-        const double *r = d + off;
-        in_segs.push_back(HostSrc{src, off * sizeof(double), static_cast<size_t>(n) * sizeof(double)});
-        off += static_cast<size_t>(n);
-        return r;
-    };
-    for (int64_t i = 0; i < count; ++i) {
-        const gsc_batch_item &x = items[i];
-        gsc_batch_item &y = dev[static_cast<size_t>(i)];
-        y = x;
-        y.cov = put(x.cov, x.dim * x.n_modes);
-        y.z1 = put(x.z1, x.n_modes);
-        y.z2 = put(x.z2, x.n_modes);
-        y.spectrum_factor = x.kind == GSC_BATCH_FOURIER ? put(x.spectrum_factor, x.n_modes) : nullptr;
-        y.pos = put(x.pos, x.dim * x.n_points);
-        y.out = x.n_points > 0 ? dout + oo : nullptr;
-        oo += static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
-    }
-    // the copies are timed here only when the plan is reused (a new plan's
-    // creation starts the call's timing afresh)
-    TimedLaunch tc(st);
-    tc.begin(K_COPY_H2D);
-    const int rc = h2d_packed(st, d, h, in_segs);
-    tc.end();
-    GSC_TRY(rc);
-    // the plan of the previous call is reused when the shapes match
-    std::vector<int64_t> sig = {reinterpret_cast<int64_t>(ctx->io.ptr), ro.form,
-                                static_cast<int64_t>(ro.tolerance * 1e15), count};
-    if (config)
-        sig.insert(sig.end(), {config->points_per_thread, config->tile_modes, config->units_per_block});
-    for (auto &y : dev) sig.insert(sig.end(), {y.dim, y.kind, y.n_modes, y.n_points});
-    if (!ctx->batch || sig != ctx->batch_sig) {
-        if (ctx->batch) {
-            GSC_CUDA(cudaStreamSynchronize(st));
-            gsc_batch_destroy(ctx->batch);
-            ctx->batch = nullptr;
+    for (int gi = 0; gi < G; ++gi) {
+        auto &segs = in_segs[static_cast<size_t>(gi)];
+        auto put = [&](const double *src, int64_t n) -> const double * {
+            if (n <= 0) return nullptr;
+            const double *r = d + off;
+            segs.push_back(HostSrc{src, off * sizeof(double), static_cast<size_t>(n) * sizeof(double)});
+            off += static_cast<size_t>(n);
+            return r;
+        };
+        for (int64_t i = gstart[static_cast<size_t>(gi)]; i < gstart[static_cast<size_t>(gi) + 1]; ++i) {
+            const gsc_batch_item &x = items[i];
+            gsc_batch_item &y = dev[static_cast<size_t>(i)];
+            y = x;
+            y.cov = put(x.cov, x.dim * x.n_modes);
+            y.z1 = put(x.z1, x.n_modes);
+            y.z2 = put(x.z2, x.n_modes);
+            y.spectrum_factor =
+                x.kind == GSC_BATCH_FOURIER ? put(x.spectrum_factor, x.n_modes) : nullptr;
+            y.pos = put(x.pos, x.dim * x.n_points);
+            y.out = x.n_points > 0 ? dout + oo : nullptr;
+            oo += static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
         }
-        GSC_CUDA(cudaStreamSynchronize(st));   // the plan's tuner reads the inputs
-        gsc_opts o{};
-        o.struct_size = sizeof(gsc_opts);
-        o.form = ro.form;
-        o.device = ctx->device;
-        o.flags = ro.flags;
-        o.stream = nullptr;
-        o.tolerance = ro.tolerance;
-        GSC_TRY(gsc_batch_create(dev.data(), count, &o, config, &ctx->batch));
-        ctx->batch_sig = sig;
-        timing_reset(ro.flags & GSC_FLAG_TIMING);
     }
-    ctx->batch->flags = ro.flags;               // this call's timing request
-    GSC_TRY(enqueue_run(*ctx->batch, st));      // (gsc_batch_run would restart the timing records)
-    // fault in the output pages while the GPU computes, then DMA straight
-    // into the caller's arrays
-    std::vector<HostSeg> segs;
+    // fault in pageable output pages on host threads while the GPU works
+    std::vector<HostSeg> osegs;
     for (int64_t i = 0; i < count; ++i) {
         const gsc_batch_item &x = items[i];
         const size_t n = static_cast<size_t>((x.kind == GSC_BATCH_INCOMPR ? x.dim : 1) * x.n_points);
-        segs.push_back(HostSeg{is_pinned_host(x.out) ? nullptr : x.out, n * sizeof(double)});
+        osegs.push_back(HostSeg{is_pinned_host(x.out) ? nullptr : x.out, n * sizeof(double)});
     }
     Prefault pf;
-    pf.start_many(segs);
-    pf.join();
-    oo = 0;
-    tc.begin(K_COPY_D2H);
-    for (int64_t i = 0; i < count; ++i) {
-        const size_t n = segs[static_cast<size_t>(i)].bytes;
-        if (n > 0)
-            GSC_CUDA(cudaMemcpyAsync(items[i].out, dout + oo, n, cudaMemcpyDeviceToHost, st));
-        oo += n / sizeof(double);
+    pf.start_many(osegs);
+    std::vector<cudaEvent_t> ev(static_cast<size_t>(2 * G), nullptr);
+    auto destroy_events = [&] {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    };
+    int rc = GSC_OK;
+    for (auto &e : ev)
+        if (rc == GSC_OK) rc = cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (ctx->batch.size() != static_cast<size_t>(G)) {
+        for (gsc_batch *b : ctx->batch) {
+            if (rc == GSC_OK) rc = cuda_ok(cudaStreamSynchronize(st));
+            gsc_batch_destroy(b);
+        }
+        ctx->batch.assign(static_cast<size_t>(G), nullptr);
+        ctx->batch_sig.assign(static_cast<size_t>(G), {});
     }
-    tc.end();
-    GSC_CUDA(cudaStreamSynchronize(st));
-    return GSC_OK;
+    // the second compute stream starts after the work queued before this call
+    if (rc == GSC_OK && G > 1) {
+        cudaEvent_t e0 = ev[static_cast<size_t>(2 * G - 1)];
+        rc = cuda_ok(cudaEventRecord(e0, st));
+        if (rc == GSC_OK) rc = cuda_ok(cudaStreamWaitEvent(ctx->stream2, e0, 0));
+    }
+    for (int gi = 0; gi < G && rc == GSC_OK; ++gi) {
+        const int64_t i0 = gstart[static_cast<size_t>(gi)], i1 = gstart[static_cast<size_t>(gi) + 1];
+        cudaStream_t gs = (gi & 1) ? ctx->stream2 : st;
+        // the copies are timed here only when the plan is reused (a new
+        // plan's creation starts the call's timing afresh)
+        TimedLaunch tc(cs);
+        tc.begin(K_COPY_H2D);
+        rc = h2d_packed(cs, d, h, in_segs[static_cast<size_t>(gi)]);
+        tc.end();
+        if (rc == GSC_OK) rc = cuda_ok(cudaEventRecord(ev[static_cast<size_t>(gi)], cs));
+        if (rc == GSC_OK) rc = cuda_ok(cudaStreamWaitEvent(gs, ev[static_cast<size_t>(gi)], 0));
+        if (rc != GSC_OK) break;
+        if (i1 == i0) {            // an empty group (a few items hold most of the work)
+            rc = cuda_ok(cudaEventRecord(ev[static_cast<size_t>(G + gi)], gs));
+            continue;
+        }
+        // the group's plan of the previous call is reused when the shapes match
+        std::vector<int64_t> sig = {reinterpret_cast<int64_t>(ctx->io.ptr), ro.form,
+                                    static_cast<int64_t>(ro.tolerance * 1e15), i1 - i0, gi};
+        if (config)
+            sig.insert(sig.end(),
+                       {config->points_per_thread, config->tile_modes, config->units_per_block});
+        for (int64_t i = i0; i < i1; ++i) {
+            const auto &y = dev[static_cast<size_t>(i)];
+            // the device addresses too: they move with the earlier groups' sizes
+            sig.insert(sig.end(), {y.dim, y.kind, y.n_modes, y.n_points,
+                                   reinterpret_cast<int64_t>(y.cov), reinterpret_cast<int64_t>(y.pos),
+                                   reinterpret_cast<int64_t>(y.out)});
+        }
+        gsc_batch *&plan = ctx->batch[static_cast<size_t>(gi)];
+        if (!plan || sig != ctx->batch_sig[static_cast<size_t>(gi)]) {
+            // the old plan's runs and this group's inputs must be done (the
+            // new plan's tuner reads the inputs)
+            rc = cuda_ok(cudaStreamSynchronize(gs));
+            if (rc == GSC_OK) rc = cuda_ok(cudaStreamSynchronize(cs));
+            if (plan) {
+                gsc_batch_destroy(plan);
+                plan = nullptr;
+            }
+            gsc_opts o{};
+            o.struct_size = sizeof(gsc_opts);
+            o.form = ro.form;
+            o.device = ctx->device;
+            o.flags = ro.flags;
+            o.stream = nullptr;
+            o.tolerance = ro.tolerance;
+            if (rc == GSC_OK) rc = gsc_batch_create(dev.data() + i0, i1 - i0, &o, config, &plan);
+            if (rc != GSC_OK) break;
+            ctx->batch_sig[static_cast<size_t>(gi)] = sig;
+            timing_reset(ro.flags & GSC_FLAG_TIMING);
+        }
+        plan->flags = ro.flags;                       // this call's timing request
+        rc = enqueue_run(*plan, gs);                  // (gsc_batch_run would restart the timing records)
+        if (rc == GSC_OK) rc = cuda_ok(cudaEventRecord(ev[static_cast<size_t>(G + gi)], gs));
+    }
+    pf.join();
+    // each group's results, once it is done, straight into the callers' arrays
+    oo = 0;
+    for (int gi = 0; gi < G && rc == GSC_OK; ++gi) {
+        rc = cuda_ok(cudaStreamWaitEvent(cs, ev[static_cast<size_t>(G + gi)], 0));
+        TimedLaunch tc(cs);
+        tc.begin(K_COPY_D2H);
+        for (int64_t i = gstart[static_cast<size_t>(gi)];
+             i < gstart[static_cast<size_t>(gi) + 1] && rc == GSC_OK; ++i) {
+            const size_t n = osegs[static_cast<size_t>(i)].bytes;
+            if (n > 0)
+                rc = cuda_ok(cudaMemcpyAsync(items[i].out, dout + oo, n, cudaMemcpyDeviceToHost, cs));
+            oo += n / sizeof(double);
+        }
+        tc.end();
+    }
+    // on an error, let the queued work on the buffers finish before returning
+    int rs = cuda_ok(cudaStreamSynchronize(st));
+    if (G > 1) {
+        const int r2 = cuda_ok(cudaStreamSynchronize(ctx->stream2));
+        if (rs == GSC_OK) rs = r2;
+    }
+    const int rcs = cuda_ok(cudaStreamSynchronize(cs));
+    destroy_events();
+    GSC_TRY(rc);
+    GSC_TRY(rs);
+    return rcs;
 }
 
 int gsc_selftest_batch_queue(const gsc_batch_item *items, int64_t count, int32_t form,
@@ -846,8 +939,22 @@ int gsc_last_batch_config(int32_t device, gsc_batch_config *config) {
     DeviceCtx *ctx = nullptr;
     GSC_TRY(get_ctx(device, &ctx));
     std::lock_guard<std::mutex> lk(ctx->mu);
-    if (!ctx->batch) return set_error(GSC_ERR_INVALID, "no batch has run on this device");
-    return gsc_batch_get_config(ctx->batch, config);
+    if (ctx->batch.empty() || !ctx->batch[0])
+        return set_error(GSC_ERR_INVALID, "no batch has run on this device");
+    // a call split into groups reports the first group's launch choices and
+    // the totals of all groups
+    GSC_TRY(gsc_batch_get_config(ctx->batch[0], config));
+    for (size_t i = 1; i < ctx->batch.size(); ++i) {
+        gsc_batch_config c = *config;
+        if (!ctx->batch[i]) continue;
+        GSC_TRY(gsc_batch_get_config(ctx->batch[i], &c));
+        config->units += c.units;
+        config->work += c.work;
+        config->tune_ms += c.tune_ms;
+        config->tuned = config->tuned || c.tuned;
+        config->max_splits = std::max(config->max_splits, c.max_splits);
+    }
+    return GSC_OK;
 }
 
 }  // extern "C"

@@ -419,9 +419,13 @@ void parallel_copy(void *dst, const void *src, size_t n) {
 
 int h2d_packed(cudaStream_t st, void *d, void *h, const std::vector<HostSrc> &segs) {
     constexpr size_t kChunk = size_t(64) << 20;
-    size_t total = 0;
-    for (const auto &sg : segs) total = std::max(total, sg.off + sg.bytes);
-    if (total == 0) return GSC_OK;
+    if (segs.empty()) return GSC_OK;
+    size_t total = 0, first = segs.front().off;
+    for (const auto &sg : segs) {
+        total = std::max(total, sg.off + sg.bytes);
+        first = std::min(first, sg.off);
+    }
+    if (total <= first) return GSC_OK;
     const unsigned hw = std::thread::hardware_concurrency();
     const size_t T = std::max<size_t>(1, std::min<size_t>(16, hw ? hw : 1));
     // bytes [a, b) of the packed image, from the segments they belong to
@@ -438,7 +442,7 @@ int h2d_packed(cudaStream_t st, void *d, void *h, const std::vector<HostSrc> &se
                        static_cast<const char *>(segs[k].src) + (lo - segs[k].off), hi - lo);
         }
     };
-    for (size_t c0 = 0; c0 < total; c0 += kChunk) {
+    for (size_t c0 = first; c0 < total; c0 += kChunk) {
         const size_t c1 = std::min(total, c0 + kChunk);
         const size_t n = c1 - c0;
         const size_t t_used = std::max<size_t>(1, std::min<size_t>(T, n / (size_t(1) << 20)));
@@ -1399,8 +1403,8 @@ int gsc_release_buffers(int32_t device) {
     if (ctx->sampling_pinned) GSC_CUDA(cudaFreeHost(ctx->sampling_pinned));
     ctx->sampling_pinned = nullptr;
     ctx->sampling_pinned_bytes = 0;
-    if (ctx->batch) gsc_batch_destroy(ctx->batch);
-    ctx->batch = nullptr;
+    for (gsc_batch *b : ctx->batch) gsc_batch_destroy(b);
+    ctx->batch.clear();
     ctx->batch_sig.clear();
     return GSC_OK;
 }

@@ -92,9 +92,12 @@ struct DeviceCtx {
     int *status = nullptr;           // sticky kernel status word (device)
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};   // pipelined device-to-host staging
     cudaStream_t copy_stream = nullptr;  // result copies overlapping later launches
+    cudaStream_t stream2 = nullptr;      // second compute stream of grouped batch calls
     cudaEvent_t chunk_ev = nullptr;      // "rows so far are done" on the compute stream
-    gsc_batch *batch = nullptr;      // plan of the last host-pointer batch call
-    std::vector<int64_t> batch_sig;  // its shape signature (reused when equal)
+    // plans of the last host-pointer batch call, one per group of items, and
+    // their shape signatures (a plan is reused when its signature is equal)
+    std::vector<gsc_batch *> batch;
+    std::vector<std::vector<int64_t>> batch_sig;
 };
 
 // Makes `dev` current for the guard's lifetime.

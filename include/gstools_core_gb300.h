@@ -382,15 +382,19 @@ int gsc_batch_get_config(const gsc_batch *plan, gsc_batch_config *config);
 int gsc_batch_destroy(gsc_batch *plan);
 
 /* Host-pointer ensemble: items as for gsc_batch_create but with HOST
- * pointers to dense row-major arrays.  Copies all inputs to the GPU in one
- * transfer, runs the ensemble (the plan of the previous call on the device
- * is reused when the shapes match), and copies every output back before
- * returning. */
+ * pointers to dense row-major arrays.  Packs the inputs into pinned staging
+ * and copies them to the GPU, runs the ensemble (the plans of the previous
+ * call on the device are reused when the shapes match), and copies every
+ * output back before returning.  An ensemble of at least 4e9 point*modes and
+ * 8 items runs as 4 groups of consecutive items (1/16, then 5/16 of the work
+ * each), one plan each: a group's inputs are copied while the previous group
+ * computes, and its results while the next one computes. */
 int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
                           const gsc_batch_config *config);
 
 /* Configuration of the plan used by the last gsc_summate_batch_f64 call on
- * `device` (-1 = current). */
+ * `device` (-1 = current); for a call run in groups, the first group's
+ * launch choices with the units, work and tuning time of all groups. */
 int gsc_last_batch_config(int32_t device, gsc_batch_config *config);
 
 /* ---- autotuner cache ------------------------------------------------------ */

@@ -184,3 +184,34 @@ def test_batch_mixed_both_product_forms(gsc):
                       "z2": rng.standard_normal(n), "pos": rng.uniform(0.0, span, (3, p))})
     outs = gsc.summate_batch(items, form="mixed")
     _check(items, outs, "mixed")
+
+
+def test_summate_batch_host_api_groups(gsc):
+    """An ensemble of at least 4e9 point*modes and 8 items runs as four
+    groups whose copies overlap the computing of their neighbours.  Every
+    item against the oracle on a seeded subset of its points, on two calls
+    (the second reuses the plans with new values), and the reported totals
+    cover all groups."""
+    rng = np.random.default_rng(41)
+    items = []
+    for i in range(16):
+        dim = 2 + i % 2
+        n, p = int(rng.integers(2000, 3000)), int(rng.integers(150_000, 250_000))
+        cov = rng.standard_normal((dim, n)) / np.sqrt(rng.chisquare(1, n)) / 10.0
+        items.append({"kind": "scalar", "cov": cov, "z1": rng.standard_normal(n),
+                      "z2": rng.standard_normal(n), "pos": rng.uniform(0.0, 500.0, (dim, p))})
+    work = sum(it["pos"].shape[1] * it["z1"].size for it in items)
+    assert work >= 4e9
+    for call in range(2):
+        if call:
+            for it in items:
+                it["z1"][:] = rng.standard_normal(it["z1"].size)
+        outs = gsc.summate_batch(items, form="mixed")
+        for i, (it, out) in enumerate(zip(items, outs)):
+            idx = np.sort(rng.choice(it["pos"].shape[1], 512, replace=False))
+            ref = oracle.summator(it["cov"], it["z1"], it["z2"],
+                                  np.ascontiguousarray(it["pos"][:, idx]), num_threads=NT)
+            err = rel_err(out[idx], ref)
+            assert err <= BOUND["mixed"], f"call {call} item {i}: {err:.3e}"
+    cfg = gsc.last_batch_config()
+    assert cfg["form"] == "mixed" and cfg["work"] == work
