@@ -1041,19 +1041,21 @@ def measured_peaks():
 # FP64 pipe instructions per point*mode of the plain kernel's table path
 # (phase 2d-1, reduction + polynomials + table combine 12, accumulate 1 or d)
 PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17, (3, True): 20}
-# FMA-pipe instructions per point*mode of the mixed kernel (mixed_fx.cu),
-# counted from the source: the integer phase, 3 per dimension (the low and
-# the high integer products of BI Xh and BF Xh, and BI Xl 2^-29 as one FP32
-# FMA, or a third high product on calls with some |BI| >= 2^20; IMAD issues
-# on the FMA pipe), then 9 FP32 for the remainder float, its polynomials
-# and the term; four modes' terms are added (3 additions) before a
-# 4-instruction Kahan step, 1.75 per point*mode; the incompressible field
-# weights each pair per component (2 per pair) and adds the pairs before
-# its Kahan step, 2.25 per point*mode and component; the table index,
-# shifts, the addition of the FP32 products' bits and the table load run on
-# other pipes
-MIXED_FMA_OPS = {(1, False): 13.75, (2, False): 16.75, (3, False): 19.75, (2, True): 19.5,
-                 (3, True): 24.75}
+# Instructions per point*mode of the mixed kernel (mixed_fx.cu) on the FMA
+# pipe, by kind, counted from the source for calls whose every |BI| < 2^20
+# (all workloads here): (high integer products, low integer products, FP32
+# operations).  Per dimension one high product (BF Xh), one low product
+# (BI' Xh) and one FP32 FMA (BI Xl 2^-29 in the chain); then 9 FP32 for the
+# remainder float, its polynomials and the term; four modes' terms are added
+# (3 additions) before a 4-instruction Kahan step, 1.75 per point*mode; the
+# incompressible field weights each pair per component (2 per pair) and adds
+# the pairs before its Kahan step, 2.25 per point*mode and component.  The
+# table index, shifts, the addition of the FP32 products' bits and the table
+# load run on other pipes.  The kinds issue at different rates on the FMA
+# pipe (measured live by gsc_selftest_pipe_rates: on GB300 about 30, 60 and
+# 116 per clock per SM), so each is weighted by the FP32 rate over its own.
+MIXED_OPS = {(1, False): (1, 1, 11.75), (2, False): (2, 2, 12.75), (3, False): (3, 3, 13.75),
+             (2, True): (2, 2, 15.5), (3, True): (3, 3, 18.75)}
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
@@ -1072,10 +1074,13 @@ def roofline(args, w, dom, dom_ms, launches_per_step, units=None, op_mix=None, w
     points x 2N (the real GEMM has K = 2N per output component; "products" is
     the number of split products the kernel issues: 5 for sep_f16x5, 3 for
     sep_f16x3 / sep_bf16x3), against the measured dense 16-bit peak.
-    FP64 and FP32 forms (bounds "fp64" / "fp32"): the pipe instructions the
-    kernel issues per point*mode (PLAIN_FP64_OPS / MIXED_FMA_OPS), each
-    counted as one fused multiply-add (2 FLOPs, the unit of the peak), against
-    cuBLAS DGEMM / SGEMM (TF32 off) measured on this GPU."""
+    Plain FP64 form (bound "fp64"): the FP64 pipe instructions the kernel
+    issues per point*mode (PLAIN_FP64_OPS), each counted as one fused
+    multiply-add (2 FLOPs, the unit of the peak), against cuBLAS DGEMM
+    measured on this GPU.  Mixed form (bound "fma_pipe"): its FMA-pipe
+    instructions per point*mode by kind (MIXED_OPS), each weighted by the
+    FP32 FMA rate over its kind's rate (both measured here), i.e. in FP32-FMA
+    issue slots, times 2 FLOPs, against the FP32 FMA rate itself."""
     import torch
     if units is None:
         P, N = n_points(w), w["cov"].shape[1]
@@ -1106,26 +1111,43 @@ def _roofline_entry(args, w, dom, dom_ms, per_launch_units, op_mix, torch):
                 "peak_source": how,
                 "algorithmic_tflops_single_product": achieved / products,
                 "note": f"{products} split products x 2 x points x 2N FLOPs per launch"}
-    mixed = "mixed" in dom
     if op_mix is None:
         op_mix = {(w["dim"], bool(w["incompr"])): 1.0}
-    if mixed:
-        ops = sum(f * MIXED_FMA_OPS[k] for k, f in op_mix.items())
-    else:
-        ops = sum(f * PLAIN_FP64_OPS[k] for k, f in op_mix.items())
-    achieved = 2.0 * ops * per_launch_units / (dom_ms * 1e-3) / 1e12
-    peak, how = (fp32_peak(torch) if mixed else fp64_peak(torch))
     # the algorithmic work per point*mode: 2d+3 FLOPs and one sincos (scalar),
     # 4d+2 FLOPs and one sincos (incompressible)
     alg = sum(f * ((4 * k[0] + 2) if k[1] else (2 * k[0] + 3)) for k, f in op_mix.items())
     rate = per_launch_units / (dom_ms * 1e-3)
-    return {"bound": "fp32" if mixed else "fp64", "kernel": dom, "achieved": achieved,
+    algo = {"flops_per_point_mode": alg, "tflops": alg * rate / 1e12, "sincos_per_s": rate}
+    if dom == "mixed_f64phase":
+        return {"bound": "fp32", "kernel": dom, "achieved": None, "peak": None, "unit": "TFLOP/s",
+                "frac": None, "traffic": None, "algorithmic": algo,
+                "note": "no instruction count kept for the FP64-phase variant"}
+    if "mixed" in dom:
+        hi_r, imad_r, ffma_r = pipe_rates()
+        w_hi, w_imad = ffma_r / hi_r, ffma_r / imad_r
+        kinds = [sum(f * MIXED_OPS[k][i] for k, f in op_mix.items()) for i in range(3)]
+        slots = kinds[0] * w_hi + kinds[1] * w_imad + kinds[2]
+        achieved = 2.0 * slots * rate / 1e12
+        peak = 2.0 * ffma_r / 1e12
+        return {"bound": "fma_pipe", "kernel": dom, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": "measured here: FP32 FMA issue rate of independent chains "
+                               "(gsc_selftest_pipe_rates), x 2 FLOPs",
+                "fma_slots_per_point_mode": slots,
+                "ops_per_point_mode": {"imad_hi": kinds[0], "imad": kinds[1], "fp32": kinds[2]},
+                "weights": {"imad_hi": w_hi, "imad": w_imad, "fp32": 1.0},
+                "fp32_sgemm_tflops": fp32_peak(torch)[0],
+                "algorithmic": algo,
+                "note": "FMA-pipe issue slots per point*mode (kinds counted from the kernel "
+                        "source, weighted by their measured issue rates) x 2 FLOPs"}
+    ops = sum(f * PLAIN_FP64_OPS[k] for k, f in op_mix.items())
+    achieved = 2.0 * ops * per_launch_units / (dom_ms * 1e-3) / 1e12
+    peak, how = fp64_peak(torch)
+    return {"bound": "fp64", "kernel": dom, "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "traffic": None, "peak_source": how,
-            "pipe_ops_per_point_mode": ops,
-            "algorithmic": {"flops_per_point_mode": alg, "tflops": alg * rate / 1e12,
-                            "sincos_per_s": rate},
-            "note": f"{ops:.1f} {'FMA' if mixed else 'FP64'} pipe instructions per point*mode "
+            "pipe_ops_per_point_mode": ops, "algorithmic": algo,
+            "note": f"{ops:.1f} FP64 pipe instructions per point*mode "
                     f"(from the kernel source), each counted as one FMA = 2 FLOPs"}
 
 
@@ -1166,6 +1188,18 @@ def fp32_peak(torch):
     """FP32 (CUDA-core) peak as delivered by cuBLAS SGEMM with TF32 off."""
     return (_gemm_peak(torch, torch.float32, "fp32"),
             "measured: cuBLAS SGEMM 8192^3 (TF32 off), best of 5")
+
+
+def pipe_rates():
+    """(high integer multiply-adds, low integer multiply-adds, FP32 FMAs) per
+    second on this GPU, measured once by the library's issue-rate probe."""
+    if "pipe" not in _PEAKS:
+        import ctypes
+        from gstools_core import _native
+        r = (ctypes.c_double * 3)()
+        _native.check(_native.lib.gsc_selftest_pipe_rates(-1, r))
+        _PEAKS["pipe"] = (r[0], r[1], r[2])
+    return _PEAKS["pipe"]
 
 
 # ---------------------------------------------------------------------------

@@ -41,10 +41,93 @@ __global__ void wait_timeout_probe_kernel(int *status, uint64_t limit_ns) {
     __syncthreads();
 }
 
+// Issue-rate probes of the mixed kernel's instruction kinds: every thread
+// runs kPipeChains independent chains of one kind (no chain waits on another
+// thread), so the launch's time is the pipe's throughput for that kind.
+constexpr int kPipeChains = 8, kPipeIters = 4096;
+
+__global__ void pipe_imadhi_kernel(uint32_t *out, uint32_t a, uint32_t b) {
+    uint32_t v[kPipeChains];
+#pragma unroll
+    for (int c = 0; c < kPipeChains; ++c) v[c] = threadIdx.x + c;
+    for (int i = 0; i < kPipeIters; ++i)
+#pragma unroll
+        for (int c = 0; c < kPipeChains; ++c) v[c] = __umulhi(v[c], a) + b;
+    uint32_t s = 0;
+#pragma unroll
+    for (int c = 0; c < kPipeChains; ++c) s ^= v[c];
+    out[static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void pipe_imad_kernel(uint32_t *out, uint32_t a, uint32_t b) {
+    uint32_t v[kPipeChains];
+#pragma unroll
+    for (int c = 0; c < kPipeChains; ++c) v[c] = threadIdx.x + c;
+    for (int i = 0; i < kPipeIters; ++i)
+#pragma unroll
+        for (int c = 0; c < kPipeChains; ++c) v[c] = v[c] * a + b;
+    uint32_t s = 0;
+#pragma unroll
+    for (int c = 0; c < kPipeChains; ++c) s ^= v[c];
+    out[static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void pipe_ffma_kernel(uint32_t *out, float a, float b) {
+    float v[kPipeChains];
+#pragma unroll
+    for (int c = 0; c < kPipeChains; ++c) v[c] = static_cast<float>(threadIdx.x + c);
+    for (int i = 0; i < kPipeIters; ++i)
+#pragma unroll
+        for (int c = 0; c < kPipeChains; ++c) v[c] = fmaf(v[c], a, b);
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < kPipeChains; ++c) s += v[c];
+    out[static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x] = __float_as_uint(s);
+}
+
 }  // namespace
 }  // namespace gsc
 
 using namespace gsc;
+
+extern "C" int gsc_selftest_pipe_rates(int32_t device, double *rates) {
+    if (!rates) return set_error(GSC_ERR_INVALID, "rates is NULL");
+    DeviceCtx *ctx = nullptr;
+    GSC_TRY(get_ctx(device, &ctx));
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g;
+    GSC_TRY(g.set(ctx->device));
+    cudaStream_t st = ctx->stream;
+    int sms = 0;
+    GSC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int blocks = 8 * sms, threads = 256;
+    const double ops = static_cast<double>(blocks) * threads * kPipeIters * kPipeChains;
+    uint32_t *out = nullptr;
+    GSC_CUDA(cudaMalloc(reinterpret_cast<void **>(&out), sizeof(uint32_t) * blocks * threads));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = cuda_ok(cudaEventCreate(&e0));
+    if (rc == GSC_OK) rc = cuda_ok(cudaEventCreate(&e1));
+    for (int kind = 0; kind < 3 && rc == GSC_OK; ++kind) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 3 && rc == GSC_OK; ++rep) {
+            rc = cuda_ok(cudaEventRecord(e0, st));
+            if (kind == 0) pipe_imadhi_kernel<<<blocks, threads, 0, st>>>(out, 0x9E3779B9u, 7u);
+            else if (kind == 1) pipe_imad_kernel<<<blocks, threads, 0, st>>>(out, 0x9E3779B9u, 7u);
+            else pipe_ffma_kernel<<<blocks, threads, 0, st>>>(out, 0.999f, 1e-3f);
+            if (rc == GSC_OK) rc = cuda_ok(cudaGetLastError());
+            if (rc == GSC_OK) rc = cuda_ok(cudaEventRecord(e1, st));
+            if (rc == GSC_OK) rc = cuda_ok(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            if (rc == GSC_OK) rc = cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
+            if (rc == GSC_OK && ms < best) best = ms;
+        }
+        rates[kind] = ops / (static_cast<double>(best) * 1e-3);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(out);
+    return rc;
+}
 
 extern "C" int gsc_selftest_wait_timeout(int32_t device, int64_t limit_us) {
     if (limit_us < 1000 || limit_us > 2000000)

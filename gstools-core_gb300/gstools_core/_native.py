@@ -161,6 +161,7 @@ SIGNATURES = {
     "gsc_sample_modes_f64": (ctypes.c_int, [_I32, _I32, _I64, ctypes.c_double, ctypes.c_uint64,
                                             _I64, _P, _P, _P, _OPTS]),
     "gsc_selftest_wait_timeout": (ctypes.c_int, [_I32, _I64]),
+    "gsc_selftest_pipe_rates": (ctypes.c_int, [_I32, ctypes.POINTER(ctypes.c_double)]),
     "gsc_selftest_fail_alloc": (ctypes.c_int, [_I32]),
     "gsc_selftest_detect_grid": (ctypes.c_int, [_P, _I64, _I64, _I64, _I64,
                                                 ctypes.POINTER(ctypes.c_int64)]),

@@ -427,6 +427,14 @@ int gsc_tune_set_mode(int32_t mode);
  * and the device remains usable.  No reference counterpart. */
 int gsc_selftest_wait_timeout(int32_t device, int64_t limit_us);
 
+/* Issue rates of the instruction kinds the mixed form's inner loop is made
+ * of, measured on `device` (-1 = current): rates[0] high 32-bit integer
+ * multiply-adds (__umulhi), rates[1] low 32-bit integer multiply-adds,
+ * rates[2] FP32 fused multiply-adds, each in thread operations per second
+ * over the whole GPU (best of 3 launches of independent chains).  A
+ * measurement for roofline accounting; no reference counterpart. */
+int gsc_selftest_pipe_rates(int32_t device, double *rates);
+
 /* Allocation-failure injection: the `countdown`-th next allocation of a
  * library buffer (0 = the next one; device scratch, pinned staging, batch
  * plan memory) fails as GSC_ERR_NOMEM with "injected allocation failure" in
