@@ -683,6 +683,32 @@ static bool grid_candidate(const double *pos, int64_t sd, int64_t sp, int64_t di
 // Every point of pos against the candidate axes, bit for bit, slice by
 // slice on all host cores (the check reads the whole array once; no
 // divisions in the loops, which vectorise for contiguous rows).
+// Every point of one x-slice of a C-order mesh against the candidate axes:
+// the rows read once, with no early exit inside the slice, so that the
+// compiler can vectorize the loads and compares (the check is bound by host
+// memory bandwidth).  `good` stays an integer mask: a NaN coordinate
+// compares unequal and fails the check.
+__attribute__((optimize("O3"))) static bool grid_verify_rows(
+    const double *__restrict__ p0, const double *__restrict__ p1, const double *__restrict__ p2,
+    int64_t dim, const double *a0, const double *a1, const double *a2, int64_t a, int64_t n1,
+    int64_t n2) {
+    const int64_t L0 = n1 * n2;
+    const double x0 = a0[a];
+    uint64_t bad = 0;
+    for (int64_t i = 0; i < L0; ++i) bad |= static_cast<uint64_t>(p0[i] != x0);
+    if (dim == 3) {
+        for (int64_t b = 0; b < n1; ++b) {
+            const double x1 = a1[b];
+            const double *r1 = p1 + b * n2, *r2 = p2 + b * n2;
+            for (int64_t c = 0; c < n2; ++c)
+                bad |= static_cast<uint64_t>(r1[c] != x1) | static_cast<uint64_t>(r2[c] != a2[c]);
+        }
+    } else {
+        for (int64_t b = 0; b < n1; ++b) bad |= static_cast<uint64_t>(p1[b] != a1[b]);
+    }
+    return bad == 0;
+}
+
 static bool grid_verify(const double *pos, int64_t sd, int64_t sp, int64_t dim,
                         const std::vector<double> ax[3], const int64_t n[3],
                         int64_t max_threads = 64) {
@@ -693,18 +719,24 @@ static bool grid_verify(const double *pos, int64_t sd, int64_t sp, int64_t dim,
     parallel_ranges(n[0], std::max<int64_t>(1, (int64_t(1) << 18) / L0), [&](int64_t s0, int64_t s1) {
         for (int64_t a = s0; a < s1 && ok.load(std::memory_order_relaxed); ++a) {
             const int64_t base = a * L0;
-            const double x0 = a0[a];
             bool good = true;
-            for (int64_t i = 0; i < L0; ++i) good &= at(0, base + i) == x0;
-            if (dim == 3) {
-                for (int64_t b = 0; b < n1; ++b) {
-                    const double x1 = a1[b];
-                    const int64_t off = base + b * L1;
-                    for (int64_t c = 0; c < n2; ++c)
-                        good &= (at(1, off + c) == x1) & (at(2, off + c) == a2[c]);
-                }
+            if (sp == 1) {      // C-contiguous rows: the vectorizable form
+                good = grid_verify_rows(pos + base, pos + sd + base,
+                                        dim == 3 ? pos + 2 * sd + base : nullptr, dim, a0, a1, a2,
+                                        a, n1, n2);
             } else {
-                for (int64_t b = 0; b < n1; ++b) good &= at(1, base + b) == a1[b];
+                const double x0 = a0[a];
+                for (int64_t i = 0; i < L0; ++i) good &= at(0, base + i) == x0;
+                if (dim == 3) {
+                    for (int64_t b = 0; b < n1; ++b) {
+                        const double x1 = a1[b];
+                        const int64_t off = base + b * L1;
+                        for (int64_t c = 0; c < n2; ++c)
+                            good &= (at(1, off + c) == x1) & (at(2, off + c) == a2[c]);
+                    }
+                } else {
+                    for (int64_t b = 0; b < n1; ++b) good &= at(1, base + b) == a1[b];
+                }
             }
             if (!good) ok.store(false, std::memory_order_relaxed);
         }
