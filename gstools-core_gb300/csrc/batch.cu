@@ -481,7 +481,9 @@ int autotune(gsc_batch &b, cudaStream_t st) {
         std::vector<BatchUnit> units;
         if ((rc = make_units(b, c, blocks, units)) != GSC_OK) break;
         if ((rc = prepare_items(b)) != GSC_OK) break;
-        const size_t want = std::max<size_t>(2 * static_cast<size_t>(blocks), units.size() / 32);
+        // at least 8 units per block: with fewer, the time is that of the
+        // largest sampled unit, which favours small units
+        const size_t want = std::max<size_t>(8 * static_cast<size_t>(blocks), units.size() / 32);
         const size_t step = std::max<size_t>(1, units.size() / std::max<size_t>(1, want));
         std::vector<BatchUnit> sample;
         double work = 0.0;
@@ -497,15 +499,21 @@ int autotune(gsc_batch &b, cudaStream_t st) {
         if (sample.empty() || work <= 0.0) continue;
         if ((rc = upload_units(b, sample)) != GSC_OK) break;
         const int64_t ns = static_cast<int64_t>(sample.size());
-        // one untimed pass (first launch of the instantiation), one timed
+        // one untimed pass (first launch of the instantiation), then the
+        // faster of two timed ones
         if ((rc = enqueue_sum(b, c, blocks, ns, st)) != GSC_OK) break;
-        GSC_CUDA(cudaEventRecord(e0, st));
-        if ((rc = enqueue_sum(b, c, blocks, ns, st)) != GSC_OK) break;
-        GSC_CUDA(cudaEventRecord(e1, st));
-        GSC_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        GSC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        b.tune_ms += ms;
+        float ms = 1e30f;
+        for (int t = 0; t < 2 && rc == GSC_OK; ++t) {
+            GSC_CUDA(cudaEventRecord(e0, st));
+            if ((rc = enqueue_sum(b, c, blocks, ns, st)) != GSC_OK) break;
+            GSC_CUDA(cudaEventRecord(e1, st));
+            GSC_CUDA(cudaEventSynchronize(e1));
+            float m = 0.f;
+            GSC_CUDA(cudaEventElapsedTime(&m, e0, e1));
+            b.tune_ms += m;
+            ms = std::min(ms, m);
+        }
+        if (rc != GSC_OK) break;
         const double rate = work / std::max(1e-6, static_cast<double>(ms));
         if (rate > best_rate) {
             best_rate = rate;
@@ -795,6 +803,42 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     int rc = GSC_OK;
     for (auto &e : ev)
         if (rc == GSC_OK) rc = cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // Launch choices of the groups: the caller's, else one set for the whole
+    // ensemble -- from the autotuner's cache under the ensemble's key, or
+    // tuned on the group with the most work and stored there -- so that a
+    // small group's noisy timing does not choose for the rest.  Groups
+    // created before that one run on the defaults (4 points per thread, 16
+    // units per block).
+    // (a config whose fields are zero asks the autotuner, as for one plan)
+    const bool cfg_given = config && config->points_per_thread > 0 && config->units_per_block > 0;
+    gsc_batch_config gcfg{};
+    gcfg.struct_size = sizeof(gsc_batch_config);
+    bool have_cfg = cfg_given;
+    if (cfg_given) gcfg = *config;
+    int gmax = 0;
+    std::string gkey;
+    if (G > 1 && !cfg_given) {
+        std::vector<double> gw(static_cast<size_t>(G), 0.0);
+        double pts = 0.0;
+        for (int gi = 0; gi < G; ++gi)
+            for (int64_t i = gstart[static_cast<size_t>(gi)]; i < gstart[static_cast<size_t>(gi) + 1]; ++i) {
+                gw[static_cast<size_t>(gi)] += work[static_cast<size_t>(i)];
+                pts += static_cast<double>(items[i].n_points);
+            }
+        for (int gi = 1; gi < G; ++gi)
+            if (gw[static_cast<size_t>(gi)] > gw[static_cast<size_t>(gmax)]) gmax = gi;
+        gkey = device_name(ctx->device) + "|batchg|f" + std::to_string(ro.form) + "|t" +
+               std::to_string(static_cast<int64_t>(ro.tolerance * 1e15)) + "|c" +
+               std::to_string(count) + "|w" + std::to_string(tune_bucket(total_work)) + "|p" +
+               std::to_string(tune_bucket(pts));
+        int v[4] = {0, 0, 0, 0};
+        if (tune_mode() != 0 && tune_get(gkey, v) && v[0] > 0 && v[2] > 0) {
+            gcfg.points_per_thread = v[0];
+            gcfg.tile_modes = v[1];
+            gcfg.units_per_block = v[2];
+            have_cfg = true;
+        }
+    }
     if (ctx->batch.size() != static_cast<size_t>(G)) {
         for (gsc_batch *b : ctx->batch) {
             if (rc == GSC_OK) rc = cuda_ok(cudaStreamSynchronize(st));
@@ -855,8 +899,34 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
             o.flags = ro.flags;
             o.stream = nullptr;
             o.tolerance = ro.tolerance;
-            if (rc == GSC_OK) rc = gsc_batch_create(dev.data() + i0, i1 - i0, &o, config, &plan);
+            const gsc_batch_config *pc = config;
+            gsc_batch_config dflt = gcfg;
+            if (G > 1 && !cfg_given) {
+                if (have_cfg) {
+                    pc = &gcfg;
+                } else if (gi != gmax) {
+                    dflt.points_per_thread = 4;
+                    dflt.tile_modes = 8;
+                    dflt.units_per_block = 16;
+                    pc = &dflt;
+                }                   // the largest group: the autotuner chooses
+            }
+            if (rc == GSC_OK) rc = gsc_batch_create(dev.data() + i0, i1 - i0, &o, pc, &plan);
             if (rc != GSC_OK) break;
+            if (G > 1 && !cfg_given && !have_cfg && gi == gmax) {
+                gsc_batch_config c{};
+                c.struct_size = sizeof(gsc_batch_config);
+                rc = gsc_batch_get_config(plan, &c);
+                if (rc != GSC_OK) break;
+                gcfg.points_per_thread = c.points_per_thread;
+                gcfg.tile_modes = c.tile_modes;
+                gcfg.units_per_block = c.units_per_block;
+                have_cfg = true;
+                if (tune_mode() == 2) {
+                    const int v[4] = {c.points_per_thread, c.tile_modes, c.units_per_block, 0};
+                    tune_put(gkey, v);
+                }
+            }
             ctx->batch_sig[static_cast<size_t>(gi)] = sig;
             timing_reset(ro.flags & GSC_FLAG_TIMING);
         }

@@ -388,7 +388,9 @@ int gsc_batch_destroy(gsc_batch *plan);
  * output back before returning.  An ensemble of at least 4e9 point*modes and
  * 8 items runs as 4 groups of consecutive items (1/16, then 5/16 of the work
  * each), one plan each: a group's inputs are copied while the previous group
- * computes, and its results while the next one computes. */
+ * computes, and its results while the next one computes.  Without a config
+ * (or with zero fields), the groups share one set of launch choices, tuned
+ * on the group with the most work and cached under the ensemble's shape. */
 int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
                           const gsc_batch_config *config);
 
