@@ -764,6 +764,17 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
                            double *out, bool incompr, const gsc_opts *opts,
                            const double *sf, int64_t sfs, bool interleave = false);
 
+// Whether kernels on `device` may read pageable host memory in place
+// (coherent access through the host's page tables).
+static bool pageable_access(int device) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return v != 0;
+}
+
 // ---------------------------------------------------------------------------
 // host-pointer path shared by the scalar and incompressible summators
 // ---------------------------------------------------------------------------
@@ -846,7 +857,15 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(g.set(ctx->device));
     cudaStream_t st = ctx->stream;
 
-    const size_t n_cov = static_cast<size_t>(dim * N), n_pos = static_cast<size_t>(dim * P);
+    // Large C-ordered positions stay where they are when the GPU reads
+    // pageable host memory coherently (GB300's host link with address
+    // translation, cudaDevAttrPageableMemoryAccess): the kernels read them in
+    // place, once per mode split, and no host core packs them into staging.
+    const size_t n_cov = static_cast<size_t>(dim * N);
+    const bool pos_in_place = ps_p == 1 && (dim == 1 || ps_d == P) &&
+                              static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(64) << 20) &&
+                              pageable_access(ctx->device);
+    const size_t n_pos = pos_in_place ? 0 : static_cast<size_t>(dim * P);
     const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_pos;
     const size_t n_out = static_cast<size_t>(nout * P);
     const size_t bytes = (n_in + n_out) * sizeof(double);
@@ -865,7 +884,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     stage2(segs, h, n_cov, z1, 0, z1s, 1, N);
     stage2(segs, h, n_cov + N, z2, 0, z2s, 1, N);
     if (sf) stage2(segs, h, n_cov + 2 * N, sf, 0, sfs, 1, N);
-    stage2(segs, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P);
+    if (!pos_in_place) stage2(segs, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P);
     GSC_TRY(h2d_packed(st, d, h, segs));
     tc.end();
     if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
@@ -874,7 +893,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     a.cov = d;
     a.z1 = d + n_cov;
     a.z2 = d + n_cov + N;
-    a.pos = d + n_cov + 2 * N + n_sf;
+    a.pos = pos_in_place ? pos : d + n_cov + 2 * N + n_sf;
     a.dim = dim;
     a.n_modes = N;
     a.n_points = P;

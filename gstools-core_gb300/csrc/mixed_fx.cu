@@ -506,17 +506,26 @@ int dispatch_fx(int R, int64_t dim, bool inc, dim3 grid, cudaStream_t st, const 
 }
 
 // Launch shape of one configuration: R points per thread, mode splits so that
-// about W blocks per SM exist when the points alone are few.
+// about W blocks per SM exist when the points alone are few.  W < 0 asks for
+// whole waves instead: at most -W times the blocks that fit on the GPU at
+// once (occ per SM), so that no partial wave is left (a small call whose
+// blocks fill 1.3 waves runs at the speed of two).
 struct FxShape {
     int R, W;
     int64_t bx, S, mps;
 };
-FxShape fx_shape(int R, int W, int64_t P, int64_t chunk, int sms) {
+FxShape fx_shape(int R, int W, int64_t P, int64_t chunk, int sms, int occ = 4) {
     FxShape f{R, W, 0, 1, 0};
     const int64_t pts_per_block = static_cast<int64_t>(kFxThreads) * R;
     f.bx = (P + pts_per_block - 1) / pts_per_block;
-    const int64_t want_blocks = static_cast<int64_t>(sms) * W;
-    int64_t S = std::max<int64_t>(1, (want_blocks + f.bx - 1) / f.bx);
+    int64_t S;
+    if (W < 0) {
+        const int64_t slots = static_cast<int64_t>(sms) * std::max(1, occ) * (-W);
+        S = std::max<int64_t>(1, slots / f.bx);
+    } else {
+        const int64_t want_blocks = static_cast<int64_t>(sms) * W;
+        S = std::max<int64_t>(1, (want_blocks + f.bx - 1) / f.bx);
+    }
     S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kFxTile)));
     S = std::min<int64_t>(S, 64);
     int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
@@ -526,6 +535,26 @@ FxShape fx_shape(int R, int W, int64_t P, int64_t chunk, int sms) {
     f.S = S;
     f.mps = mps;
     return f;
+}
+
+// Resident blocks per SM of the sums kernel for (dim, kind, R).
+template <int D, bool INC>
+int fx_occ_t(int R) {
+    int n = 0;
+    cudaError_t e;
+    if (R == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mixed_fx_kernel<D, INC, 2>, kFxThreads, 0);
+    else if (R == 8) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mixed_fx_kernel<D, INC, 8>, kFxThreads, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mixed_fx_kernel<D, INC, 4>, kFxThreads, 0);
+    if (e != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 4;
+    }
+    return n;
+}
+int fx_occupancy(int64_t dim, bool inc, int R) {
+    if (dim == 1) return fx_occ_t<1, false>(R);
+    if (dim == 2) return inc ? fx_occ_t<2, true>(R) : fx_occ_t<2, false>(R);
+    return inc ? fx_occ_t<3, true>(R) : fx_occ_t<3, false>(R);
 }
 
 int fx_sm_count(int device) {
@@ -649,13 +678,17 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
         tv[1] = kFxW;
         tune = mode == 2 && N <= kChunk && static_cast<double>(P) * N >= 67108864.0;
     }
-    static const int kCandR[3] = {2, 4, 8}, kCandW[3] = {4, 8, 16};
-    FxShape shp = fx_shape(tv[0], tv[1], P, chunk, sms);
+    // blocks per SM targets, and one or two whole waves (W < 0)
+    static const int kCandR[3] = {2, 4, 8}, kCandW[5] = {4, 8, 16, -1, -2};
+    auto shape_of = [&](int r, int w) {
+        return fx_shape(r, w, P, chunk, sms, w < 0 ? fx_occupancy(dim, a.incompr, r) : 4);
+    };
+    FxShape shp = shape_of(tv[0], tv[1]);
     if (shp.bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
     int64_t S_max = shp.S;
     if (tune)
         for (int r : kCandR)
-            for (int w : kCandW) S_max = std::max(S_max, fx_shape(r, w, P, chunk, sms).S);
+            for (int w : kCandW) S_max = std::max(S_max, shape_of(r, w).S);
 
     const size_t rec_bytes = static_cast<size_t>(chunk) * kFxRecBytesPerMode;
     const size_t part_bytes = S_max > 1 ? static_cast<size_t>(S_max) * nout * P * sizeof(double) : 0;
@@ -721,7 +754,7 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
         int rc = GSC_OK;
         for (int r : kCandR)
             for (int w : kCandW) {
-                const FxShape f = fx_shape(r, w, P, chunk, sms);
+                const FxShape f = shape_of(r, w);
                 if (rc == GSC_OK) rc = cuda_ok(cudaEventRecord(e0, st));
                 if (rc == GSC_OK) rc = sums(f, chunk, true, false);
                 if (rc == GSC_OK && f.S > 1)
@@ -741,7 +774,7 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
         GSC_TRY(rc);
         const int v[4] = {br, bw, 0, 0};
         tune_put(key, v);
-        shp = fx_shape(br, bw, P, chunk, sms);
+        shp = shape_of(br, bw);
         GSC_TRY(sums(shp, chunk, true, true));
         if (shp.S > 1) GSC_TRY(split_reduce(part, shp.S, nout, P, a.out, a.out_sd, a.out_sp, st));
         GSC_CUDA(cudaEventRecord(ctx.scratch_ready, st));
