@@ -857,23 +857,25 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(g.set(ctx->device));
     cudaStream_t st = ctx->stream;
 
-    // Large C-ordered positions stay where they are when the GPU reads
-    // pageable host memory coherently (GB300's host link with address
-    // translation, cudaDevAttrPageableMemoryAccess): the kernels read them in
-    // place, once per mode split, and no host core packs them into staging.
+    // C-ordered positions (256 KiB and more) stay where they are when the
+    // GPU reads pageable host memory coherently (GB300's host link with
+    // address translation, cudaDevAttrPageableMemoryAccess): the kernels read
+    // them in place, once per mode split, and no host core packs them into
+    // staging.  The modes, a few KB to MB, are still packed and copied.
     const size_t n_cov = static_cast<size_t>(dim * N);
     const bool pos_in_place = ps_p == 1 && (dim == 1 || ps_d == P) &&
-                              static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(64) << 20) &&
+                              static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(256) << 10) &&
                               pageable_access(ctx->device);
     const size_t n_pos = pos_in_place ? 0 : static_cast<size_t>(dim * P);
     const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_pos;
     const size_t n_out = static_cast<size_t>(nout * P);
     const size_t bytes = (n_in + n_out) * sizeof(double);
-    GSC_TRY(ensure_pinned(*ctx, bytes));
+    GSC_TRY(ensure_pinned(*ctx, bytes + 64));           // + the range flag's slot
     GSC_TRY(ensure_dev(*ctx, ctx->io, bytes));
 
     double *h = static_cast<double *>(ctx->pinned);
     double *d = static_cast<double *>(ctx->io.ptr);
+    volatile int *hflag = reinterpret_cast<volatile int *>(h + n_in + n_out);
     TimedLaunch tc(st);
     tc.begin(K_COPY_H2D);
     // the inputs as one packed image, moved through the pinned buffer in
@@ -909,29 +911,40 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     const bool fx = point_form(ro, a) == GSC_FORM_MIXED;
     if (fx) GSC_CUDA(cudaMemsetAsync(ctx->status + kStatusFxFlag, 0, sizeof(int), st));
     GSC_TRY(run_points(*ctx, ro, a, st, ctx->status + kStatusFxFlag));
-    if (fx) {
-        // wave numbers past the integer phase range: AUTO recomputes on the
-        // plain FP64 kernel, an explicit mixed form reports it
-        int flag = 0;
-        GSC_CUDA(cudaMemcpyAsync(&flag, ctx->status + kStatusFxFlag, sizeof(int),
-                                 cudaMemcpyDeviceToHost, st));
-        GSC_CUDA(cudaStreamSynchronize(st));
-        if (flag) {
-            if (ro.form != GSC_FORM_AUTO) return set_error(GSC_ERR_KERNEL, kFxRangeMsg);
-            Resolved rp = ro;
-            rp.form = GSC_FORM_PLAIN_F64;
-            GSC_TRY(run_points(*ctx, rp, a, st, nullptr));
-        }
-    }
+    // wave numbers past the mixed form's integer phase range: AUTO recomputes
+    // on the plain FP64 kernel, an explicit mixed form reports it.  The flag
+    // is read back with the result (one synchronisation); a flagged result
+    // is discarded.
+    *hflag = 0;
+    auto recompute = [&]() -> int {
+        if (ro.form != GSC_FORM_AUTO) return set_error(GSC_ERR_KERNEL, kFxRangeMsg);
+        Resolved rp = ro;
+        rp.form = GSC_FORM_PLAIN_F64;
+        return run_points(*ctx, rp, a, st, nullptr);
+    };
     if (c_order || f_order) {
         Prefault pf;
         if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
         pf.join();
-        tc.begin(K_COPY_D2H);
-        GSC_CUDA(cudaMemcpyAsync(out, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
-        tc.end();
-        GSC_CUDA(cudaStreamSynchronize(st));
+        for (int pass = 0; pass < 2; ++pass) {
+            if (fx && pass == 0)
+                GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), ctx->status + kStatusFxFlag,
+                                         sizeof(int), cudaMemcpyDeviceToHost, st));
+            tc.begin(K_COPY_D2H);
+            GSC_CUDA(cudaMemcpyAsync(out, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+            tc.end();
+            GSC_CUDA(cudaStreamSynchronize(st));
+            if (!*hflag) return GSC_OK;
+            *hflag = 0;
+            GSC_TRY(recompute());
+        }
         return GSC_OK;
+    }
+    if (fx) {
+        GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), ctx->status + kStatusFxFlag,
+                                 sizeof(int), cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        if (*hflag) GSC_TRY(recompute());
     }
     double *ho = h + n_in;
     tc.begin(K_COPY_D2H);

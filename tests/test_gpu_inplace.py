@@ -1,7 +1,7 @@
 """Positions read in place from host memory (GPU tests).
 
 Where the GPU reads pageable host memory coherently (cudaDevAttrPageableMemoryAccess,
-GB300's host link), host-array calls with 64 MiB or more of C-ordered
+GB300's host link), host-array calls with 256 KiB or more of C-ordered
 positions leave them where they are and the point kernels read them in
 place; other layouts go through the pinned staging.  Both routes feed the
 same kernels the same values, so their results must agree bit for bit; a
@@ -24,21 +24,22 @@ def _case(seed, n, p):
     rng = np.random.default_rng(seed)
     cov = rng.standard_normal((3, n)) / np.sqrt(rng.chisquare(1, n)) / 5.0
     z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
-    pos = rng.uniform(0.0, 1000.0, (3, p))            # 3 x 2^22 doubles: 96 MiB
+    pos = rng.uniform(0.0, 1000.0, (3, p))
     return cov, z1, z2, pos
 
 
 @pytest.mark.parametrize("form,bar", [("mixed", 1e-6), ("plain", 1e-12)])
 @pytest.mark.parametrize("kind", ["scalar", "incompr"])
-def test_positions_in_place_match_staged(gsc, form, bar, kind):
-    cov, z1, z2, pos = _case(5, 64, 1 << 22)
-    assert pos.flags.c_contiguous and pos.nbytes >= 64 << 20
+@pytest.mark.parametrize("p", [20_000, 1 << 22])          # 480 KB and 96 MiB of positions
+def test_positions_in_place_match_staged(gsc, form, bar, kind, p):
+    cov, z1, z2, pos = _case(5, 64, p)
+    assert pos.flags.c_contiguous and pos.nbytes >= 256 << 10
     staged = np.asfortranarray(pos)                   # rows not contiguous: staged
     fn = gsc.summate_incompr if kind == "incompr" else gsc.summate
     got = fn(cov, z1, z2, pos, form=form)
     ref = fn(cov, z1, z2, staged, form=form)
     assert np.array_equal(got, ref, equal_nan=True)
-    idx = np.sort(np.random.default_rng(6).choice(pos.shape[1], 4096, replace=False))
+    idx = np.sort(np.random.default_rng(6).choice(pos.shape[1], min(p, 4096), replace=False))
     sub = np.ascontiguousarray(pos[:, idx])
     if kind == "incompr":
         want = oracle.summator_incompr(cov, z1, z2, sub, num_threads=NT)

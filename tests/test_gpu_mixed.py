@@ -119,3 +119,30 @@ def test_mixed_on_structured_grid(gsc):
     pos = np.array(np.meshgrid(*axes, indexing="ij")).reshape(3, -1)
     ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
     assert rel_err(gsc.summate_structured(cov, z1, z2, axes, form="mixed"), ref) <= TOL
+
+
+@pytest.mark.parametrize("kind", ["scalar", "incompr"])
+def test_mixed_phase_range_falls_back(gsc, kind):
+    """A wave number whose phase across the domain passes 2^30 turns does
+    not fit the integer phase.  AUTO at tolerance 1e-6 (the mixed form)
+    recomputes such a call on the plain FP64 kernel, so the FP64 bar holds;
+    an explicit mixed form reports the error, and the next call computes.
+    Scalar (C-ordered result) and incompressible (Fortran-ordered result)."""
+    rng = np.random.default_rng(8)
+    n, p = 50, 3000
+    cov = rng.normal(0.0, 0.5, (3, n))
+    cov[0, 7] = 40.0                          # 40 x 2e8 / 2 pi = 1.3e9 turns > 2^30
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(0.0, 2.0e8, (3, p))
+    fn = gsc.summate_incompr if kind == "incompr" else gsc.summate
+    ofn = oracle.summator_incompr if kind == "incompr" else oracle.summator
+    ref = ofn(cov, z1, z2, pos, num_threads=NT)
+    out = fn(cov, z1, z2, pos, tolerance=1e-6)
+    err = rel_err(out, ref)
+    print(f"range fallback ({kind}): {err:.3e}")
+    assert err <= 1e-12
+    with pytest.raises(gsc.GscError, match="2\\^30 turns"):
+        fn(cov, z1, z2, pos, form="mixed")
+    ok = rel_err(fn(cov[:, :7], z1[:7], z2[:7], pos, form="mixed"),
+                 ofn(cov[:, :7], z1[:7], z2[:7], pos, num_threads=NT))
+    assert ok <= TOL
