@@ -364,7 +364,7 @@ static int structured_form(const Resolved &r, int64_t dim) {
 //   [4] sticky: a mixed call on device pointers (or a batch) met a wave
 //       number past the integer phase range (its output is invalid)
 constexpr int kStatusPipeline = 0, kStatusX5Flag = 1, kStatusX5Sticky = 2, kStatusFxFlag = 3,
-              kStatusFxSticky = 4;
+              kStatusFxSticky = 4, kStatusMeshCheck = 5;
 
 static const char *kFxRangeMsg =
     "mixed: a wave number times the largest coordinate exceeds 2^30 turns, past the range of "
@@ -680,9 +680,6 @@ static bool grid_candidate(const double *pos, int64_t sd, int64_t sp, int64_t di
     return true;
 }
 
-// Every point of pos against the candidate axes, bit for bit, slice by
-// slice on all host cores (the check reads the whole array once; no
-// divisions in the loops, which vectorise for contiguous rows).
 // Every point of one x-slice of a C-order mesh against the candidate axes:
 // the rows read once, with no early exit inside the slice, so that the
 // compiler can vectorize the loads and compares (the check is bound by host
@@ -709,15 +706,18 @@ __attribute__((optimize("O3"))) static bool grid_verify_rows(
     return bad == 0;
 }
 
+// Every point of x-slices [a_begin, n0) of pos against the candidate axes,
+// bit for bit, slice by slice on all host cores (the check reads those
+// slices once; no divisions in the loops).
 static bool grid_verify(const double *pos, int64_t sd, int64_t sp, int64_t dim,
                         const std::vector<double> ax[3], const int64_t n[3],
-                        int64_t max_threads = 64) {
+                        int64_t max_threads = 64, int64_t a_begin = 0) {
     auto at = [=](int64_t d, int64_t i) { return pos[d * sd + i * sp]; };
     std::atomic<bool> ok(true);
     const double *a0 = ax[0].data(), *a1 = ax[1].data(), *a2 = dim == 3 ? ax[2].data() : nullptr;
     const int64_t n1 = n[1], n2 = dim == 3 ? n[2] : 1, L0 = n1 * n2, L1 = n2;
-    parallel_ranges(n[0], std::max<int64_t>(1, (int64_t(1) << 18) / L0), [&](int64_t s0, int64_t s1) {
-        for (int64_t a = s0; a < s1 && ok.load(std::memory_order_relaxed); ++a) {
+    parallel_ranges(n[0] - a_begin, std::max<int64_t>(1, (int64_t(1) << 18) / L0), [&](int64_t s0, int64_t s1) {
+        for (int64_t a = a_begin + s0; a < a_begin + s1 && ok.load(std::memory_order_relaxed); ++a) {
             const int64_t base = a * L0;
             bool good = true;
             if (sp == 1) {      // C-contiguous rows: the vectorizable form
@@ -758,11 +758,65 @@ static void view_span(const double *p, int64_t s0, int64_t s1, int64_t rows, int
     hi = reinterpret_cast<uintptr_t>(p + b + 1);
 }
 
+// The device's share of the check of a flattened mesh: x-slices [0, na) of
+// C-ordered positions, and the candidate axes, read in place from host
+// memory while the separable form computes.  bad is the result.
+struct MeshCheck {
+    const double *pos;       // host, rows of P contiguous coordinates
+    int64_t sd;              // row stride (elements)
+    int64_t na;              // x-slices checked on the device
+    const double *ax[3];     // candidate axes, host
+    int64_t n[3];
+    int dim;
+    int bad = 1;             // out: 0 only when every checked point matched
+};
+
+// Any point of slices [0, na) that differs from the candidate axes (or is
+// NaN) sets *bad.  Grid-stride over the points, two per thread and pass so
+// that six host reads are in flight per thread.
+__global__ void __launch_bounds__(1024) mesh_check_kernel(const double *__restrict__ pos,
+                                                          int64_t sd, int64_t na, int64_t n1,
+                                                          int64_t n2, int dim,
+                                                          const double *__restrict__ a0,
+                                                          const double *__restrict__ a1,
+                                                          const double *__restrict__ a2, int *bad) {
+    const int64_t L0 = n1 * n2, total = na * L0;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    int miss = 0;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+         i += 2 * stride) {
+        const int64_t j = i + stride;
+        const bool two = j < total;
+        const double x0 = pos[i], y0 = pos[sd + i], w0 = dim == 3 ? pos[2 * sd + i] : 0.0;
+        const double x1 = two ? pos[j] : 0.0, y1 = two ? pos[sd + j] : 0.0,
+                     w1 = two && dim == 3 ? pos[2 * sd + j] : 0.0;
+        const int64_t a = i / L0, r = i - a * L0, b = dim == 3 ? r / n2 : r;
+        miss |= (x0 != a0[a]) | (y0 != a1[b]);
+        if (dim == 3) miss |= w0 != a2[r - b * n2];
+        if (two) {
+            const int64_t aj = j / L0, rj = j - aj * L0, bj = dim == 3 ? rj / n2 : rj;
+            miss |= (x1 != a0[aj]) | (y1 != a1[bj]);
+            if (dim == 3) miss |= w1 != a2[rj - bj * n2];
+        }
+    }
+    if (__syncthreads_or(miss) && threadIdx.x == 0) atomicOr(bad, 1);
+}
+
 static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,
                            int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
                            const double *const *ax, const int64_t *n, const int64_t *sx,
                            double *out, bool incompr, const gsc_opts *opts,
-                           const double *sf, int64_t sfs, bool interleave = false);
+                           const double *sf, int64_t sfs, bool interleave = false,
+                           MeshCheck *mc = nullptr);
+
+static int current_device() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess) {
+        cudaGetLastError();
+        d = 0;
+    }
+    return d;
+}
 
 // Whether kernels on `device` may read pageable host memory in place
 // (coherent access through the host's page tables).
@@ -829,10 +883,30 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
                 // one core stays free for this thread, which issues the GPU work
                 const unsigned hw = std::thread::hardware_concurrency();
                 const int64_t workers = std::max<int64_t>(1, static_cast<int64_t>(hw ? hw : 2) - 1);
-                std::thread check([&] { is_grid = grid_verify(pos, ps_d, ps_p, dim, axv, n, workers); });
+                // Where the GPU reads pageable host memory in place, it checks
+                // the first half of the x-slices of C-ordered rows while the
+                // host cores check the rest (both read at about 185 GB/s)
+                MeshCheck mc;
+                const bool dev_check = ps_p == 1 && n[0] >= 4 &&
+                                       static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(32) << 20) &&
+                                       pageable_access(ro.device >= 0 ? ro.device : current_device());
+                if (dev_check) {
+                    mc.pos = pos;
+                    mc.sd = ps_d;
+                    mc.na = n[0] / 2;
+                    for (int k = 0; k < 3; ++k) {
+                        mc.ax[k] = k < dim ? axv[k].data() : nullptr;
+                        mc.n[k] = n[k];
+                    }
+                    mc.dim = static_cast<int>(dim);
+                }
+                const int64_t a_host = dev_check ? mc.na : 0;
+                bool host_ok = false;
+                std::thread check([&] { host_ok = grid_verify(pos, ps_d, ps_p, dim, axv, n, workers, a_host); });
                 rc = host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx, dst,
-                                     incompr, opts, sf, sfs, f_out);
+                                     incompr, opts, sf, sfs, f_out, dev_check ? &mc : nullptr);
                 check.join();
+                is_grid = host_ok && (!dev_check || mc.bad == 0);
             } else if ((is_grid = grid_verify(pos, ps_d, ps_p, dim, axv, n))) {
                 rc = host_structured(cov, cs_d, cs_n, z1, z1s, z2, z2s, dim, N, axp, n, sx, dst,
                                      incompr, opts, sf, sfs, f_out);
@@ -1121,7 +1195,7 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
                            int64_t z1s, const double *z2, int64_t z2s, int64_t dim, int64_t N,
                            const double *const *ax, const int64_t *n, const int64_t *sx,
                            double *out, bool incompr, const gsc_opts *opts,
-                           const double *sf, int64_t sfs, bool interleave) {
+                           const double *sf, int64_t sfs, bool interleave, MeshCheck *mc) {
     // interleave: out is a Fortran-ordered (nout, P) array, i.e. (P, nout)
     // row-major; the result is rearranged on the device before its copy
     Resolved ro;
@@ -1143,6 +1217,51 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
     DeviceGuard g;
     GSC_TRY(g.set(ctx->device));
     cudaStream_t st = ctx->stream;
+    // The device's share of a flattened mesh's check runs on the second
+    // stream, launched before the tables and the GEMM: its 16 blocks hold a
+    // few SMs while they wait on host reads, and the GEMM takes the rest.
+    // (Run after the GEMM instead, the call took 2.9 against 2.5 ms on the
+    // 256^3 mesh.)  Its flag is read on every return path, with the context
+    // still locked.
+    struct CheckRead {
+        MeshCheck *mc = nullptr;
+        cudaStream_t s = nullptr;
+        int *flag = nullptr;
+        ~CheckRead() {
+            if (!mc) return;
+            int v = 1;
+            if (cudaMemcpyAsync(&v, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) {
+                cudaGetLastError();
+                v = 1;
+            }
+            mc->bad = v;
+        }
+    } check_read;
+    auto launch_check = [&]() -> int {
+        if (!mc) return GSC_OK;
+        if (mc->na <= 0) {
+            mc->bad = 0;
+            return GSC_OK;
+        }
+        if (!ctx->stream2)
+            GSC_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+        // after the work queued before this call
+        if (!ctx->chunk_ev)
+            GSC_CUDA(cudaEventCreateWithFlags(&ctx->chunk_ev, cudaEventDisableTiming));
+        GSC_CUDA(cudaEventRecord(ctx->chunk_ev, st));
+        GSC_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->chunk_ev, 0));
+        int *flag = ctx->status + kStatusMeshCheck;
+        GSC_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream2));
+        mesh_check_kernel<<<16, 1024, 0, ctx->stream2>>>(
+            mc->pos, mc->sd, mc->na, mc->n[1], mc->dim == 3 ? mc->n[2] : 1, mc->dim, mc->ax[0],
+            mc->ax[1], mc->dim == 3 ? mc->ax[2] : nullptr, flag);
+        GSC_CUDA(cudaGetLastError());
+        check_read.mc = mc;
+        check_read.s = ctx->stream2;
+        check_read.flag = flag;
+        return GSC_OK;
+    };
 
     const int64_t nout = incompr ? dim : 1;
     const size_t n_cov = static_cast<size_t>(dim * N);
@@ -1213,6 +1332,7 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         rows_copied = hi;
         return GSC_OK;
     };
+    GSC_TRY(launch_check());
     int rc = run_structured(*ctx, ro, d, d + n_cov, d + n_cov + N, dim, N, dax, n, incompr, dout,
                             st, pinned ? &on_rows : nullptr, true);
     if (copying) {

@@ -138,3 +138,33 @@ def test_incompr_any_output_strides(gsc, grid):
     assert np.isnan(buf[:, 3]).all()
     ref = oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)
     assert rel_err(buf[:, :3].T, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("where", ["clean", "device_half", "host_half", "nan_device_half"])
+def test_large_mesh_check_shared_with_the_device(gsc, where):
+    """Meshes of 32 MiB and more, where the GPU reads host memory in place:
+    the GPU checks the first half of the x-slices over the host link while
+    the host cores check the rest.  A clean mesh takes the separable form;
+    one coordinate moved by an ulp (or a NaN) in either half sends the call
+    to the point kernels.  Against the oracle on a subset that holds the
+    changed point."""
+    shape = (64, 128, 256)                                  # 2.1 M points, 50 MB
+    cov, z1, z2, axes = _case(7, shape, 64)
+    pos = _flat(axes)
+    p = 1234 + (5 if where != "host_half" else shape[0] - 3) * shape[1] * shape[2]
+    if where == "nan_device_half":
+        pos[2, p] = np.nan
+    elif where != "clean":
+        pos[1, p] = np.nextafter(pos[1, p], np.inf)
+    out = gsc.summate(cov, z1, z2, pos, timing=True)
+    ks = _kernels(gsc)
+    if where == "clean":
+        assert "sep_f64_dmma" in ks
+    else:
+        assert "sep_f64_dmma" not in ks and any(k.startswith("plain") for k in ks), ks
+    idx = np.unique(np.concatenate([np.random.default_rng(8).choice(pos.shape[1], 2048, replace=False), [p]]))
+    ref = oracle.summator(cov, z1, z2, np.ascontiguousarray(pos[:, idx]), num_threads=NT)
+    got = out[idx]
+    bad = np.isnan(ref)
+    assert np.array_equal(np.isnan(got), bad)
+    assert rel_err(got[~bad], ref[~bad]) <= 1e-12
