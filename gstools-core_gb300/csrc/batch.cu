@@ -724,11 +724,17 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     // group are copied back while the next one computes.  Groups alternate
     // between two compute streams, so that a group's persistent kernel takes
     // the SMs that the previous group's last units leave idle.
-    // The first group is small (1/16 of the work), since its copy is the one
-    // that nothing hides; the other three take 5/16 each, whose inputs copy
-    // (about 5 times faster than they compute) within the previous group.
-    const int G = (total_work >= 4.0e9 && count >= 8) ? 4 : 1;
-    static const double kGroupEnd[4] = {1.0 / 16, 6.0 / 16, 11.0 / 16, 1.0};
+    // The first group is small (1/(4G) of the work), since its copy is the
+    // one that nothing hides; the others share the rest equally, and their
+    // inputs copy (about 5 times faster than they compute) within the
+    // previous group.  More groups shorten the first copy and the last
+    // group's result copy.
+    const int G = (total_work >= 4.0e10 && count >= 16) ? 8
+                  : (total_work >= 4.0e9 && count >= 8) ? 4 : 1;
+    auto group_end = [G](int g) {          // fraction of the work in groups [0, g]
+        const double first = 1.0 / (4.0 * G);
+        return g == 0 ? first : first + (1.0 - first) * g / (G - 1);
+    };
     std::vector<int64_t> gstart(static_cast<size_t>(G) + 1, count);
     gstart[0] = 0;
     {
@@ -736,7 +742,7 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         int g = 1;
         for (int64_t i = 0; i < count && g < G; ++i) {
             acc += work[static_cast<size_t>(i)];
-            while (g < G && acc >= total_work * kGroupEnd[g - 1]) gstart[static_cast<size_t>(g++)] = i + 1;
+            while (g < G && acc >= total_work * group_end(g - 1)) gstart[static_cast<size_t>(g++)] = i + 1;
         }
         for (; g < G; ++g) gstart[static_cast<size_t>(g)] = count;
     }

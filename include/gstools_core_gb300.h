@@ -386,9 +386,10 @@ int gsc_batch_destroy(gsc_batch *plan);
  * and copies them to the GPU, runs the ensemble (the plans of the previous
  * call on the device are reused when the shapes match), and copies every
  * output back before returning.  An ensemble of at least 4e9 point*modes and
- * 8 items runs as 4 groups of consecutive items (1/16, then 5/16 of the work
- * each), one plan each: a group's inputs are copied while the previous group
- * computes, and its results while the next one computes.  Without a config
+ * 8 items runs as G = 4 groups of consecutive items (8 from 4e10 point*modes
+ * and 16 items): the first holds 1/(4G) of the work, the others share the
+ * rest equally; one plan each.  A group's inputs are copied while the
+ * previous group computes, and its results while the next one computes.  Without a config
  * (or with zero fields), the groups share one set of launch choices, tuned
  * on the group with the most work and cached under the ensemble's shape. */
 int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
