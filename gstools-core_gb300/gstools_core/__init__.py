@@ -49,7 +49,12 @@ native_version = _native.lib.gsc_version().decode()
 # ---------------------------------------------------------------------------
 # argument extraction with PyO3/numpy's error behaviour
 # ---------------------------------------------------------------------------
+_F64 = np.dtype(np.float64)
+
+
 def _array(obj, name: str, ndim: int) -> np.ndarray:
+    if type(obj) is np.ndarray and obj.ndim == ndim and obj.dtype is _F64:
+        return obj                       # the common case, checked first
     if not isinstance(obj, np.ndarray):
         raise TypeError(f"argument '{name}': '{type(obj).__name__}' object cannot be "
                         f"converted to 'PyArray<T, D>'")
@@ -568,8 +573,9 @@ def summate_batch(items, *, form="auto", tolerance=None, device=-1, timing=False
     fields: (n_points,) per scalar or Fourier item, (dim, n_points) C order
     per incompressible item."""
     keep, outs = [], []
-    arr = (_native.GscBatchItem * max(1, len(items)))()
-    for i, it in enumerate(items):
+    cols = [[] for _ in range(10)]       # the gsc_batch_item fields, by column
+    (c_dim, c_kind, c_n, c_p, c_cov, c_z1, c_z2, c_sf, c_pos, c_out) = cols
+    for it in items:
         kind = _batch_kind(it)
         cov = np.ascontiguousarray(_array(it["modes"] if kind == "fourier" and "modes" in it
                                           else it["cov"], "cov", 2))
@@ -588,14 +594,25 @@ def summate_batch(items, *, form="auto", tolerance=None, device=-1, timing=False
         out = _result((dim, p) if kind == "incompr" else p)
         keep += [cov, z1, z2, pos, sf, out]
         outs.append(out)
-        arr[i] = _native.GscBatchItem(dim, _native.BATCH_KINDS[kind], n, p, cov.ctypes.data,
-                                      z1.ctypes.data, z2.ctypes.data,
-                                      None if sf is None else sf.ctypes.data, pos.ctypes.data,
-                                      out.ctypes.data)
+        c_dim.append(dim)
+        c_kind.append(_native.BATCH_KINDS[kind])
+        c_n.append(n)
+        c_p.append(p)
+        c_cov.append(cov.ctypes.data)
+        c_z1.append(z1.ctypes.data)
+        c_z2.append(z2.ctypes.data)
+        c_sf.append(0 if sf is None else sf.ctypes.data)
+        c_pos.append(pos.ctypes.data)
+        c_out.append(out.ctypes.data)
+    arr = np.zeros(max(1, len(outs)), dtype=_native.BATCH_ITEM_DTYPE)
+    if outs:
+        for name, col in zip(_native.BATCH_ITEM_DTYPE.names, cols):
+            arr[name] = col
     o = _opts(form, tolerance, timing, device)
     cfg = _native.make_batch_config(points_per_thread, tile_modes, units_per_block)
-    _native.check(_native.lib.gsc_summate_batch_f64(arr, len(items), ctypes.byref(o),
-                                                    ctypes.byref(cfg)))
+    _native.check(_native.lib.gsc_summate_batch_f64(
+        arr.ctypes.data_as(ctypes.POINTER(_native.GscBatchItem)), len(outs), ctypes.byref(o),
+        ctypes.byref(cfg)))
     return outs
 
 

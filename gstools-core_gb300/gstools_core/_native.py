@@ -7,6 +7,8 @@ built, the import fails: there is no CPU implementation behind this package.
 from __future__ import annotations
 
 import ctypes
+
+import numpy as np
 import os
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgstools_core_gb300.so")
@@ -67,6 +69,14 @@ class GscBatchItem(ctypes.Structure):
         ("pos", ctypes.c_void_p),
         ("out", ctypes.c_void_p),
     ]
+
+
+# The same layout as a numpy structured type, so that a list of many items is
+# filled by columns instead of one ctypes structure at a time.
+BATCH_ITEM_DTYPE = np.dtype([("dim", "<i4"), ("kind", "<i4"), ("n_modes", "<i8"),
+                             ("n_points", "<i8"), ("cov", "<u8"), ("z1", "<u8"), ("z2", "<u8"),
+                             ("spectrum_factor", "<u8"), ("pos", "<u8"), ("out", "<u8")],
+                            align=True)
 
 
 class GscBatchConfig(ctypes.Structure):

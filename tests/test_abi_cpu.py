@@ -114,3 +114,13 @@ def test_struct_layouts_match_the_binding(gsc, tmp_path):
         assert c[(cname, "size")] == ctypes.sizeof(st), cname
         for field, _ in st._fields_:
             assert c[(cname, field)] == getattr(st, field).offset, (cname, field)
+
+
+def test_batch_item_numpy_layout_matches_the_struct():
+    """summate_batch fills its items through a numpy structured type; it must
+    have the C struct's size and field offsets."""
+    n = pytest.importorskip("gstools_core._native")
+    dt = n.BATCH_ITEM_DTYPE
+    assert dt.itemsize == ctypes.sizeof(n.GscBatchItem)
+    for name, _ in n.GscBatchItem._fields_:
+        assert dt.fields[name][1] == getattr(n.GscBatchItem, name).offset, name
