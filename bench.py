@@ -1064,6 +1064,9 @@ PROFILED_TRAFFIC = {
     ("sep_tc_f16x5", "c2"): (12.49e6 + 88.12e6, "profiles/sep_tc_f16x5_c2.md"),
     ("sep_tc_f16x5", "c4"): (167.4e6, "profiles/sep_tc_f16x5_c4.md"),
     ("plain_f64_scalar", "c1"): (5.8e6, "profiles/plain_f64_scalar_c1.md"),
+    ("mixed_scalar", "c1"): (1.906e6, "profiles/mixed_fx_c1.md"),
+    ("mixed_scalar", "c3"): (411.2e6 + 114.3e6, "profiles/mixed_fx_c3.md"),
+    ("batch_mixed", "c5"): (2277.3e6 + 668.4e6, "profiles/batch_fx_c5.md"),
 }
 
 
