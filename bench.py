@@ -833,7 +833,9 @@ def run_ours_batch(args, world, rank, local, cpu_seconds, form_arg="auto"):
         "error_vs_oracle": err,
         "plain_fp64": plain,
         "kernels_ms_per_step": kern,
-        "gpu_launches": int(len(kt) * args.steps),
+        # one replay: the range and table kernels (one timing record), the
+        # persistent kernel, and the split reduction when items are split
+        "gpu_launches": int((3 + (1 if cfg.get("max_splits", 1) > 1 else 0)) * args.steps),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "dropin_e2e": dropin,
         "clocks": clk.summary(),
     }
