@@ -363,6 +363,8 @@ static int structured_form(const Resolved &r, int64_t dim) {
 //   [3] the last host-pointer mixed call's range flag (cleared by the call)
 //   [4] sticky: a mixed call on device pointers (or a batch) met a wave
 //       number past the integer phase range (its output is invalid)
+//   [5] the device half of a host call's flattened-mesh check: 1 when a
+//       point differs from the candidate axes (cleared by the call)
 constexpr int kStatusPipeline = 0, kStatusX5Flag = 1, kStatusX5Sticky = 2, kStatusFxFlag = 3,
               kStatusFxSticky = 4, kStatusMeshCheck = 5;
 
