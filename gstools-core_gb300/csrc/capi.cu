@@ -365,8 +365,10 @@ static int structured_form(const Resolved &r, int64_t dim) {
 //       number past the integer phase range (its output is invalid)
 //   [5] the device half of a host call's flattened-mesh check: 1 when a
 //       point differs from the candidate axes (cleared by the call)
+//   [6] the range flag of the current device-pointer mixed call under AUTO
+//       (cleared by the call; the plain FP64 launches behind it run on it)
 constexpr int kStatusPipeline = 0, kStatusX5Flag = 1, kStatusX5Sticky = 2, kStatusFxFlag = 3,
-              kStatusFxSticky = 4, kStatusMeshCheck = 5;
+              kStatusFxSticky = 4, kStatusMeshCheck = 5, kStatusFxDev = 6;
 
 static const char *kFxRangeMsg =
     "mixed: a wave number times the largest coordinate exceeds 2^30 turns, past the range of "
@@ -376,6 +378,23 @@ static const char *kX5BoundMsg =
     "sep_f16x5: these inputs break the bound that keeps its leading sum exact (weights far "
     "from random, e.g. in phase at a grid point); the output is invalid.  Use form AUTO (which "
     "recomputes such calls on sep_f64) or sep_f64";
+
+// Point kernels on device pointers.  A mixed call under AUTO writes its
+// range flag to a word of its own, and the plain FP64 kernels are queued
+// behind it, predicated on that word: a wave number past the integer
+// phase's range is recomputed on the device, with no host synchronisation.
+// An explicit mixed form leaves its output invalid and sets the sticky word.
+static int run_points_dev(DeviceCtx &ctx, const Resolved &ro, PlainArgs &a, cudaStream_t st) {
+    if (ro.form != GSC_FORM_AUTO || point_form(ro, a) != GSC_FORM_MIXED)
+        return run_points(ctx, ro, a, st, ctx.status + kStatusFxSticky);
+    int *flag = ctx.status + kStatusFxDev;
+    GSC_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    GSC_TRY(run_points(ctx, ro, a, st, flag));
+    PlainArgs b = a;
+    b.variant = 0;
+    b.run_if = flag;
+    return plain_run(ctx, b, st);
+}
 
 // Reads and clears the sticky status words after the stream has finished.
 static int check_status(DeviceCtx &ctx, cudaStream_t st) {
@@ -1091,7 +1110,7 @@ static int dev_plain(const double *cov, const double *z1, const double *z2, cons
     a.out = out;
     a.out_sd = P;
     a.out_sp = 1;
-    return run_points(*ctx, ro, a, ro.stream, ctx->status + kStatusFxSticky);
+    return run_points_dev(*ctx, ro, a, ro.stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -1189,8 +1208,9 @@ static int run_structured(DeviceCtx &ctx, const Resolved &ro, const double *cov,
     a.out_sd = P;
     a.out_sp = 1;
     Resolved rp = ro;
-    rp.form = form;
-    return run_points(ctx, rp, a, st, ctx.status + kStatusFxSticky);
+    // AUTO that chose the mixed form stays AUTO, which keeps its FP64 fallback
+    rp.form = (ro.form == GSC_FORM_AUTO && form == GSC_FORM_MIXED) ? GSC_FORM_AUTO : form;
+    return run_points_dev(ctx, rp, a, st);
 }
 
 static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const double *z1,

@@ -221,6 +221,9 @@ struct PlainArgs {
     double *out;         // device
     int64_t out_sd, out_sp;  // element strides of out[i, p] (scalar: 0, 1)
     int variant;         // 0 table-driven sincos, 1 CUDA sincos()
+    // plain_run only: null, or a device word; every launch does nothing
+    // while the word is 0 (a fallback queued behind another form's launches)
+    const int *run_if = nullptr;
 };
 int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st);
 

@@ -109,7 +109,8 @@ __global__ void __launch_bounds__(kM)
 mode_table_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
                   const double *__restrict__ z2, int64_t dim, int64_t n_modes, int64_t j0,
                   int incompr, int want_table, double2 *__restrict__ wtab,
-                  double *__restrict__ rec) {
+                  double *__restrict__ rec, const int *__restrict__ run_if) {
+    if (run_if && *run_if == 0) return;      // a predicated launch that is not wanted
     const int64_t jl = blockIdx.x;
     const int64_t j = j0 + jl;
     mode_entry(cov, z1[j], z2[j], dim, n_modes, j, incompr, want_table, wtab + jl * kM,
@@ -296,7 +297,9 @@ template <int D, int R, bool INC, bool LIBM>
 __global__ void __launch_bounds__(kThreads)
 plain_kernel(const double *__restrict__ pos, int64_t P, const double2 *__restrict__ wtab,
              const double *__restrict__ rec, int64_t nc, int64_t mps, int accumulate,
-             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride) {
+             double *__restrict__ dst, int64_t sd, int64_t sp, int64_t split_stride,
+             const int *__restrict__ run_if) {
+    if (run_if && *run_if == 0) return;      // a predicated launch that is not wanted
     extern __shared__ __align__(16) unsigned char smem[];
     const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
     const int64_t je = min(nc, jb + mps);
@@ -360,7 +363,9 @@ batch_plain_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restr
 
 // out[i*sd + p*sp] = sum_s part[s][i][p], s ascending
 __global__ void split_reduce_kernel(const double *__restrict__ part, int64_t S, int64_t nout,
-                                    int64_t P, double *__restrict__ out, int64_t sd, int64_t sp) {
+                                    int64_t P, double *__restrict__ out, int64_t sd, int64_t sp,
+                                    const int *__restrict__ run_if) {
+    if (run_if && *run_if == 0) return;      // a predicated launch that is not wanted
     const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= nout * P) return;
     const int64_t i = t / P, p = t - i * P;
@@ -373,7 +378,8 @@ __global__ void split_reduce_kernel(const double *__restrict__ part, int64_t S, 
 __global__ void generic_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
                                const double *__restrict__ z2, const double *__restrict__ pos,
                                int64_t dim, int64_t N, int64_t P, double *__restrict__ out,
-                               int64_t sp) {
+                               int64_t sp, const int *__restrict__ run_if) {
+    if (run_if && *run_if == 0) return;      // a predicated launch that is not wanted
     const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (p >= P) return;
     double sum = 0.0;
@@ -390,11 +396,11 @@ __global__ void generic_kernel(const double *__restrict__ cov, const double *__r
 template <int D, int R, bool INC, bool LIBM>
 int launch_main(dim3 grid, size_t smem, cudaStream_t st, const double *pos, int64_t P,
                 const double2 *wtab, const double *rec, int64_t nc, int64_t mps, int accumulate,
-                double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+                double *dst, int64_t sd, int64_t sp, int64_t split_stride, const int *run_if) {
     auto fn = plain_kernel<D, R, INC, LIBM>;
     GSC_TRY(smem_attr(reinterpret_cast<const void *>(fn), smem));   // once per device
     fn<<<grid, kThreads, smem, st>>>(pos, P, wtab, rec, nc, mps, accumulate, dst, sd, sp,
-                                     split_stride);
+                                     split_stride, run_if);
     GSC_CUDA(cudaGetLastError());
     return GSC_OK;
 }
@@ -402,19 +408,20 @@ int launch_main(dim3 grid, size_t smem, cudaStream_t st, const double *pos, int6
 template <int R, bool INC, bool LIBM>
 int dispatch_dim(int64_t dim, dim3 grid, size_t smem, cudaStream_t st, const double *pos,
                  int64_t P, const double2 *wtab, const double *rec, int64_t nc, int64_t mps,
-                 int accumulate, double *dst, int64_t sd, int64_t sp, int64_t split_stride) {
+                 int accumulate, double *dst, int64_t sd, int64_t sp, int64_t split_stride,
+                 const int *run_if = nullptr) {
     switch (dim) {
         case 1:
             if (!INC)
                 return launch_main<1, R, INC, LIBM>(grid, smem, st, pos, P, wtab, rec, nc, mps,
-                                                    accumulate, dst, sd, sp, split_stride);
+                                                    accumulate, dst, sd, sp, split_stride, run_if);
             break;
         case 2:
             return launch_main<2, R, INC, LIBM>(grid, smem, st, pos, P, wtab, rec, nc, mps,
-                                                accumulate, dst, sd, sp, split_stride);
+                                                accumulate, dst, sd, sp, split_stride, run_if);
         case 3:
             return launch_main<3, R, INC, LIBM>(grid, smem, st, pos, P, wtab, rec, nc, mps,
-                                                accumulate, dst, sd, sp, split_stride);
+                                                accumulate, dst, sd, sp, split_stride, run_if);
     }
     return set_error(GSC_ERR_DIM, "unsupported dimension for the plain kernel");
 }
@@ -493,7 +500,7 @@ int split_reduce(const double *part, int64_t S, int64_t nout, int64_t P, double 
     tl.begin(K_SPLIT_REDUCE);
     const int64_t tot = nout * P;
     split_reduce_kernel<<<static_cast<unsigned>((tot + 255) / 256), 256, 0, st>>>(part, S, nout, P,
-                                                                                 out, sd, sp);
+                                                                                 out, sd, sp, nullptr);
     tl.end();
     GSC_CUDA(cudaGetLastError());
     return GSC_OK;
@@ -535,7 +542,7 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
         tl.begin(K_GENERIC);
         const int tpb = 128;
         generic_kernel<<<static_cast<unsigned>((P + tpb - 1) / tpb), tpb, 0, st>>>(
-            a.cov, a.z1, a.z2, a.pos, dim, N, P, a.out, a.out_sp);
+            a.cov, a.z1, a.z2, a.pos, dim, N, P, a.out, a.out_sp, a.run_if);
         tl.end();
         GSC_CUDA(cudaGetLastError());
         return GSC_OK;
@@ -585,7 +592,7 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
             TimedLaunch tl(st);
             tl.begin(K_MODE_TABLE);
             mode_table_kernel<<<static_cast<unsigned>(nc), kM, 0, st>>>(
-                a.cov, a.z1, a.z2, dim, N, j0, a.incompr ? 1 : 0, libm ? 0 : 1, wtab, rec);
+                a.cov, a.z1, a.z2, dim, N, j0, a.incompr ? 1 : 0, libm ? 0 : 1, wtab, rec, a.run_if);
             tl.end();
             GSC_CUDA(cudaGetLastError());
         }
@@ -600,14 +607,14 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
         int rc;
         if (a.incompr) {
             rc = libm ? dispatch_dim<R, true, true>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
-                                                    mps_c, !first, dst, sd, sp, split_stride)
+                                                    mps_c, !first, dst, sd, sp, split_stride, a.run_if)
                       : dispatch_dim<R, true, false>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
-                                                     mps_c, !first, dst, sd, sp, split_stride);
+                                                     mps_c, !first, dst, sd, sp, split_stride, a.run_if);
         } else {
             rc = libm ? dispatch_dim<R, false, true>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
-                                                     mps_c, !first, dst, sd, sp, split_stride)
+                                                     mps_c, !first, dst, sd, sp, split_stride, a.run_if)
                       : dispatch_dim<R, false, false>(dim, gl, smem, st, a.pos, P, wtab, rec, nc,
-                                                      mps_c, !first, dst, sd, sp, split_stride);
+                                                      mps_c, !first, dst, sd, sp, split_stride, a.run_if);
         }
         tl.end();
         if (rc != GSC_OK) return rc;
@@ -620,7 +627,7 @@ int plain_run(DeviceCtx &ctx, const PlainArgs &a, cudaStream_t st) {
         tl.begin(K_SPLIT_REDUCE);
         const int64_t tot = nout * P;
         split_reduce_kernel<<<static_cast<unsigned>((tot + 255) / 256), 256, 0, st>>>(
-            part, S, nout, P, a.out, a.out_sd, a.out_sp);
+            part, S, nout, P, a.out, a.out_sd, a.out_sp, a.run_if);
         tl.end();
         GSC_CUDA(cudaGetLastError());
     }
@@ -767,7 +774,7 @@ int plain_noalloc_run(int device, const PlainArgs &a, cudaStream_t st) {
     if (bx > 0x7fffffff) return set_error(GSC_ERR_INVALID, "too many points for one launch");
     if (N > 0) {
         mode_table_kernel<<<static_cast<unsigned>(N), kM, 0, st>>>(a.cov, a.z1, a.z2, a.dim, N, 0,
-                                                                      0, 1, wtab, rec);
+                                                                      0, 1, wtab, rec, nullptr);
         GSC_CUDA(cudaGetLastError());
     }
     const size_t smem = 2 * (kTileModes * kM * 16 + kTileModes * kRec * 8);

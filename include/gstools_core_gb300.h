@@ -74,13 +74,13 @@ extern "C" {
                                   (weights far from random) are flagged:
                                   see gsc_device_status                      */
 #define GSC_FORM_MIXED      6  /* any points: phase k.x mod one turn in
-                                  32-bit fixed point (three integer
-                                  multiply-adds per dimension, within 2^-30
-                                  turns), FP32 table and polynomial sincos,
-                                  FP32 sums per 32 modes with a compensated
-                                  total; below 1e-6 of the field RMS.
-                                  |k| * max|x| beyond 2^30 turns is flagged
-                                  (see gsc_device_status)                    */
+                                  32-bit fixed point (two integer products
+                                  and one exact FP32 product per dimension,
+                                  within 2^-30 turns), FP32 table and
+                                  polynomial sincos, FP32 sums per 32 modes
+                                  with a compensated total; below 1e-6 of
+                                  the field RMS.  |k| * max|x| beyond 2^30
+                                  turns is flagged (see gsc_device_status)  */
 #define GSC_FORM_MIXED_F64PHASE 7 /* as GSC_FORM_MIXED with the phase and its
                                   reduction in FP64                          */
 #define GSC_FORM_SEP_F64    8  /* structured grids: separable contraction in
@@ -133,9 +133,10 @@ const char *gsc_kernel_name(int32_t kernel_id);
  * call met inputs past the bound that keeps its leading sum exact; the
  * output of that call is invalid), and clears the status.  Host-pointer
  * calls check it themselves.  With GSC_FORM_AUTO such calls are recomputed
- * on an FP64 form: host-pointer calls after the check, device-pointer x5
- * calls by a GSC_FORM_SEP_F64 computation queued behind the x5 launch that
- * does nothing unless the device flagged the inputs. */
+ * on an FP64 form: host-pointer calls after the check; device-pointer calls
+ * by an FP64 computation queued behind the mixed or x5 launches
+ * (GSC_FORM_PLAIN_F64 or GSC_FORM_SEP_F64) that does nothing unless the
+ * device flagged the inputs, and they leave no status. */
 int gsc_device_status(int32_t device);
 
 /* Frees the scratch memory the library keeps on `device` (-1 = current)

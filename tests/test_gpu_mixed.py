@@ -146,3 +146,44 @@ def test_mixed_phase_range_falls_back(gsc, kind):
     ok = rel_err(fn(cov[:, :7], z1[:7], z2[:7], pos, form="mixed"),
                  ofn(cov[:, :7], z1[:7], z2[:7], pos, num_threads=NT))
     assert ok <= TOL
+
+
+@pytest.mark.parametrize("kind", ["scalar", "incompr"])
+def test_device_auto_falls_back_on_the_device(gsc, kind):
+    """Device arrays under AUTO at tolerance 1e-6: the mixed form, with the
+    plain FP64 kernels queued behind it and predicated on its range word.
+    In range, the predicated launches leave the mixed result as it is (bit
+    for bit the explicit mixed form's); past the range (2^30 turns), they
+    recompute it at the FP64 bar and no status is left; an explicit mixed
+    form past the range leaves the sticky status."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(12)
+    n, p = 64, 5000
+    cov = rng.normal(0.0, 0.5, (3, n))
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(0.0, 100.0, (3, p))
+    fn = gsc.summate_incompr_device if kind == "incompr" else gsc.summate_device
+    ofn = oracle.summator_incompr if kind == "incompr" else oracle.summator
+    shape = (3, p) if kind == "incompr" else (p,)
+
+    def run(c, ps, **kw):
+        dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (c, z1, z2, ps)]
+        out = torch.full(shape, float("nan"), dtype=torch.float64, device="cuda")
+        fn(*dev, out, **kw)
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
+
+    auto = run(cov, pos, tolerance=1e-6)
+    mixed = run(cov, pos, form="mixed")
+    assert np.array_equal(auto, mixed)
+    assert rel_err(auto, ofn(cov, z1, z2, pos, num_threads=NT)) <= TOL
+    gsc.device_status()                                  # nothing reported
+    far = pos * 2.0e6                                    # [0, 2e8]
+    big = cov.copy()
+    big[0, 3] = 40.0                                     # 40 x 2e8 / 2 pi > 2^30 turns
+    got = run(big, far, tolerance=1e-6)
+    gsc.device_status()                                  # handled on the device
+    assert rel_err(got, ofn(big, z1, z2, far, num_threads=NT)) <= 1e-12
+    run(big, far, form="mixed")
+    with pytest.raises(gsc.GscError):
+        gsc.device_status()
