@@ -693,10 +693,12 @@ int gsc_batch_destroy(gsc_batch *b) {
     return GSC_OK;
 }
 
-int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
-                          const gsc_batch_config *config) {
-    Resolved ro;
-    GSC_TRY(resolve_opts(opts, &ro));
+// The host-array ensemble call under the device context's lock.  *range_hit
+// is set when a mixed-form item met a wave number past its integer phase
+// range (its output is then invalid).
+static int summate_batch_host(const gsc_batch_item *items, int64_t count, const Resolved &ro,
+                              const gsc_batch_config *config, bool *range_hit) {
+    *range_hit = false;
     if (count < 0 || (count > 0 && !items)) return set_error(GSC_ERR_INVALID, "bad item list");
     // host-side validation (the plan re-checks shapes and forms)
     size_t n_in = 0, n_out = 0;
@@ -853,6 +855,9 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
         ctx->batch.assign(static_cast<size_t>(G), nullptr);
         ctx->batch_sig.assign(static_cast<size_t>(G), {});
     }
+    // the range word of this call's plans (device calls keep the sticky word)
+    int *range_word = ctx->status + 7;
+    if (rc == GSC_OK) rc = cuda_ok(cudaMemsetAsync(range_word, 0, sizeof(int), st));
     // the second compute stream starts after the work queued before this call
     if (rc == GSC_OK && G > 1) {
         cudaEvent_t e0 = ev[static_cast<size_t>(2 * G - 1)];
@@ -933,6 +938,7 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
                     tune_put(gkey, v);
                 }
             }
+            plan->range_flag = range_word;
             ctx->batch_sig[static_cast<size_t>(gi)] = sig;
             timing_reset(ro.flags & GSC_FLAG_TIMING);
         }
@@ -966,7 +972,31 @@ int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_
     destroy_events();
     GSC_TRY(rc);
     GSC_TRY(rs);
-    return rcs;
+    GSC_TRY(rcs);
+    int hit = 0;
+    GSC_CUDA(cudaMemcpy(&hit, range_word, sizeof(int), cudaMemcpyDeviceToHost));
+    *range_hit = hit != 0;
+    return GSC_OK;
+}
+
+int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
+                          const gsc_batch_config *config) {
+    Resolved ro;
+    GSC_TRY(resolve_opts(opts, &ro));
+    bool range_hit = false;
+    GSC_TRY(summate_batch_host(items, count, ro, config, &range_hit));
+    if (!range_hit) return GSC_OK;
+    // a wave number past the mixed form's integer phase range: AUTO recomputes
+    // the ensemble on the plain FP64 form, an explicit mixed form reports it
+    if (ro.form != GSC_FORM_AUTO)
+        return set_error(GSC_ERR_KERNEL,
+                         "mixed: a wave number times the largest coordinate of its item exceeds "
+                         "2^30 turns, past the range of its integer phase; the outputs are "
+                         "invalid.  Use form AUTO (which recomputes such ensembles on the plain "
+                         "FP64 form) or plain");
+    Resolved rp = ro;
+    rp.form = GSC_FORM_PLAIN_F64;
+    return summate_batch_host(items, count, rp, nullptr, &range_hit);
 }
 
 int gsc_selftest_batch_queue(const gsc_batch_item *items, int64_t count, int32_t form,

@@ -367,6 +367,8 @@ static int structured_form(const Resolved &r, int64_t dim) {
 //       point differs from the candidate axes (cleared by the call)
 //   [6] the range flag of the current device-pointer mixed call under AUTO
 //       (cleared by the call; the plain FP64 launches behind it run on it)
+//   [7] the range flag of the current host-array batch call (batch.cu;
+//       cleared by the call)
 constexpr int kStatusPipeline = 0, kStatusX5Flag = 1, kStatusX5Sticky = 2, kStatusFxFlag = 3,
               kStatusFxSticky = 4, kStatusMeshCheck = 5, kStatusFxDev = 6;
 

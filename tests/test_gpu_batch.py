@@ -215,3 +215,28 @@ def test_summate_batch_host_api_groups(gsc):
             assert err <= BOUND["mixed"], f"call {call} item {i}: {err:.3e}"
     cfg = gsc.last_batch_config()
     assert cfg["form"] == "mixed" and cfg["work"] == work
+
+
+def test_summate_batch_phase_range(gsc):
+    """An item whose wave number times extent passes 2^30 turns does not fit
+    the mixed form's integer phase.  The host-array call under AUTO at
+    tolerance 1e-6 recomputes the ensemble on the plain FP64 form (the FP64
+    bar holds for every item); an explicit mixed form reports it; neither
+    leaves a device status behind."""
+    rng = np.random.default_rng(44)
+    items = []
+    for k in range(3):
+        n, p = 40, 2000
+        cov = rng.normal(0.0, 0.5, (3, n))
+        span = 100.0
+        if k == 1:
+            cov[0, 5] = 40.0
+            span = 2.0e8                     # 40 x 2e8 / 2 pi > 2^30 turns
+        items.append({"kind": "scalar", "cov": cov, "z1": rng.standard_normal(n),
+                      "z2": rng.standard_normal(n), "pos": rng.uniform(0.0, span, (3, p))})
+    cfg = dict(points_per_thread=4, tile_modes=8, units_per_block=16)
+    outs = gsc.summate_batch(items, tolerance=1e-6, **cfg)
+    _check(items, outs, "plain")
+    with pytest.raises(gsc.GscError, match="2\\^30 turns"):
+        gsc.summate_batch(items, form="mixed", **cfg)
+    gsc.device_status()
