@@ -390,9 +390,13 @@ int gsc_batch_destroy(gsc_batch *plan);
  * 8 items runs as G = 4 groups of consecutive items (8 from 4e10 point*modes
  * and 16 items): the first holds 1/(4G) of the work, the others share the
  * rest equally; one plan each.  A group's inputs are copied while the
- * previous group computes, and its results while the next one computes.  Without a config
- * (or with zero fields), the groups share one set of launch choices, tuned
- * on the group with the most work and cached under the ensemble's shape. */
+ * previous group computes, and its results while the next one computes.
+ * Without a config (or with zero fields), the groups share one set of
+ * launch choices, tuned on the group with the most work and cached under the
+ * ensemble's shape.  A mixed-form item whose wave number times extent passes
+ * 2^30 turns makes the call recompute the ensemble on GSC_FORM_PLAIN_F64
+ * under GSC_FORM_AUTO and return GSC_ERR_KERNEL under an explicit
+ * GSC_FORM_MIXED. */
 int gsc_summate_batch_f64(const gsc_batch_item *items, int64_t count, const gsc_opts *opts,
                           const gsc_batch_config *config);
 
