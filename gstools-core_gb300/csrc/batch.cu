@@ -151,9 +151,14 @@ int dmalloc(void **p, size_t bytes) {
 
 bool is_plain(const gsc_batch &b) { return b.form == GSC_FORM_PLAIN_F64; }
 bool is_fx(const gsc_batch &b) { return b.form == GSC_FORM_MIXED; }
+bool scalar_only(const gsc_batch &b) {
+    for (const auto &it : b.items)
+        if (it.incompr) return false;
+    return true;
+}
 
 int occupancy(const gsc_batch &b, const Cfg &c) {
-    if (is_fx(b)) return batch_fx_occupancy(c.R);
+    if (is_fx(b)) return batch_fx_occupancy(c.R, scalar_only(b));
     return is_plain(b) ? batch_plain_occupancy(c.R, c.tile, b.device)
                        : batch_mixed_occupancy(c.R, true, b.device);
 }
@@ -410,8 +415,9 @@ int enqueue_sum(gsc_batch &b, const Cfg &c, int blocks, int64_t n_units, cudaStr
     GSC_CUDA(cudaMemsetAsync(b.d_counter, 0, sizeof(int), st));
     if (n_units == 0) return GSC_OK;
     if (is_fx(b))
-        return batch_fx_launch(c.R, blocks, b.d_items, b.d_units, n_units, b.d_counter,
-                               reinterpret_cast<const uint32_t *>(b.d_frec), b.d_fxrange, st);
+        return batch_fx_launch(c.R, scalar_only(b), blocks, b.d_items, b.d_units, n_units,
+                               b.d_counter, reinterpret_cast<const uint32_t *>(b.d_frec),
+                               b.d_fxrange, st);
     if (is_plain(b))
         return batch_plain_launch(c.R, c.tile, blocks, b.d_items, b.d_units, n_units, b.d_counter,
                                   b.d_tab, b.d_rec, st);
@@ -456,7 +462,10 @@ std::vector<Cfg> candidates(const gsc_batch &b) {
         for (auto &x : rt)
             for (int u : upbs) out.push_back(Cfg{x[0], x[1], u});
     } else {
-        const int rs[3] = {2, 4, 8};
+        // 8 points per thread is left out: its samples timed faster than 4 on
+        // parts of C5, but whole runs with it were slower (220 against 215 ms
+        // end to end)
+        const int rs[2] = {2, 4};
         for (int r : rs)
             for (int u : upbs) out.push_back(Cfg{r, 32, u});
     }
@@ -464,8 +473,8 @@ std::vector<Cfg> candidates(const gsc_batch &b) {
 }
 
 // Times every candidate on an evenly spaced sample of its own cost-sorted
-// queue (about 3% of the work, at least two units per resident block) and
-// keeps the fastest per point*mode.
+// queue (at least 8 units per resident block and 1/32 of the queue, the
+// faster of two timed passes) and keeps the fastest per point*mode.
 int autotune(gsc_batch &b, cudaStream_t st) {
     cudaEvent_t e0, e1;
     GSC_CUDA(cudaEventCreate(&e0));

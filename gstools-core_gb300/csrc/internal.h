@@ -325,8 +325,10 @@ int batch_fx_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t 
                     int64_t total_modes, uint32_t *rec, unsigned long long *maxbits,
                     int *range_flag, cudaStream_t st);
 bool batch_fx_config_ok(int R);
-int batch_fx_occupancy(int R);
-int batch_fx_launch(int R, int blocks, const BatchItem *items, const BatchUnit *units,
+// scalar: the ensemble has no incompressible item (a kernel without those
+// variants)
+int batch_fx_occupancy(int R, bool scalar);
+int batch_fx_launch(int R, bool scalar, int blocks, const BatchItem *items, const BatchUnit *units,
                     int64_t n_units, int *counter, const uint32_t *rec,
                     const unsigned long long *maxbits, cudaStream_t st);
 

@@ -599,9 +599,11 @@ __global__ void batch_fx_table_kernel(const BatchItem *__restrict__ items,
                   rec + g * kFxRecWords, range_flag);
 }
 
-// Persistent batch kernel (see batch_plain_kernel in plain.cu).
-template <int R>
-__global__ void __launch_bounds__(kFxThreads, R >= 8 ? 2 : 4)
+// Persistent batch kernel (see batch_plain_kernel in plain.cu).  SCALAR:
+// an ensemble without incompressible items, whose kernel carries only the
+// scalar variants (fewer registers, so R = 8 keeps 3 blocks per SM).
+template <int R, bool SCALAR>
+__global__ void __launch_bounds__(kFxThreads, R >= 8 ? (SCALAR ? 3 : 2) : 4)
 batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict__ units,
                 int64_t n_units, int *__restrict__ counter, const uint32_t *__restrict__ rec,
                 const unsigned long long *__restrict__ maxbits) {
@@ -628,13 +630,15 @@ batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict
                 fx_block<2, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
                 break;
             case 5:
-                fx_block<2, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                if constexpr (!SCALAR)
+                    fx_block<2, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
                 break;
             case 6:
                 fx_block<3, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
                 break;
             case 7:
-                fx_block<3, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                if constexpr (!SCALAR)
+                    fx_block<3, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
                 break;
             default:
                 break;
@@ -644,10 +648,10 @@ batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict
 
 using BatchFxFn = void (*)(const BatchItem *, const BatchUnit *, int64_t, int *, const uint32_t *,
                            const unsigned long long *);
-BatchFxFn batch_fx_fn(int R) {
-    if (R == 2) return batch_fx_kernel<2>;
-    if (R == 4) return batch_fx_kernel<4>;
-    if (R == 8) return batch_fx_kernel<8>;
+BatchFxFn batch_fx_fn(int R, bool scalar) {
+    if (R == 2) return scalar ? batch_fx_kernel<2, true> : batch_fx_kernel<2, false>;
+    if (R == 4) return scalar ? batch_fx_kernel<4, true> : batch_fx_kernel<4, false>;
+    if (R == 8) return scalar ? batch_fx_kernel<8, true> : batch_fx_kernel<8, false>;
     return nullptr;
 }
 
@@ -814,10 +818,10 @@ int batch_fx_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t 
     return GSC_OK;
 }
 
-bool batch_fx_config_ok(int R) { return batch_fx_fn(R) != nullptr; }
+bool batch_fx_config_ok(int R) { return batch_fx_fn(R, false) != nullptr; }
 
-int batch_fx_occupancy(int R) {
-    BatchFxFn fn = batch_fx_fn(R);
+int batch_fx_occupancy(int R, bool scalar) {
+    BatchFxFn fn = batch_fx_fn(R, scalar);
     if (!fn) return 0;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kFxThreads, 0) != cudaSuccess) {
@@ -827,10 +831,10 @@ int batch_fx_occupancy(int R) {
     return n;
 }
 
-int batch_fx_launch(int R, int blocks, const BatchItem *items, const BatchUnit *units,
-                    int64_t n_units, int *counter, const uint32_t *rec,
+int batch_fx_launch(int R, bool scalar, int blocks, const BatchItem *items,
+                    const BatchUnit *units, int64_t n_units, int *counter, const uint32_t *rec,
                     const unsigned long long *maxbits, cudaStream_t st) {
-    BatchFxFn fn = batch_fx_fn(R);
+    BatchFxFn fn = batch_fx_fn(R, scalar);
     if (!fn) return set_error(GSC_ERR_INVALID, "unsupported batch configuration");
     TimedLaunch tl(st);
     tl.begin(K_BATCH_MIXED);
