@@ -29,7 +29,7 @@ benchmark data):
 One step = one full summation of the workload.  `value` is timed with CUDA
 events on the launch stream, inputs resident in HBM, L2 flushed (a 256 MiB
 write) before every timed step; `e2e` is the same metric through the public
-host API at the benchmark spec's tolerance 1e-6 (numpy in, numpy out, host<->device
+host API at tolerance 1e-6 (numpy in, numpy out, host<->device
 copies inside the timed call).  Every workload's output is compared, value
 by value, with an FP64 form on the GPU that is itself checked against the
 oracle in the same run (error_vs_fp64_full), and a seeded subset with the
@@ -449,7 +449,7 @@ def run_ours(args, world, rank, local, wname, cpu_seconds, form_arg="auto"):
                     "reference": "oracle (field.rs restatement), FP64"}
         err = check(out_d)
 
-    # ---- e2e through the public host API at the benchmark spec's tolerance (before
+    # ---- e2e through the public host API at tolerance 1e-6 (before
     # the long comparison arms, so that it runs in the same state of the GPU
     # as the timed steps).  The call GSTools makes -- summate(cov_samples, z1,
     # z2, pos) with pos the flattened meshgrid on structured grids -- plus

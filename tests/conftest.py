@@ -66,7 +66,7 @@ def rms(a):
 
 
 def rel_err(got, ref):
-    """max |got - ref| / RMS(ref) (the spec error measure)."""
+    """max |got - ref| / RMS(ref) (the error measure of every parity bar)."""
     got = np.asarray(got, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)
     if ref.size == 0:

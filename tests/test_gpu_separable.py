@@ -4,7 +4,7 @@ The oracle evaluates the reference's summator (src/field.rs:37-65,
 src/field.rs:97-182) on pos = meshgrid(*axes, indexing="ij") flattened, the
 points GSTools passes for a structured mesh.  Bars (max |err| / field RMS):
   plain FP64 on the expanded grid              1e-12
-  sep_f16x5 (tcgen05, exact leading product)   1e-6   (the spec bar)
+  sep_f16x5 (tcgen05, exact leading product)   1e-6   (the bar of the reduced-precision forms)
   sep_f16x3 (tcgen05, f16 hi/lo)               1e-5
   sep_bf16x3 (tcgen05, bf16 hi/lo)             1e-4
 """
