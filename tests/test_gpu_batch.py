@@ -240,3 +240,37 @@ def test_summate_batch_phase_range(gsc):
     with pytest.raises(gsc.GscError, match="2\\^30 turns"):
         gsc.summate_batch(items, form="mixed", **cfg)
     gsc.device_status()
+
+
+def test_summate_batch_eight_groups_with_empty_items(gsc):
+    """From 4e10 point*modes and 16 items the host-array call runs in eight
+    groups (the first 1/32 of the work).  Items without points or without
+    modes among them; every item against the oracle on a seeded subset."""
+    rng = np.random.default_rng(45)
+    items = []
+    for i in range(20):
+        dim = 2 + i % 2
+        n, p = 4000 + 7 * i, 600_000 + 1000 * i
+        if i == 3:
+            p = 0
+        if i == 11:
+            n = 0
+        cov = rng.standard_normal((dim, n)) / np.sqrt(rng.chisquare(1, n)) / 10.0
+        items.append({"kind": "scalar", "cov": cov, "z1": rng.standard_normal(n),
+                      "z2": rng.standard_normal(n), "pos": rng.uniform(0.0, 500.0, (dim, p))})
+    work = sum(it["pos"].shape[1] * it["z1"].size for it in items)
+    assert work >= 4e10
+    outs = gsc.summate_batch(items, form="mixed")
+    for i, (it, out) in enumerate(zip(items, outs)):
+        p = it["pos"].shape[1]
+        assert out.shape == (p,)
+        if p == 0:
+            continue
+        if it["z1"].size == 0:
+            assert np.all(out == 0.0)
+            continue
+        idx = np.sort(rng.choice(p, 256, replace=False))
+        ref = oracle.summator(it["cov"], it["z1"], it["z2"],
+                              np.ascontiguousarray(it["pos"][:, idx]), num_threads=NT)
+        err = rel_err(out[idx], ref)
+        assert err <= BOUND["mixed"], f"item {i}: {err:.3e}"
