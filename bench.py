@@ -1048,16 +1048,16 @@ PLAIN_FP64_OPS = {(1, False): 14, (2, False): 16, (3, False): 18, (2, True): 17,
 # (all workloads here): (high integer products, low integer products, FP32
 # operations).  Per dimension one high product (BF Xh), one low product
 # (BI' Xh) and one FP32 FMA (BI Xl 2^-29 in the chain); then 9 FP32 for the
-# remainder float, its polynomials and the term; four modes' terms are added
-# (3 additions) before a 4-instruction Kahan step, 1.75 per point*mode; the
+# remainder float, its polynomials and the term; eight modes' terms are added
+# (7 additions) before a 4-instruction Kahan step, 1.375 per point*mode; the
 # incompressible field weights each pair per component (2 per pair) and adds
-# the pairs before its Kahan step, 2.25 per point*mode and component.  The
+# the pairs before its Kahan step, 1.875 per point*mode and component.  The
 # table index, shifts, the addition of the FP32 products' bits and the table
 # load run on other pipes.  The kinds issue at different rates on the FMA
 # pipe (measured live by gsc_selftest_pipe_rates: on GB300 about 30, 60 and
 # 116 per clock per SM), so each is weighted by the FP32 rate over its own.
-MIXED_OPS = {(1, False): (1, 1, 11.75), (2, False): (2, 2, 12.75), (3, False): (3, 3, 13.75),
-             (2, True): (2, 2, 15.5), (3, True): (3, 3, 18.75)}
+MIXED_OPS = {(1, False): (1, 1, 11.375), (2, False): (2, 2, 12.375), (3, False): (3, 3, 13.375),
+             (2, True): (2, 2, 14.75), (3, True): (3, 3, 17.625)}
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu

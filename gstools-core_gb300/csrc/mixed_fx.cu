@@ -367,14 +367,15 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
-        // modes in groups of four: two pair sums per point, added, then one
+        // modes in groups of eight: four pair sums per point, added, then one
         // Kahan step; a tile shorter than kFxTile (the last) goes in pairs,
         // the second mode of an odd tile's last pair counting zero times
+        constexpr int kGroupPairs = 4;
         const int tq = tm == kFxTile ? kFxTile : 0;
-        for (int m = 0; m < tq; m += 4) {
+        for (int m = 0; m < tq; m += 2 * kGroupPairs) {
             float pend[R][NOUT];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
+            for (int h = 0; h < kGroupPairs; ++h) {
                 const FxModeWords ma = fx_mode_words<INC>(srec, sbase, m + 2 * h, 1.0f);
                 const FxModeWords mb = fx_mode_words<INC>(srec, sbase, m + 2 * h + 1, 1.0f);
 #pragma unroll
@@ -388,6 +389,8 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
                         const float ps = INC ? fmaf(ma.w[i], ta, mb.w[i] * tb) : ta + tb;
                         if (h == 0)
                             pend[r][i] = ps;
+                        else if (h < kGroupPairs - 1)
+                            pend[r][i] += ps;
                         else
                             fx_kahan(acc[r][i], cmp[r][i], pend[r][i] + ps);
                     }

@@ -19,7 +19,7 @@ exact rational phase of the FP64 inputs (Python integers): within 4 units
 (2^-30 turns) in 1-3 dimensions, heavy-tailed wave numbers and coordinates of
 either sign.  Then the table and polynomial evaluation of the term (the remainder read
 from the phase word's bits as the mantissa of a float in [1, 2)), the sums of
-four modes' terms, and a whole field against the oracle at the form's 1e-6
+eight modes' terms, and a whole field against the oracle at the form's 1e-6
 bar, in FP32 as the kernel computes it.
 """
 from fractions import Fraction
@@ -182,7 +182,7 @@ def test_remainder_float_and_polynomials():
 
 def fx_field(cov, z1, z2, pos):
     """The kernel's arithmetic for a scalar field, FP32 where the kernel
-    uses FP32 (table, polynomial, sums of four modes, Kahan tile sums,
+    uses FP32 (table, polynomial, sums of eight modes, Kahan tile sums,
     double-float total)."""
     dim, n = cov.shape
     P = pos.shape[1]
@@ -221,9 +221,12 @@ def fx_field(cov, z1, z2, pos):
                     t = (t + ((bf * pw[d][0]) >> 32)) & U32
                     t = (t + bi * pw[d][0]) & U32
                 terms.append(fx_term(t, tabs[j]))
-            if len(terms) == 32:          # a full tile: groups of four modes
-                groups = [f32(f32(terms[q] + terms[q + 1]) + f32(terms[q + 2] + terms[q + 3]))
-                          for q in range(0, 32, 4)]
+            if len(terms) == 32:          # a full tile: groups of eight modes
+                groups = []
+                for q in range(0, 32, 8):
+                    pairs = [f32(terms[q + 2 * k] + terms[q + 2 * k + 1]) for k in range(4)]
+                    pend = f32(f32(pairs[0] + pairs[1]) + pairs[2])
+                    groups.append(f32(pend + pairs[3]))
             else:                         # the last, shorter tile: pairs
                 groups = [terms[q] if q + 1 == len(terms) else f32(terms[q] + terms[q + 1])
                           for q in range(0, len(terms), 2)]
