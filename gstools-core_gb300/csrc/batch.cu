@@ -151,6 +151,8 @@ int dmalloc(void **p, size_t bytes) {
 
 bool is_plain(const gsc_batch &b) { return b.form == GSC_FORM_PLAIN_F64; }
 bool is_fx(const gsc_batch &b) { return b.form == GSC_FORM_MIXED; }
+// modes per staged tile of the point-mixed kernels: mixed_fx.cu 64, mixed.cu 32
+int mixed_tile(const gsc_batch &b) { return is_fx(b) ? 64 : 32; }
 bool scalar_only(const gsc_batch &b) {
     for (const auto &it : b.items)
         if (it.incompr) return false;
@@ -224,7 +226,7 @@ int fill_items(gsc_batch &b, const gsc_batch_item *items, int64_t count, bool ch
 // counts they imply.  Fills b.items[*].splits.
 int make_units(gsc_batch &b, const Cfg &c, int blocks, std::vector<BatchUnit> &units) {
     const int64_t ppb = static_cast<int64_t>(kBatchThreads) * c.R;
-    const int tile = is_plain(b) ? c.tile : 32;
+    const int tile = is_plain(b) ? c.tile : mixed_tile(b);
     const double target = std::max(1.0, b.total_work / (static_cast<double>(blocks) * c.upb));
     units.clear();
     std::vector<double> cost;
@@ -604,7 +606,7 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
                        (!is_plain(*b) || config->tile_modes > 0);
     if (given) {
         c.R = config->points_per_thread;
-        c.tile = is_plain(*b) ? config->tile_modes : 32;
+        c.tile = is_plain(*b) ? config->tile_modes : mixed_tile(*b);
         c.upb = config->units_per_block;
         const bool ok = is_plain(*b) ? batch_plain_config_ok(c.R, c.tile)
                          : is_fx(*b) ? batch_fx_config_ok(c.R) : batch_mixed_config_ok(c.R);
@@ -642,7 +644,7 @@ int gsc_batch_create(const gsc_batch_item *items, int64_t count, const gsc_opts 
             const int nv[4] = {c.R, c.tile, c.upb, 0};
             tune_put(key, nv);
         }
-        if (!is_plain(*b)) c.tile = 32;          // the mixed forms stage 32 modes
+        if (!is_plain(*b)) c.tile = mixed_tile(*b);   // the mixed forms' staged tiles
     }
     GSC_TRY(apply_config(*b, c));
     GSC_CUDA(cudaStreamSynchronize(b->cap_stream));
@@ -685,7 +687,7 @@ int gsc_batch_get_config(const gsc_batch *b, gsc_batch_config *cfg) {
     if (cfg->struct_size < static_cast<int32_t>(sizeof(gsc_batch_config)))
         return set_error(GSC_ERR_INVALID, "gsc_batch_config.struct_size is too small");
     cfg->points_per_thread = b->cfg.R;
-    cfg->tile_modes = is_plain(*b) ? b->cfg.tile : 32;
+    cfg->tile_modes = is_plain(*b) ? b->cfg.tile : mixed_tile(*b);
     cfg->units_per_block = b->cfg.upb;
     cfg->form = b->form;
     cfg->blocks = b->blocks;
@@ -1023,7 +1025,7 @@ int gsc_selftest_batch_queue(const gsc_batch_item *items, int64_t count, int32_t
     GSC_TRY(fill_items(b, items, count, false));
     Cfg c;
     c.R = config->points_per_thread;
-    c.tile = is_plain(b) ? config->tile_modes : 32;
+    c.tile = is_plain(b) ? config->tile_modes : mixed_tile(b);
     c.upb = config->units_per_block;
     const bool ok = c.upb > 0 && (is_plain(b) ? batch_plain_config_ok(c.R, c.tile)
                                   : is_fx(b)  ? batch_fx_config_ok(c.R)

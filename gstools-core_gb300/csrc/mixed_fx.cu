@@ -19,20 +19,23 @@
 //    dimension, where a double-float product takes eight FP32 instructions
 //    and an FP64 one 1/64 of the pipe.  BI is stored biased by 2^31, so
 //    both high products are unsigned; the bias's effect is a per-point
-//    constant taken out once per point;
+//    constant taken out once per point.  When every mode of a call (or batch
+//    item) has |BI| < 2^20, sum_d BI Xl 2^-29 is one chain of FP32 fused
+//    multiply-adds instead (the high products issue at a quarter of the
+//    FP32 rate);
 //  * e^{i theta}: theta + 2^27 + 16 selects by its top 4 bits one of 16
 //    entries of the mode's table T[m] = (z1 - i z2) e^{2 pi i (m/16 - phi)}
 //    (phi the per-mode constant; built in FP64 per mode, stored as FP32).
 //    Bits 5..27 of the same word, placed under the exponent of 1.0f, give
 //    1 + u 2^-23 exactly; minus 1.5 that is the remainder r in sixteenths
 //    of a turn (|r| <= 1/2, rounded to 2^-27 turn by the + 16) with no
-//    integer-to-float conversion.  sin and cos of r pi/8 are Taylor
-//    polynomials of degree 5 and 6 in r (truncation below 2.3e-9), and the
-//    term is Re(T e^{i r pi/8});
-//  * the terms of two modes are added, and the pair sums are summed in FP32
-//    over tiles of 32 modes with Kahan compensation; each tile is folded
-//    into a double-float (TwoSum) running total, converted to FP64 at the
-//    end.
+//    integer-to-float conversion.  sin and cos of r pi/8 are minimax
+//    polynomials of degree 5 and 4 in r (within 6e-9), and the term is
+//    Re(T e^{i r pi/8});
+//  * the terms of eight modes are added (four pair sums), and the group sums
+//    are summed in FP32 over tiles of 64 modes with Kahan compensation; each
+//    tile is folded into a double-float (TwoSum) running total, converted to
+//    FP64 at the end.
 // Phases beyond 2^30 turns (|k| * max|x| > 6.7e9) do not fit the integer
 // range; such calls are flagged in the range word (the caller recomputes them
 // on the FP64 kernel or reports it).  Non-finite coordinates give NaN, as the
@@ -52,10 +55,11 @@ constexpr int kFxThreads = 128;
 static_assert(kFxThreads == kBatchThreads, "batch units assume the block size");
 constexpr int kFxR = 4;                 // points per thread when untuned
 constexpr int kFxW = 8;                 // target blocks per SM when untuned
-constexpr int kFxTile = 32;             // modes per staged tile = accumulation tile
+constexpr int kFxTile = 64;             // modes per staged tile = accumulation tile
 // 32-bit words per mode: [0..2] BI' (BI + 2^31), [3] w0, [4..6] BF, [7] w1,
-// [8] w2 (projector weights of the incompressible field, FP32), [32..63] the
-// table T[m] as (re, im) FP32 pairs; words 9..31 are unused.  A record is
+// [8] w2 (projector weights of the incompressible field, FP32), [9..11] BI
+// as FP32, [32..63] the table T[m] as (re, im) FP32 pairs; words 12..31 are
+// unused.  A record is
 // 256 bytes and the tile of records in shared memory 256-byte aligned, so
 // a table starts on a 128-byte boundary (its entry's address is one OR) and
 // its 16 entries fill the 32 shared-memory banks once: a warp's gather from

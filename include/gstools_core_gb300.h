@@ -77,7 +77,7 @@ extern "C" {
                                   32-bit fixed point (two integer products
                                   and one exact FP32 product per dimension,
                                   within 2^-30 turns), FP32 table and
-                                  polynomial sincos, FP32 sums per 32 modes
+                                  polynomial sincos, FP32 sums per 64 modes
                                   with a compensated total; below 1e-6 of
                                   the field RMS.  |k| * max|x| beyond 2^30
                                   turns is flagged (see gsc_device_status)  */
