@@ -1067,8 +1067,8 @@ PROFILED_TRAFFIC = {
     ("sep_tc_f16x5", "c4"): (167.4e6, "profiles/sep_tc_f16x5_c4.md"),
     ("plain_f64_scalar", "c1"): (5.8e6, "profiles/plain_f64_scalar_c1.md"),
     ("mixed_scalar", "c1"): (1.906e6, "profiles/mixed_fx_c1.md"),
-    ("mixed_scalar", "c3"): (411.2e6 + 114.3e6, "profiles/mixed_fx_c3.md"),
-    ("batch_mixed", "c5"): (2279.3e6 + 669.0e6, "profiles/batch_fx_c5.md"),
+    ("mixed_scalar", "c3"): (411.7e6 + 115.0e6, "profiles/mixed_fx_c3.md"),
+    ("batch_mixed", "c5"): (2274.0e6 + 668.3e6, "profiles/batch_fx_c5.md"),
 }
 
 

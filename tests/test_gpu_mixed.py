@@ -187,3 +187,21 @@ def test_device_auto_falls_back_on_the_device(gsc, kind):
     run(big, far, form="mixed")
     with pytest.raises(gsc.GscError):
         gsc.device_status()
+
+
+def test_issue_rate_probe_is_ordered_and_repeatable(gsc):
+    """gsc_selftest_pipe_rates measures the issue rates the mixed form's
+    roofline weighs its instructions with: FP32 FMAs issue faster than low
+    32-bit integer multiply-adds, and those faster than high ones; two
+    measurements agree within 10 %."""
+    import ctypes
+    from gstools_core import _native
+    runs = []
+    for _ in range(2):
+        r = (ctypes.c_double * 3)()
+        _native.check(_native.lib.gsc_selftest_pipe_rates(-1, r))
+        runs.append(np.array(r[:]))
+    for hi, lo, ffma in runs:
+        assert 0 < hi < lo < ffma
+        assert 1.2 < ffma / lo < 3.0 and 2.0 < ffma / hi < 6.0
+    assert np.all(np.abs(runs[0] / runs[1] - 1.0) < 0.10)
