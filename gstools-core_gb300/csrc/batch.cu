@@ -737,16 +737,16 @@ static int summate_batch_host(const gsc_batch_item *items, int64_t count, const 
     // group are copied back while the next one computes.  Groups alternate
     // between two compute streams, so that a group's persistent kernel takes
     // the SMs that the previous group's last units leave idle.
-    // The first group is small (1/(4G) of the work), since its copy is the
-    // one that nothing hides; the others share the rest equally, and their
-    // inputs copy (about 5 times faster than they compute) within the
-    // previous group.  More groups shorten the first copy and the last
-    // group's result copy.
+    // The first and the last group are small (1/(4G) of the work each): the
+    // first group's input copy and the last group's result copy are the ones
+    // that nothing hides.  The others share the rest equally; their inputs
+    // copy (about 5 times faster than they compute) within the previous
+    // group, and their results while the next one computes.
     const int G = (total_work >= 4.0e10 && count >= 16) ? 8
                   : (total_work >= 4.0e9 && count >= 8) ? 4 : 1;
     auto group_end = [G](int g) {          // fraction of the work in groups [0, g]
-        const double first = 1.0 / (4.0 * G);
-        return g == 0 ? first : first + (1.0 - first) * g / (G - 1);
+        const double edge = 1.0 / (4.0 * G);
+        return g >= G - 1 ? 1.0 : edge + (1.0 - 2.0 * edge) * g / (G - 2);
     };
     std::vector<int64_t> gstart(static_cast<size_t>(G) + 1, count);
     gstart[0] = 0;

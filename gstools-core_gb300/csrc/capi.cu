@@ -1457,6 +1457,25 @@ int gsc_device_count(int32_t *count) {
     return GSC_OK;
 }
 
+int gsc_last_timeline(int32_t *ids, double *start_ms, double *ms, int32_t cap) {
+    int32_t n = 0;
+    for (auto &r : t_recs) {
+        if (n >= cap) break;
+        float f = 0.f, s = 0.f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&f, r.a, r.b) != cudaSuccess ||
+            cudaEventElapsedTime(&s, t_recs.front().a, r.a) != cudaSuccess) {
+            cudaGetLastError();
+            f = -1.f;
+            s = -1.f;
+        }
+        if (ids) ids[n] = r.id;
+        if (start_ms) start_ms[n] = s;
+        if (ms) ms[n] = f;
+        ++n;
+    }
+    return n;
+}
+
 int gsc_last_timings(int32_t *ids, double *ms, int32_t cap) {
     int32_t n = 0;
     for (auto &r : t_recs) {

@@ -31,7 +31,7 @@ import operator
 import numpy as np
 
 from . import _native
-from ._native import GscError, device_count, last_timings
+from ._native import GscError, device_count, last_timeline, last_timings
 
 __all__ = ["summate", "summate_incompr", "summate_fourier", "randomization_field", "summate_device",
            "summate_incompr_device", "summate_fourier_device",
@@ -40,7 +40,7 @@ __all__ = ["summate", "summate_incompr", "summate_fourier", "randomization_field
            "summate_fourier_structured_device", "Batch", "summate_batch", "last_batch_config",
            "sample_modes", "sample_modes_batch_device",
            "device_status", "release_buffers", "host_pool_stats", "host_pool_trim",
-           "device_count", "last_timings", "GscError", "__version__"]
+           "device_count", "last_timings", "last_timeline", "GscError", "__version__"]
 
 __version__ = "1.1.0"          # the reference crate version this mirrors (Cargo.toml:3)
 native_version = _native.lib.gsc_version().decode()
@@ -95,6 +95,12 @@ def _result(shape, order="C") -> np.ndarray:
     array and every view of it are gone: repeated calls reuse resident pages
     instead of faulting in fresh ones (the result is still a new array each
     call, as the reference returns)."""
+    return _result_ptr(shape, order)[0]
+
+
+def _result_ptr(shape, order="C"):
+    """_result and the address of its data (known here without asking the
+    array, which costs about a microsecond per call)."""
     n = 1
     for s in shape if isinstance(shape, tuple) else (shape,):
         n *= int(s)
@@ -102,8 +108,9 @@ def _result(shape, order="C") -> np.ndarray:
     if nbytes >= _POOL_MIN_BYTES:
         ptr = ctypes.c_void_p()
         if _native.lib.gsc_host_alloc(nbytes, ctypes.byref(ptr)) == 0:
-            return np.asarray(_PoolBlock(ptr.value, shape, order))
-    return np.empty(shape, dtype=np.float64, order=order)
+            return np.asarray(_PoolBlock(ptr.value, shape, order)), ptr.value
+    a = np.empty(shape, dtype=np.float64, order=order)
+    return a, a.ctypes.data
 
 
 class _PoolBlock:
@@ -591,8 +598,8 @@ def summate_batch(items, *, form="auto", tolerance=None, device=-1, timing=False
         if kind == "fourier":
             sf = np.ascontiguousarray(_array(it["spectrum_factor"], "spectrum_factor", 1))
             _assert_eq(sf.shape[0], n)
-        out = _result((dim, p) if kind == "incompr" else p)
-        keep += [cov, z1, z2, pos, sf, out]
+        out, out_ptr = _result_ptr((dim, p) if kind == "incompr" else p)
+        keep += [cov, z1, z2, pos, sf]
         outs.append(out)
         c_dim.append(dim)
         c_kind.append(_native.BATCH_KINDS[kind])
@@ -603,7 +610,7 @@ def summate_batch(items, *, form="auto", tolerance=None, device=-1, timing=False
         c_z2.append(z2.ctypes.data)
         c_sf.append(0 if sf is None else sf.ctypes.data)
         c_pos.append(pos.ctypes.data)
-        c_out.append(out.ctypes.data)
+        c_out.append(out_ptr)
     arr = np.zeros(max(1, len(outs)), dtype=_native.BATCH_ITEM_DTYPE)
     if outs:
         for name, col in zip(_native.BATCH_ITEM_DTYPE.names, cols):

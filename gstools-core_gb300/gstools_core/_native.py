@@ -125,6 +125,7 @@ SIGNATURES = {
     "gsc_last_error": (ctypes.c_char_p, []),
     "gsc_device_count": (ctypes.c_int, [ctypes.POINTER(_I32)]),
     "gsc_last_timings": (ctypes.c_int, [_P, _P, _I32]),
+    "gsc_last_timeline": (ctypes.c_int, [_P, _P, _P, _I32]),
     "gsc_kernel_name": (ctypes.c_char_p, [_I32]),
     "gsc_summate_f64": (ctypes.c_int, [_P, _I64, _I64, _P, _I64, _P, _I64, _P, _I64, _I64,
                                        _I64, _I64, _I64, _P, _I64, _OPTS]),
@@ -236,3 +237,14 @@ def last_timings(cap: int = 64):
     ms = (ctypes.c_double * cap)()
     n = lib.gsc_last_timings(ids, ms, cap)
     return [(lib.gsc_kernel_name(ids[i]).decode(), float(ms[i])) for i in range(n)]
+
+
+def last_timeline(cap: int = 256):
+    """[(kernel_name, start_ms, ms), ...] of the last call made with
+    GSC_FLAG_TIMING: each record's start after the first record's start (all
+    of the call's streams on one clock) and its duration."""
+    ids = (_I32 * cap)()
+    st = (ctypes.c_double * cap)()
+    ms = (ctypes.c_double * cap)()
+    n = lib.gsc_last_timeline(ids, st, ms, cap)
+    return [(lib.gsc_kernel_name(ids[i]).decode(), float(st[i]), float(ms[i])) for i in range(n)]

@@ -124,6 +124,10 @@ int gsc_device_count(int32_t *count);
  * writes up to `cap` (name-index, milliseconds) pairs and returns how many
  * kernels were recorded.  Names come from gsc_kernel_name(). */
 int gsc_last_timings(int32_t *kernel_ids, double *ms, int32_t cap);
+/* The same records as a timeline: also each record's start in milliseconds
+ * after the first record's start (the launches of all of the call's streams
+ * on one clock).  Returns how many records were written. */
+int gsc_last_timeline(int32_t *kernel_ids, double *start_ms, double *ms, int32_t cap);
 const char *gsc_kernel_name(int32_t kernel_id);
 
 /* Status of the kernels launched by device-pointer calls on `device`
@@ -388,8 +392,8 @@ int gsc_batch_destroy(gsc_batch *plan);
  * call on the device are reused when the shapes match), and copies every
  * output back before returning.  An ensemble of at least 4e9 point*modes and
  * 8 items runs as G = 4 groups of consecutive items (8 from 4e10 point*modes
- * and 16 items): the first holds 1/(4G) of the work, the others share the
- * rest equally; one plan each.  A group's inputs are copied while the
+ * and 16 items): the first and the last hold 1/(4G) of the work each, the
+ * others share the rest equally; one plan each.  A group's inputs are copied while the
  * previous group computes, and its results while the next one computes.
  * Without a config (or with zero fields), the groups share one set of
  * launch choices, tuned on the group with the most work and cached under the

@@ -206,13 +206,24 @@ def test_summate_batch_host_api_groups(gsc):
         if call:
             for it in items:
                 it["z1"][:] = rng.standard_normal(it["z1"].size)
-        outs = gsc.summate_batch(items, form="mixed")
+        outs = gsc.summate_batch(items, form="mixed", timing=call == 1)
         for i, (it, out) in enumerate(zip(items, outs)):
             idx = np.sort(rng.choice(it["pos"].shape[1], 512, replace=False))
             ref = oracle.summator(it["cov"], it["z1"], it["z2"],
                                   np.ascontiguousarray(it["pos"][:, idx]), num_threads=NT)
             err = rel_err(out[idx], ref)
             assert err <= BOUND["mixed"], f"call {call} item {i}: {err:.3e}"
+    # the timed call's records on one clock: four groups, each copied in,
+    # computed and copied out in that order
+    tl = gsc.last_timeline()
+    assert [(k, ms) for k, _, ms in tl] == gsc.last_timings()
+    assert tl[0][1] == 0.0 and all(s >= 0 and ms >= 0 for _, s, ms in tl)
+    h2d = [s for k, s, _ in tl if k == "copy_h2d"]
+    sums = [(s, s + ms) for k, s, ms in tl if k == "batch_mixed"]
+    d2h = [s + ms for k, s, ms in tl if k == "copy_d2h"]
+    assert len(h2d) == len(sums) == len(d2h) == 4
+    assert all(a <= b for a, (b, _) in zip(h2d, sums))
+    assert all(e <= f + 1e-3 for (_, e), f in zip(sums, d2h))
     cfg = gsc.last_batch_config()
     assert cfg["form"] == "mixed" and cfg["work"] == work
 
@@ -244,7 +255,7 @@ def test_summate_batch_phase_range(gsc):
 
 def test_summate_batch_eight_groups_with_empty_items(gsc):
     """From 4e10 point*modes and 16 items the host-array call runs in eight
-    groups (the first 1/32 of the work).  Items without points or without
+    groups (the first and the last 1/32 of the work each).  Items without points or without
     modes among them; every item against the oracle on a seeded subset."""
     rng = np.random.default_rng(45)
     items = []
