@@ -954,17 +954,23 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     GSC_TRY(g.set(ctx->device));
     cudaStream_t st = ctx->stream;
 
-    // C-ordered positions (256 KiB and more) stay where they are when the
-    // GPU reads pageable host memory coherently (GB300's host link with
-    // address translation, cudaDevAttrPageableMemoryAccess): the kernels read
-    // them in place, once per mode split, and no host core packs them into
-    // staging.  The modes, a few KB to MB, are still packed and copied.
+    // C-ordered positions stay where they are when the GPU reads pageable
+    // host memory coherently (GB300's host link with address translation,
+    // cudaDevAttrPageableMemoryAccess): the kernels read them in place, once
+    // per mode split, and no host core packs them into staging.  Dense modes of the scalar and incompressible methods are read
+    // in place too, by the one kernel that turns them into per-mode records
+    // (dimensions 1-3; the generic kernel of other dimensions reads every
+    // mode per point, and Fourier weights are scaled into staging first): a
+    // call then copies nothing to the GPU, which saves the copy's fixed cost
+    // of about 20 us.
     const size_t n_cov = static_cast<size_t>(dim * N);
-    const bool pos_in_place = ps_p == 1 && (dim == 1 || ps_d == P) &&
-                              static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(256) << 10) &&
-                              pageable_access(ctx->device);
+    const bool pageable = pageable_access(ctx->device);
+    const bool pos_in_place = ps_p == 1 && (dim == 1 || ps_d == P) && pageable;
+    const bool modes_in_place = !sf && N > 0 && dim >= 1 && dim <= 3 && cs_n == 1 &&
+                                (dim == 1 || cs_d == N) && z1s == 1 && z2s == 1 && pageable;
     const size_t n_pos = pos_in_place ? 0 : static_cast<size_t>(dim * P);
-    const size_t n_in = n_cov + 2 * static_cast<size_t>(N) + n_sf + n_pos;
+    const size_t n_m = modes_in_place ? 0 : n_cov + 2 * static_cast<size_t>(N);
+    const size_t n_in = n_m + n_sf + n_pos;
     const size_t n_out = static_cast<size_t>(nout * P);
     const size_t bytes = (n_in + n_out) * sizeof(double);
     GSC_TRY(ensure_pinned(*ctx, bytes + 64));           // + the range flag's slot
@@ -979,20 +985,22 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     // chunks (a DMA straight from a large pageable array runs at a fraction
     // of the link)
     std::vector<HostSrc> segs;
-    stage2(segs, h, 0, cov, cs_d, cs_n, dim, N);
-    stage2(segs, h, n_cov, z1, 0, z1s, 1, N);
-    stage2(segs, h, n_cov + N, z2, 0, z2s, 1, N);
-    if (sf) stage2(segs, h, n_cov + 2 * N, sf, 0, sfs, 1, N);
-    if (!pos_in_place) stage2(segs, h, n_cov + 2 * N + n_sf, pos, ps_d, ps_p, dim, P);
+    if (!modes_in_place) {
+        stage2(segs, h, 0, cov, cs_d, cs_n, dim, N);
+        stage2(segs, h, n_cov, z1, 0, z1s, 1, N);
+        stage2(segs, h, n_cov + N, z2, 0, z2s, 1, N);
+    }
+    if (sf) stage2(segs, h, n_m, sf, 0, sfs, 1, N);
+    if (!pos_in_place) stage2(segs, h, n_m + n_sf, pos, ps_d, ps_p, dim, P);
     GSC_TRY(h2d_packed(st, d, h, segs));
     tc.end();
-    if (sf) GSC_TRY(fourier_scale(d + n_cov + 2 * N, d + n_cov, d + n_cov + N, N, d + n_cov,
+    if (sf) GSC_TRY(fourier_scale(d + n_m, d + n_cov, d + n_cov + N, N, d + n_cov,
                                   d + n_cov + N, st));
     PlainArgs a;
-    a.cov = d;
-    a.z1 = d + n_cov;
-    a.z2 = d + n_cov + N;
-    a.pos = pos_in_place ? pos : d + n_cov + 2 * N + n_sf;
+    a.cov = modes_in_place ? cov : d;
+    a.z1 = modes_in_place ? z1 : d + n_cov;
+    a.z2 = modes_in_place ? z2 : d + n_cov + N;
+    a.pos = pos_in_place ? pos : d + n_m + n_sf;
     a.dim = dim;
     a.n_modes = N;
     a.n_points = P;

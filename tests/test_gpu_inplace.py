@@ -1,12 +1,12 @@
-"""Positions read in place from host memory (GPU tests).
+"""Positions and modes read in place from host memory (GPU tests).
 
 Where the GPU reads pageable host memory coherently (cudaDevAttrPageableMemoryAccess,
-GB300's host link), host-array calls with 256 KiB or more of C-ordered
-positions leave them where they are and the point kernels read them in
-place; other layouts go through the pinned staging.  Both routes feed the
-same kernels the same values, so their results must agree bit for bit; a
-seeded subset of points is also checked against the oracle at the form's bar
-(reference src/field.rs:37-65, :97-182).
+GB300's host link), host-array calls leave C-ordered positions and dense
+modes where they are: the point kernels read the positions in place and the
+record kernel the modes; other layouts go through the pinned staging.  Both
+routes feed the same kernels the same values, so their results must agree
+bit for bit; a seeded subset of points is also checked against the oracle at
+the form's bar (reference src/field.rs:37-65, :97-182).
 """
 import os
 
@@ -30,15 +30,20 @@ def _case(seed, n, p):
 
 @pytest.mark.parametrize("form,bar", [("mixed", 1e-6), ("plain", 1e-12)])
 @pytest.mark.parametrize("kind", ["scalar", "incompr"])
-@pytest.mark.parametrize("p", [20_000, 1 << 22])          # 480 KB and 96 MiB of positions
+@pytest.mark.parametrize("p", [300, 20_000, 1 << 22])     # 7 KB, 480 KB and 96 MiB of positions
 def test_positions_in_place_match_staged(gsc, form, bar, kind, p):
     cov, z1, z2, pos = _case(5, 64, p)
-    assert pos.flags.c_contiguous and pos.nbytes >= 256 << 10
+    assert pos.flags.c_contiguous and cov.flags.c_contiguous
     staged = np.asfortranarray(pos)                   # rows not contiguous: staged
     fn = gsc.summate_incompr if kind == "incompr" else gsc.summate
     got = fn(cov, z1, z2, pos, form=form)
     ref = fn(cov, z1, z2, staged, form=form)
     assert np.array_equal(got, ref, equal_nan=True)
+    # modes in a strided layout go through the staging as well
+    zz = np.empty((z1.size, 2))
+    zz[:, 0], zz[:, 1] = z1, z2                       # z1, z2 with a stride of 2
+    ref_m = fn(np.asfortranarray(cov), zz[:, 0], zz[:, 1], staged, form=form)
+    assert np.array_equal(got, ref_m, equal_nan=True)
     idx = np.sort(np.random.default_rng(6).choice(pos.shape[1], min(p, 4096), replace=False))
     sub = np.ascontiguousarray(pos[:, idx])
     if kind == "incompr":
