@@ -93,10 +93,21 @@ __constant__ double kSixteenthCos[16] = {
 // Fixed-point scale s_d of dimension d from the largest finite |x_d|
 // (bits of that non-negative double, 0 when none): |x| * 2^s < 2^60.
 __device__ __forceinline__ int fx_scale(unsigned long long maxbits) {
-    const double m = __longlong_as_double(static_cast<long long>(maxbits));
+    // e with m in [2^(e-1), 2^e): from the exponent field when m is normal
+    // (what frexp returns), frexp itself for a subnormal m
+    const int biased = static_cast<int>(maxbits >> 52);
     int e = 0;
-    if (m > 0.0) frexp(m, &e);                  // m in [2^(e-1), 2^e)
+    if (biased != 0) e = biased - 1022;
+    else if (maxbits != 0ull) frexp(__longlong_as_double(static_cast<long long>(maxbits)), &e);
     return 60 - e;
+}
+
+// x 2^q, as ldexp(x, q) returns it (both round once, to nearest): a product
+// with the power of two where that is a normal double
+__device__ __forceinline__ double fx_ldexp(double x, int q) {
+    if (q >= -1022 && q <= 1023)
+        return x * __longlong_as_double(static_cast<long long>(q + 1023) << 52);
+    return ldexp(x, q);
 }
 
 // Largest finite |x_d| of pos (dim, P) into maxbits[d] (as the bit pattern
@@ -122,21 +133,47 @@ __device__ __forceinline__ void fx_range_part(const double *__restrict__ pos, in
     }
 }
 
-__global__ void fx_range_kernel(const double *__restrict__ pos, int64_t P, int dim,
-                                unsigned long long *maxbits) {
-    fx_range_part(pos, P, dim, static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x,
-                  static_cast<int64_t>(gridDim.x) * blockDim.x, maxbits);
+// Single calls: block b writes the largest finite |x_d| of its share of the
+// points to part[3 b + d] (no atomics, nothing to zero first), and block 0
+// clears the product-form word maxbits[3] that the record kernel sets.
+constexpr int kFxRangeThreads = 256;
+__global__ void __launch_bounds__(kFxRangeThreads)
+fx_range_kernel(const double *__restrict__ pos, int64_t P, int dim,
+                unsigned long long *__restrict__ part, unsigned long long *maxbits) {
+    __shared__ unsigned long long wm[kFxRangeThreads / 32][3];
+    unsigned long long m[3] = {0ull, 0ull, 0ull};
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < P; i += stride)
+        for (int d = 0; d < dim && d < 3; ++d) {
+            const unsigned long long v =
+                static_cast<unsigned long long>(__double_as_longlong(pos[d * P + i])) &
+                0x7fffffffffffffffull;
+            if (v < 0x7ff0000000000000ull) m[d] = max(m[d], v);
+        }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        unsigned long long v = m[d];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) wm[warp][d] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        unsigned long long v = 0ull;
+        for (int w = 0; w < kFxRangeThreads / 32; ++w) v = max(v, wm[w][threadIdx.x]);
+        part[3 * static_cast<int64_t>(blockIdx.x) + threadIdx.x] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) maxbits[3] = 0ull;
 }
 
-// The record of mode j (see kFxRecWords).  range_flag (may be null) is set
-// to 1 when a wave number is too large for the integer phase at these
-// positions.
-__device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double z2, int dim,
-                              int64_t n_modes, int64_t j, int incompr,
-                              unsigned long long *maxbits, uint32_t *__restrict__ r,
-                              int *range_flag) {
-    double k[3] = {0.0, 0.0, 0.0};
-    for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
+// The record of mode j (see kFxRecWords).  mb[d]: the range words of the
+// positions (largest |x_d| as bits); small_word: set when a wave number
+// needs the general product form.  range_flag (may be null) is set to 1
+// when a wave number is too large for the integer phase at these positions.
+__device__ void fx_mode_entry(const double *k, double z1, double z2, int dim, int incompr,
+                              const unsigned long long *mb, unsigned long long *small_word,
+                              uint32_t *__restrict__ r, int *range_flag) {
     bool finite = isfinite(z1) && isfinite(z2);
     bool small = true;                              // every |BI| < 2^20
     double phi = 0.0;                               // units of 2^-32 turn
@@ -145,9 +182,9 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
         uint32_t bf = 0;
         if (d < dim) {
             finite = finite && isfinite(k[d]);
-            const double B = ldexp(k[d] * kInv2Pi, 61 - fx_scale(maxbits[d]));
+            const double B = fx_ldexp(k[d] * kInv2Pi, 61 - fx_scale(mb[d]));
             if (fabs(B) < 2147483648.0) {
-                const long long bq = __double2ll_rn(ldexp(B, 32));     // B to 2^-32
+                const long long bq = __double2ll_rn(B * 4294967296.0);  // B to 2^-32 (exact scaling)
                 bi = static_cast<int32_t>(bq >> 32);
                 bf = static_cast<uint32_t>(bq);
                 // B 2^31 mod 2^32: what the offset 2^60 of X adds to theta
@@ -173,9 +210,10 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
     r[3] = __float_as_uint(__double2float_rn(w[0]));
     r[7] = __float_as_uint(__double2float_rn(w[1]));
     r[8] = __float_as_uint(__double2float_rn(w[2]));
-    if (!small) atomicOr(maxbits + 3, 1ull);
+    if (!small) atomicOr(small_word, 1ull);
     for (int q = 12; q < kFxTab; ++q) r[q] = 0u;
-    phi = fmod(phi, 4294967296.0);
+    // phi mod 2^32, exactly (0 <= phi < 3 2^32, a multiple of 1/2)
+    phi -= 4294967296.0 * floor(phi * 2.3283064365386963e-10);
     // T[m] = (z1 - i z2) e^{-2 pi i phi / 2^32} e^{2 pi i m / 16}: one FP64
     // sincos for the mode's rotation, the sixteenth turns from a table (FP64
     // products, a few FP64 ulps)
@@ -193,16 +231,43 @@ __device__ void fx_mode_entry(const double *__restrict__ cov, double z1, double 
     }
 }
 
-__global__ void fx_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
-                               const double *__restrict__ z2, int dim, int64_t n_modes,
-                               int64_t j0, int64_t nc, int incompr,
-                               unsigned long long *maxbits, uint32_t *__restrict__ rec,
-                               int *range_flag) {
-    const int64_t jl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (jl >= nc) return;
+// One warp of modes per block.  A record is one thread's dependent chain of
+// FP64 operations (about 13 us on GB300 for any number of modes per warp),
+// so the kernel takes that latency once.  Each block first reduces the range
+// kernel's per-block maxima; block 0 stores them as the range words of the
+// sums.
+constexpr int kFxModeThreads = 32;
+__global__ void __launch_bounds__(kFxModeThreads)
+fx_mode_kernel(const double *__restrict__ cov, const double *__restrict__ z1,
+               const double *__restrict__ z2, int dim, int64_t n_modes, int64_t j0, int64_t nc,
+               int incompr, const unsigned long long *__restrict__ range_part, int range_blocks,
+               unsigned long long *maxbits, uint32_t *__restrict__ rec, int *range_flag) {
+    // the mode's inputs first (they may come over the host link), so that
+    // their latency overlaps the reduction of the range words
+    const int64_t jl = static_cast<int64_t>(blockIdx.x) * kFxModeThreads + threadIdx.x;
     const int64_t j = j0 + jl;
-    fx_mode_entry(cov, z1[j], z2[j], dim, n_modes, j, incompr, maxbits, rec + jl * kFxRecWords,
-                  range_flag);
+    const bool mine = jl < nc;
+    double k[3] = {0.0, 0.0, 0.0}, z1j = 0.0, z2j = 0.0;
+    if (mine) {
+        for (int d = 0; d < dim && d < 3; ++d) k[d] = cov[d * n_modes + j];
+        z1j = z1[j];
+        z2j = z2[j];
+    }
+    unsigned long long mb[3] = {0ull, 0ull, 0ull};
+    for (int b = threadIdx.x; b < range_blocks; b += kFxModeThreads)
+        for (int d = 0; d < dim && d < 3; ++d)
+            mb[d] = max(mb[d], range_part[3 * static_cast<int64_t>(b) + d]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mb[d] = max(mb[d], __shfl_xor_sync(0xffffffffu, mb[d], o));
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        maxbits[0] = mb[0];
+        maxbits[1] = mb[1];
+        maxbits[2] = mb[2];
+    }
+    if (!mine) return;
+    fx_mode_entry(k, z1j, z2j, dim, incompr, mb, maxbits + 3, rec + jl * kFxRecWords, range_flag);
 }
 
 // Kahan step: (sum, cmp) += a, cmp holding minus the lost low-order part
@@ -602,7 +667,9 @@ __global__ void batch_fx_table_kernel(const BatchItem *__restrict__ items,
         z1j = __dmul_rn(f, z1j);
         z2j = __dmul_rn(f, z2j);
     }
-    fx_mode_entry(it.cov, z1j, z2j, it.dim, it.n_modes, j, it.incompr, maxbits + 4 * lo,
+    double k[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < it.dim && d < 3; ++d) k[d] = it.cov[d * it.n_modes + j];
+    fx_mode_entry(k, z1j, z2j, it.dim, it.incompr, maxbits + 4 * lo, maxbits + 4 * lo + 3,
                   rec + g * kFxRecWords, range_flag);
 }
 
@@ -701,24 +768,27 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
         for (int r : kCandR)
             for (int w : kCandW) S_max = std::max(S_max, shape_of(r, w).S);
 
+    // range blocks: enough to stream the positions, at most four per SM
+    const int64_t rb = std::max<int64_t>(
+        1, std::min<int64_t>((P + kFxRangeThreads - 1) / kFxRangeThreads, 4 * static_cast<int64_t>(sms)));
     const size_t rec_bytes = static_cast<size_t>(chunk) * kFxRecBytesPerMode;
     const size_t part_bytes = S_max > 1 ? static_cast<size_t>(S_max) * nout * P * sizeof(double) : 0;
     const size_t off_mb = (rec_bytes + 255) / 256 * 256;
-    const size_t off_part = off_mb + 256;
+    const size_t off_rp = off_mb + 256;
+    const size_t off_part = off_rp + (static_cast<size_t>(rb) * 3 * sizeof(unsigned long long) + 255) / 256 * 256;
     GSC_TRY(ensure_dev(ctx, ctx.scratch, off_part + part_bytes + 256));
     GSC_CUDA(cudaStreamWaitEvent(st, ctx.scratch_ready, 0));
     unsigned char *sbase = static_cast<unsigned char *>(ctx.scratch.ptr);
     uint32_t *rec = reinterpret_cast<uint32_t *>(sbase);
     unsigned long long *maxbits = reinterpret_cast<unsigned long long *>(sbase + off_mb);
+    unsigned long long *range_part = reinterpret_cast<unsigned long long *>(sbase + off_rp);
     double *part = reinterpret_cast<double *>(sbase + off_part);
 
     {
         TimedLaunch tl(st);
         tl.begin(K_MIXED_MODES);
-        GSC_CUDA(cudaMemsetAsync(maxbits, 0, 4 * sizeof(unsigned long long), st));
-        const int64_t rb = std::min<int64_t>((P + 255) / 256, 4 * static_cast<int64_t>(sms));
-        fx_range_kernel<<<static_cast<unsigned>(std::max<int64_t>(rb, 1)), 256, 0, st>>>(
-            a.pos, P, static_cast<int>(dim), maxbits);
+        fx_range_kernel<<<static_cast<unsigned>(rb), kFxRangeThreads, 0, st>>>(
+            a.pos, P, static_cast<int>(dim), range_part, maxbits);
         tl.end();
         GSC_CUDA(cudaGetLastError());
     }
@@ -726,9 +796,10 @@ int mixed_fx_run(DeviceCtx &ctx, const PlainArgs &a, int *range_flag, cudaStream
         if (nc <= 0) return GSC_OK;
         TimedLaunch tl(st);
         tl.begin(K_MIXED_MODES);
-        fx_mode_kernel<<<static_cast<unsigned>((nc + 127) / 128), 128, 0, st>>>(
-            a.cov, a.z1, a.z2, static_cast<int>(dim), N, j0, nc, a.incompr ? 1 : 0, maxbits, rec,
-            range_flag);
+        fx_mode_kernel<<<static_cast<unsigned>((nc + kFxModeThreads - 1) / kFxModeThreads),
+                         kFxModeThreads, 0, st>>>(
+            a.cov, a.z1, a.z2, static_cast<int>(dim), N, j0, nc, a.incompr ? 1 : 0, range_part,
+            static_cast<int>(rb), maxbits, rec, range_flag);
         tl.end();
         GSC_CUDA(cudaGetLastError());
         return GSC_OK;
