@@ -361,6 +361,8 @@ static int structured_form(const Resolved &r, int64_t dim) {
 //   [2] sticky: an explicit sep_f16x5 call on device pointers was flagged
 //       and left its output invalid
 //   [3] the last host-pointer mixed call's range flag (cleared by the call)
+//       where the device does not map the pinned staging word that takes
+//       it otherwise
 //   [4] sticky: a mixed call on device pointers (or a batch) met a wave
 //       number past the integer phase range (its output is invalid)
 //   [5] the device half of a host call's flattened-mesh check: 1 when a
@@ -1014,13 +1016,26 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     a.out_sd = f_order ? 1 : P;
     a.out_sp = f_order ? nout : 1;
     const bool fx = point_form(ro, a) == GSC_FORM_MIXED;
-    if (fx) GSC_CUDA(cudaMemsetAsync(ctx->status + kStatusFxFlag, 0, sizeof(int), st));
-    GSC_TRY(run_points(*ctx, ro, a, st, ctx->status + kStatusFxFlag));
     // wave numbers past the mixed form's integer phase range: AUTO recomputes
-    // on the plain FP64 kernel, an explicit mixed form reports it.  The flag
-    // is read back with the result (one synchronisation); a flagged result
-    // is discarded.
+    // on the plain FP64 kernel, an explicit mixed form reports it.  The
+    // record kernel writes the range flag straight into its pinned host word
+    // where the device maps that memory (no clearing launch, no read-back
+    // copy), else into the device status word, which is copied back with the
+    // result.  Either way one synchronisation; a flagged result is discarded.
     *hflag = 0;
+    int *dflag = ctx->status + kStatusFxFlag;
+    bool flag_mapped = false;
+    if (fx) {
+        void *dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, const_cast<int *>(hflag), 0) == cudaSuccess && dp) {
+            dflag = static_cast<int *>(dp);
+            flag_mapped = true;
+        } else {
+            cudaGetLastError();
+            GSC_CUDA(cudaMemsetAsync(dflag, 0, sizeof(int), st));
+        }
+    }
+    GSC_TRY(run_points(*ctx, ro, a, st, dflag));
     auto recompute = [&]() -> int {
         if (ro.form != GSC_FORM_AUTO) return set_error(GSC_ERR_KERNEL, kFxRangeMsg);
         Resolved rp = ro;
@@ -1032,9 +1047,9 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
         if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
         pf.join();
         for (int pass = 0; pass < 2; ++pass) {
-            if (fx && pass == 0)
-                GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), ctx->status + kStatusFxFlag,
-                                         sizeof(int), cudaMemcpyDeviceToHost, st));
+            if (fx && pass == 0 && !flag_mapped)
+                GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), dflag, sizeof(int),
+                                         cudaMemcpyDeviceToHost, st));
             tc.begin(K_COPY_D2H);
             GSC_CUDA(cudaMemcpyAsync(out, a.out, n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
             tc.end();
@@ -1046,8 +1061,9 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
         return GSC_OK;
     }
     if (fx) {
-        GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), ctx->status + kStatusFxFlag,
-                                 sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (!flag_mapped)
+            GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), dflag, sizeof(int),
+                                     cudaMemcpyDeviceToHost, st));
         GSC_CUDA(cudaStreamSynchronize(st));
         if (*hflag) GSC_TRY(recompute());
     }

@@ -205,3 +205,29 @@ def test_issue_rate_probe_is_ordered_and_repeatable(gsc):
         assert 0 < hi < lo < ffma
         assert 1.2 < ffma / lo < 3.0 and 2.0 < ffma / hi < 6.0
     assert np.all(np.abs(runs[0] / runs[1] - 1.0) < 0.10)
+
+
+@pytest.mark.parametrize("in_range", [True, False])
+def test_mixed_padded_output_and_range(gsc, in_range):
+    """A result buffer neither C- nor Fortran-ordered (a padded (P, 4) array
+    through the C ABI) at tolerance 1e-6: in range the mixed form's result,
+    past the phase range the plain FP64 recomputation; the padding stays
+    untouched."""
+    import ctypes
+    from gstools_core import _native
+    rng = np.random.default_rng(12)
+    n, p = 40, 5000
+    cov = rng.normal(0.0, 0.5, (3, n))
+    if not in_range:
+        cov[1, 5] = 40.0                      # 40 x 2e8 / 2 pi > 2^30 turns
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(0.0, 2.0e8, (3, p))
+    buf = np.full((p, 4), np.nan)
+    o = gsc._opts("auto", 1e-6, False, -1)
+    rc = _native.lib.gsc_summate_incompr_f64(
+        cov.ctypes.data, n, 1, z1.ctypes.data, 1, z2.ctypes.data, 1,
+        pos.ctypes.data, p, 1, 3, n, p, buf.ctypes.data, 1, 4, ctypes.byref(o))
+    assert rc == 0, _native.lib.gsc_last_error()
+    assert np.isnan(buf[:, 3]).all()
+    ref = oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)
+    assert rel_err(buf[:, :3].T, ref) <= (TOL if in_range else 1e-12)
