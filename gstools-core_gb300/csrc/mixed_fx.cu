@@ -33,7 +33,7 @@
 //    polynomials of degree 5 and 4 in r (within 6e-9), and the term is
 //    Re(T e^{i r pi/8});
 //  * the terms of eight modes are added (four pair sums), and the group sums
-//    are summed in FP32 over tiles of 64 modes with Kahan compensation; each
+//    are summed in FP32 over tiles of 128 modes with Kahan compensation; each
 //    tile is folded into a double-float (TwoSum) running total, converted to
 //    FP64 at the end.
 // Phases beyond 2^30 turns (|k| * max|x| > 6.7e9) do not fit the integer
@@ -55,7 +55,8 @@ constexpr int kFxThreads = 128;
 static_assert(kFxThreads == kBatchThreads, "batch units assume the block size");
 constexpr int kFxR = 4;                 // points per thread when untuned
 constexpr int kFxW = 8;                 // target blocks per SM when untuned
-constexpr int kFxTile = 64;             // modes per staged tile = accumulation tile
+constexpr int kFxTile = 128;            // modes per staged tile = accumulation tile
+constexpr int kFxSplitModes = 64;       // mode splits are multiples of this
 // 32-bit words per mode: [0..2] BI' (BI + 2^31), [3] w0, [4..6] BF, [7] w1,
 // [8] w2 (projector weights of the incompressible field, FP32), [9..11] BI
 // as FP32, [32..63] the table T[m] as (re, im) FP32 pairs; words 12..31 are
@@ -598,10 +599,10 @@ FxShape fx_shape(int R, int W, int64_t P, int64_t chunk, int sms, int occ = 4) {
         const int64_t want_blocks = static_cast<int64_t>(sms) * W;
         S = std::max<int64_t>(1, (want_blocks + f.bx - 1) / f.bx);
     }
-    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kFxTile)));
+    S = std::min<int64_t>(S, std::max<int64_t>(1, chunk / (2 * kFxSplitModes)));
     S = std::min<int64_t>(S, 64);
     int64_t mps = chunk > 0 ? (chunk + S - 1) / S : 0;
-    mps = (mps + kFxTile - 1) / kFxTile * kFxTile;
+    mps = (mps + kFxSplitModes - 1) / kFxSplitModes * kFxSplitModes;
     if (mps > 0) S = std::max<int64_t>(1, (chunk + mps - 1) / mps);
     if (chunk == 0) S = 1;
     f.S = S;

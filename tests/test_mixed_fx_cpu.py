@@ -49,6 +49,7 @@ def point_words(x, s, small=False):
 
 
 MAGIC_BITS = 0x4B400000          # bits of 1.5 2^23
+TILE = 128                       # modes per accumulation tile
 SMALL_BI = 1 << 20
 
 
@@ -206,10 +207,10 @@ def fx_field(cov, z1, z2, pos):
         for d in range(dim):
             c = (c - pw[d][2]) & U32
         hi = lo = f32(0)
-        for t0 in range(0, n, 32):
+        for t0 in range(0, n, TILE):
             acc = cmp = f32(0)
             terms = []
-            for j in range(t0, min(n, t0 + 32)):
+            for j in range(t0, min(n, t0 + TILE)):
                 t = c
                 if small:
                     t = (t + small_products([words[j][d][0] for d in range(dim)],
@@ -221,9 +222,9 @@ def fx_field(cov, z1, z2, pos):
                     t = (t + ((bf * pw[d][0]) >> 32)) & U32
                     t = (t + bi * pw[d][0]) & U32
                 terms.append(fx_term(t, tabs[j]))
-            if len(terms) == 32:          # a full tile: groups of eight modes
+            if len(terms) == TILE:        # a full tile: groups of eight modes
                 groups = []
-                for q in range(0, 32, 8):
+                for q in range(0, TILE, 8):
                     pairs = [f32(terms[q + 2 * k] + terms[q + 2 * k + 1]) for k in range(4)]
                     pend = f32(f32(pairs[0] + pairs[1]) + pairs[2])
                     groups.append(f32(pend + pairs[3]))
