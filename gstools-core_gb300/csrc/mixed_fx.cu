@@ -55,7 +55,7 @@ constexpr int kFxThreads = 128;
 static_assert(kFxThreads == kBatchThreads, "batch units assume the block size");
 constexpr int kFxR = 4;                 // points per thread when untuned
 constexpr int kFxW = 8;                 // target blocks per SM when untuned
-constexpr int kFxTile = 128;            // modes per staged tile = accumulation tile
+constexpr int kFxTile = 128;            // modes per staged tile = accumulation tile (largest)
 constexpr int kFxSplitModes = 64;       // mode splits are multiples of this
 // 32-bit words per mode: [0..2] BI' (BI + 2^31), [3] w0, [4..6] BF, [7] w1,
 // [8] w2 (projector weights of the incompressible field, FP32), [9..11] BI
@@ -364,8 +364,8 @@ __device__ __forceinline__ FxModeWords fx_mode_words(const uint32_t *srec, uint3
 // One block's work: the kFxThreads*R points from p_first (thread t owns
 // p_first + t + r*kFxThreads), modes [jb, je) of the records `rec`; sums
 // written (accumulate=0) or added at dst + i*sd + p*sp.  maxbits: the
-// positions' range words (scales); srec: shared staging of kFxTile records.
-template <int D, int R, bool INC, bool SMALL>
+// positions' range words (scales); srec: shared staging of TILE records.
+template <int D, int R, bool INC, bool SMALL, int TILE>
 __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_t P, int64_t p_first,
                                          const uint32_t *__restrict__ rec, int64_t jb, int64_t je,
                                          int accumulate, double *__restrict__ dst, int64_t sd,
@@ -419,8 +419,8 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
     }
 
     const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(srec));
-    for (int64_t t0 = jb; t0 < je; t0 += kFxTile) {
-        const int tm = static_cast<int>(min(static_cast<int64_t>(kFxTile), je - t0));
+    for (int64_t t0 = jb; t0 < je; t0 += TILE) {
+        const int tm = static_cast<int>(min(static_cast<int64_t>(TILE), je - t0));
         __syncthreads();
         {
             // the header (words 0..11) and the table (words 32..63) of each record
@@ -438,10 +438,10 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
 #pragma unroll
             for (int i = 0; i < NOUT; ++i) acc[r][i] = cmp[r][i] = 0.f;
         // modes in groups of eight: four pair sums per point, added, then one
-        // Kahan step; a tile shorter than kFxTile (the last) goes in pairs,
+        // Kahan step; a tile shorter than TILE (the last) goes in pairs,
         // the second mode of an odd tile's last pair counting zero times
         constexpr int kGroupPairs = 4;
-        const int tq = tm == kFxTile ? kFxTile : 0;
+        const int tq = tm == TILE ? TILE : 0;
         for (int m = 0; m < tq; m += 2 * kGroupPairs) {
             float pend[R][NOUT];
 #pragma unroll
@@ -510,35 +510,39 @@ __device__ __forceinline__ void fx_block_(const double *__restrict__ pos, int64_
 // The block's work with the product form its modes allow: maxbits[3] is
 // set when some mode of the call (or batch item) has |BI| >= 2^20; the
 // branch is the same for the whole block.
-template <int D, int R, bool INC>
+template <int D, int R, bool INC, int TILE>
 __device__ __forceinline__ void fx_block(const double *__restrict__ pos, int64_t P, int64_t p_first,
                                          const uint32_t *__restrict__ rec, int64_t jb, int64_t je,
                                          int accumulate, double *__restrict__ dst, int64_t sd,
                                          int64_t sp, const unsigned long long *maxbits,
                                          uint32_t *srec) {
     if (maxbits[3] == 0ull)
-        fx_block_<D, R, INC, true>(pos, P, p_first, rec, jb, je, accumulate, dst, sd, sp, maxbits,
-                                   srec);
+        fx_block_<D, R, INC, true, TILE>(pos, P, p_first, rec, jb, je, accumulate, dst, sd, sp,
+                                         maxbits, srec);
     else
-        fx_block_<D, R, INC, false>(pos, P, p_first, rec, jb, je, accumulate, dst, sd, sp, maxbits,
-                                    srec);
+        fx_block_<D, R, INC, false, TILE>(pos, P, p_first, rec, jb, je, accumulate, dst, sd, sp,
+                                          maxbits, srec);
 }
 
 // R points per thread (2, 4 or 8; the autotuner picks).  The launch bound
 // leaves room for several resident blocks, so that the R points' integer and
-// FP32 chains interleave with other warps'.
+// FP32 chains interleave with other warps'.  Tiles of 128 modes for R = 8
+// (three blocks per SM, limited by registers); 64 for R = 2, 4, whose
+// launches keep more blocks per SM than 32 KB tiles of shared memory allow.
 template <int D, bool INC, int R>
 __global__ void __launch_bounds__(kFxThreads, R >= 8 ? 3 : 4)
 mixed_fx_kernel(const double *__restrict__ pos, int64_t P, const uint32_t *__restrict__ rec,
                 const unsigned long long *__restrict__ maxbits, int64_t nc, int64_t mps,
                 int accumulate, double *__restrict__ dst, int64_t sd, int64_t sp,
                 int64_t split_stride) {
-    __shared__ __align__(256) uint32_t srec[kFxTile * kFxRecWords];
+    constexpr int TILE = R >= 8 ? kFxTile : kFxTile / 2;
+    __shared__ __align__(256) uint32_t srec[TILE * kFxRecWords];
     const int64_t jb = static_cast<int64_t>(blockIdx.y) * mps;
     const int64_t je = min(nc, jb + mps);
-    fx_block<D, R, INC>(pos, P, static_cast<int64_t>(blockIdx.x) * (kFxThreads * R), rec, jb, je,
-                        accumulate, dst + static_cast<int64_t>(blockIdx.y) * split_stride, sd, sp,
-                        maxbits, srec);
+    fx_block<D, R, INC, TILE>(pos, P, static_cast<int64_t>(blockIdx.x) * (kFxThreads * R), rec, jb,
+                              je, accumulate,
+                              dst + static_cast<int64_t>(blockIdx.y) * split_stride, sd, sp,
+                              maxbits, srec);
 }
 
 template <int D, bool INC>
@@ -699,21 +703,26 @@ batch_fx_kernel(const BatchItem *__restrict__ items, const BatchUnit *__restrict
         const unsigned long long *mb = maxbits + 4 * w.item;
         switch (it.dim * 2 + it.incompr) {
             case 2:
-                fx_block<1, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                fx_block<1, R, false, kFxTile>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P,
+                                              1, mb, srec);
                 break;
             case 4:
-                fx_block<2, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                fx_block<2, R, false, kFxTile>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P,
+                                              1, mb, srec);
                 break;
             case 5:
                 if constexpr (!SCALAR)
-                    fx_block<2, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                    fx_block<2, R, true, kFxTile>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P,
+                                                  1, mb, srec);
                 break;
             case 6:
-                fx_block<3, R, false>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                fx_block<3, R, false, kFxTile>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P,
+                                              1, mb, srec);
                 break;
             case 7:
                 if constexpr (!SCALAR)
-                    fx_block<3, R, true>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P, 1, mb, srec);
+                    fx_block<3, R, true, kFxTile>(it.pos, P, w.p_first, rc, w.jb, w.je, 0, dst, P,
+                                                  1, mb, srec);
                 break;
             default:
                 break;
