@@ -1077,7 +1077,7 @@ PROFILED_TRAFFIC = {
     ("plain_f64_scalar", "c1"): (5.8e6, "profiles/plain_f64_scalar_c1.md"),
     ("mixed_scalar", "c1"): (1.906e6, "profiles/mixed_fx_c1.md"),
     ("mixed_scalar", "c3"): (411.7e6 + 115.0e6, "profiles/mixed_fx_c3.md"),
-    ("batch_mixed", "c5"): (2274.0e6 + 668.3e6, "profiles/batch_fx_c5.md"),
+    ("batch_mixed", "c5"): (2275.9e6 + 668.5e6, "profiles/batch_fx_c5.md"),
 }
 
 
