@@ -231,3 +231,33 @@ def test_mixed_padded_output_and_range(gsc, in_range):
     assert np.isnan(buf[:, 3]).all()
     ref = oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)
     assert rel_err(buf[:, :3].T, ref) <= (TOL if in_range else 1e-12)
+
+
+@pytest.mark.parametrize("case", ["subnormal", "zero", "tiny", "huge"])
+def test_mixed_extreme_coordinate_magnitudes(gsc, case):
+    """The fixed-point scale comes from the exponent of the largest |x|: a
+    subnormal largest coordinate (frexp), all coordinates zero (no finite
+    nonzero value), and magnitudes near the ends of the FP64 range with wave
+    numbers scaled the other way (phases of order one, the scaling outside
+    the range of a normal power of two).  Against the oracle at 1e-6."""
+    rng = np.random.default_rng(21)
+    n, p = 64, 4000
+    cov = rng.normal(0.0, 1.0, (3, n))
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(-1.0, 1.0, (3, p))
+    if case == "subnormal":
+        pos *= 1e-310
+    elif case == "zero":
+        pos[:] = 0.0
+    elif case == "tiny":
+        pos *= 1e-300
+        cov *= 1e300
+    else:
+        pos *= 1e300
+        cov *= 1e-300
+    ref = oracle.summator(cov, z1, z2, pos, num_threads=NT)
+    got = gsc.summate(cov, z1, z2, pos, form="mixed")
+    assert rel_err(got, ref) <= TOL
+    if case != "huge":             # |k|^2 underflows there: the reference's projector is NaN
+        gi = gsc.summate_incompr(cov, z1, z2, pos, form="mixed")
+        assert rel_err(gi, oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)) <= TOL
