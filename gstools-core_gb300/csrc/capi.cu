@@ -45,6 +45,7 @@ const char *kernel_name(int32_t id) {
         "grid_expand", "sep_tc_f16x5", "mixed_modes", "mixed_scalar", "mixed_incompr",
         "mixed_f64phase", "sep_f64_dmma", "fourier_scale", "batch_tables", "batch_plain",
         "batch_mixed", "sample_modes", "sep_split", "copy_h2d", "copy_d2h", "interleave",
+        "mesh_check",
     };
     return (id >= 0 && id < K_COUNT) ? names[id] : "unknown";
 }
@@ -797,31 +798,35 @@ struct MeshCheck {
 };
 
 // Any point of slices [0, na) that differs from the candidate axes (or is
-// NaN) sets *bad.  Grid-stride over the points, two per thread and pass so
-// that six host reads are in flight per thread.
+// NaN) sets *bad.  Warps take rows of contiguous points -- (x-slice, y) rows
+// of n2 points in 3-D, x-slices of n1 points in 2-D -- so that the axis
+// indices cost one division per row; lanes stride along the row with four
+// iterations' host reads in flight.
 __global__ void __launch_bounds__(1024) mesh_check_kernel(const double *__restrict__ pos,
                                                           int64_t sd, int64_t na, int64_t n1,
                                                           int64_t n2, int dim,
                                                           const double *__restrict__ a0,
                                                           const double *__restrict__ a1,
                                                           const double *__restrict__ a2, int *bad) {
-    const int64_t L0 = n1 * n2, total = na * L0;
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int lane = static_cast<int>(threadIdx.x & 31);
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t L = dim == 3 ? n2 : n1;                 // points per row
+    const int64_t rows = dim == 3 ? na * n1 : na;
     int miss = 0;
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
-         i += 2 * stride) {
-        const int64_t j = i + stride;
-        const bool two = j < total;
-        const double x0 = pos[i], y0 = pos[sd + i], w0 = dim == 3 ? pos[2 * sd + i] : 0.0;
-        const double x1 = two ? pos[j] : 0.0, y1 = two ? pos[sd + j] : 0.0,
-                     w1 = two && dim == 3 ? pos[2 * sd + j] : 0.0;
-        const int64_t a = i / L0, r = i - a * L0, b = dim == 3 ? r / n2 : r;
-        miss |= (x0 != a0[a]) | (y0 != a1[b]);
-        if (dim == 3) miss |= w0 != a2[r - b * n2];
-        if (two) {
-            const int64_t aj = j / L0, rj = j - aj * L0, bj = dim == 3 ? rj / n2 : rj;
-            miss |= (x1 != a0[aj]) | (y1 != a1[bj]);
-            if (dim == 3) miss |= w1 != a2[rj - bj * n2];
+    for (int64_t row = warp; row < rows; row += n_warps) {
+        const int64_t a = dim == 3 ? row / n1 : row;
+        const double xa = a0[a];
+        const double *px = pos + row * L, *py = px + sd;
+        if (dim == 3) {
+            const double yb = a1[row - a * n1];
+            const double *pz = px + 2 * sd;
+#pragma unroll 4
+            for (int64_t c = lane; c < L; c += 32)
+                miss |= (px[c] != xa) | (py[c] != yb) | (pz[c] != a2[c]);
+        } else {
+#pragma unroll 4
+            for (int64_t c = lane; c < L; c += 32) miss |= (px[c] != xa) | (py[c] != a1[c]);
         }
     }
     if (__syncthreads_or(miss) && threadIdx.x == 0) atomicOr(bad, 1);
@@ -909,8 +914,11 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
                 const unsigned hw = std::thread::hardware_concurrency();
                 const int64_t workers = std::max<int64_t>(1, static_cast<int64_t>(hw ? hw : 2) - 1);
                 // Where the GPU reads pageable host memory in place, it checks
-                // the first half of the x-slices of C-ordered rows while the
-                // host cores check the rest (both read at about 185 GB/s)
+                // the first 65 % of the x-slices of C-ordered rows while the
+                // host cores check the rest: the host threads share the host's
+                // memory with the result's copy, and on a GB300 node this
+                // split ends both checks together (C2's 403 MB mesh: 2.2 ms
+                // per call, 2.4-2.6 ms at half and half)
                 MeshCheck mc;
                 const bool dev_check = ps_p == 1 && n[0] >= 4 &&
                                        static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(32) << 20) &&
@@ -918,7 +926,7 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
                 if (dev_check) {
                     mc.pos = pos;
                     mc.sd = ps_d;
-                    mc.na = n[0] / 2;
+                    mc.na = std::max<int64_t>(1, std::min<int64_t>(n[0] - 1, n[0] * 13 / 20));
                     for (int k = 0; k < 3; ++k) {
                         mc.ax[k] = k < dim ? axv[k].data() : nullptr;
                         mc.n[k] = n[k];
@@ -1301,9 +1309,12 @@ static int host_structured(const double *cov, int64_t cs_d, int64_t cs_n, const 
         GSC_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->chunk_ev, 0));
         int *flag = ctx->status + kStatusMeshCheck;
         GSC_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream2));
+        TimedLaunch tl(ctx->stream2);
+        tl.begin(K_MESH_CHECK);
         mesh_check_kernel<<<16, 1024, 0, ctx->stream2>>>(
             mc->pos, mc->sd, mc->na, mc->n[1], mc->dim == 3 ? mc->n[2] : 1, mc->dim, mc->ax[0],
             mc->ax[1], mc->dim == 3 ? mc->ax[2] : nullptr, flag);
+        tl.end();
         GSC_CUDA(cudaGetLastError());
         check_read.mc = mc;
         check_read.s = ctx->stream2;

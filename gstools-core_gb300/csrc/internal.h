@@ -62,6 +62,7 @@ enum KernelId : int32_t {
     K_COPY_H2D = 22,       // host-to-device copies of a host-pointer call (not a kernel)
     K_COPY_D2H = 23,       // device-to-host copies of a host-pointer call (not a kernel)
     K_INTERLEAVE = 24,     // (nout, P) rows to the (P, nout) layout of a Fortran-ordered result
+    K_MESH_CHECK = 25,     // the device's share of the check of a flattened mesh
     K_COUNT
 };
 const char *kernel_name(int32_t id);

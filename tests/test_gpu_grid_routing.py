@@ -143,7 +143,7 @@ def test_incompr_any_output_strides(gsc, grid):
 @pytest.mark.parametrize("where", ["clean", "device_half", "host_half", "nan_device_half"])
 def test_large_mesh_check_shared_with_the_device(gsc, where):
     """Meshes of 32 MiB and more, where the GPU reads host memory in place:
-    the GPU checks the first half of the x-slices over the host link while
+    the GPU checks the first 65 % of the x-slices over the host link while
     the host cores check the rest.  A clean mesh takes the separable form;
     one coordinate moved by an ulp (or a NaN) in either half sends the call
     to the point kernels.  Against the oracle on a subset that holds the
