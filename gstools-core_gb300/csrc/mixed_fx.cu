@@ -644,11 +644,18 @@ int fx_sm_count(int device) {
 }
 
 // ---- batched ensembles ------------------------------------------------------------
-// Range words of every item: block b of the grid walks item b's positions.
-__global__ void batch_fx_range_kernel(const BatchItem *__restrict__ items,
-                                      unsigned long long *maxbits) {
+// Range words of every item: the kBatchRangeBlocks blocks (blockIdx.y) of
+// column blockIdx.x walk item blockIdx.x's positions.  Small blocks, so
+// that the next ensemble's tables fit beside a persistent kernel's last
+// blocks instead of waiting for whole SMs.
+constexpr int kBatchRangeThreads = 128, kBatchRangeBlocks = 8;
+__global__ void __launch_bounds__(kBatchRangeThreads)
+batch_fx_range_kernel(const BatchItem *__restrict__ items, unsigned long long *maxbits) {
     const BatchItem &it = items[blockIdx.x];
-    fx_range_part(it.pos, it.n_points, it.dim, threadIdx.x, blockDim.x, maxbits + 4 * blockIdx.x);
+    fx_range_part(it.pos, it.n_points, it.dim,
+                  static_cast<int64_t>(blockIdx.y) * kBatchRangeThreads + threadIdx.x,
+                  static_cast<int64_t>(kBatchRangeThreads) * kBatchRangeBlocks,
+                  maxbits + 4 * blockIdx.x);
 }
 
 // Records of every item, one thread per mode (Fourier factor folded into z1,
@@ -897,7 +904,8 @@ int batch_fx_tables(const BatchItem *items, const int64_t *mode_prefix, int64_t 
     tl.begin(K_BATCH_TABLES);
     GSC_CUDA(cudaMemsetAsync(maxbits, 0, static_cast<size_t>(n_items) * 4 * sizeof(unsigned long long),
                              st));
-    batch_fx_range_kernel<<<static_cast<unsigned>(n_items), 1024, 0, st>>>(items, maxbits);
+    batch_fx_range_kernel<<<dim3(static_cast<unsigned>(n_items), kBatchRangeBlocks),
+                            kBatchRangeThreads, 0, st>>>(items, maxbits);
     if (total_modes > 0)
         batch_fx_table_kernel<<<static_cast<unsigned>((total_modes + 127) / 128), 128, 0, st>>>(
             items, mode_prefix, n_items, total_modes, maxbits, rec, range_flag);
