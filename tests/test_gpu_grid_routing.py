@@ -140,7 +140,13 @@ def test_incompr_any_output_strides(gsc, grid):
     assert rel_err(buf[:, :3].T, ref) <= 1e-12
 
 
-@pytest.mark.parametrize("where", ["clean", "device_half", "host_half", "nan_device_half"])
+def _device_slices(n0):
+    """x-slices the device checks: the first 65 % (at least one, not all)."""
+    return max(1, min(n0 - 1, n0 * 13 // 20))
+
+
+@pytest.mark.parametrize("where", ["clean", "device_half", "host_half", "nan_device_half",
+                                   "device_last", "host_first"])
 def test_large_mesh_check_shared_with_the_device(gsc, where):
     """Meshes of 32 MiB and more, where the GPU reads host memory in place:
     the GPU checks the first 65 % of the x-slices over the host link while
@@ -151,7 +157,10 @@ def test_large_mesh_check_shared_with_the_device(gsc, where):
     shape = (64, 128, 256)                                  # 2.1 M points, 50 MB
     cov, z1, z2, axes = _case(7, shape, 64)
     pos = _flat(axes)
-    p = 1234 + (5 if where != "host_half" else shape[0] - 3) * shape[1] * shape[2]
+    L0 = shape[1] * shape[2]
+    na = _device_slices(shape[0])
+    p = {"device_last": na * L0 - 1, "host_first": na * L0}.get(
+        where, 1234 + (5 if where != "host_half" else shape[0] - 3) * L0)
     if where == "nan_device_half":
         pos[2, p] = np.nan
     elif where != "clean":
@@ -168,3 +177,26 @@ def test_large_mesh_check_shared_with_the_device(gsc, where):
     bad = np.isnan(ref)
     assert np.array_equal(np.isnan(got), bad)
     assert rel_err(got[~bad], ref[~bad]) <= 1e-12
+
+
+@pytest.mark.parametrize("where", ["clean", "device_row", "host_row"])
+def test_large_2d_mesh_check(gsc, where):
+    """A 2-D flattened mesh of 64 MiB: the device checks whole x-slices as
+    rows.  One coordinate moved by an ulp in a device or a host slice sends
+    the call to the point kernels."""
+    shape = (2048, 2048)
+    cov, z1, z2, axes = _case(9, shape, 48)
+    pos = _flat(axes)
+    na = _device_slices(shape[0])
+    p = {"device_row": (na - 1) * shape[1] + 77, "host_row": na * shape[1] + 5}.get(where, 0)
+    if where != "clean":
+        pos[1, p] = np.nextafter(pos[1, p], -np.inf)
+    out = gsc.summate(cov, z1, z2, pos, timing=True)
+    ks = _kernels(gsc)
+    if where == "clean":
+        assert "sep_f64_dmma" in ks
+    else:
+        assert "sep_f64_dmma" not in ks, ks
+    idx = np.unique(np.concatenate([np.random.default_rng(10).choice(pos.shape[1], 2048, replace=False), [p]]))
+    ref = oracle.summator(cov, z1, z2, np.ascontiguousarray(pos[:, idx]), num_threads=NT)
+    assert rel_err(out[idx], ref) <= 1e-12
