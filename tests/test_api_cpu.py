@@ -59,3 +59,15 @@ def test_batch_checks(gsc):
 def test_sampling_checks(gsc):
     with pytest.raises(ValueError):
         gsc.sample_modes("matern", 2, 10, 1.0, 0)
+
+
+def test_data_address_of_any_layout():
+    """The Python layer's data address agrees with numpy's for C-ordered,
+    Fortran-ordered, strided, offset, empty and read-only arrays."""
+    import numpy as np
+    import gstools_core as gsc
+    a = np.arange(12.0).reshape(3, 4)
+    ro = a.copy()
+    ro.setflags(write=False)
+    for x in (a, np.asfortranarray(a), a[:, ::2], a[1:], a[::-1], np.zeros(0), ro):
+        assert gsc._ptr(x) == x.ctypes.data
