@@ -914,11 +914,13 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
                 const unsigned hw = std::thread::hardware_concurrency();
                 const int64_t workers = std::max<int64_t>(1, static_cast<int64_t>(hw ? hw : 2) - 1);
                 // Where the GPU reads pageable host memory in place, it checks
-                // the first 65 % of the x-slices of C-ordered rows while the
-                // host cores check the rest: the host threads share the host's
-                // memory with the result's copy, and on a GB300 node this
-                // split ends both checks together (C2's 403 MB mesh: 2.2 ms
-                // per call, 2.4-2.6 ms at half and half)
+                // the first x-slices of C-ordered rows while the host cores
+                // check the rest.  Its share f balances the host link, which
+                // carries the device's reads and the result's copy (about 180
+                // GB/s together on a GB300 node), against the host cores'
+                // reads (about 82 GB/s while the copy writes into host
+                // memory): f = 0.687 - 0.313 r, r = result bytes / mesh
+                // bytes = components / dimensions (C2 0.58, C4 0.37)
                 MeshCheck mc;
                 const bool dev_check = ps_p == 1 && n[0] >= 4 &&
                                        static_cast<size_t>(dim * P) * sizeof(double) >= (size_t(32) << 20) &&
@@ -926,7 +928,8 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
                 if (dev_check) {
                     mc.pos = pos;
                     mc.sd = ps_d;
-                    mc.na = std::max<int64_t>(1, std::min<int64_t>(n[0] - 1, n[0] * 13 / 20));
+                    const int64_t f_milli = 687 - 313 * nout / dim;
+                    mc.na = std::max<int64_t>(1, std::min<int64_t>(n[0] - 1, n[0] * f_milli / 1000));
                     for (int k = 0; k < 3; ++k) {
                         mc.ax[k] = k < dim ? axv[k].data() : nullptr;
                         mc.n[k] = n[k];

@@ -140,17 +140,19 @@ def test_incompr_any_output_strides(gsc, grid):
     assert rel_err(buf[:, :3].T, ref) <= 1e-12
 
 
-def _device_slices(n0):
-    """x-slices the device checks: the first 65 % (at least one, not all)."""
-    return max(1, min(n0 - 1, n0 * 13 // 20))
+def _device_slices(n0, dim, nout=1):
+    """x-slices the device checks: the first n0 (0.687 - 0.313 nout / dim)
+    (at least one, not all)."""
+    return max(1, min(n0 - 1, n0 * (687 - 313 * nout // dim) // 1000))
 
 
 @pytest.mark.parametrize("where", ["clean", "device_half", "host_half", "nan_device_half",
                                    "device_last", "host_first"])
 def test_large_mesh_check_shared_with_the_device(gsc, where):
     """Meshes of 32 MiB and more, where the GPU reads host memory in place:
-    the GPU checks the first 65 % of the x-slices over the host link while
-    the host cores check the rest.  A clean mesh takes the separable form;
+    the GPU checks the first x-slices over the host link (a share that
+    balances the link against the host cores) while the host cores check
+    the rest.  A clean mesh takes the separable form;
     one coordinate moved by an ulp (or a NaN) in either half sends the call
     to the point kernels.  Against the oracle on a subset that holds the
     changed point."""
@@ -158,7 +160,7 @@ def test_large_mesh_check_shared_with_the_device(gsc, where):
     cov, z1, z2, axes = _case(7, shape, 64)
     pos = _flat(axes)
     L0 = shape[1] * shape[2]
-    na = _device_slices(shape[0])
+    na = _device_slices(shape[0], 3)
     p = {"device_last": na * L0 - 1, "host_first": na * L0}.get(
         where, 1234 + (5 if where != "host_half" else shape[0] - 3) * L0)
     if where == "nan_device_half":
@@ -187,7 +189,7 @@ def test_large_2d_mesh_check(gsc, where):
     shape = (2048, 2048)
     cov, z1, z2, axes = _case(9, shape, 48)
     pos = _flat(axes)
-    na = _device_slices(shape[0])
+    na = _device_slices(shape[0], 2)
     p = {"device_row": (na - 1) * shape[1] + 77, "host_row": na * shape[1] + 5}.get(where, 0)
     if where != "clean":
         pos[1, p] = np.nextafter(pos[1, p], -np.inf)
