@@ -1023,7 +1023,25 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
     // one contiguous copy
     const bool c_order = os_p == 1 && (nout == 1 || os_d == P);
     const bool f_order = !c_order && os_d == 1 && os_p == nout;
-    a.out = d + n_in;
+    // A pinned C- or Fortran-ordered result (the Python layer's pool blocks)
+    // is written by the kernels in place over the coherent host link: no
+    // copy back and none of its fixed cost.  Not where the result's bytes
+    // overlap an input that is read in place.
+    bool direct_out = (c_order || f_order) && pageable && is_pinned_host(out);
+    if (direct_out) {
+        uintptr_t olo, ohi;
+        view_span(out, os_d, os_p, nout, P, olo, ohi);
+        auto apart = [&](const double *q, int64_t s0, int64_t s1, int64_t rows, int64_t cols) {
+            uintptr_t lo, hi;
+            view_span(q, s0, s1, rows, cols, lo, hi);
+            return ohi <= lo || hi <= olo;
+        };
+        if (pos_in_place && !apart(pos, ps_d, ps_p, dim, P)) direct_out = false;
+        if (modes_in_place && (!apart(cov, cs_d, cs_n, dim, N) || !apart(z1, 0, z1s, 1, N) ||
+                               !apart(z2, 0, z2s, 1, N)))
+            direct_out = false;
+    }
+    a.out = direct_out ? out : d + n_in;
     a.out_sd = f_order ? 1 : P;
     a.out_sp = f_order ? nout : 1;
     const bool fx = point_form(ro, a) == GSC_FORM_MIXED;
@@ -1053,6 +1071,18 @@ static int host_plain(const double *cov, int64_t cs_d, int64_t cs_n, const doubl
         rp.form = GSC_FORM_PLAIN_F64;
         return run_points(*ctx, rp, a, st, nullptr);
     };
+    if (direct_out) {
+        if (fx && !flag_mapped)
+            GSC_CUDA(cudaMemcpyAsync(const_cast<int *>(hflag), dflag, sizeof(int),
+                                     cudaMemcpyDeviceToHost, st));
+        GSC_CUDA(cudaStreamSynchronize(st));
+        if (*hflag) {
+            *hflag = 0;
+            GSC_TRY(recompute());
+            GSC_CUDA(cudaStreamSynchronize(st));
+        }
+        return GSC_OK;
+    }
     if (c_order || f_order) {
         Prefault pf;
         if (!is_pinned_host(out)) pf.start(out, n_out * sizeof(double));
