@@ -261,3 +261,23 @@ def test_mixed_extreme_coordinate_magnitudes(gsc, case):
     if case != "huge":             # |k|^2 underflows there: the reference's projector is NaN
         gi = gsc.summate_incompr(cov, z1, z2, pos, form="mixed")
         assert rel_err(gi, oracle.summator_incompr(cov, z1, z2, pos, num_threads=NT)) <= TOL
+
+
+@pytest.mark.parametrize("kind", ["scalar", "incompr"])
+def test_range_fallback_into_a_pinned_result(gsc, kind):
+    """A result of 64 KiB and more comes from the pinned pool, and the
+    kernels write it in place; past the phase range AUTO recomputes it on
+    the plain FP64 kernel over the mixed form's invalid values.  C-ordered
+    (scalar) and Fortran-ordered (incompressible) results."""
+    rng = np.random.default_rng(31)
+    n, p = 40, 20_000                                  # 160 KB per component
+    cov = rng.normal(0.0, 0.5, (3, n))
+    cov[2, 9] = 40.0                                   # 40 x 2e8 / 2 pi > 2^30 turns
+    z1, z2 = rng.standard_normal(n), rng.standard_normal(n)
+    pos = rng.uniform(0.0, 2.0e8, (3, p))
+    fn = gsc.summate_incompr if kind == "incompr" else gsc.summate
+    ofn = oracle.summator_incompr if kind == "incompr" else oracle.summator
+    out = fn(cov, z1, z2, pos, tolerance=1e-6)
+    assert rel_err(out, ofn(cov, z1, z2, pos, num_threads=NT)) <= 1e-12
+    ok = fn(cov[:, :9], z1[:9], z2[:9], pos, tolerance=1e-6)
+    assert rel_err(ok, ofn(cov[:, :9], z1[:9], z2[:9], pos, num_threads=NT)) <= TOL
